@@ -1,0 +1,542 @@
+"""CPU oracle: the reference's merged two-site DMRG path, restated in NumPy.
+
+Test infrastructure only (imported by ``tests/``, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py``).  Each function cites the reference
+file:line it follows (paths relative to the mpsxx project root).  Single root
+(``nroots = 1``): the Davidson functor then applies no projections
+(``src/diagonalize.hpp:217-233``).
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from .qsd import (NoTrans, Trans, ZERO, MergeInfo, QSDArray, axpy, contract, copy_into, dimm_cols,
+                  dimm_rows, dotc, expand_cols, expand_rows, gemm, merge_cols, merge_rows, normalize,
+                  nrm2, orthogonalize, qadd, qneg, scal, tie_02)
+
+# relative window inside which singular values count as ties of the cutoff
+SVD_TIE_RTOL = 1e-10
+
+
+# ----------------------------------------------------------------------------
+# a6: sigma vector (src/compute_sigma_vector.hpp:85-96)
+# ----------------------------------------------------------------------------
+
+def compute_sigma_vector(lopr: QSDArray, ropr: QSDArray, wfn0: QSDArray, sgv0: QSDArray,
+                         tasks: Optional[list] = None):
+    """sgv0 += sum_{w,A',B'} L[A,w,A'] psi[A',B'] R[B,w,B'] (two Gemm's)."""
+    scr1 = QSDArray()
+    t1 = gemm(NoTrans, NoTrans, 1.0, lopr, wfn0, 1.0, scr1, nc=3, return_tasks=True)
+    t2 = gemm(NoTrans, Trans, 1.0, scr1, ropr, 1.0, sgv0, nc=2, return_tasks=True)
+    if tasks is not None:
+        tasks.append(("LxPsi", t1))
+        tasks.append(("ScrxRt", t2))
+    return scr1
+
+
+# ----------------------------------------------------------------------------
+# a9: renormalize merged operator / overlap (src/renormalize.hpp:57-95)
+# ----------------------------------------------------------------------------
+
+def renormalize_merged(forward: bool, opr0: QSDArray, bra0: QSDArray, ket0: QSDArray,
+                       tasks: Optional[list] = None) -> QSDArray:
+    opr1 = QSDArray()
+    scr1 = QSDArray()
+    if forward:
+        t1 = gemm(Trans, NoTrans, 1.0, bra0.conjugate(), opr0, 1.0, scr1, nc=3, return_tasks=True)
+        t2 = gemm(NoTrans, NoTrans, 1.0, scr1, ket0, 1.0, opr1, nc=3, return_tasks=True)
+    else:
+        t1 = gemm(NoTrans, NoTrans, 1.0, bra0.conjugate(), opr0, 1.0, scr1, nc=3, return_tasks=True)
+        t2 = gemm(NoTrans, Trans, 1.0, scr1, ket0, 1.0, opr1, nc=3, return_tasks=True)
+    if tasks is not None:
+        tasks.append(("BraxOp", t1))
+        tasks.append(("ScrxKet", t2))
+    return opr1
+
+
+# ----------------------------------------------------------------------------
+# one-site MPO renormalisation, used to build the initial environments
+# (src/renormalize.hpp:10-32)
+# ----------------------------------------------------------------------------
+
+def renormalize_mpo(forward: bool, mpo0: QSDArray, opr0: QSDArray, bra0: QSDArray,
+                    ket0: QSDArray) -> QSDArray:
+    if forward:
+        # opr1[m,w',m'] = sum opr0[l,w,l'] bra[l,n,m] mpo[w,n,n',w'] ket[l',n',m']
+        scr1 = contract(opr0, "lwx", bra0.conjugate(), "lnm", "wxnm")
+        scr2 = contract(scr1, "wxnm", mpo0, "wnsv", "xmsv")
+        return contract(scr2, "xmsv", ket0, "xsy", "mvy")
+    # opr1[b,w,b'] = sum bra[b,n,r] opr0[r,w',r'] mpo[w,n,n',w'] ket[b',n',r']
+    scr1 = contract(bra0.conjugate(), "bnr", opr0, "rvx", "bnvx")
+    scr2 = contract(scr1, "bnvx", mpo0, "wnsv", "bxws")
+    return contract(scr2, "bxws", ket0, "ysx", "bwy")
+
+
+# ----------------------------------------------------------------------------
+# a5: diagonal of H_eff (src/compute_diagonal_elements.hpp:65-80)
+# ----------------------------------------------------------------------------
+
+def compute_diagonal_elements(lopr: QSDArray, ropr: QSDArray, diag: QSDArray):
+    """diag[A,B] += sum_w L[A,w,A] R[B,w,B] on the blocks diag's quantum numbers allow."""
+    ld = tie_02(lopr)
+    rd = tie_02(ropr)
+    # Gemm(NoTrans, Trans) over the un-quantised tied arrays: c(i,j) = sum_w a(i,w) b(j,w)
+    scr: Dict[tuple, np.ndarray] = {}
+    rbyw: Dict[int, list] = {}
+    for (j, w), blk in sorted(rd.items()):
+        rbyw.setdefault(w, []).append((j, blk))
+    for (i, w), ablk in sorted(ld.items()):
+        for j, bblk in rbyw.get(w, []):
+            v = ablk @ bblk.T
+            if (i, j) in scr:
+                scr[(i, j)] = scr[(i, j)] + v
+            else:
+                scr[(i, j)] = v
+    # Copy(scr, diag, 1): keep blocks allowed by diag's quantum numbers
+    for (i, j), blk in scr.items():
+        if diag.allowed((i, j)):
+            t = diag.tag((i, j))
+            if t in diag.blocks:
+                diag.blocks[t] = diag.blocks[t] + blk
+            else:
+                diag.blocks[t] = blk.copy()
+
+
+# ----------------------------------------------------------------------------
+# a7: Davidson (src/diagonalize.hpp:283-449), single root
+# ----------------------------------------------------------------------------
+
+@dataclass
+class DavidsonStats:
+    n_sigma: int = 0
+    macro: int = 0
+    micro: int = 0
+    rnorm: float = 0.0
+    converged: bool = False
+
+
+def precondition(eval_: float, diag: QSDArray, errv: QSDArray):
+    """(E - diag)^-1 with |.| floored at 1e-8; 1/E where diag has no block (``:283-304``)."""
+    for t in errv.blocks:
+        d = diag.blocks.get(t)
+        if d is not None:
+            denm = eval_ - d
+            denm = np.where(np.abs(denm) < 1.0e-8, 1.0e-8, denm)
+            errv.blocks[t] = errv.blocks[t] / denm
+        else:
+            errv.blocks[t] = errv.blocks[t] * (1.0 / eval_)
+
+
+def davidson(multH, diag: QSDArray, wfnc: QSDArray, tolerance: float = 1.0e-8,
+             stats: Optional[DavidsonStats] = None) -> float:
+    """``Davidson::diagonalize`` (``src/diagonalize.hpp:310-449``)."""
+    max_ritz = 10
+    eval_ = 0.0
+    trial = [QSDArray() for _ in range(max_ritz)]
+    sigma = [QSDArray() for _ in range(max_ritz)]
+    copy_into(wfnc, trial[0])
+    niter = 0
+    iconv = 0
+    st = stats if stats is not None else DavidsonStats()
+    while iconv < 1 and niter < 4:
+        normalize(trial[0])
+        sigma[0] = QSDArray()
+        multH(trial[0], sigma[0])
+        st.n_sigma += 1
+        for m in range(1, max_ritz + 1):
+            heff = np.zeros((m, m))
+            for i in range(m):
+                heff[i, i] = dotc(trial[i], sigma[i])
+                for j in range(i):
+                    hij = dotc(trial[i], sigma[j])
+                    heff[i, j] = hij
+                    heff[j, i] = hij
+            rval, rvec = np.linalg.eigh(heff)
+            eval_ = float(rval[0])
+            st.micro += 1
+            trial_save = [t.copy() for t in trial[:m]]
+            sigma_save = [s.copy() for s in sigma[:m]]
+            for i in range(m):
+                scal(rvec[i, i], trial[i])
+                scal(rvec[i, i], sigma[i])
+            for i in range(m):
+                for j in range(m):
+                    if i != j:
+                        axpy(rvec[i, j], trial_save[i], trial[j])
+                        axpy(rvec[i, j], sigma_save[i], sigma[j])
+            errv = sigma[0].copy()
+            axpy(-eval_, trial[0], errv)
+            rnorm = dotc(errv, errv)
+            st.rnorm = rnorm
+            if rnorm < tolerance:
+                iconv += 1
+                break
+            if m < max_ritz:
+                precondition(eval_, diag, errv)
+                for i in range(m):
+                    normalize(errv)
+                    orthogonalize(trial[i], errv)
+                normalize(errv)
+                trial[m] = errv.copy()
+                sigma[m] = QSDArray()
+                multH(trial[m], sigma[m])
+                st.n_sigma += 1
+        niter += 1
+    st.macro = niter
+    st.converged = iconv > 0
+    copy_into(trial[0], wfnc)
+    normalize(wfnc)  # Functor<2>::orthonormalize with no lower roots
+    return eval_
+
+
+# ----------------------------------------------------------------------------
+# a8: truncated SVD + canonicalize (include/btas/QSPARSE/QSTLAPACK.h:121-288,
+#     src/canonicalize.hpp:48-106)
+# ----------------------------------------------------------------------------
+
+def select_kept(svals: Dict[int, np.ndarray], M: int, tie_rtol: float = SVD_TIE_RTOL):
+    """Global top-M selection (``QSTLAPACK.h:204-232``).
+
+    cutoff = s_sorted[M-1] when 0 < M < #s, else 1e-16; a sector keeps its
+    leading values >= cutoff.  Values within ``tie_rtol`` (relative) below the
+    cutoff count as ties and are kept: degenerate spin-flip sectors otherwise
+    split on last-bit rounding.
+    """
+    allv = np.concatenate([v for _, v in sorted(svals.items())]) if svals else np.zeros(0)
+    s_sorted = np.sort(allv)[::-1]
+    cutoff = 1.0e-16
+    if 0 < M < s_sorted.size:
+        cutoff = float(s_sorted[M - 1]) * (1.0 - tie_rtol)
+    kept = {}
+    dnorm = 0.0
+    for sec, v in sorted(svals.items()):
+        n = int(np.sum(v >= cutoff))
+        # values come sorted descending; keep the prefix
+        kept[sec] = n
+        dnorm += float(np.sum(v[n:] ** 2))
+    return kept, dnorm
+
+
+def gesvd_merged(a: QSDArray, M: int, left_arrow: bool, tie_rtol: float = SVD_TIE_RTOL):
+    """Truncated SVD of a 2-index merged array (``QSTLAPACK.h:121-288``).
+
+    Returns (s_blocks by new-bond sector, U [rows, s], Vt [s, cols], kept map).
+    LeftArrow: U carries zero quantum number, s sectors = row sectors.
+    RightArrow: Vt carries zero quantum number, s sectors = column sectors.
+    """
+    q_rows = a.qshape[0]
+    q_cols = a.qshape[1]
+    ncols = a.shape[1]
+    svals: Dict[int, np.ndarray] = {}
+    uvs: Dict[int, tuple] = {}
+    for t in sorted(a.blocks):
+        blk = a.blocks[t]
+        if blk.size == 0:
+            continue
+        i, j = t // ncols, t % ncols
+        u, s, vt = np.linalg.svd(blk, full_matrices=False)
+        sec = i if left_arrow else j
+        svals[sec] = s
+        uvs[sec] = (i, j, u, vt)
+    kept, dnorm = select_kept(svals, M, tie_rtol)
+    q_sval = q_rows if left_arrow else [qneg(q) for q in q_cols]
+    secs = [sec for sec in sorted(svals) if kept[sec] > 0]
+    q_nz = [q_sval[sec] for sec in secs]
+    d_nz = [kept[sec] for sec in secs]
+    newidx = {sec: n for n, sec in enumerate(secs)}
+    if left_arrow:
+        U = QSDArray(ZERO, [q_rows, [qneg(q) for q in q_nz]], [a.dshape[0], d_nz])
+        V = QSDArray(a.q, [q_nz, q_cols], [d_nz, a.dshape[1]])
+    else:
+        U = QSDArray(a.q, [q_rows, [qneg(q) for q in q_nz]], [a.dshape[0], d_nz])
+        V = QSDArray(ZERO, [q_nz, q_cols], [d_nz, a.dshape[1]])
+    s_out = {}
+    for sec in secs:
+        i, j, u, vt = uvs[sec]
+        k = kept[sec]
+        n = newidx[sec]
+        s_out[n] = svals[sec][:k].copy()
+        U.blocks[U.tag((i, n))] = u[:, :k].copy()
+        V.blocks[V.tag((n, j))] = vt[:k, :].copy()
+    return s_out, U, V, kept, dnorm
+
+
+def canonicalize_merged(forward: bool, wfnc: QSDArray, M: int, noise: float = 0.0):
+    """``canonicalize`` for merged MPS (``src/canonicalize.hpp:88-106``); noise < 1e-8 only."""
+    if noise >= 1.0e-8:
+        raise NotImplementedError("noise injection is not part of the oracle")
+    if forward:
+        s, U, V, kept, dn = gesvd_merged(wfnc, M, True)
+        dimm_rows(s, V)
+    else:
+        s, U, V, kept, dn = gesvd_merged(wfnc, M, False)
+        dimm_cols(U, s)
+    return U, V, kept
+
+
+def canonicalize_onesite_backward(wfnc: QSDArray, lmps: QSDArray, M: int):
+    """One-site backward canonicalize (``src/canonicalize.hpp:77-85``):
+    Gesvd<3,2,RightArrow>(wfnc -> g, rmps), g *= s, lmps <- lmps * g."""
+    rinfo = MergeInfo(wfnc.qshape[1:], wfnc.dshape[1:])
+    lq = MergeInfo(wfnc.qshape[:1], wfnc.dshape[:1])
+    a2 = merge_rows(lq, merge_cols(wfnc, rinfo))
+    s, U, V, kept, dn = gesvd_merged(a2, M, False)
+    g = expand_rows(lq, U)
+    rmps = expand_cols(V, rinfo)
+    dimm_cols(g, s)
+    out = QSDArray()
+    gemm(NoTrans, NoTrans, 1.0, lmps, g, 1.0, out, nc=3)
+    return out, rmps
+
+
+# ----------------------------------------------------------------------------
+# a3: merged super-block operators (src/optimize.hpp:273-368)
+# ----------------------------------------------------------------------------
+
+def compute_merged_operator(forward: bool, mpo: QSDArray, hopr: QSDArray):
+    if forward:
+        m_bra = MergeInfo([hopr.qshape[0], mpo.qshape[1]], [hopr.dshape[0], mpo.dshape[1]])
+        m_ket = MergeInfo([hopr.qshape[2], mpo.qshape[2]], [hopr.dshape[2], mpo.dshape[2]])
+        # Contract(xHopr(0,1,2), xmpo(1,3,4,5)) -> (0,3,5,2,4) = [a, s, w', a', s']
+        t5 = contract(hopr, "awx", mpo, "wstv", "asvxt")
+        t4 = merge_rows(m_bra, t5)
+        return merge_cols(t4, m_ket)
+    m_bra = MergeInfo([mpo.qshape[1], hopr.qshape[0]], [mpo.dshape[1], hopr.dshape[0]])
+    m_ket = MergeInfo([mpo.qshape[2], hopr.qshape[2]], [mpo.dshape[1], hopr.dshape[0]])
+    # Contract(xmpo(0,1,2,3), xHopr(4,3,5)) -> (1,4,0,2,5) = [s, b, w, s', b']
+    t5 = contract(mpo, "wstv", hopr, "bvy", "sbwty")
+    t4 = merge_rows(m_bra, t5)
+    return merge_cols(t4, m_ket)
+
+
+def wave_merge_infos(lmpo: QSDArray, rmpo: QSDArray, lopr: QSDArray, ropr: QSDArray):
+    """Ket merge infos of ``optimize_twosite_merged`` (``src/optimize.hpp:542-551``)."""
+    q_l = [qneg(q) for q in lopr.qshape[2]]
+    q_m = [qneg(q) for q in lmpo.qshape[2]]
+    ql_info = MergeInfo([q_l, q_m], [lopr.dshape[0], lmpo.dshape[1]])
+    q_n = [qneg(q) for q in rmpo.qshape[2]]
+    q_r = [qneg(q) for q in ropr.qshape[2]]
+    qr_info = MergeInfo([q_n, q_r], [rmpo.dshape[1], ropr.dshape[0]])
+    return ql_info, qr_info
+
+
+# ----------------------------------------------------------------------------
+# a10: one bond (src/optimize.hpp:495-651), single root, one operator group
+# ----------------------------------------------------------------------------
+
+@dataclass
+class BondResult:
+    energy: float
+    n_sigma: int
+    kept: Dict[int, int]
+    davidson: DavidsonStats
+    times: Dict[str, float] = field(default_factory=dict)
+
+
+def optimize_twosite_merged(forward: bool, lmpo: QSDArray, rmpo: QSDArray, lopr: QSDArray,
+                            ropr: QSDArray, lwfn: QSDArray, rwfn: QSDArray, tole: float, M: int):
+    """Returns (BondResult, new_env, new_lwfn, new_rwfn); new_env is the renormalised
+    left (forward) or right (backward) operator."""
+    times = {}
+    t0 = time.perf_counter()
+    mL = compute_merged_operator(True, lmpo, lopr)
+    mR = compute_merged_operator(False, rmpo, ropr)
+    ql_info, qr_info = wave_merge_infos(lmpo, rmpo, lopr, ropr)
+    twf = QSDArray()
+    gemm(NoTrans, NoTrans, 1.0, lwfn, rwfn, 1.0, twf, nc=4)
+    psi = merge_cols(merge_rows(ql_info, twf), qr_info)
+    t1 = time.perf_counter()
+    times["merge"] = t1 - t0
+    diag = QSDArray(psi.q, psi.qshape, psi.dshape)
+    compute_diagonal_elements(mL, mR, diag)
+    t2 = time.perf_counter()
+    times["diag"] = t2 - t1
+
+    def multH(c, v):
+        compute_sigma_vector(mL, mR, c, v)
+
+    st = DavidsonStats()
+    energy = davidson(multH, diag, psi, tole, st)
+    t3 = time.perf_counter()
+    times["davidson"] = t3 - t2
+    U, V, kept = canonicalize_merged(forward, psi, M)
+    t4 = time.perf_counter()
+    times["svd"] = t4 - t3
+    if forward:
+        new_env = renormalize_merged(True, mL, U, U)
+    else:
+        new_env = renormalize_merged(False, mR, V, V)
+    t5 = time.perf_counter()
+    times["renorm"] = t5 - t4
+    new_l = expand_rows(ql_info, U)
+    new_r = expand_cols(V, qr_info)
+    return BondResult(energy, st.n_sigma, kept, st, times), new_env, new_l, new_r
+
+
+# ----------------------------------------------------------------------------
+# initial MPS (src/make_random_mpss.cpp:15-271) and sweeps (src/make_sweep.cpp,
+# src/dmrg.cpp:21-132)
+# ----------------------------------------------------------------------------
+
+SITE_QUANTA = [(0, 0), (1, 1), (1, -1), (2, 0)]
+
+
+def _unique_sorted_product(qa, qb):
+    return sorted({qadd(x, y) for x in qa for y in qb})
+
+
+def generate_quantum_states(nsite: int, qt, max_blocks: int):
+    """``generate_quantum_states`` (``src/make_random_mpss.cpp:15-94``)."""
+    sites = [list(SITE_QUANTA) for _ in range(nsite)]
+    qb = [None] * nsite
+    qb[0] = list(sites[0])
+    for i in range(1, nsite - 1):
+        bare = _unique_sorted_product(qb[i - 1], sites[i])
+        qb[i] = [q for q in bare if q[0] <= qt[0]]
+    qb[nsite - 1] = [tuple(qt)]
+    for i in range(nsite - 1, 0, -1):
+        qn = sites[i]
+        qr = qb[i]
+        qb[i - 1] = [ql for ql in qb[i - 1] if any(r == qadd(n, ql) for n in qn for r in qr)]
+        assert qb[i - 1]
+    for i in range(nsite - 1):
+        qn = sites[i]
+        if max_blocks > 0 and len(qb[i]) > max_blocks:
+            offs = (len(qb[i]) - max_blocks) // 2
+            qb[i] = qb[i][offs:offs + max_blocks]
+            qb[i + 1] = [r for r in qb[i + 1] if any(r == qadd(l, n) for l in qb[i] for n in qn)]
+            assert qb[i + 1]
+    return qb
+
+
+def site_tensor(ql, qr, q_total, fill=1.0) -> QSDArray:
+    qn = list(SITE_QUANTA)
+    a = QSDArray(q_total, [ql, qn, [qneg(q) for q in qr]], [[1] * len(ql), [1] * 4, [1] * len(qr)])
+    a.allocate(fill)
+    normalize(a)
+    return a
+
+
+def boundary_operator() -> QSDArray:
+    op = QSDArray(ZERO, [[ZERO]] * 3, [[1]] * 3)
+    op.allocate(1.0)
+    return op
+
+
+@dataclass
+class MPSState:
+    """In-memory sweep state: MPO sites, MPS site tensors, environments."""
+    mpo: List[QSDArray]
+    wave: List[Optional[QSDArray]]
+    lenv: List[Optional[QSDArray]]
+    renv: List[Optional[QSDArray]]
+    M: int
+
+
+def make_initial_state(mpo: List[QSDArray], n_elec: int, two_sz: int, M: int) -> MPSState:
+    """Constant-filled, normalised site tensors then backward canonicalisation and
+    right environments (``src/make_random_mpss.cpp:97-271``).  The reference fills
+    each site with one uniform draw; after normalisation only its sign survives,
+    which changes no energy, so +1 is used."""
+    N = len(mpo)
+    qt = (n_elec, two_sz)
+    qb = generate_quantum_states(N, qt, M)
+    wave: List[Optional[QSDArray]] = [None] * N
+    ql = [ZERO]
+    for i in range(N - 1):
+        wave[i] = site_tensor(ql, qb[i], ZERO)
+        ql = qb[i]
+    wave[N - 1] = site_tensor(ql, [ZERO], qt)
+    renv: List[Optional[QSDArray]] = [None] * N
+    lenv: List[Optional[QSDArray]] = [None] * N
+    renv[N - 1] = boundary_operator()
+    wfnc = wave[N - 1]
+    rmps = [None] * N
+    for i in range(N - 1, 0, -1):
+        lm, rm = canonicalize_onesite_backward(wfnc, wave[i - 1], M)
+        wfnc = lm
+        normalize(wfnc)
+        wave[i - 1] = wfnc
+        rmps[i] = rm
+        renv[i - 1] = renormalize_mpo(False, mpo[i], renv[i], rm, rm)
+    for i in range(1, N):
+        wave[i] = rmps[i]
+    lenv[0] = boundary_operator()
+    return MPSState(mpo, wave, lenv, renv, M)
+
+
+@dataclass
+class SweepLog:
+    energy: float
+    bond_energies: List[float]
+    n_sigma: int
+    seconds: float
+    times: Dict[str, float]
+
+
+def make_sweep(state: MPSState, tole: float, bond_hook=None) -> SweepLog:
+    """Forward then backward two-site sweep (``src/make_sweep.cpp:12-253``).
+
+    Davidson tolerance is 0.1*tole (``src/make_sweep.cpp:112,215``); the sweep
+    energy is the minimum over bonds."""
+    N = len(state.mpo)
+    t0 = time.perf_counter()
+    emin = 1.0e8
+    es = []
+    nsig = 0
+    times: Dict[str, float] = {}
+    wave = state.wave
+    # forward: bond (i, i+1)
+    for i in range(N - 1):
+        res, env, nl, nr = optimize_twosite_merged(True, state.mpo[i], state.mpo[i + 1], state.lenv[i],
+                                                   state.renv[i + 1], wave[i], wave[i + 1], 0.1 * tole,
+                                                   state.M)
+        if bond_hook:
+            bond_hook(True, i, res)
+        state.lenv[i + 1] = env
+        wave[i] = nl
+        wave[i + 1] = nr
+        emin = min(emin, res.energy)
+        es.append(res.energy)
+        nsig += res.n_sigma
+        for k, v in res.times.items():
+            times[k] = times.get(k, 0.0) + v
+    # backward: bond (i-1, i)
+    for i in range(N - 1, 0, -1):
+        res, env, nl, nr = optimize_twosite_merged(False, state.mpo[i - 1], state.mpo[i], state.lenv[i - 1],
+                                                   state.renv[i], wave[i - 1], wave[i], 0.1 * tole, state.M)
+        if bond_hook:
+            bond_hook(False, i - 1, res)
+        state.renv[i - 1] = env
+        wave[i - 1] = nl
+        wave[i] = nr
+        emin = min(emin, res.energy)
+        es.append(res.energy)
+        nsig += res.n_sigma
+        for k, v in res.times.items():
+            times[k] = times.get(k, 0.0) + v
+    return SweepLog(emin, es, nsig, time.perf_counter() - t0, times)
+
+
+def dmrg(mpo: List[QSDArray], n_elec: int, two_sz: int, M: int, tole: float, max_sweeps: int,
+         min_sweeps: int = 0, state: Optional[MPSState] = None, verbose: bool = False):
+    """Sweeps until |dE| < tole after at least one iteration (``src/dmrg.cpp:37-79``)."""
+    if state is None:
+        state = make_initial_state(mpo, n_elec, two_sz, M)
+    e_prev = 0.0
+    logs = []
+    for it in range(max_sweeps):
+        log = make_sweep(state, tole)
+        logs.append(log)
+        de = log.energy - e_prev
+        e_prev = log.energy
+        if verbose:
+            print(f"sweep {it}: E = {log.energy:.16f} dE = {de:.2e} ({log.seconds:.2f}s)", flush=True)
+        if it > 0 and abs(de) < tole and it + 1 >= min_sweeps:
+            break
+    return state, logs
