@@ -1,0 +1,159 @@
+/*
+ * C ABI of the GB300-native two-site DMRG hot path.
+ *
+ * Tensors are block-sparse with U(1)xU(1) (N, 2Sz) quantum numbers, the data
+ * model of the reference's btas::QSDArray<N,fermion> = QSTArray<double,N,fermion>
+ * (include/btas/QSPARSE/QSDArray.h:14-19, include/btas/QSPARSE/QSTArray.h:17-328):
+ *   - per index: a list of sectors, each with a quantum number (p, 2Sz) and a dim;
+ *   - a block with sector index (i_0..i_{N-1}) may be non-zero iff
+ *     q_total == sum_k q[k][i_k]  (QSTArray.h:34-36);
+ *   - blocks are identified by their row-major sparse tag
+ *     (include/btas/SPARSE/STArray.h:338-348) and stored packed in ascending
+ *     tag order in one device allocation, each block dense row-major.
+ *
+ * Every function returns an mpsxx_status; mpsxx_last_error() gives the message
+ * of the last failure on the calling thread (the reference throws
+ * std::runtime_error with the same texts, include/btas/common/btas.h:19-20).
+ * Functions that take a context run on its stream and return after the work
+ * has completed unless stated otherwise.
+ */
+#ifndef MPSXX_GB300_H
+#define MPSXX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mpsxx_context mpsxx_context;
+typedef struct mpsxx_tensor mpsxx_tensor;
+
+enum mpsxx_status {
+  MPSXX_OK = 0,
+  MPSXX_QSHAPE_MISMATCH = 1,
+  MPSXX_ALLOC = 2,
+  MPSXX_NO_CONVERGENCE = 3,
+  MPSXX_DEVICE_TIMEOUT = 4,
+  MPSXX_INVALID_ARGUMENT = 5,
+  MPSXX_CUDA = 6,
+  MPSXX_SOLVER = 7,
+  MPSXX_INTERNAL = 8
+};
+
+enum mpsxx_trans { MPSXX_NOTRANS = 0, MPSXX_TRANS = 1 };
+
+/* Library version (major*10000 + minor*100 + patch). */
+int mpsxx_version(void);
+/* Message of the last failure on this thread ("" if none). */
+const char* mpsxx_last_error(void);
+
+/* ---- context: one device, one stream ------------------------------------ */
+/* stream may be NULL (the context creates its own non-blocking stream). */
+int mpsxx_context_create(int device, void* stream, mpsxx_context** out);
+int mpsxx_context_destroy(mpsxx_context* ctx);
+int mpsxx_context_sync(mpsxx_context* ctx);
+/* Kernel launches issued, FP64-equivalent sigma FLOPs and sigma calls so far. */
+int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* sigma_flops, int64_t* sigma_calls);
+
+/* ---- tensors ------------------------------------------------------------- */
+/* Create a block-sparse tensor.  qn holds 2*sum(nsec) ints (p, 2Sz per sector,
+ * index by index), dims holds sum(nsec) ints.  nblocks < 0 allocates every
+ * allowed block of non-zero size (STArray.h:219-237); otherwise tags lists the
+ * stored blocks in ascending order.  ctx == NULL gives a host-only descriptor
+ * (no device storage) usable by the planner.  Device storage is zero-filled. */
+int mpsxx_tensor_create(mpsxx_context* ctx, int rank, const int* q, const int* nsec, const int* qn, const int* dims,
+                        int64_t nblocks, const int64_t* tags, mpsxx_tensor** out);
+/* Same shape and block layout as `like`, zero-filled. */
+int mpsxx_tensor_create_like(mpsxx_context* ctx, const mpsxx_tensor* like, mpsxx_tensor** out);
+int mpsxx_tensor_destroy(mpsxx_tensor* t);
+int mpsxx_tensor_info(const mpsxx_tensor* t, int* rank, int* q, int64_t* nblocks, int64_t* nnz);
+/* nsec[rank], qn[2*sum nsec], dims[sum nsec] (caller-sized, see mpsxx_tensor_info). */
+int mpsxx_tensor_shape(const mpsxx_tensor* t, int* nsec, int* qn, int* dims);
+int mpsxx_tensor_blocks(const mpsxx_tensor* t, int64_t* tags, int64_t* offsets);
+/* Host <-> device copies of all nnz elements (block-packed order). */
+int mpsxx_tensor_upload(mpsxx_tensor* t, const double* host);
+int mpsxx_tensor_download(const mpsxx_tensor* t, double* host);
+int mpsxx_tensor_device_ptr(const mpsxx_tensor* t, double** out);
+
+/* ---- planner (host only) --------------------------------------------------- */
+/* Block-task enumeration of btas::Gemm (include/btas/QSPARSE/QSTBLAS.h:182-226,
+ * include/btas/SPARSE/STBLAS.h:297-359) for c = op(a) op(b) with c of rank c_rank.
+ * Call with c_tags == NULL to get ntasks/npairs; then with arrays of those sizes:
+ * c_tags[ntasks], pair_ptr[ntasks+1], a_tags[npairs], b_tags[npairs] (original,
+ * un-viewed tags), in the reference's enumeration order. */
+int mpsxx_gemm_tasks(int transa, int transb, const mpsxx_tensor* a, const mpsxx_tensor* b, int c_rank,
+                     int64_t* ntasks, int64_t* npairs, int64_t* c_tags, int64_t* pair_ptr, int64_t* a_tags,
+                     int64_t* b_tags);
+
+/* ---- hot path ------------------------------------------------------------- */
+/* sgv += H_eff * wfn for merged two-site operators:
+ * sgv[A,B] += sum_{w,A',B'} lopr[A,w,A'] wfn[A',B'] ropr[B,w,B']
+ * Replaces mpsxx::compute_sigma_vector(lopr, ropr, wfn0, sgv0)
+ * (src/compute_sigma_vector.hpp:85-96).  sgv must have wfn's block layout. */
+int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                               const mpsxx_tensor* wfn, mpsxx_tensor* sgv);
+
+/* diag[A,B] += sum_w lopr[A,w,A] ropr[B,w,B] on diag's blocks.
+ * Replaces mpsxx::compute_diagonal_elements(lopr, ropr, diag)
+ * (src/compute_diagonal_elements.hpp:65-80). */
+int mpsxx_compute_diagonal_elements(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                                    mpsxx_tensor* diag);
+
+/* opr1 = bra^T opr0 ket (forward) or bra opr0 ket^T (backward), allocated by the callee.
+ * Replaces mpsxx::renormalize(forward, opr0, bra0, ket0, opr1) for merged operators
+ * (src/renormalize.hpp:57-95). */
+int mpsxx_renormalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* opr0, const mpsxx_tensor* bra,
+                      const mpsxx_tensor* ket, mpsxx_tensor** opr1);
+
+/* Merged super-block operator of one MPO site and one block operator.
+ * Replaces the per-group body of mpsxx::compute_merged_operator
+ * (src/optimize.hpp:273-368).  mpo must have been uploaded from the host. */
+int mpsxx_compute_merged_operator(mpsxx_context* ctx, int forward, const mpsxx_tensor* mpo,
+                                  const mpsxx_tensor* opr, mpsxx_tensor** out);
+
+/* Davidson lowest eigenpair of H_eff = (lopr, ropr) starting from wfnc (overwritten).
+ * Replaces mpsxx::Davidson::diagonalize (src/diagonalize.hpp:310-449) for one root.
+ * stats (may be NULL): [n_sigma, macro, micro, converged]. */
+int mpsxx_diagonalize(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                      const mpsxx_tensor* diag, mpsxx_tensor* wfnc, double tol, double* energy, int* stats);
+
+/* Truncated SVD of a merged wavefunction; forward: lmat = U, rmat = s V^T;
+ * backward: lmat = U s, rmat = V^T.  Replaces mpsxx::canonicalize(forward, wfnc,
+ * lmat, rmat, M, noise) (src/canonicalize.hpp:88-106).  noise must be < 1e-8. */
+int mpsxx_canonicalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* wfnc, int M, double noise,
+                       mpsxx_tensor** lmat, mpsxx_tensor** rmat);
+
+/* One bond of the two-site sweep (src/optimize.hpp:495-651), single root and one
+ * operator group: returns the Ritz value, the renormalised operator of the grown
+ * block and the new site tensors.  stats (may be NULL, 8 doubles): n_sigma,
+ * sigma FLOPs, t_merge, t_diag, t_davidson, t_svd, t_renorm, converged. */
+int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_tensor* lmpo,
+                                  const mpsxx_tensor* rmpo, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                                  const mpsxx_tensor* lwfn, const mpsxx_tensor* rwfn, double tole, int M,
+                                  double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
+                                  mpsxx_tensor** new_rwfn, double* stats);
+
+/* Merge the last two indices of a 3-index site tensor in place of the
+ * reference's QSTmerge(a, cols_info, b) (include/btas/QSPARSE/QSTmerge.h:85-140). */
+int mpsxx_merge_cols(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** out);
+
+/* c = alpha * op(a) op(b) into a new tensor of rank c_rank whose blocks are the
+ * enumerated task results (btas::Gemm into an empty array,
+ * include/btas/QSPARSE/QSTBLAS.h:182-226). */
+int mpsxx_gemm(mpsxx_context* ctx, int transa, int transb, double alpha, const mpsxx_tensor* a,
+               const mpsxx_tensor* b, int c_rank, mpsxx_tensor** c);
+
+/* Expand the last index of b into the last two indices of `like` (a 3-index
+ * tensor whose trailing index shapes define the merge), the reference's
+ * QSTexpand(b, cols_info, a) (include/btas/QSPARSE/QSTmerge.h:297-372). */
+int mpsxx_expand_cols(mpsxx_context* ctx, const mpsxx_tensor* b, const mpsxx_tensor* like, mpsxx_tensor** out);
+
+/* x /= ||x||_2 (btas::Normalize, include/btas/QSPARSE/QSTBLAS.h:239-243); norm may be NULL. */
+int mpsxx_normalize(mpsxx_context* ctx, mpsxx_tensor* x, double* norm);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPSXX_GB300_H */

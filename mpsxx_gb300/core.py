@@ -1,0 +1,309 @@
+"""Python mirror of the reference's hot-path call surface over the C ABI.
+
+``Tensor`` is a device-resident block-sparse QSDArray (see include/mpsxx_gb300.h
+for the layout); the free functions keep the reference's names and argument
+meaning (src/compute_sigma_vector.hpp, src/renormalize.hpp,
+src/compute_diagonal_elements.hpp, src/diagonalize.hpp, src/canonicalize.hpp,
+src/optimize.hpp).  Errors raise ``MpsxxError`` carrying the C status code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from ._lib import check, lib
+
+Q = Tuple[int, int]
+
+
+def _i32(a) -> C.Array:
+    arr = (C.c_int * max(1, len(a)))(*[int(x) for x in a])
+    return arr
+
+
+class Context:
+    """One device and one CUDA stream (``stream`` is a raw cudaStream_t or None)."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None):
+        h = C.c_void_p()
+        check(lib().mpsxx_context_create(int(device), C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+
+    def sync(self):
+        check(lib().mpsxx_context_sync(self.h))
+
+    def counters(self):
+        la = C.c_int64()
+        fl = C.c_double()
+        ca = C.c_int64()
+        check(lib().mpsxx_context_counters(self.h, C.byref(la), C.byref(fl), C.byref(ca)))
+        return {"launches": la.value, "sigma_flops": fl.value, "sigma_calls": ca.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mpsxx_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Tensor:
+    """Block-sparse quantum-number tensor held by the library (device or host-only)."""
+
+    def __init__(self, handle: C.c_void_p, ctx: Optional[Context]):
+        self.h = handle
+        self.ctx = ctx  # keeps the context alive
+
+    # -- construction ---------------------------------------------------------
+    @classmethod
+    def create(cls, ctx: Optional[Context], q: Q, qshape: Sequence[Sequence[Q]], dshape: Sequence[Sequence[int]],
+               tags: Optional[Sequence[int]] = None) -> "Tensor":
+        rank = len(qshape)
+        nsec = [len(x) for x in qshape]
+        qn = [v for x in qshape for qq in x for v in qq]
+        dims = [d for x in dshape for d in x]
+        h = C.c_void_p()
+        if tags is None:
+            nb, tg = -1, None
+        else:
+            tl = [int(t) for t in tags]
+            nb = len(tl)
+            tg = (C.c_int64 * max(1, nb))(*tl)
+        check(lib().mpsxx_tensor_create(ctx.h if ctx else None, rank, _i32(q), _i32(nsec), _i32(qn), _i32(dims),
+                                        nb, tg, C.byref(h)))
+        return cls(h, ctx)
+
+    @classmethod
+    def from_dict(cls, ctx: Optional[Context], d: dict) -> "Tensor":
+        """From the neutral exchange dict {"q","qshape","dshape","blocks": {tag: ndarray}}."""
+        tags = sorted(int(t) for t in d["blocks"])
+        t = cls.create(ctx, tuple(d["q"]), d["qshape"], d["dshape"], tags)
+        t.upload_blocks(d["blocks"])
+        return t
+
+    def like(self) -> "Tensor":
+        h = C.c_void_p()
+        check(lib().mpsxx_tensor_create_like(self.ctx.h, self.h, C.byref(h)))
+        return Tensor(h, self.ctx)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().mpsxx_tensor_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    # -- inspection -------------------------------------------------------------
+    def info(self):
+        r = C.c_int()
+        q = (C.c_int * 2)()
+        nb = C.c_int64()
+        nnz = C.c_int64()
+        check(lib().mpsxx_tensor_info(self.h, C.byref(r), q, C.byref(nb), C.byref(nnz)))
+        return r.value, (q[0], q[1]), nb.value, nnz.value
+
+    @property
+    def rank(self) -> int:
+        return self.info()[0]
+
+    @property
+    def q(self) -> Q:
+        return self.info()[1]
+
+    @property
+    def nnz(self) -> int:
+        return self.info()[3]
+
+    def shape(self):
+        rank, _, _, _ = self.info()
+        nsec = (C.c_int * rank)()
+        check(lib().mpsxx_tensor_shape(self.h, nsec, None, None))
+        tot = sum(nsec)
+        qn = (C.c_int * max(1, 2 * tot))()
+        dims = (C.c_int * max(1, tot))()
+        check(lib().mpsxx_tensor_shape(self.h, nsec, qn, dims))
+        qshape, dshape, pos = [], [], 0
+        for i in range(rank):
+            qshape.append([(qn[2 * (pos + j)], qn[2 * (pos + j) + 1]) for j in range(nsec[i])])
+            dshape.append([dims[pos + j] for j in range(nsec[i])])
+            pos += nsec[i]
+        return qshape, dshape
+
+    def blocks(self):
+        _, _, nb, _ = self.info()
+        tags = np.zeros(max(1, nb), dtype=np.int64)
+        offs = np.zeros(max(1, nb), dtype=np.int64)
+        check(lib().mpsxx_tensor_blocks(self.h, tags.ctypes.data_as(C.POINTER(C.c_int64)),
+                                        offs.ctypes.data_as(C.POINTER(C.c_int64))))
+        return tags[:nb], offs[:nb]
+
+    def device_ptr(self) -> int:
+        p = C.POINTER(C.c_double)()
+        check(lib().mpsxx_tensor_device_ptr(self.h, C.byref(p)))
+        return C.cast(p, C.c_void_p).value or 0
+
+    # -- data -------------------------------------------------------------------
+    def upload(self, flat: np.ndarray):
+        a = np.ascontiguousarray(flat, dtype=np.float64)
+        if a.size != self.nnz:
+            raise ValueError("upload: size does not match the tensor's nnz")
+        check(lib().mpsxx_tensor_upload(self.h, a.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def download(self) -> np.ndarray:
+        out = np.zeros(max(1, self.nnz), dtype=np.float64)
+        check(lib().mpsxx_tensor_download(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out[: self.nnz]
+
+    def _strides(self, qshape):
+        n = [len(x) for x in qshape]
+        st = [1] * len(n)
+        for i in range(len(n) - 2, -1, -1):
+            st[i] = st[i + 1] * n[i + 1]
+        return st
+
+    def block_dims(self, tag: int, qshape=None, dshape=None):
+        if qshape is None:
+            qshape, dshape = self.shape()
+        st = self._strides(qshape)
+        idx = []
+        for s in st:
+            idx.append(tag // s)
+            tag %= s
+        return tuple(dshape[i][k] for i, k in enumerate(idx))
+
+    def upload_blocks(self, blocks: Dict[int, np.ndarray]):
+        qshape, dshape = self.shape()
+        tags, offs = self.blocks()
+        flat = np.zeros(self.nnz)
+        for t, o in zip(tags, offs):
+            b = blocks.get(int(t))
+            if b is None:
+                continue
+            dims = self.block_dims(int(t), qshape, dshape)
+            n = int(np.prod(dims))
+            flat[o:o + n] = np.asarray(b, dtype=np.float64).reshape(-1)
+        self.upload(flat)
+
+    def to_blocks(self) -> Dict[int, np.ndarray]:
+        qshape, dshape = self.shape()
+        tags, offs = self.blocks()
+        flat = self.download()
+        out = {}
+        for t, o in zip(tags, offs):
+            dims = self.block_dims(int(t), qshape, dshape)
+            n = int(np.prod(dims))
+            out[int(t)] = flat[o:o + n].reshape(dims).copy()
+        return out
+
+    def to_dict(self) -> dict:
+        qshape, dshape = self.shape()
+        return {"q": self.q, "qshape": qshape, "dshape": dshape, "blocks": self.to_blocks()}
+
+
+def _out():
+    return C.c_void_p()
+
+
+# ---------------------------------------------------------------------------
+# planner
+# ---------------------------------------------------------------------------
+
+def gemm_tasks(transa: int, transb: int, a: Tensor, b: Tensor, c_rank: int):
+    """Reference block-task list [(c_tag, [(a_tag, b_tag), ...]), ...] (host only)."""
+    nt = C.c_int64()
+    npr = C.c_int64()
+    check(lib().mpsxx_gemm_tasks(transa, transb, a.h, b.h, c_rank, C.byref(nt), C.byref(npr), None, None, None, None))
+    ct = np.zeros(max(1, nt.value), dtype=np.int64)
+    pp = np.zeros(nt.value + 1, dtype=np.int64)
+    at = np.zeros(max(1, npr.value), dtype=np.int64)
+    bt = np.zeros(max(1, npr.value), dtype=np.int64)
+    P = C.POINTER(C.c_int64)
+    check(lib().mpsxx_gemm_tasks(transa, transb, a.h, b.h, c_rank, C.byref(nt), C.byref(npr), ct.ctypes.data_as(P),
+                                 pp.ctypes.data_as(P), at.ctypes.data_as(P), bt.ctypes.data_as(P)))
+    tasks = []
+    for i in range(nt.value):
+        tasks.append((int(ct[i]), [(int(at[p]), int(bt[p])) for p in range(pp[i], pp[i + 1])]))
+    return tasks
+
+
+# ---------------------------------------------------------------------------
+# hot path (reference names)
+# ---------------------------------------------------------------------------
+
+def compute_sigma_vector(ctx: Context, lopr: Tensor, ropr: Tensor, wfn: Tensor, sgv: Tensor):
+    check(lib().mpsxx_compute_sigma_vector(ctx.h, lopr.h, ropr.h, wfn.h, sgv.h))
+
+
+def compute_diagonal_elements(ctx: Context, lopr: Tensor, ropr: Tensor, diag: Tensor):
+    check(lib().mpsxx_compute_diagonal_elements(ctx.h, lopr.h, ropr.h, diag.h))
+
+
+def renormalize(ctx: Context, forward: bool, opr0: Tensor, bra: Tensor, ket: Tensor) -> Tensor:
+    o = _out()
+    check(lib().mpsxx_renormalize(ctx.h, int(bool(forward)), opr0.h, bra.h, ket.h, C.byref(o)))
+    return Tensor(o, ctx)
+
+
+def compute_merged_operator(ctx: Context, forward: bool, mpo: Tensor, opr: Tensor) -> Tensor:
+    o = _out()
+    check(lib().mpsxx_compute_merged_operator(ctx.h, int(bool(forward)), mpo.h, opr.h, C.byref(o)))
+    return Tensor(o, ctx)
+
+
+def diagonalize(ctx: Context, lopr: Tensor, ropr: Tensor, diag: Tensor, wfnc: Tensor, tol: float = 1e-8):
+    e = C.c_double()
+    st = (C.c_int * 4)()
+    check(lib().mpsxx_diagonalize(ctx.h, lopr.h, ropr.h, diag.h, wfnc.h, float(tol), C.byref(e), st))
+    return e.value, {"n_sigma": st[0], "macro": st[1], "micro": st[2], "converged": st[3]}
+
+
+def canonicalize(ctx: Context, forward: bool, wfnc: Tensor, M: int = 0, noise: float = 0.0):
+    lo, ro = _out(), _out()
+    check(lib().mpsxx_canonicalize(ctx.h, int(bool(forward)), wfnc.h, int(M), float(noise), C.byref(lo), C.byref(ro)))
+    return Tensor(lo, ctx), Tensor(ro, ctx)
+
+
+def gemm(ctx: Context, transa: int, transb: int, alpha: float, a: Tensor, b: Tensor, c_rank: int) -> Tensor:
+    o = _out()
+    check(lib().mpsxx_gemm(ctx.h, transa, transb, float(alpha), a.h, b.h, int(c_rank), C.byref(o)))
+    return Tensor(o, ctx)
+
+
+def merge_cols(ctx: Context, a: Tensor) -> Tensor:
+    o = _out()
+    check(lib().mpsxx_merge_cols(ctx.h, a.h, C.byref(o)))
+    return Tensor(o, ctx)
+
+
+def expand_cols(ctx: Context, b: Tensor, like: Tensor) -> Tensor:
+    o = _out()
+    check(lib().mpsxx_expand_cols(ctx.h, b.h, like.h, C.byref(o)))
+    return Tensor(o, ctx)
+
+
+def normalize(ctx: Context, x: Tensor) -> float:
+    n = C.c_double()
+    check(lib().mpsxx_normalize(ctx.h, x.h, C.byref(n)))
+    return n.value
+
+
+BOND_STAT_KEYS = ("n_sigma", "sigma_flops", "t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "converged")
+
+
+def optimize_twosite_merged(ctx: Context, forward: bool, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor,
+                            lwfn: Tensor, rwfn: Tensor, tole: float, M: int):
+    e = C.c_double()
+    env, nl, nr = _out(), _out(), _out()
+    st = (C.c_double * 8)()
+    check(lib().mpsxx_optimize_twosite_merged(ctx.h, int(bool(forward)), lmpo.h, rmpo.h, lopr.h, ropr.h, lwfn.h,
+                                              rwfn.h, float(tole), int(M), C.byref(e), C.byref(env), C.byref(nl),
+                                              C.byref(nr), st))
+    stats = dict(zip(BOND_STAT_KEYS, list(st)))
+    return e.value, Tensor(env, ctx), Tensor(nl, ctx), Tensor(nr, ctx), stats

@@ -1,0 +1,417 @@
+// extern "C" boundary of libmpsxx_gb300 (declared in include/mpsxx_gb300.h).
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+
+#include "../../include/mpsxx_gb300.h"
+#include "engine.hpp"
+
+using namespace mpsxx;
+
+struct mpsxx_context {
+  std::unique_ptr<Context> ctx;
+};
+struct mpsxx_tensor {
+  std::unique_ptr<DTensor> t;
+  mpsxx_context* owner = nullptr;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+template <class F>
+int guard(F&& f) {
+  try {
+    g_last_error.clear();
+    f();
+    return MPSXX_OK;
+  } catch (const Error& e) {
+    return fail(e.code, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(MPSXX_ALLOC, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(MPSXX_INTERNAL, e.what());
+  }
+}
+
+void need(bool c, const char* msg) {
+  if (!c) throw Error(kInvalidArgument, msg);
+}
+
+Context& ctx_of(mpsxx_context* c) {
+  need(c && c->ctx, "null context");
+  return *c->ctx;
+}
+
+const DTensor& ten(const mpsxx_tensor* t) {
+  need(t && t->t, "null tensor");
+  return *t->t;
+}
+
+DTensor& ten_mut(mpsxx_tensor* t) {
+  need(t && t->t, "null tensor");
+  return *t->t;
+}
+
+void need_device(const DTensor& t) { need(t.d != nullptr || t.nnz == 0, "tensor has no device storage"); }
+
+mpsxx_tensor* wrap(std::unique_ptr<DTensor> t, mpsxx_context* owner) {
+  auto* w = new mpsxx_tensor;
+  w->t = std::move(t);
+  w->owner = owner;
+  return w;
+}
+}  // namespace
+
+extern "C" {
+
+int mpsxx_version(void) { return 100; }
+
+const char* mpsxx_last_error(void) { return g_last_error.c_str(); }
+
+int mpsxx_context_create(int device, void* stream, mpsxx_context** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    auto* c = new mpsxx_context;
+    try {
+      c->ctx = std::make_unique<Context>(device, static_cast<cudaStream_t>(stream));
+    } catch (...) {
+      delete c;
+      throw;
+    }
+    *out = c;
+  });
+}
+
+int mpsxx_context_destroy(mpsxx_context* ctx) {
+  return guard([&] { delete ctx; });
+}
+
+int mpsxx_context_sync(mpsxx_context* ctx) {
+  return guard([&] { ctx_of(ctx).sync(); });
+}
+
+int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* sigma_flops, int64_t* sigma_calls) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    if (launches) *launches = ctx->ctx->kernel_launches;
+    if (sigma_flops) *sigma_flops = ctx->ctx->sigma_flops;
+    if (sigma_calls) *sigma_calls = ctx->ctx->sigma_calls;
+  });
+}
+
+int mpsxx_tensor_create(mpsxx_context* ctx, int rank, const int* q, const int* nsec, const int* qn, const int* dims,
+                        int64_t nblocks, const int64_t* tags, mpsxx_tensor** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    need(rank >= 1 && rank <= kMaxRank, "tensor rank out of range");
+    need(q && nsec && qn && dims, "null shape argument");
+    auto t = std::make_unique<DTensor>();
+    t->sh.rank = rank;
+    t->sh.q = Qn{q[0], q[1]};
+    int pos = 0;
+    for (int i = 0; i < rank; ++i) {
+      need(nsec[i] >= 0, "negative sector count");
+      std::vector<Qn> qs;
+      std::vector<int> ds;
+      for (int j = 0; j < nsec[i]; ++j, ++pos) {
+        qs.push_back(Qn{qn[2 * pos], qn[2 * pos + 1]});
+        need(dims[pos] >= 0, "negative sector dimension");
+        ds.push_back(dims[pos]);
+      }
+      t->sh.qshape.push_back(qs);
+      t->sh.dshape.push_back(ds);
+    }
+    t->sh.finalize();
+    if (nblocks < 0) {
+      t->allocate_allowed();
+    } else {
+      need(nblocks == 0 || tags != nullptr, "null tags");
+      t->set_blocks(std::vector<int64_t>(tags, tags + nblocks));
+    }
+    if (ctx) {
+      Context& c = ctx_of(ctx);
+      t->ctx = &c;
+      t->alloc_device(c.stream, true);
+      c.sync();
+    }
+    *out = wrap(std::move(t), ctx);
+  });
+}
+
+int mpsxx_tensor_create_like(mpsxx_context* ctx, const mpsxx_tensor* like, mpsxx_tensor** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    const DTensor& l = ten(like);
+    Context& c = ctx_of(ctx);
+    auto t = std::make_unique<DTensor>();
+    static_cast<Tensor&>(*t) = static_cast<const Tensor&>(l);
+    t->d = nullptr;
+    t->own = false;
+    t->ctx = &c;
+    t->alloc_device(c.stream, true);
+    c.sync();
+    *out = wrap(std::move(t), ctx);
+  });
+}
+
+int mpsxx_tensor_destroy(mpsxx_tensor* t) {
+  return guard([&] { delete t; });
+}
+
+int mpsxx_tensor_info(const mpsxx_tensor* t, int* rank, int* q, int64_t* nblocks, int64_t* nnz) {
+  return guard([&] {
+    const DTensor& x = ten(t);
+    if (rank) *rank = x.sh.rank;
+    if (q) {
+      q[0] = x.sh.q.p;
+      q[1] = x.sh.q.s;
+    }
+    if (nblocks) *nblocks = static_cast<int64_t>(x.tags.size());
+    if (nnz) *nnz = x.nnz;
+  });
+}
+
+int mpsxx_tensor_shape(const mpsxx_tensor* t, int* nsec, int* qn, int* dims) {
+  return guard([&] {
+    const DTensor& x = ten(t);
+    int pos = 0;
+    for (int i = 0; i < x.sh.rank; ++i) {
+      if (nsec) nsec[i] = x.sh.nsec(i);
+      for (int j = 0; j < x.sh.nsec(i); ++j, ++pos) {
+        if (qn) {
+          qn[2 * pos] = x.sh.qshape[i][j].p;
+          qn[2 * pos + 1] = x.sh.qshape[i][j].s;
+        }
+        if (dims) dims[pos] = x.sh.dshape[i][j];
+      }
+    }
+  });
+}
+
+int mpsxx_tensor_blocks(const mpsxx_tensor* t, int64_t* tags, int64_t* offsets) {
+  return guard([&] {
+    const DTensor& x = ten(t);
+    for (size_t b = 0; b < x.tags.size(); ++b) {
+      if (tags) tags[b] = x.tags[b];
+      if (offsets) offsets[b] = x.offsets[b];
+    }
+  });
+}
+
+int mpsxx_tensor_upload(mpsxx_tensor* t, const double* host) {
+  return guard([&] {
+    DTensor& x = ten_mut(t);
+    need(host != nullptr || x.nnz == 0, "null host buffer");
+    x.host.assign(host, host + x.nnz);
+    if (x.ctx) {
+      need_device(x);
+      if (x.nnz)
+        cuda_check(cudaMemcpyAsync(x.d, host, x.nnz * sizeof(double), cudaMemcpyHostToDevice, x.ctx->stream), "upload");
+      x.ctx->sync();
+    }
+  });
+}
+
+int mpsxx_tensor_download(const mpsxx_tensor* t, double* host) {
+  return guard([&] {
+    const DTensor& x = ten(t);
+    need(host != nullptr || x.nnz == 0, "null host buffer");
+    if (!x.ctx) {
+      need(static_cast<int64_t>(x.host.size()) == x.nnz, "host-only tensor has no data");
+      std::memcpy(host, x.host.data(), x.nnz * sizeof(double));
+      return;
+    }
+    if (x.nnz)
+      cuda_check(cudaMemcpyAsync(host, x.d, x.nnz * sizeof(double), cudaMemcpyDeviceToHost, x.ctx->stream), "download");
+    x.ctx->sync();
+  });
+}
+
+int mpsxx_tensor_device_ptr(const mpsxx_tensor* t, double** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    *out = ten(t).d;
+  });
+}
+
+int mpsxx_gemm_tasks(int transa, int transb, const mpsxx_tensor* a, const mpsxx_tensor* b, int c_rank,
+                     int64_t* ntasks, int64_t* npairs, int64_t* c_tags, int64_t* pair_ptr, int64_t* a_tags,
+                     int64_t* b_tags) {
+  return guard([&] {
+    const DTensor& A = ten(a);
+    const DTensor& B = ten(b);
+    int K = 0;
+    const Trans ta = transa ? kTrans : kNoTrans, tb = transb ? kTrans : kNoTrans;
+    Shape c = gemm_result_shape(ta, tb, A.sh, B.sh, c_rank, &K);
+    auto tasks = enumerate_gemm(ta, tb, A, B, c, K);
+    int64_t np = 0;
+    for (const auto& t : tasks) np += static_cast<int64_t>(t.pairs.size());
+    if (ntasks) *ntasks = static_cast<int64_t>(tasks.size());
+    if (npairs) *npairs = np;
+    if (!c_tags) return;
+    need(pair_ptr && a_tags && b_tags, "null output arrays");
+    int64_t p = 0;
+    for (size_t i = 0; i < tasks.size(); ++i) {
+      c_tags[i] = tasks[i].c_tag;
+      pair_ptr[i] = p;
+      for (const auto& pr : tasks[i].pairs) {
+        a_tags[p] = pr.a_tag;
+        b_tags[p] = pr.b_tag;
+        ++p;
+      }
+    }
+    pair_ptr[tasks.size()] = p;
+  });
+}
+
+int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                               const mpsxx_tensor* wfn, mpsxx_tensor* sgv) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    const DTensor &L = ten(lopr), &R = ten(ropr), &P = ten(wfn);
+    DTensor& S = ten_mut(sgv);
+    need_device(L);
+    need_device(R);
+    need_device(P);
+    need_device(S);
+    compute_sigma_vector(c, L, R, P, S);
+    c.sync();
+  });
+}
+
+int mpsxx_compute_diagonal_elements(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                                    mpsxx_tensor* diag) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    const DTensor &L = ten(lopr), &R = ten(ropr);
+    DTensor& D = ten_mut(diag);
+    need_device(L);
+    need_device(R);
+    need_device(D);
+    compute_diagonal_elements(c, L, R, D);
+    c.sync();
+  });
+}
+
+int mpsxx_renormalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* opr0, const mpsxx_tensor* bra,
+                      const mpsxx_tensor* ket, mpsxx_tensor** opr1) {
+  return guard([&] {
+    need(opr1 != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    auto r = renormalize(c, forward != 0, ten(opr0), ten(bra), ten(ket));
+    *opr1 = wrap(std::move(r), ctx);
+  });
+}
+
+int mpsxx_compute_merged_operator(mpsxx_context* ctx, int forward, const mpsxx_tensor* mpo,
+                                  const mpsxx_tensor* opr, mpsxx_tensor** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    auto r = compute_merged_operator(c, forward != 0, ten(mpo), ten(opr));
+    *out = wrap(std::move(r), ctx);
+  });
+}
+
+int mpsxx_diagonalize(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                      const mpsxx_tensor* diag, mpsxx_tensor* wfnc, double tol, double* energy, int* stats) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    DavidsonStats st;
+    const double e = diagonalize(c, ten(lopr), ten(ropr), ten(diag), ten_mut(wfnc), tol, &st);
+    if (energy) *energy = e;
+    if (stats) {
+      stats[0] = st.n_sigma;
+      stats[1] = st.macro;
+      stats[2] = st.micro;
+      stats[3] = st.converged;
+    }
+  });
+}
+
+int mpsxx_canonicalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* wfnc, int M, double noise,
+                       mpsxx_tensor** lmat, mpsxx_tensor** rmat) {
+  return guard([&] {
+    need(lmat && rmat, "null output");
+    Context& c = ctx_of(ctx);
+    CanonResult r = canonicalize(c, forward != 0, ten(wfnc), M, noise);
+    *lmat = wrap(std::move(r.lmat), ctx);
+    *rmat = wrap(std::move(r.rmat), ctx);
+  });
+}
+
+int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_tensor* lmpo,
+                                  const mpsxx_tensor* rmpo, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                                  const mpsxx_tensor* lwfn, const mpsxx_tensor* rwfn, double tole, int M,
+                                  double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
+                                  mpsxx_tensor** new_rwfn, double* stats) {
+  return guard([&] {
+    need(env && new_lwfn && new_rwfn, "null output");
+    Context& c = ctx_of(ctx);
+    BondOut b = optimize_twosite_merged(c, forward != 0, ten(lmpo), ten(rmpo), ten(lopr), ten(ropr), ten(lwfn),
+                                        ten(rwfn), tole, M);
+    if (energy) *energy = b.stats.energy;
+    if (stats) {
+      stats[0] = b.stats.dav.n_sigma;
+      stats[1] = b.stats.sigma_flops;
+      stats[2] = b.stats.t_merge;
+      stats[3] = b.stats.t_diag;
+      stats[4] = b.stats.t_davidson;
+      stats[5] = b.stats.t_svd;
+      stats[6] = b.stats.t_renorm;
+      stats[7] = b.stats.dav.converged;
+    }
+    *env = wrap(std::move(b.env), ctx);
+    *new_lwfn = wrap(std::move(b.lwfn), ctx);
+    *new_rwfn = wrap(std::move(b.rwfn), ctx);
+  });
+}
+
+int mpsxx_merge_cols(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    const DTensor& A = ten(a);
+    need(A.sh.rank == 3, "merge_cols: expects a 3-index tensor");
+    MergeInfo info({A.sh.qshape[1], A.sh.qshape[2]}, {A.sh.dshape[1], A.sh.dshape[2]});
+    *out = wrap(merge_cols(c, A, info), ctx);
+  });
+}
+
+int mpsxx_gemm(mpsxx_context* ctx, int transa, int transb, double alpha, const mpsxx_tensor* a,
+               const mpsxx_tensor* b, int c_rank, mpsxx_tensor** c) {
+  return guard([&] {
+    need(c != nullptr, "null output");
+    Context& cx = ctx_of(ctx);
+    *c = wrap(gemm_new(cx, transa ? kTrans : kNoTrans, transb ? kTrans : kNoTrans, alpha, ten(a), ten(b), c_rank),
+              ctx);
+  });
+}
+
+int mpsxx_expand_cols(mpsxx_context* ctx, const mpsxx_tensor* b, const mpsxx_tensor* like, mpsxx_tensor** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    const DTensor& L = ten(like);
+    need(L.sh.rank == 3, "expand_cols: `like` must be a 3-index tensor");
+    MergeInfo info({L.sh.qshape[1], L.sh.qshape[2]}, {L.sh.dshape[1], L.sh.dshape[2]});
+    *out = wrap(expand_cols(c, ten(b), info), ctx);
+  });
+}
+
+int mpsxx_normalize(mpsxx_context* ctx, mpsxx_tensor* x, double* norm) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    const double n = normalize_tensor(c, ten_mut(x));
+    if (norm) *norm = n;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,1140 @@
+// Device engine of the merged two-site DMRG hot path: plans built once per
+// layout on the host, executed by the sm_103a kernels.
+#include "engine.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "jacobi.hpp"
+
+namespace mpsxx {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw Error(kCuda, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+static void solver_check(cusolverStatus_t s, const char* what) {
+  if (s != CUSOLVER_STATUS_SUCCESS) throw Error(kSolver, std::string(what) + ": cusolver status " + std::to_string(s));
+}
+
+void DevBuf::ensure(size_t bytes) {
+  if (bytes <= cap) return;
+  release();
+  const size_t nb = std::max<size_t>(bytes, 256);
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, nb);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(kAlloc, std::string("device allocation of ") + std::to_string(nb) + " bytes failed: " +
+                            cudaGetErrorString(e));
+  }
+  p = q;
+  cap = nb;
+}
+
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+}
+
+template <class T>
+void DevArray<T>::upload(const std::vector<T>& h, cudaStream_t st) {
+  n = h.size();
+  buf.ensure(std::max<size_t>(1, n) * sizeof(T));
+  if (n) cuda_check(cudaMemcpyAsync(buf.p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice, st), "plan upload");
+}
+template struct DevArray<DTile>;
+template struct DevArray<DGemmTask>;
+template struct DevArray<DGemmPair>;
+template struct DevArray<DDiagTask>;
+template struct DevArray<DDiagPair>;
+template struct DevArray<DCopy>;
+template struct DevArray<DScatterDst>;
+template struct DevArray<DScatterSrc>;
+template struct DevArray<double>;
+template struct DevArray<int64_t>;
+template struct DevArray<int>;
+
+void DTensor::alloc_device(cudaStream_t st, bool zero) {
+  store.ensure(std::max<int64_t>(nnz, 1) * sizeof(double));
+  d = store.as<double>();
+  if (zero && nnz) cuda_check(cudaMemsetAsync(d, 0, nnz * sizeof(double), st), "tensor zero");
+}
+
+Context::Context(int dev, cudaStream_t st) : device(dev) {
+  cuda_check(cudaSetDevice(dev), "cudaSetDevice");
+  if (st) {
+    stream = st;
+  } else {
+    cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream create");
+    own_stream = true;
+  }
+  solver_check(cusolverDnCreate(&solver), "cusolverDnCreate");
+  solver_check(cusolverDnSetStream(solver, stream), "cusolverDnSetStream");
+}
+
+Context::~Context() {
+  if (solver) cusolverDnDestroy(solver);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+void Context::sync() { cuda_check(cudaStreamSynchronize(stream), "stream sync"); }
+
+// ---------------------------------------------------------------------------
+// grouped GEMM plans
+// ---------------------------------------------------------------------------
+static int64_t prod(const int* d, int lo, int hi) {
+  int64_t p = 1;
+  for (int i = lo; i < hi; ++i) p *= d[i];
+  return p;
+}
+
+struct CMap {
+  int64_t off;
+  int m, n, ldc;
+};
+
+template <class F>
+static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a, const Tensor& b, int K,
+                            std::vector<GemmTaskRef>&& tasks, F cmap) {
+  plan.ta = ta;
+  plan.tb = tb;
+  plan.K = K;
+  plan.tasks = std::move(tasks);
+  plan.h_tiles.clear();
+  plan.h_tasks.clear();
+  plan.h_pairs.clear();
+  plan.flops = 0.0;
+  plan.c_elems = 0;
+  const int L = a.sh.rank, M = b.sh.rank;
+  for (const auto& t : plan.tasks) {
+    const CMap c = cmap(t.c_tag);
+    DGemmTask dt;
+    dt.c_off = c.off;
+    dt.m = c.m;
+    dt.n = c.n;
+    dt.ldc = c.ldc;
+    dt.p0 = static_cast<int>(plan.h_pairs.size());
+    for (const auto& pr : t.pairs) {
+      const int32_t as = a.find(pr.a_tag), bs = b.find(pr.b_tag);
+      if (as < 0 || bs < 0) throw Error(kInternal, "gemm plan: operand block missing");
+      int ad[kMaxRank], bd[kMaxRank];
+      a.block_dims(as, ad);
+      b.block_dims(bs, bd);
+      int64_t ma, ka, lda, kb, nb, ldb;
+      if (ta == kNoTrans) {
+        ma = prod(ad, 0, L - K);
+        ka = prod(ad, L - K, L);
+        lda = ka;
+      } else {
+        ka = prod(ad, 0, K);
+        ma = prod(ad, K, L);
+        lda = ma;
+      }
+      if (tb == kNoTrans) {
+        kb = prod(bd, 0, K);
+        nb = prod(bd, K, M);
+        ldb = nb;
+      } else {
+        nb = prod(bd, 0, M - K);
+        kb = prod(bd, M - K, M);
+        ldb = kb;
+      }
+      if (ma != c.m || nb != c.n || ka != kb) throw Error(kInternal, "gemm plan: inconsistent block dims");
+      if (ka == 0 || ma == 0 || nb == 0) continue;
+      DGemmPair p;
+      p.a_off = a.offsets[as];
+      p.b_off = b.offsets[bs];
+      p.k = static_cast<int>(ka);
+      p.lda = static_cast<int>(lda);
+      p.ldb = static_cast<int>(ldb);
+      p.pad = 0;
+      plan.h_pairs.push_back(p);
+      plan.flops += 2.0 * double(ma) * double(nb) * double(ka);
+    }
+    dt.p1 = static_cast<int>(plan.h_pairs.size());
+    if (dt.p1 == dt.p0) continue;
+    const int ti = static_cast<int>(plan.h_tasks.size());
+    plan.h_tasks.push_back(dt);
+    plan.c_elems += int64_t(c.m) * c.n;
+    for (int tm = 0; tm * kGemmTile < c.m; ++tm)
+      for (int tn = 0; tn * kGemmTile < c.n; ++tn) plan.h_tiles.push_back(DTile{ti, tm, tn, 0});
+  }
+}
+
+void build_gemm_plan(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a, const Tensor& b, const Tensor& c, int K,
+                     std::vector<GemmTaskRef>&& tasks) {
+  const int L = a.sh.rank;
+  build_plan_impl(plan, ta, tb, a, b, K, std::move(tasks), [&](int64_t ctag) {
+    const int32_t cs = c.find(ctag);
+    if (cs < 0) throw Error(kInternal, "gemm plan: result block missing from the result layout");
+    int cd[kMaxRank];
+    c.block_dims(cs, cd);
+    CMap m;
+    m.off = c.offsets[cs];
+    m.m = static_cast<int>(prod(cd, 0, L - K));
+    m.n = static_cast<int>(prod(cd, L - K, c.sh.rank));
+    m.ldc = m.n;
+    return m;
+  });
+}
+
+void GemmPlan::upload(cudaStream_t st) {
+  tiles.upload(h_tiles, st);
+  dtasks.upload(h_tasks, st);
+  pairs.upload(h_pairs, st);
+}
+
+void GemmPlan::run(double alpha, const double* A, const double* B, double* C, cudaStream_t st) const {
+  launch_gemm_f64(ta, tb, alpha, A, B, C, tiles.get(), static_cast<int>(h_tiles.size()), dtasks.get(), pairs.get(),
+                  st);
+}
+
+// Result tensor whose blocks are exactly the task results (a Gemm into an empty array).
+static void layout_from_tasks(Tensor& c, const Shape& sh, const std::vector<GemmTaskRef>& tasks) {
+  c.sh = sh;
+  std::vector<int64_t> t;
+  t.reserve(tasks.size());
+  for (const auto& x : tasks) t.push_back(x.c_tag);
+  std::sort(t.begin(), t.end());
+  c.set_blocks(t);
+}
+
+static Tensor conj_view(const Tensor& t) {
+  Tensor c;
+  c.sh = t.sh.conjugate();
+  c.tags = t.tags;
+  c.offsets = t.offsets;
+  c.slot = t.slot;
+  c.nnz = t.nnz;
+  c.d = t.d;
+  c.layout_id = t.layout_id;
+  return c;
+}
+
+static bool same_qshape(const Shape& a, const Shape& b) {
+  if (a.rank != b.rank || a.q != b.q) return false;
+  for (int i = 0; i < a.rank; ++i) {
+    if (a.qshape[i].size() != b.qshape[i].size()) return false;
+    for (size_t j = 0; j < a.qshape[i].size(); ++j)
+      if (a.qshape[i][j] != b.qshape[i][j]) return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// sigma vector
+// ---------------------------------------------------------------------------
+SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi) {
+  auto key = std::make_tuple(L.layout_id, R.layout_id, psi.layout_id);
+  auto it = ctx.sigma_plans.find(key);
+  if (it != ctx.sigma_plans.end()) return *it->second;
+  if (L.sh.rank != 3 || R.sh.rank != 3 || psi.sh.rank != 2)
+    throw Error(kInvalidArgument, "compute_sigma_vector: expects 3-index operators and a 2-index wavefunction");
+  auto p = std::make_unique<SigmaPlan>();
+  p->l_id = L.layout_id;
+  p->r_id = R.layout_id;
+  p->psi_id = psi.layout_id;
+  int K1 = 0, K2 = 0;
+  Shape s1 = gemm_result_shape(kNoTrans, kNoTrans, L.sh, psi.sh, 3, &K1);
+  auto t1 = enumerate_gemm(kNoTrans, kNoTrans, L, psi, s1, K1);
+  layout_from_tasks(p->scr1, s1, t1);
+  Shape s2 = gemm_result_shape(kNoTrans, kTrans, s1, R.sh, 2, &K2);
+  if (!same_qshape(s2, psi.sh))
+    throw Error(kQShapeMismatch, "Gemm(QSPARSE): c must have the same quantum shape of [ a * b ].");
+  auto t2 = enumerate_gemm(kNoTrans, kTrans, p->scr1, R, s2, K2);
+  build_gemm_plan(p->s1, kNoTrans, kNoTrans, L, psi, p->scr1, K1, std::move(t1));
+  build_gemm_plan(p->s2, kNoTrans, kTrans, p->scr1, R, psi, K2, std::move(t2));
+  p->s1.upload(ctx.stream);
+  p->s2.upload(ctx.stream);
+  p->flops = p->s1.flops + p->s2.flops;
+  p->bytes_min = 8 * (L.nnz + R.nnz + 2 * psi.nnz);
+  auto& ref = *p;
+  ctx.sigma_plans[key] = std::move(p);
+  return ref;
+}
+
+static void sigma_run(Context& ctx, const SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi,
+                      double* sigma) {
+  ctx.scr1.ensure(std::max<int64_t>(p.scr1.nnz, 1) * sizeof(double));
+  double* scr = ctx.scr1.as<double>();
+  if (p.scr1.nnz) cuda_check(cudaMemsetAsync(scr, 0, p.scr1.nnz * sizeof(double), ctx.stream), "scr1 zero");
+  p.s1.run(1.0, L.d, psi, scr, ctx.stream);
+  p.s2.run(1.0, scr, R.d, sigma, ctx.stream);
+  ctx.kernel_launches += 2;
+  ctx.sigma_flops += p.flops;
+  ctx.sigma_calls += 1;
+}
+
+void compute_sigma_vector(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma) {
+  if (sigma.nnz != psi.nnz || sigma.tags != psi.tags)
+    throw Error(kInvalidArgument, "compute_sigma_vector: sigma must have the wavefunction's block layout");
+  SigmaPlan& p = sigma_plan(ctx, L, R, psi);
+  sigma_run(ctx, p, L, R, psi.d, sigma.d);
+}
+
+// ---------------------------------------------------------------------------
+// diagonal
+// ---------------------------------------------------------------------------
+DiagPlan& diag_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag) {
+  auto key = std::make_tuple(L.layout_id, R.layout_id, diag.layout_id);
+  auto it = ctx.diag_plans.find(key);
+  if (it != ctx.diag_plans.end()) return *it->second;
+  auto p = std::make_unique<DiagPlan>();
+  // tied arrays: row sector -> [(w, block slot)] for blocks (i, w, i), ascending w
+  auto tied = [](const Tensor& t) {
+    std::map<int, std::vector<std::pair<int, int32_t>>> m;
+    int idx[kMaxRank];
+    for (size_t b = 0; b < t.tags.size(); ++b) {
+      t.sh.index(t.tags[b], idx);
+      if (idx[0] == idx[2]) m[idx[0]].push_back({idx[1], static_cast<int32_t>(b)});
+    }
+    for (auto& kv : m) std::sort(kv.second.begin(), kv.second.end());
+    return m;
+  };
+  auto lt = tied(L);
+  auto rt = tied(R);
+  int idx[kMaxRank];
+  for (size_t b = 0; b < diag.tags.size(); ++b) {
+    diag.sh.index(diag.tags[b], idx);
+    auto li = lt.find(idx[0]);
+    auto ri = rt.find(idx[1]);
+    if (li == lt.end() || ri == rt.end()) continue;
+    DDiagTask t;
+    t.out_off = diag.offsets[b];
+    t.m = diag.sh.dshape[0][idx[0]];
+    t.n = diag.sh.dshape[1][idx[1]];
+    t.p0 = static_cast<int>(p->h_pairs.size());
+    std::vector<std::pair<int64_t, int64_t>> refp;
+    size_t x = 0, y = 0;
+    const auto& lv = li->second;
+    const auto& rv = ri->second;
+    while (x < lv.size() && y < rv.size()) {
+      if (lv[x].first == rv[y].first) {
+        p->h_pairs.push_back(DDiagPair{L.offsets[lv[x].second], R.offsets[rv[y].second]});
+        refp.push_back({L.tags[lv[x].second], R.tags[rv[y].second]});
+        ++x;
+        ++y;
+      } else if (lv[x].first < rv[y].first) {
+        ++x;
+      } else {
+        ++y;
+      }
+    }
+    t.p1 = static_cast<int>(p->h_pairs.size());
+    if (t.p1 == t.p0) continue;
+    p->h_tasks.push_back(t);
+    p->ref.push_back({diag.tags[b], std::move(refp)});
+  }
+  p->tasks.upload(p->h_tasks, ctx.stream);
+  p->pairs.upload(p->h_pairs, ctx.stream);
+  auto& ref = *p;
+  ctx.diag_plans[key] = std::move(p);
+  return ref;
+}
+
+void compute_diagonal_elements(Context& ctx, const DTensor& L, const DTensor& R, DTensor& diag) {
+  DiagPlan& p = diag_plan(ctx, L, R, diag);
+  launch_diag(p.tasks.get(), static_cast<int>(p.h_tasks.size()), p.pairs.get(), L.d, R.d, diag.d, ctx.stream);
+  ctx.kernel_launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// renormalize (merged operator)
+// ---------------------------------------------------------------------------
+std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& opr0, const DTensor& bra,
+                                     const DTensor& ket) {
+  Tensor cbra = conj_view(bra);
+  int K1 = 0, K2 = 0;
+  GemmPlan p1, p2;
+  Tensor scr;
+  Shape s2;
+  if (forward) {
+    Shape s1 = gemm_result_shape(kTrans, kNoTrans, cbra.sh, opr0.sh, 3, &K1);
+    auto t1 = enumerate_gemm(kTrans, kNoTrans, cbra, opr0, s1, K1);
+    layout_from_tasks(scr, s1, t1);
+    build_gemm_plan(p1, kTrans, kNoTrans, cbra, opr0, scr, K1, std::move(t1));
+    s2 = gemm_result_shape(kNoTrans, kNoTrans, scr.sh, ket.sh, 3, &K2);
+  } else {
+    Shape s1 = gemm_result_shape(kNoTrans, kNoTrans, cbra.sh, opr0.sh, 3, &K1);
+    auto t1 = enumerate_gemm(kNoTrans, kNoTrans, cbra, opr0, s1, K1);
+    layout_from_tasks(scr, s1, t1);
+    build_gemm_plan(p1, kNoTrans, kNoTrans, cbra, opr0, scr, K1, std::move(t1));
+    s2 = gemm_result_shape(kNoTrans, kTrans, scr.sh, ket.sh, 3, &K2);
+  }
+  const Trans tb2 = forward ? kNoTrans : kTrans;
+  auto t2 = enumerate_gemm(kNoTrans, tb2, scr, ket, s2, K2);
+  auto out = std::make_unique<DTensor>();
+  layout_from_tasks(*out, s2, t2);
+  build_gemm_plan(p2, kNoTrans, tb2, scr, ket, *out, K2, std::move(t2));
+  p1.upload(ctx.stream);
+  p2.upload(ctx.stream);
+  out->ctx = &ctx;
+  out->alloc_device(ctx.stream, true);
+  ctx.scr2.ensure(std::max<int64_t>(scr.nnz, 1) * sizeof(double));
+  double* sp = ctx.scr2.as<double>();
+  if (scr.nnz) cuda_check(cudaMemsetAsync(sp, 0, scr.nnz * sizeof(double), ctx.stream), "renorm scr zero");
+  p1.run(1.0, bra.d, opr0.d, sp, ctx.stream);
+  p2.run(1.0, sp, ket.d, out->d, ctx.stream);
+  ctx.kernel_launches += 2;
+  // plans (device task arrays) must outlive the kernels
+  ctx.sync();
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// merged super-block operators (scatter of scalar MPO blocks)
+// ---------------------------------------------------------------------------
+std::unique_ptr<DTensor> compute_merged_operator(Context& ctx, bool forward, const DTensor& mpo,
+                                                 const DTensor& opr) {
+  if (mpo.sh.rank != 4 || opr.sh.rank != 3) throw Error(kInvalidArgument, "merged operator: bad ranks");
+  if (static_cast<int64_t>(mpo.host.size()) != mpo.nnz)
+    throw Error(kInvalidArgument, "merged operator: MPO coefficients must be available on the host");
+  // MPO block lookup by left/right bond index
+  int idx[kMaxRank];
+  MergeInfo mb, mk;
+  auto out = std::make_unique<DTensor>();
+  out->sh.rank = 3;
+  out->sh.q = opr.sh.q + mpo.sh.q;
+  struct Contrib {
+    int64_t src_off;
+    int sld;
+    double coef;
+  };
+  struct DstKey {
+    int64_t otag;
+    int ipr, ipc;
+    bool operator<(const DstKey& o) const {
+      if (otag != o.otag) return otag < o.otag;
+      if (ipr != o.ipr) return ipr < o.ipr;
+      return ipc < o.ipc;
+    }
+  };
+  std::map<DstKey, std::pair<std::pair<int, int>, std::vector<Contrib>>> dst;
+  const int ns = mpo.sh.nsec(1);
+  if (forward) {
+    // mL[A=(a,s), v, A'=(x,t)] += W[w,s,t,v] * L[a,w,x]
+    mb = MergeInfo({opr.sh.qshape[0], mpo.sh.qshape[1]}, {opr.sh.dshape[0], mpo.sh.dshape[1]});
+    mk = MergeInfo({opr.sh.qshape[2], mpo.sh.qshape[2]}, {opr.sh.dshape[2], mpo.sh.dshape[2]});
+    out->sh.qshape = {mb.q_merged, mpo.sh.qshape[3], mk.q_merged};
+    out->sh.dshape = {mb.d_merged, mpo.sh.dshape[3], mk.d_merged};
+    out->sh.finalize();
+    std::map<int, std::vector<int32_t>> wblocks;  // w -> mpo block slots
+    for (size_t b = 0; b < mpo.tags.size(); ++b) {
+      mpo.sh.index(mpo.tags[b], idx);
+      wblocks[idx[0]].push_back(static_cast<int32_t>(b));
+    }
+    const int nt = mpo.sh.nsec(2);
+    for (size_t lb = 0; lb < opr.tags.size(); ++lb) {
+      opr.sh.index(opr.tags[lb], idx);
+      const int a = idx[0], w = idx[1], x = idx[2];
+      auto wi = wblocks.find(w);
+      if (wi == wblocks.end()) continue;
+      const int da = opr.sh.dshape[0][a], dx = opr.sh.dshape[2][x];
+      for (int32_t mbk : wi->second) {
+        int mi[kMaxRank];
+        mpo.sh.index(mpo.tags[mbk], mi);
+        const int s = mi[1], t = mi[2], v = mi[3];
+        const int ipr = a * ns + s, ipc = x * nt + t;
+        const int A = mb.merged_of[ipr], Ap = mk.merged_of[ipc];
+        int oi[3] = {A, v, Ap};
+        if (!out->sh.allowed(oi)) throw Error(kQShapeMismatch, "merged operator: contribution not allowed");
+        DstKey key{out->sh.tag(oi), ipr, ipc};
+        auto& e = dst[key];
+        e.first = {da * mpo.sh.dshape[1][s], dx * mpo.sh.dshape[2][t]};
+        e.second.push_back({opr.offsets[lb], dx, mpo.host[mpo.offsets[mbk]]});
+      }
+    }
+  } else {
+    // mR[B=(s,b), w, B'=(t,y)] += W[w,s,t,v] * R[b,v,y]
+    mb = MergeInfo({mpo.sh.qshape[1], opr.sh.qshape[0]}, {mpo.sh.dshape[1], opr.sh.dshape[0]});
+    mk = MergeInfo({mpo.sh.qshape[2], opr.sh.qshape[2]}, {mpo.sh.dshape[1], opr.sh.dshape[0]});
+    out->sh.qshape = {mb.q_merged, mpo.sh.qshape[0], mk.q_merged};
+    out->sh.dshape = {mb.d_merged, mpo.sh.dshape[0], mk.d_merged};
+    out->sh.finalize();
+    std::map<int, std::vector<int32_t>> vblocks;  // v -> mpo block slots
+    for (size_t b = 0; b < mpo.tags.size(); ++b) {
+      mpo.sh.index(mpo.tags[b], idx);
+      vblocks[idx[3]].push_back(static_cast<int32_t>(b));
+    }
+    const int nb = opr.sh.nsec(0), ny = opr.sh.nsec(2);
+    for (size_t rb = 0; rb < opr.tags.size(); ++rb) {
+      opr.sh.index(opr.tags[rb], idx);
+      const int b = idx[0], v = idx[1], y = idx[2];
+      auto vi = vblocks.find(v);
+      if (vi == vblocks.end()) continue;
+      const int db = opr.sh.dshape[0][b], dy = opr.sh.dshape[2][y];
+      for (int32_t mbk : vi->second) {
+        int mi[kMaxRank];
+        mpo.sh.index(mpo.tags[mbk], mi);
+        const int w = mi[0], s = mi[1], t = mi[2];
+        const int ipr = s * nb + b, ipc = t * ny + y;
+        const int B = mb.merged_of[ipr], Bp = mk.merged_of[ipc];
+        int oi[3] = {B, w, Bp};
+        if (!out->sh.allowed(oi)) throw Error(kQShapeMismatch, "merged operator: contribution not allowed");
+        DstKey key{out->sh.tag(oi), ipr, ipc};
+        auto& e = dst[key];
+        e.first = {db * mpo.sh.dshape[1][s], dy * mpo.sh.dshape[2][t]};
+        e.second.push_back({opr.offsets[rb], dy, mpo.host[mpo.offsets[mbk]]});
+      }
+    }
+  }
+  std::vector<int64_t> tags;
+  for (const auto& kv : dst)
+    if (tags.empty() || tags.back() != kv.first.otag) tags.push_back(kv.first.otag);
+  out->set_blocks(tags);
+  std::vector<DScatterDst> hd;
+  std::vector<DScatterSrc> hs;
+  hd.reserve(dst.size());
+  for (const auto& kv : dst) {
+    const int32_t os = out->find(kv.first.otag);
+    out->sh.index(kv.first.otag, idx);
+    const int dcols = out->sh.dshape[2][idx[2]];
+    DScatterDst d;
+    d.dst_off = out->offsets[os] + int64_t(mb.offset_packed[kv.first.ipr]) * dcols + mk.offset_packed[kv.first.ipc];
+    d.rows = kv.second.first.first;
+    d.cols = kv.second.first.second;
+    d.dld = dcols;
+    d.s0 = static_cast<int>(hs.size());
+    for (const auto& c : kv.second.second) hs.push_back(DScatterSrc{c.src_off, c.sld, 0, c.coef});
+    d.s1 = static_cast<int>(hs.size());
+    d.pad = 0;
+    if (d.rows > 0 && d.cols > 0) hd.push_back(d);
+  }
+  out->ctx = &ctx;
+  out->alloc_device(ctx.stream, true);
+  DevArray<DScatterDst> dd;
+  DevArray<DScatterSrc> ds;
+  dd.upload(hd, ctx.stream);
+  ds.upload(hs, ctx.stream);
+  launch_scatter(dd.get(), static_cast<int>(hd.size()), ds.get(), opr.d, out->d, ctx.stream);
+  ctx.kernel_launches += 1;
+  ctx.sync();
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// wavefunction merge / expand
+// ---------------------------------------------------------------------------
+WaveMerge wave_merge_infos(const DTensor& lmpo, const DTensor& rmpo, const DTensor& lopr, const DTensor& ropr) {
+  auto neg = [](const std::vector<Qn>& v) {
+    std::vector<Qn> o(v.size());
+    for (size_t i = 0; i < v.size(); ++i) o[i] = -v[i];
+    return o;
+  };
+  WaveMerge wm;
+  wm.ql = MergeInfo({neg(lopr.sh.qshape[2]), neg(lmpo.sh.qshape[2])}, {lopr.sh.dshape[0], lmpo.sh.dshape[1]});
+  wm.qr = MergeInfo({neg(rmpo.sh.qshape[2]), neg(ropr.sh.qshape[2])}, {rmpo.sh.dshape[1], ropr.sh.dshape[0]});
+  return wm;
+}
+
+std::unique_ptr<DTensor> merge_wave(Context& ctx, const WaveMerge& wm, const DTensor& lwfn, const DTensor& rwfn) {
+  int K = 0;
+  Shape t4 = gemm_result_shape(kNoTrans, kNoTrans, lwfn.sh, rwfn.sh, 4, &K);
+  auto tasks = enumerate_gemm(kNoTrans, kNoTrans, lwfn, rwfn, t4, K);
+  auto psi = std::make_unique<DTensor>();
+  psi->sh.rank = 2;
+  psi->sh.q = t4.q;
+  psi->sh.qshape = {wm.ql.q_merged, wm.qr.q_merged};
+  psi->sh.dshape = {wm.ql.d_merged, wm.qr.d_merged};
+  psi->sh.finalize();
+  psi->allocate_allowed();
+  const int nn = t4.nsec(1), nr = t4.nsec(3);
+  GemmPlan plan;
+  build_plan_impl(plan, kNoTrans, kNoTrans, lwfn, rwfn, K, std::move(tasks), [&](int64_t ctag) {
+    int ti[kMaxRank];
+    t4.index(ctag, ti);
+    const int ipr = ti[0] * nn + ti[1], ipc = ti[2] * nr + ti[3];
+    const int A = wm.ql.merged_of[ipr], B = wm.qr.merged_of[ipc];
+    int pi[2] = {A, B};
+    const int32_t ps = psi->find(psi->sh.tag(pi));
+    if (ps < 0) throw Error(kInternal, "merge_wave: psi block missing");
+    const int dB = psi->sh.dshape[1][B];
+    CMap m;
+    m.off = psi->offsets[ps] + int64_t(wm.ql.offset_packed[ipr]) * dB + wm.qr.offset_packed[ipc];
+    m.m = t4.dshape[0][ti[0]] * t4.dshape[1][ti[1]];
+    m.n = t4.dshape[2][ti[2]] * t4.dshape[3][ti[3]];
+    m.ldc = dB;
+    return m;
+  });
+  plan.upload(ctx.stream);
+  psi->ctx = &ctx;
+  psi->alloc_device(ctx.stream, true);
+  plan.run(1.0, lwfn.d, rwfn.d, psi->d, ctx.stream);
+  ctx.kernel_launches += 1;
+  ctx.sync();
+  return psi;
+}
+
+static std::vector<std::vector<Qn>> split_q(const MergeInfo& info) { return info.qshape; }
+
+std::unique_ptr<DTensor> expand_rows(Context& ctx, const MergeInfo& info, const DTensor& b) {
+  // b[A, x...] -> a[(i,j), x...]  (QSTexpand, include/btas/QSPARSE/QSTmerge.h:218-295)
+  const int MR = static_cast<int>(info.qshape.size());
+  auto a = std::make_unique<DTensor>();
+  a->sh.rank = MR + b.sh.rank - 1;
+  a->sh.q = b.sh.q;
+  a->sh.qshape = split_q(info);
+  a->sh.dshape = info.dshape;
+  for (int i = 1; i < b.sh.rank; ++i) {
+    a->sh.qshape.push_back(b.sh.qshape[i]);
+    a->sh.dshape.push_back(b.sh.dshape[i]);
+  }
+  a->sh.finalize();
+  const int64_t b_stride = b.sh.rank > 1 ? b.sh.stride[0] : 1;
+  const int64_t a_stride = a->sh.stride[MR - 1];
+  struct Pend {
+    int64_t atag, src_off;
+    int rows, cols, sld;
+  };
+  std::vector<Pend> pend;
+  int idx[kMaxRank];
+  for (size_t bb = 0; bb < b.tags.size(); ++bb) {
+    const int64_t i = b.tags[bb] / b_stride, j = b.tags[bb] % b_stride;
+    b.sh.index(b.tags[bb], idx);
+    int64_t rest = 1;
+    for (int k = 1; k < b.sh.rank; ++k) rest *= b.sh.dshape[k][idx[k]];
+    for (int ip : info.members[i]) {
+      const int d = info.d_packed[ip];
+      if (d == 0) continue;
+      const int64_t at = ip * a_stride + j;
+      if (!a->sh.allowed_tag(at)) continue;
+      pend.push_back({at, b.offsets[bb] + int64_t(info.offset_packed[ip]) * rest, d, static_cast<int>(rest),
+                      static_cast<int>(rest)});
+    }
+  }
+  std::sort(pend.begin(), pend.end(), [](const Pend& x, const Pend& y) { return x.atag < y.atag; });
+  std::vector<int64_t> tags;
+  for (auto& p : pend) tags.push_back(p.atag);
+  a->set_blocks(tags);
+  std::vector<DCopy> cp;
+  for (auto& p : pend) {
+    const int32_t s = a->find(p.atag);
+    cp.push_back(DCopy{a->offsets[s], p.src_off, p.rows, p.cols, p.cols, p.sld, 1.0});
+  }
+  a->ctx = &ctx;
+  a->alloc_device(ctx.stream, false);
+  DevArray<DCopy> dc;
+  dc.upload(cp, ctx.stream);
+  launch_copy(dc.get(), static_cast<int>(cp.size()), b.d, a->d, 0, ctx.stream);
+  ctx.kernel_launches += 1;
+  ctx.sync();
+  return a;
+}
+
+std::unique_ptr<DTensor> expand_cols(Context& ctx, const DTensor& b, const MergeInfo& info) {
+  // b[x..., B] -> a[x..., (i,j)]
+  const int MC = static_cast<int>(info.qshape.size());
+  const int MR = b.sh.rank - 1;
+  auto a = std::make_unique<DTensor>();
+  a->sh.rank = MR + MC;
+  a->sh.q = b.sh.q;
+  for (int i = 0; i < MR; ++i) {
+    a->sh.qshape.push_back(b.sh.qshape[i]);
+    a->sh.dshape.push_back(b.sh.dshape[i]);
+  }
+  for (int i = 0; i < MC; ++i) {
+    a->sh.qshape.push_back(info.qshape[i]);
+    a->sh.dshape.push_back(info.dshape[i]);
+  }
+  a->sh.finalize();
+  const int64_t b_stride = b.sh.stride[MR - 1];
+  const int64_t a_stride = a->sh.stride[MR - 1];
+  struct Pend {
+    int64_t atag, src_off;
+    int rows, cols, sld;
+  };
+  std::vector<Pend> pend;
+  int idx[kMaxRank];
+  for (size_t bb = 0; bb < b.tags.size(); ++bb) {
+    const int64_t i = b.tags[bb] / b_stride, j = b.tags[bb] % b_stride;
+    b.sh.index(b.tags[bb], idx);
+    int64_t rows = 1;
+    for (int k = 0; k < MR; ++k) rows *= b.sh.dshape[k][idx[k]];
+    const int dB = b.sh.dshape[MR][idx[MR]];
+    for (int ip : info.members[j]) {
+      const int d = info.d_packed[ip];
+      if (d == 0) continue;
+      const int64_t at = i * a_stride + ip;
+      if (!a->sh.allowed_tag(at)) continue;
+      pend.push_back({at, b.offsets[bb] + info.offset_packed[ip], static_cast<int>(rows), d, dB});
+    }
+  }
+  std::sort(pend.begin(), pend.end(), [](const Pend& x, const Pend& y) { return x.atag < y.atag; });
+  std::vector<int64_t> tags;
+  for (auto& p : pend) tags.push_back(p.atag);
+  a->set_blocks(tags);
+  std::vector<DCopy> cp;
+  for (auto& p : pend) {
+    const int32_t s = a->find(p.atag);
+    cp.push_back(DCopy{a->offsets[s], p.src_off, p.rows, p.cols, p.cols, p.sld, 1.0});
+  }
+  a->ctx = &ctx;
+  a->alloc_device(ctx.stream, false);
+  DevArray<DCopy> dc;
+  dc.upload(cp, ctx.stream);
+  launch_copy(dc.get(), static_cast<int>(cp.size()), b.d, a->d, 0, ctx.stream);
+  ctx.kernel_launches += 1;
+  ctx.sync();
+  return a;
+}
+
+std::unique_ptr<DTensor> merge_cols(Context& ctx, const DTensor& a, const MergeInfo& info) {
+  const int MC = static_cast<int>(info.qshape.size());
+  const int MR = a.sh.rank - MC;
+  if (MR < 1) throw Error(kInvalidArgument, "merge_cols: nothing left to keep as rows");
+  auto b = std::make_unique<DTensor>();
+  b->sh.rank = MR + 1;
+  b->sh.q = a.sh.q;
+  for (int i = 0; i < MR; ++i) {
+    b->sh.qshape.push_back(a.sh.qshape[i]);
+    b->sh.dshape.push_back(a.sh.dshape[i]);
+  }
+  b->sh.qshape.push_back(info.q_merged);
+  b->sh.dshape.push_back(info.d_merged);
+  b->sh.finalize();
+  const int64_t a_stride = a.sh.stride[MR - 1];
+  const int64_t b_stride = b->sh.stride[MR - 1];
+  struct Pend {
+    int64_t btag, src_off;
+    int rows, cols, coff;
+  };
+  std::vector<Pend> pend;
+  int idx[kMaxRank];
+  for (size_t ab = 0; ab < a.tags.size(); ++ab) {
+    const int64_t i = a.tags[ab] / a_stride, ip = a.tags[ab] % a_stride;
+    const int B = info.merged_of[ip];
+    const int64_t bt = i * b_stride + B;
+    if (!b->sh.allowed_tag(bt)) continue;
+    a.sh.index(a.tags[ab], idx);
+    int64_t rows = 1;
+    for (int k = 0; k < MR; ++k) rows *= a.sh.dshape[k][idx[k]];
+    pend.push_back({bt, a.offsets[ab], static_cast<int>(rows), info.d_packed[ip], info.offset_packed[ip]});
+  }
+  std::vector<int64_t> tags;
+  for (auto& p : pend) tags.push_back(p.btag);
+  std::sort(tags.begin(), tags.end());
+  tags.erase(std::unique(tags.begin(), tags.end()), tags.end());
+  b->set_blocks(tags);
+  std::vector<DCopy> cp;
+  for (auto& p : pend) {
+    const int32_t s = b->find(p.btag);
+    b->sh.index(p.btag, idx);
+    const int dB = b->sh.dshape[MR][idx[MR]];
+    cp.push_back(DCopy{b->offsets[s] + p.coff, p.src_off, p.rows, p.cols, dB, p.cols, 1.0});
+  }
+  b->ctx = &ctx;
+  b->alloc_device(ctx.stream, true);
+  DevArray<DCopy> dc;
+  dc.upload(cp, ctx.stream);
+  launch_copy(dc.get(), static_cast<int>(cp.size()), a.d, b->d, 0, ctx.stream);
+  ctx.kernel_launches += 1;
+  ctx.sync();
+  return b;
+}
+
+std::unique_ptr<DTensor> gemm_new(Context& ctx, Trans ta, Trans tb, double alpha, const DTensor& a, const DTensor& b,
+                                  int c_rank) {
+  int K = 0;
+  Shape cs = gemm_result_shape(ta, tb, a.sh, b.sh, c_rank, &K);
+  auto tasks = enumerate_gemm(ta, tb, a, b, cs, K);
+  auto c = std::make_unique<DTensor>();
+  layout_from_tasks(*c, cs, tasks);
+  GemmPlan plan;
+  build_gemm_plan(plan, ta, tb, a, b, *c, K, std::move(tasks));
+  plan.upload(ctx.stream);
+  c->ctx = &ctx;
+  c->alloc_device(ctx.stream, true);
+  plan.run(alpha, a.d, b.d, c->d, ctx.stream);
+  ctx.kernel_launches += 1;
+  ctx.sync();
+  return c;
+}
+
+double normalize_tensor(Context& ctx, DTensor& x) {
+  const int64_t n = x.nnz;
+  if (n == 0) return 0.0;
+  const int nblk = multidot_blocks(n);
+  ctx.partial.ensure(size_t(nblk) * 100 * sizeof(double));
+  ctx.scalars.ensure(256 * sizeof(double));
+  double* sc = ctx.scalars.as<double>();
+  launch_multidot(x.d, 1, x.d, 1, n, n, sc + 100, ctx.partial.as<double>(), nblk, ctx.stream);
+  launch_scal_dev(x.d, n, sc + 100, 1, ctx.stream);
+  ctx.kernel_launches += 3;
+  double nrm2 = 0.0;
+  cuda_check(cudaMemcpyAsync(&nrm2, sc + 100, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream), "norm d2h");
+  ctx.sync();
+  return std::sqrt(nrm2);
+}
+
+// ---------------------------------------------------------------------------
+// Davidson (single root)
+// ---------------------------------------------------------------------------
+double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag, DTensor& wfnc, double tol,
+                   DavidsonStats* stats) {
+  const int max_ritz = 10;
+  const int64_t n = wfnc.nnz;
+  if (diag.nnz != wfnc.nnz)
+    throw Error(kInvalidArgument, "diagonalize: diag and wavefunction layouts differ");
+  cudaStream_t st = ctx.stream;
+  SigmaPlan& sp = sigma_plan(ctx, L, R, wfnc);
+  ctx.work.ensure(size_t(2 * max_ritz + 1) * std::max<int64_t>(n, 1) * sizeof(double));
+  double* trial = ctx.work.as<double>();
+  double* sigma = trial + int64_t(max_ritz) * n;
+  double* errv = sigma + int64_t(max_ritz) * n;
+  const int nblk = multidot_blocks(n);
+  ctx.partial.ensure(size_t(nblk) * 100 * sizeof(double));
+  ctx.scalars.ensure(256 * sizeof(double));
+  double* part = ctx.partial.as<double>();
+  double* sc = ctx.scalars.as<double>();  // [0..99] dots, [100] norm, [101] dot, [128..227] rvec
+  double* rvec_d = sc + 128;
+  DavidsonStats local;
+  DavidsonStats& S = stats ? *stats : local;
+  S = DavidsonStats{};
+
+  auto sigma_of = [&](int k) {
+    cuda_check(cudaMemsetAsync(sigma + k * n, 0, n * sizeof(double), st), "sigma zero");
+    sigma_run(ctx, sp, L, R, trial + k * n, sigma + k * n);
+    S.n_sigma += 1;
+  };
+  auto normalize = [&](double* x) {
+    launch_multidot(x, 1, x, 1, n, n, sc + 100, part, nblk, st);
+    launch_scal_dev(x, n, sc + 100, 1, st);
+    ctx.kernel_launches += 3;
+  };
+
+  launch_copy_vec(trial, wfnc.d, n, st);
+  double eval = 0.0;
+  int niter = 0, iconv = 0;
+  std::vector<double> hdots(100), heff, rvec, rval;
+  while (iconv < 1 && niter < 4) {
+    normalize(trial);
+    sigma_of(0);
+    for (int m = 1; m <= max_ritz; ++m) {
+      launch_multidot(trial, m, sigma, m, n, n, sc, part, nblk, st);
+      ctx.kernel_launches += 2;
+      cuda_check(cudaMemcpyAsync(hdots.data(), sc, m * m * sizeof(double), cudaMemcpyDeviceToHost, st), "heff d2h");
+      ctx.sync();
+      heff.assign(m * m, 0.0);
+      for (int i = 0; i < m; ++i)
+        for (int j = 0; j <= i; ++j) {
+          const double h = hdots[i * m + j];  // trial_i . sigma_j
+          heff[i * m + j] = h;
+          heff[j * m + i] = h;
+        }
+      jacobi_eigh(m, heff, rval, rvec);  // rvec[i*m + j]: component i of eigenvector j
+      eval = rval[0];
+      S.micro += 1;
+      cuda_check(cudaMemcpyAsync(rvec_d, rvec.data(), m * m * sizeof(double), cudaMemcpyHostToDevice, st),
+                 "rvec h2d");
+      launch_rotate(trial, m, n, n, rvec_d, m, nullptr, st);
+      launch_rotate(sigma, m, n, n, rvec_d, m, nullptr, st);
+      launch_copy_vec(errv, sigma, n, st);
+      launch_axpy(errv, trial, n, -eval, st);
+      launch_multidot(errv, 1, errv, 1, n, n, sc + 101, part, nblk, st);
+      ctx.kernel_launches += 6;
+      double rnorm = 0.0;
+      cuda_check(cudaMemcpyAsync(&rnorm, sc + 101, sizeof(double), cudaMemcpyDeviceToHost, st), "rnorm d2h");
+      ctx.sync();
+      S.rnorm = rnorm;
+      if (rnorm < tol) {
+        ++iconv;
+        break;
+      }
+      if (m < max_ritz) {
+        launch_precondition(errv, diag.d, n, eval, st);
+        ctx.kernel_launches += 1;
+        for (int i = 0; i < m; ++i) {
+          normalize(errv);
+          launch_multidot(trial + i * n, 1, errv, 1, n, n, sc + 102, part, nblk, st);
+          launch_axpy_dev(errv, trial + i * n, n, sc + 102, -1.0, st);
+          ctx.kernel_launches += 3;
+        }
+        normalize(errv);
+        launch_copy_vec(trial + m * n, errv, n, st);
+        ctx.kernel_launches += 1;
+        sigma_of(m);
+      }
+    }
+    ++niter;
+  }
+  S.macro = niter;
+  S.converged = iconv;
+  launch_copy_vec(wfnc.d, trial, n, st);
+  normalize(wfnc.d);
+  ctx.sync();
+  return eval;
+}
+
+// ---------------------------------------------------------------------------
+// canonicalize: per-block SVD, global top-M truncation, Dimm
+// ---------------------------------------------------------------------------
+std::vector<int> select_kept(const std::vector<std::vector<double>>& svals, int M, double tie_rtol,
+                             double* discarded) {
+  std::vector<double> all;
+  for (const auto& v : svals) all.insert(all.end(), v.begin(), v.end());
+  std::sort(all.rbegin(), all.rend());
+  double cutoff = 1.0e-16;
+  if (M > 0 && static_cast<size_t>(M) < all.size()) cutoff = all[M - 1] * (1.0 - tie_rtol);
+  std::vector<int> kept(svals.size(), 0);
+  double dn = 0.0;
+  for (size_t s = 0; s < svals.size(); ++s) {
+    int k = 0;
+    while (k < static_cast<int>(svals[s].size()) && svals[s][k] >= cutoff) ++k;
+    kept[s] = k;
+    for (size_t x = k; x < svals[s].size(); ++x) dn += svals[s][x] * svals[s][x];
+  }
+  if (discarded) *discarded = dn;
+  return kept;
+}
+
+CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise) {
+  if (noise >= 1.0e-8) throw Error(kInvalidArgument, "canonicalize: noise injection is not supported");
+  if (wfnc.sh.rank != 2) throw Error(kInvalidArgument, "canonicalize: expects a merged (2-index) wavefunction");
+  cudaStream_t st = ctx.stream;
+  const int ncols = wfnc.sh.nsec(1);
+  struct Blk {
+    int32_t slot;
+    int i, j, m, n, k;
+    int64_t u_off, s_off, v_off;  // inside svd_mats
+  };
+  std::vector<Blk> blks;
+  int64_t tot = 0;
+  int64_t maxmn = 0;
+  for (size_t b = 0; b < wfnc.tags.size(); ++b) {
+    const int i = static_cast<int>(wfnc.tags[b] / ncols), j = static_cast<int>(wfnc.tags[b] % ncols);
+    const int m = wfnc.sh.dshape[0][i], n = wfnc.sh.dshape[1][j];
+    if (m == 0 || n == 0) continue;
+    const int k = std::min(m, n);
+    Blk x{static_cast<int32_t>(b), i, j, m, n, k, 0, 0, 0};
+    x.u_off = tot;
+    tot += int64_t(m) * k;
+    x.s_off = tot;
+    tot += k;
+    x.v_off = tot;
+    tot += int64_t(k) * n;
+    maxmn = std::max<int64_t>(maxmn, int64_t(m) * n);
+    blks.push_back(x);
+  }
+  // workspace: matrices + one transposed copy + per-call solver buffers
+  int lwork = 0;
+  for (const auto& x : blks) {
+    const int M_ = std::max(x.m, x.n), N_ = std::min(x.m, x.n);
+    int lw = 0;
+    solver_check(cusolverDnDgesvd_bufferSize(ctx.solver, M_, N_, &lw), "gesvd bufferSize");
+    lwork = std::max(lwork, lw);
+  }
+  const int64_t tmp_elems = 3 * maxmn + 16;
+  ctx.svd_mats.ensure(size_t(tot + tmp_elems) * sizeof(double));
+  ctx.svd_work.ensure(size_t(lwork + 64) * sizeof(double) + size_t(std::max<int64_t>(maxmn, 1)) * sizeof(double) +
+                      64);
+  double* mats = ctx.svd_mats.as<double>();
+  double* tA = mats + tot;                // col-major working copy of the block
+  double* tU = tA + maxmn;                // col-major U when transposes are needed
+  double* tV = tU + maxmn;                // col-major VT when transposes are needed
+  double* work = ctx.svd_work.as<double>();
+  double* rwork = work + lwork + 8;
+  int* info = reinterpret_cast<int*>(rwork + std::max<int64_t>(maxmn, 1));
+  for (const auto& x : blks) {
+    const double* a = wfnc.d + wfnc.offsets[x.slot];
+    double* U = mats + x.u_off;
+    double* S = mats + x.s_off;
+    double* V = mats + x.v_off;
+    if (x.n >= x.m) {
+      // row-major A (m x n) is col-major A^T (n x m): A^T = Ux S VxT, so U_A = VxT buffer, Vt_A = Ux buffer
+      cuda_check(cudaMemcpyAsync(tA, a, int64_t(x.m) * x.n * sizeof(double), cudaMemcpyDeviceToDevice, st),
+                 "svd copy");
+      solver_check(cusolverDnDgesvd(ctx.solver, 'S', 'S', x.n, x.m, tA, x.n, S, V, x.n, U, x.m, work, lwork, rwork,
+                                    info),
+                   "gesvd");
+    } else {
+      // col-major copy of A (m x n) = row-major A^T (n x m)
+      launch_transpose(a, tA, x.m, x.n, st);
+      solver_check(cusolverDnDgesvd(ctx.solver, 'S', 'S', x.m, x.n, tA, x.m, S, tU, x.m, tV, x.n, work, lwork, rwork,
+                                    info),
+                   "gesvd");
+      // tU col-major (m x k) == row-major (k x m): transpose into row-major U (m x k)
+      launch_transpose(tU, U, x.k, x.m, st);
+      // tV col-major (k x n) == row-major (n x k): transpose into row-major Vt (k x n)
+      launch_transpose(tV, V, x.n, x.k, st);
+      ctx.kernel_launches += 3;
+    }
+  }
+  // singular values to the host
+  std::vector<double> hmats(tot);
+  if (tot) cuda_check(cudaMemcpyAsync(hmats.data(), mats, tot * sizeof(double), cudaMemcpyDeviceToHost, st), "s d2h");
+  ctx.sync();
+  // sector of each block's singular values: row sector (LeftArrow) or column sector (RightArrow)
+  std::map<int, size_t> sec_of;
+  std::vector<std::vector<double>> svals;
+  std::vector<int> secs;
+  std::vector<int> blk_sv(blks.size());
+  for (size_t b = 0; b < blks.size(); ++b) {
+    const int sec = forward ? blks[b].i : blks[b].j;
+    if (sec_of.count(sec)) throw Error(kInternal, "canonicalize: two blocks share one singular-value sector");
+    sec_of[sec] = b;
+  }
+  for (auto& kv : sec_of) {
+    const Blk& x = blks[kv.second];
+    secs.push_back(kv.first);
+    svals.emplace_back(hmats.begin() + x.s_off, hmats.begin() + x.s_off + x.k);
+    blk_sv[kv.second] = static_cast<int>(svals.size() - 1);
+  }
+  CanonResult res;
+  std::vector<int> kept = select_kept(svals, M, 1e-10, &res.discarded);
+  // new bond sectors in ascending sector order
+  std::vector<Qn> q_nz;
+  std::vector<int> d_nz;
+  std::map<int, int> newidx;
+  for (size_t s = 0; s < secs.size(); ++s) {
+    if (kept[s] <= 0) continue;
+    const Qn qs = forward ? wfnc.sh.qshape[0][secs[s]] : -wfnc.sh.qshape[1][secs[s]];
+    newidx[secs[s]] = static_cast<int>(q_nz.size());
+    q_nz.push_back(qs);
+    d_nz.push_back(kept[s]);
+    res.kept.push_back({secs[s], kept[s]});
+  }
+  std::vector<Qn> neg_q_nz(q_nz.size());
+  for (size_t s = 0; s < q_nz.size(); ++s) neg_q_nz[s] = -q_nz[s];
+  auto U = std::make_unique<DTensor>();
+  auto V = std::make_unique<DTensor>();
+  U->sh.rank = 2;
+  U->sh.q = forward ? Qn{} : wfnc.sh.q;
+  U->sh.qshape = {wfnc.sh.qshape[0], neg_q_nz};
+  U->sh.dshape = {wfnc.sh.dshape[0], d_nz};
+  U->sh.finalize();
+  V->sh.rank = 2;
+  V->sh.q = forward ? wfnc.sh.q : Qn{};
+  V->sh.qshape = {q_nz, wfnc.sh.qshape[1]};
+  V->sh.dshape = {d_nz, wfnc.sh.dshape[1]};
+  V->sh.finalize();
+  struct Pl {
+    int64_t ut, vt;
+    size_t b;
+  };
+  std::vector<Pl> pl;
+  for (size_t b = 0; b < blks.size(); ++b) {
+    const int sec = forward ? blks[b].i : blks[b].j;
+    auto it = newidx.find(sec);
+    if (it == newidx.end()) continue;
+    int ui[2] = {blks[b].i, it->second};
+    int vi[2] = {it->second, blks[b].j};
+    pl.push_back({U->sh.tag(ui), V->sh.tag(vi), b});
+  }
+  {
+    std::vector<int64_t> ut, vt;
+    for (auto& p : pl) {
+      ut.push_back(p.ut);
+      vt.push_back(p.vt);
+    }
+    std::sort(ut.begin(), ut.end());
+    std::sort(vt.begin(), vt.end());
+    U->set_blocks(ut);
+    V->set_blocks(vt);
+  }
+  U->ctx = &ctx;
+  V->ctx = &ctx;
+  U->alloc_device(st, false);
+  V->alloc_device(st, false);
+  std::vector<DCopy> cu, cv;
+  std::vector<double> s_kept;
+  std::vector<int64_t> soff, boff;
+  std::vector<int> brow, bcol;
+  for (auto& p : pl) {
+    const Blk& x = blks[p.b];
+    const int k = kept[blk_sv[p.b]];
+    const int32_t us = U->find(p.ut), vs = V->find(p.vt);
+    cu.push_back(DCopy{U->offsets[us], x.u_off, x.m, k, k, x.k, 1.0});
+    cv.push_back(DCopy{V->offsets[vs], x.v_off, k, x.n, x.n, x.n, 1.0});
+    soff.push_back(static_cast<int64_t>(s_kept.size()));
+    s_kept.insert(s_kept.end(), hmats.begin() + x.s_off, hmats.begin() + x.s_off + k);
+    if (forward) {
+      boff.push_back(V->offsets[vs]);
+      brow.push_back(k);
+      bcol.push_back(x.n);
+    } else {
+      boff.push_back(U->offsets[us]);
+      brow.push_back(x.m);
+      bcol.push_back(k);
+    }
+  }
+  DevArray<DCopy> dcu, dcv;
+  DevArray<double> ds;
+  DevArray<int64_t> dso, dbo;
+  DevArray<int> dbr, dbc;
+  dcu.upload(cu, st);
+  dcv.upload(cv, st);
+  ds.upload(s_kept, st);
+  dso.upload(soff, st);
+  dbo.upload(boff, st);
+  dbr.upload(brow, st);
+  dbc.upload(bcol, st);
+  launch_copy(dcu.get(), static_cast<int>(cu.size()), mats, U->d, 0, st);
+  launch_copy(dcv.get(), static_cast<int>(cv.size()), mats, V->d, 0, st);
+  if (forward)
+    launch_scale_blocks_rows(V->d, dbo.get(), dbr.get(), dbc.get(), dso.get(), static_cast<int>(boff.size()),
+                             ds.get(), st);
+  else
+    launch_scale_blocks_cols(U->d, dbo.get(), dbr.get(), dbc.get(), dso.get(), static_cast<int>(boff.size()),
+                             ds.get(), st);
+  ctx.kernel_launches += 3;
+  ctx.sync();
+  res.lmat = std::move(U);
+  res.rmat = std::move(V);
+  return res;
+}
+
+// ---------------------------------------------------------------------------
+// one bond
+// ---------------------------------------------------------------------------
+static double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo, const DTensor& rmpo,
+                                const DTensor& lopr, const DTensor& ropr, const DTensor& lwfn, const DTensor& rwfn,
+                                double tole, int M) {
+  BondOut out;
+  double t0 = now();
+  auto mL = compute_merged_operator(ctx, true, lmpo, lopr);
+  auto mR = compute_merged_operator(ctx, false, rmpo, ropr);
+  WaveMerge wm = wave_merge_infos(lmpo, rmpo, lopr, ropr);
+  auto psi = merge_wave(ctx, wm, lwfn, rwfn);
+  double t1 = now();
+  out.stats.t_merge = t1 - t0;
+  DTensor diag;
+  static_cast<Tensor&>(diag) = static_cast<const Tensor&>(*psi);
+  diag.d = nullptr;
+  diag.ctx = &ctx;
+  diag.alloc_device(ctx.stream, true);
+  compute_diagonal_elements(ctx, *mL, *mR, diag);
+  ctx.sync();
+  double t2 = now();
+  out.stats.t_diag = t2 - t1;
+  const double f0 = ctx.sigma_flops;
+  out.stats.energy = diagonalize(ctx, *mL, *mR, diag, *psi, tole, &out.stats.dav);
+  out.stats.sigma_flops = ctx.sigma_flops - f0;
+  double t3 = now();
+  out.stats.t_davidson = t3 - t2;
+  CanonResult cr = canonicalize(ctx, forward, *psi, M, 0.0);
+  double t4 = now();
+  out.stats.t_svd = t4 - t3;
+  if (forward)
+    out.env = renormalize(ctx, true, *mL, *cr.lmat, *cr.lmat);
+  else
+    out.env = renormalize(ctx, false, *mR, *cr.rmat, *cr.rmat);
+  double t5 = now();
+  out.stats.t_renorm = t5 - t4;
+  out.lwfn = expand_rows(ctx, wm.ql, *cr.lmat);
+  out.rwfn = expand_cols(ctx, *cr.rmat, wm.qr);
+  // the plans keyed by these layouts die with the tensors
+  ctx.sigma_plans.clear();
+  ctx.diag_plans.clear();
+  return out;
+}
+
+}  // namespace mpsxx

@@ -1,0 +1,186 @@
+// Device engine of the merged two-site DMRG hot path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kernels.hpp"
+#include "qsd.hpp"
+
+namespace mpsxx {
+
+void cuda_check(cudaError_t e, const char* what);
+
+// Grow-only device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t bytes);
+  void release();
+  ~DevBuf() { release(); }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+template <class T>
+struct DevArray {
+  DevBuf buf;
+  size_t n = 0;
+  void upload(const std::vector<T>& h, cudaStream_t st);
+  T* get() const { return buf.as<T>(); }
+};
+
+struct Context;
+
+// Device tensor: host layout descriptor + device storage (+ optional host data).
+struct DTensor : Tensor {
+  Context* ctx = nullptr;
+  DevBuf store;
+  std::vector<double> host;  // host copy for MPO coefficients (optional)
+  void alloc_device(cudaStream_t st, bool zero = true);
+};
+
+// Grouped block GEMM plan built from the reference's task enumeration.
+struct GemmPlan {
+  Trans ta = kNoTrans, tb = kNoTrans;
+  int K = 0;
+  std::vector<GemmTaskRef> tasks;
+  std::vector<DTile> h_tiles;
+  std::vector<DGemmTask> h_tasks;
+  std::vector<DGemmPair> h_pairs;
+  DevArray<DTile> tiles;
+  DevArray<DGemmTask> dtasks;
+  DevArray<DGemmPair> pairs;
+  double flops = 0.0;
+  int64_t c_elems = 0;  // elements of C touched (for traffic accounting)
+  void upload(cudaStream_t st);
+  void run(double alpha, const double* A, const double* B, double* C, cudaStream_t st) const;
+};
+
+// GEMM plan into a C whose layout is `c` (block offsets).  C blocks may be
+// sub-blocks of a larger block when `cmap` is provided (fused merges).
+void build_gemm_plan(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a, const Tensor& b, const Tensor& c,
+                     int K, std::vector<GemmTaskRef>&& tasks);
+
+struct SigmaPlan {
+  uint64_t l_id = 0, r_id = 0, psi_id = 0;
+  Tensor scr1;  // layout of L*psi
+  GemmPlan s1, s2;
+  double flops = 0.0;
+  int64_t bytes_min = 0;  // 8*(nnz L + nnz R + 2 nnz psi)
+};
+
+struct DiagPlan {
+  std::vector<DDiagTask> h_tasks;
+  std::vector<DDiagPair> h_pairs;
+  DevArray<DDiagTask> tasks;
+  DevArray<DDiagPair> pairs;
+  std::vector<std::pair<int64_t, std::vector<std::pair<int64_t, int64_t>>>> ref;  // (psi tag, [(L tag, R tag)])
+};
+
+struct DavidsonStats {
+  int n_sigma = 0;
+  int macro = 0;
+  int micro = 0;
+  double rnorm = 0.0;
+  int converged = 0;
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cusolverDnHandle_t solver = nullptr;
+  DevBuf scr1;       // sigma stage-1 intermediates
+  DevBuf scr2;       // renormalize intermediates
+  DevBuf work;       // Davidson vectors
+  DevBuf partial;    // reduction partials
+  DevBuf scalars;    // small device scalars
+  DevBuf svd_work;   // solver workspace
+  DevBuf svd_mats;   // per-block SVD matrices
+  std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<SigmaPlan>> sigma_plans;
+  std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<DiagPlan>> diag_plans;
+  // counters for measurement
+  int64_t kernel_launches = 0;
+  double sigma_flops = 0.0;
+  int64_t sigma_calls = 0;
+
+  explicit Context(int dev, cudaStream_t st);
+  ~Context();
+  void sync();
+};
+
+// --- hot-path operations (reference names) ---------------------------------
+
+// src/compute_sigma_vector.hpp:85-96: sigma += L psi R^T over (w, B').
+SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi);
+void compute_sigma_vector(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma);
+
+// src/compute_diagonal_elements.hpp:65-80
+DiagPlan& diag_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag);
+void compute_diagonal_elements(Context& ctx, const DTensor& L, const DTensor& R, DTensor& diag);
+
+// src/renormalize.hpp:57-95 (merged operator); result allocated by the callee
+std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& opr0, const DTensor& bra,
+                                     const DTensor& ket);
+
+// src/optimize.hpp:273-368 (one operator group); mpo must carry host data
+std::unique_ptr<DTensor> compute_merged_operator(Context& ctx, bool forward, const DTensor& mpo,
+                                                 const DTensor& opr);
+
+// src/diagonalize.hpp:310-449 (single root)
+double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag, DTensor& wfnc,
+                   double tol, DavidsonStats* stats);
+
+// src/canonicalize.hpp:88-106 + include/btas/QSPARSE/QSTLAPACK.h:121-288
+struct CanonResult {
+  std::unique_ptr<DTensor> lmat, rmat;
+  std::vector<std::pair<int, int>> kept;  // (sector, kept count) of the new bond
+  double discarded = 0.0;
+};
+CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise);
+
+// global top-M selection with a relative tie window (QSTLAPACK.h:204-232)
+std::vector<int> select_kept(const std::vector<std::vector<double>>& svals, int M, double tie_rtol,
+                             double* discarded);
+
+// merged wavefunction psi[A,B] from lwfn[l,n,m] * rwfn[m,n',r] (src/optimize.hpp:542-557)
+struct WaveMerge {
+  MergeInfo ql, qr;
+};
+WaveMerge wave_merge_infos(const DTensor& lmpo, const DTensor& rmpo, const DTensor& lopr, const DTensor& ropr);
+std::unique_ptr<DTensor> merge_wave(Context& ctx, const WaveMerge& wm, const DTensor& lwfn, const DTensor& rwfn);
+std::unique_ptr<DTensor> expand_rows(Context& ctx, const MergeInfo& info, const DTensor& b);
+std::unique_ptr<DTensor> expand_cols(Context& ctx, const DTensor& b, const MergeInfo& info);
+// QSTmerge column merge of the trailing indices (include/btas/QSPARSE/QSTmerge.h:85-140)
+std::unique_ptr<DTensor> merge_cols(Context& ctx, const DTensor& a, const MergeInfo& info);
+
+// btas::Gemm into an empty result (QSTBLAS.h:182-226)
+std::unique_ptr<DTensor> gemm_new(Context& ctx, Trans ta, Trans tb, double alpha, const DTensor& a, const DTensor& b,
+                                  int c_rank);
+// btas::Normalize; returns the norm before scaling
+double normalize_tensor(Context& ctx, DTensor& x);
+
+// One bond (src/optimize.hpp:495-651)
+struct BondStats {
+  double energy = 0.0;
+  DavidsonStats dav;
+  double t_merge = 0, t_diag = 0, t_davidson = 0, t_svd = 0, t_renorm = 0;
+  double sigma_flops = 0.0;
+};
+struct BondOut {
+  std::unique_ptr<DTensor> env, lwfn, rwfn;
+  BondStats stats;
+};
+BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo, const DTensor& rmpo,
+                                const DTensor& lopr, const DTensor& ropr, const DTensor& lwfn,
+                                const DTensor& rwfn, double tole, int M);
+
+}  // namespace mpsxx

@@ -1,0 +1,84 @@
+// Device work descriptors and kernel launchers (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace mpsxx {
+
+// One C block of a grouped block GEMM: C[m x n] (ldc) += alpha * sum_p op(A_p) op(B_p).
+struct DGemmTask {
+  int64_t c_off;
+  int m, n, ldc;
+  int p0, p1;  // pair range
+};
+// One (A, B) pair: op(A) is m x k, op(B) is k x n; lda/ldb are the stored row strides.
+struct DGemmPair {
+  int64_t a_off, b_off;
+  int k, lda, ldb, pad;
+};
+// One output tile of a task.
+struct DTile {
+  int task, tm, tn, pad;
+};
+
+// Dense 2-D block copy: dst[r*dld + c] (+)= scale * src[r*sld + c].
+struct DCopy {
+  int64_t dst_off, src_off;
+  int rows, cols, dld, sld;
+  double scale;
+};
+// Destination of a scatter-accumulate: sum over its sources in fixed order.
+struct DScatterDst {
+  int64_t dst_off;
+  int rows, cols, dld, s0, s1, pad;
+};
+struct DScatterSrc {
+  int64_t src_off;
+  int sld, pad;
+  double coef;
+};
+// Diagonal task: out block [m x n] (ld n) += sum_p L_p[a*(m+1)] * R_p[b*(n+1)].
+struct DDiagTask {
+  int64_t out_off;
+  int m, n, p0, p1;
+};
+struct DDiagPair {
+  int64_t l_off, r_off;
+};
+
+constexpr int kGemmTile = 64;
+
+void launch_gemm_f64(int transa, int transb, double alpha, const double* A, const double* B, double* C,
+                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DGemmPair* pairs,
+                     cudaStream_t st);
+void launch_copy(const DCopy* tasks, int ntasks, const double* src, double* dst, int accumulate,
+                 cudaStream_t st);
+void launch_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* src, double* dst,
+                    cudaStream_t st);
+void launch_diag(const DDiagTask* tasks, int ntasks, const DDiagPair* pairs, const double* L, const double* R,
+                 double* out, cudaStream_t st);
+
+// Level-1 over dense vectors of length n (the block layout of a wavefunction).
+void launch_fill(double* x, int64_t n, double v, cudaStream_t st);
+void launch_scal_dev(double* x, int64_t n, const double* s, int mode, cudaStream_t st);
+void launch_axpy_dev(double* y, const double* x, int64_t n, const double* s, double sign, cudaStream_t st);
+void launch_axpy(double* y, const double* x, int64_t n, double a, cudaStream_t st);
+void launch_copy_vec(double* y, const double* x, int64_t n, cudaStream_t st);
+// out[i*m + j] = dot(X_i, Y_j) for i < nx, j < ny (vectors strided by `stride`)
+void launch_multidot(const double* X, int nx, const double* Y, int ny, int64_t n, int64_t stride, double* out,
+                     double* partial, int nblocks, cudaStream_t st);
+// new_j = sum_i R[i*ld + j] * old_i, j < m (in place via scratch `tmp` of m*n)
+void launch_rotate(double* V, int m, int64_t n, int64_t stride, const double* R, int ldr, double* tmp,
+                   cudaStream_t st);
+void launch_precondition(double* r, const double* diag, int64_t n, double e, cudaStream_t st);
+void launch_scale_blocks_rows(double* data, const int64_t* off, const int* rows, const int* cols,
+                              const int64_t* s_off, int nb, const double* s, cudaStream_t st);
+void launch_scale_blocks_cols(double* data, const int64_t* off, const int* rows, const int* cols,
+                              const int64_t* s_off, int nb, const double* s, cudaStream_t st);
+void launch_transpose(const double* src, double* dst, int rows, int cols, cudaStream_t st);
+
+int multidot_blocks(int64_t n);
+
+}  // namespace mpsxx

@@ -1,0 +1,368 @@
+// FP64 kernels of the two-site hot path: grouped block GEMM, block copies,
+// merged-operator scatter, H_eff diagonal, and the Davidson level-1 operations.
+//
+// GB300 (sm_103a) has a very small FP64 pipe, so the FP64 path is FMA-bound on
+// CUDA cores: a 64x64 output tile per 256-thread CTA, 4x4 register micro-tiles,
+// operands staged through shared memory in 16-deep K slices.  Every output tile
+// is owned by exactly one CTA and its (A,B) pairs are accumulated in enumeration
+// order, so results are deterministic run to run.
+#include <cuda_runtime.h>
+
+#include "kernels.hpp"
+
+namespace mpsxx {
+
+namespace {
+
+constexpr int TM = kGemmTile;
+constexpr int TN = kGemmTile;
+constexpr int TK = 16;
+
+__global__ void __launch_bounds__(256) gemm_f64_kernel(int transa, int transb, double alpha,
+                                                       const double* __restrict__ A, const double* __restrict__ B,
+                                                       double* __restrict__ C, const DTile* __restrict__ tiles,
+                                                       const DGemmTask* __restrict__ tasks,
+                                                       const DGemmPair* __restrict__ pairs) {
+  __shared__ double As[TK][TM + 1];
+  __shared__ double Bs[TK][TN + 1];
+  const DTile t = tiles[blockIdx.x];
+  const DGemmTask task = tasks[t.task];
+  const int m0 = t.tm * TM, n0 = t.tn * TN;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+  for (int p = task.p0; p < task.p1; ++p) {
+    const DGemmPair pr = pairs[p];
+    for (int k0 = 0; k0 < pr.k; k0 += TK) {
+      for (int e = threadIdx.x; e < TM * TK; e += 256) {
+        int r, kk;
+        if (!transa) {
+          r = e / TK;
+          kk = e % TK;
+        } else {
+          kk = e / TM;
+          r = e % TM;
+        }
+        const int gr = m0 + r, gk = k0 + kk;
+        double v = 0.0;
+        if (gr < task.m && gk < pr.k)
+          v = transa ? A[pr.a_off + (int64_t)gk * pr.lda + gr] : A[pr.a_off + (int64_t)gr * pr.lda + gk];
+        As[kk][r] = v;
+      }
+      for (int e = threadIdx.x; e < TN * TK; e += 256) {
+        int c, kk;
+        if (!transb) {
+          kk = e / TN;
+          c = e % TN;
+        } else {
+          c = e / TK;
+          kk = e % TK;
+        }
+        const int gc = n0 + c, gk = k0 + kk;
+        double v = 0.0;
+        if (gc < task.n && gk < pr.k)
+          v = transb ? B[pr.b_off + (int64_t)gc * pr.ldb + gk] : B[pr.b_off + (int64_t)gk * pr.ldb + gc];
+        Bs[kk][c] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < TK; ++kk) {
+        double a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = m0 + ty + 16 * i;
+    if (r >= task.m) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = n0 + tx + 16 * j;
+      if (c >= task.n) continue;
+      double* dst = C + task.c_off + (int64_t)r * task.ldc + c;
+      *dst += alpha * acc[i][j];
+    }
+  }
+}
+
+__global__ void copy_kernel(const DCopy* __restrict__ tasks, const double* __restrict__ src,
+                            double* __restrict__ dst, int accumulate) {
+  const DCopy t = tasks[blockIdx.x];
+  const int64_t n = (int64_t)t.rows * t.cols;
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const int r = static_cast<int>(e / t.cols), c = static_cast<int>(e % t.cols);
+    const double v = t.scale * src[t.src_off + (int64_t)r * t.sld + c];
+    double* d = dst + t.dst_off + (int64_t)r * t.dld + c;
+    if (accumulate)
+      *d += v;
+    else
+      *d = v;
+  }
+}
+
+__global__ void scatter_kernel(const DScatterDst* __restrict__ dsts, const DScatterSrc* __restrict__ srcs,
+                               const double* __restrict__ src, double* __restrict__ dst) {
+  const DScatterDst t = dsts[blockIdx.x];
+  const int64_t n = (int64_t)t.rows * t.cols;
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const int r = static_cast<int>(e / t.cols), c = static_cast<int>(e % t.cols);
+    double acc = 0.0;
+    for (int s = t.s0; s < t.s1; ++s) {
+      const DScatterSrc q = srcs[s];
+      acc = fma(q.coef, src[q.src_off + (int64_t)r * q.sld + c], acc);
+    }
+    dst[t.dst_off + (int64_t)r * t.dld + c] += acc;
+  }
+}
+
+__global__ void diag_kernel(const DDiagTask* __restrict__ tasks, const DDiagPair* __restrict__ pairs,
+                            const double* __restrict__ L, const double* __restrict__ R, double* __restrict__ out) {
+  const DDiagTask t = tasks[blockIdx.x];
+  const int64_t n = (int64_t)t.m * t.n;
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const int a = static_cast<int>(e / t.n), b = static_cast<int>(e % t.n);
+    double acc = 0.0;
+    for (int p = t.p0; p < t.p1; ++p) {
+      const DDiagPair q = pairs[p];
+      acc = fma(L[q.l_off + (int64_t)a * (t.m + 1)], R[q.r_off + (int64_t)b * (t.n + 1)], acc);
+    }
+    out[t.out_off + e] += acc;
+  }
+}
+
+__global__ void fill_kernel(double* x, int64_t n, double v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = v;
+}
+
+// mode 0: x *= s[0]; mode 1: x *= 1/sqrt(s[0]) (s holds a squared norm)
+__global__ void scal_dev_kernel(double* x, int64_t n, const double* s, int mode) {
+  const double f = mode == 0 ? s[0] : 1.0 / sqrt(s[0]);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] *= f;
+}
+
+__global__ void axpy_dev_kernel(double* y, const double* x, int64_t n, const double* s, double sign) {
+  const double a = sign * s[0];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = fma(a, x[i], y[i]);
+}
+
+__global__ void axpy_kernel(double* y, const double* x, int64_t n, double a) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = fma(a, x[i], y[i]);
+}
+
+__global__ void copy_vec_kernel(double* y, const double* x, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = x[i];
+}
+
+constexpr int kMaxDot = 10;
+
+// Each CTA reduces a contiguous chunk into partial[blk][i*ny+j]; a fixed-order
+// second pass makes the sum deterministic.
+__global__ void __launch_bounds__(256) multidot_partial_kernel(const double* __restrict__ X, int nx,
+                                                               const double* __restrict__ Y, int ny, int64_t n,
+                                                               int64_t stride, double* __restrict__ partial) {
+  __shared__ double red[8][kMaxDot * kMaxDot];
+  double acc[kMaxDot * kMaxDot];
+  const int np = nx * ny;
+  for (int q = 0; q < np; ++q) acc[q] = 0.0;
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t lo = blockIdx.x * chunk;
+  const int64_t hi = lo + chunk < n ? lo + chunk : n;
+  for (int64_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+    double xv[kMaxDot];
+    for (int i = 0; i < nx; ++i) xv[i] = X[i * stride + e];
+    for (int j = 0; j < ny; ++j) {
+      const double yv = Y[j * stride + e];
+      for (int i = 0; i < nx; ++i) acc[i * ny + j] = fma(xv[i], yv, acc[i * ny + j]);
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = 0; q < np; ++q) {
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < np) {
+    double v = 0.0;
+    for (int w = 0; w < 8; ++w) v += red[w][threadIdx.x];
+    partial[blockIdx.x * (kMaxDot * kMaxDot) + threadIdx.x] = v;
+  }
+}
+
+__global__ void multidot_final_kernel(const double* __restrict__ partial, int nblocks, int np,
+                                      double* __restrict__ out) {
+  const int q = threadIdx.x;
+  if (q >= np) return;
+  double v = 0.0;
+  for (int b = 0; b < nblocks; ++b) v += partial[b * (kMaxDot * kMaxDot) + q];
+  out[q] = v;
+}
+
+__global__ void rotate_kernel(double* V, int m, int64_t n, int64_t stride, const double* __restrict__ R, int ldr) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    double old[kMaxDot];
+    for (int i = 0; i < m; ++i) old[i] = V[i * stride + e];
+    for (int j = 0; j < m; ++j) {
+      double v = 0.0;
+      for (int i = 0; i < m; ++i) v = fma(R[i * ldr + j], old[i], v);
+      V[j * stride + e] = v;
+    }
+  }
+}
+
+__global__ void precondition_kernel(double* r, const double* __restrict__ diag, int64_t n, double e) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double denm = e - diag[i];
+    if (fabs(denm) < 1.0e-8) denm = 1.0e-8;
+    r[i] /= denm;
+  }
+}
+
+__global__ void scale_rows_kernel(double* data, const int64_t* off, const int* rows, const int* cols,
+                                  const int64_t* s_off, const double* s) {
+  const int b = blockIdx.x;
+  const int64_t n = (int64_t)rows[b] * cols[b];
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) data[off[b] + e] *= s[s_off[b] + e / cols[b]];
+}
+
+__global__ void scale_cols_kernel(double* data, const int64_t* off, const int* rows, const int* cols,
+                                  const int64_t* s_off, const double* s) {
+  const int b = blockIdx.x;
+  const int64_t n = (int64_t)rows[b] * cols[b];
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) data[off[b] + e] *= s[s_off[b] + e % cols[b]];
+}
+
+__global__ void transpose_kernel(const double* __restrict__ src, double* __restrict__ dst, int rows, int cols) {
+  __shared__ double tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int r = by + j, c = bx + threadIdx.x;
+    if (r < rows && c < cols) tile[j][threadIdx.x] = src[(int64_t)r * cols + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int r = bx + j, c = by + threadIdx.x;  // dst is cols x rows
+    if (r < cols && c < rows) dst[(int64_t)r * rows + c] = tile[threadIdx.x][j];
+  }
+}
+
+inline int grid_for(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  if (g < 1) g = 1;
+  return static_cast<int>(g);
+}
+
+}  // namespace
+
+void launch_gemm_f64(int transa, int transb, double alpha, const double* A, const double* B, double* C,
+                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DGemmPair* pairs,
+                     cudaStream_t st) {
+  if (ntiles <= 0) return;
+  gemm_f64_kernel<<<ntiles, 256, 0, st>>>(transa, transb, alpha, A, B, C, tiles, tasks, pairs);
+}
+
+void launch_copy(const DCopy* tasks, int ntasks, const double* src, double* dst, int accumulate, cudaStream_t st) {
+  if (ntasks <= 0) return;
+  copy_kernel<<<ntasks, 256, 0, st>>>(tasks, src, dst, accumulate);
+}
+
+void launch_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* src, double* dst,
+                    cudaStream_t st) {
+  if (ndst <= 0) return;
+  scatter_kernel<<<ndst, 256, 0, st>>>(dsts, srcs, src, dst);
+}
+
+void launch_diag(const DDiagTask* tasks, int ntasks, const DDiagPair* pairs, const double* L, const double* R,
+                 double* out, cudaStream_t st) {
+  if (ntasks <= 0) return;
+  diag_kernel<<<ntasks, 256, 0, st>>>(tasks, pairs, L, R, out);
+}
+
+void launch_fill(double* x, int64_t n, double v, cudaStream_t st) {
+  if (n <= 0) return;
+  fill_kernel<<<grid_for(n), 256, 0, st>>>(x, n, v);
+}
+
+void launch_scal_dev(double* x, int64_t n, const double* s, int mode, cudaStream_t st) {
+  if (n <= 0) return;
+  scal_dev_kernel<<<grid_for(n), 256, 0, st>>>(x, n, s, mode);
+}
+
+void launch_axpy_dev(double* y, const double* x, int64_t n, const double* s, double sign, cudaStream_t st) {
+  if (n <= 0) return;
+  axpy_dev_kernel<<<grid_for(n), 256, 0, st>>>(y, x, n, s, sign);
+}
+
+void launch_axpy(double* y, const double* x, int64_t n, double a, cudaStream_t st) {
+  if (n <= 0) return;
+  axpy_kernel<<<grid_for(n), 256, 0, st>>>(y, x, n, a);
+}
+
+void launch_copy_vec(double* y, const double* x, int64_t n, cudaStream_t st) {
+  if (n <= 0) return;
+  copy_vec_kernel<<<grid_for(n), 256, 0, st>>>(y, x, n);
+}
+
+int multidot_blocks(int64_t n) {
+  int64_t b = (n + 2047) / 2048;
+  if (b > 304) b = 304;
+  if (b < 1) b = 1;
+  return static_cast<int>(b);
+}
+
+void launch_multidot(const double* X, int nx, const double* Y, int ny, int64_t n, int64_t stride, double* out,
+                     double* partial, int nblocks, cudaStream_t st) {
+  multidot_partial_kernel<<<nblocks, 256, 0, st>>>(X, nx, Y, ny, n, stride, partial);
+  multidot_final_kernel<<<1, 128, 0, st>>>(partial, nblocks, nx * ny, out);
+}
+
+void launch_rotate(double* V, int m, int64_t n, int64_t stride, const double* R, int ldr, double* tmp,
+                   cudaStream_t st) {
+  (void)tmp;
+  if (n <= 0) return;
+  rotate_kernel<<<grid_for(n), 256, 0, st>>>(V, m, n, stride, R, ldr);
+}
+
+void launch_precondition(double* r, const double* diag, int64_t n, double e, cudaStream_t st) {
+  if (n <= 0) return;
+  precondition_kernel<<<grid_for(n), 256, 0, st>>>(r, diag, n, e);
+}
+
+void launch_scale_blocks_rows(double* data, const int64_t* off, const int* rows, const int* cols,
+                              const int64_t* s_off, int nb, const double* s, cudaStream_t st) {
+  if (nb <= 0) return;
+  scale_rows_kernel<<<nb, 256, 0, st>>>(data, off, rows, cols, s_off, s);
+}
+
+void launch_scale_blocks_cols(double* data, const int64_t* off, const int* rows, const int* cols,
+                              const int64_t* s_off, int nb, const double* s, cudaStream_t st) {
+  if (nb <= 0) return;
+  scale_cols_kernel<<<nb, 256, 0, st>>>(data, off, rows, cols, s_off, s);
+}
+
+void launch_transpose(const double* src, double* dst, int rows, int cols, cudaStream_t st) {
+  if (rows <= 0 || cols <= 0) return;
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+  transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(src, dst, rows, cols);
+}
+
+}  // namespace mpsxx

@@ -1,0 +1,175 @@
+"""In-memory two-site DMRG sweeps on the device (the caller of the hot path).
+
+Replaces the reference's disk-backed sweep driver (src/make_sweep.cpp:12-253,
+src/dmrg.cpp:21-132) and initial-state builder (src/make_random_mpss.cpp:15-271):
+MPO, site tensors and block operators stay in HBM; each bond is one call of
+``optimize_twosite_merged`` through the C ABI.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from . import core
+from .core import Context, Tensor
+
+SITE_QUANTA = [(0, 0), (1, 1), (1, -1), (2, 0)]
+
+
+def _qadd(a, b):
+    return (a[0] + b[0], a[1] + b[1])
+
+
+def generate_quantum_states(nsite: int, qt, max_blocks: int):
+    """Bond quantum numbers of the initial MPS (src/make_random_mpss.cpp:15-94):
+    unique products filtered by particle number, pruned from the right, then
+    capped to ``max_blocks`` central sectors."""
+    qb = [None] * nsite
+    qb[0] = list(SITE_QUANTA)
+    for i in range(1, nsite - 1):
+        bare = sorted({_qadd(x, y) for x in qb[i - 1] for y in SITE_QUANTA})
+        qb[i] = [q for q in bare if q[0] <= qt[0]]
+    qb[nsite - 1] = [tuple(qt)]
+    for i in range(nsite - 1, 0, -1):
+        qr = qb[i]
+        qb[i - 1] = [ql for ql in qb[i - 1] if any(r == _qadd(n, ql) for n in SITE_QUANTA for r in qr)]
+        if not qb[i - 1]:
+            raise ValueError("no quantum states reach the target quantum number")
+    for i in range(nsite - 1):
+        if max_blocks > 0 and len(qb[i]) > max_blocks:
+            offs = (len(qb[i]) - max_blocks) // 2
+            qb[i] = qb[i][offs:offs + max_blocks]
+            qb[i + 1] = [r for r in qb[i + 1] if any(r == _qadd(l, n) for l in qb[i] for n in SITE_QUANTA)]
+    return qb
+
+
+def _site_tensor(ctx: Context, ql, qr, q_total) -> Tensor:
+    qshape = [list(ql), list(SITE_QUANTA), [(-q[0], -q[1]) for q in qr]]
+    dshape = [[1] * len(ql), [1] * 4, [1] * len(qr)]
+    t = Tensor.create(ctx, q_total, qshape, dshape)  # every allowed block
+    t.upload(np.ones(t.nnz))
+    core.normalize(ctx, t)
+    return t
+
+
+def _boundary(ctx: Context) -> Tensor:
+    t = Tensor.create(ctx, (0, 0), [[(0, 0)]] * 3, [[1]] * 3)
+    t.upload(np.ones(1))
+    return t
+
+
+@dataclass
+class DeviceState:
+    mpo: List[Tensor]
+    wave: List[Tensor]
+    lenv: List[Optional[Tensor]]
+    renv: List[Optional[Tensor]]
+    M: int
+
+
+def make_initial_state(ctx: Context, mpo: List[Tensor], n_elec: int, two_sz: int, M: int) -> DeviceState:
+    """Constant-filled normalised site tensors, backward canonicalisation with
+    truncation M, and the right block operators (src/make_random_mpss.cpp:97-271).
+    The reference fills each site with one uniform draw; after normalisation only
+    its sign survives, which changes no energy, so +1 is used."""
+    N = len(mpo)
+    qt = (n_elec, two_sz)
+    qb = generate_quantum_states(N, qt, M)
+    wave: List[Optional[Tensor]] = [None] * N
+    ql = [(0, 0)]
+    for i in range(N - 1):
+        wave[i] = _site_tensor(ctx, ql, qb[i], (0, 0))
+        ql = qb[i]
+    wave[N - 1] = _site_tensor(ctx, ql, [(0, 0)], qt)
+    renv: List[Optional[Tensor]] = [None] * N
+    lenv: List[Optional[Tensor]] = [None] * N
+    renv[N - 1] = _boundary(ctx)
+    wfnc = wave[N - 1]
+    for i in range(N - 1, 0, -1):
+        # one-site backward canonicalize (src/canonicalize.hpp:77-85)
+        m2 = core.merge_cols(ctx, wfnc)
+        g, v = core.canonicalize(ctx, False, m2, M)
+        rmps = core.expand_cols(ctx, v, wfnc)
+        lm = core.gemm(ctx, 0, 0, 1.0, wave[i - 1], g, 3)
+        core.normalize(ctx, lm)
+        wfnc = lm
+        wave[i - 1] = lm
+        wave[i] = rmps
+        # right block operator through the merged-operator path
+        mR = core.compute_merged_operator(ctx, False, mpo[i], renv[i])
+        vm = core.merge_cols(ctx, rmps)
+        renv[i - 1] = core.renormalize(ctx, False, mR, vm, vm)
+    lenv[0] = _boundary(ctx)
+    return DeviceState(mpo, wave, lenv, renv, M)
+
+
+@dataclass
+class SweepLog:
+    energy: float
+    bond_energies: List[float]
+    n_sigma: int
+    sigma_flops: float
+    seconds: float
+    times: Dict[str, float] = field(default_factory=dict)
+
+
+def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None) -> SweepLog:
+    """Forward then backward sweep; Davidson tolerance 0.1*tole; sweep energy =
+    minimum over bonds (src/make_sweep.cpp:12-253)."""
+    N = len(st.mpo)
+    t0 = time.perf_counter()
+    es: List[float] = []
+    nsig = 0
+    flops = 0.0
+    times: Dict[str, float] = {}
+
+    def acc(stats):
+        nonlocal nsig, flops
+        nsig += int(stats["n_sigma"])
+        flops += stats["sigma_flops"]
+        for k in ("t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm"):
+            times[k] = times.get(k, 0.0) + stats[k]
+
+    for i in range(N - 1):
+        e, env, nl, nr, stats = core.optimize_twosite_merged(ctx, True, st.mpo[i], st.mpo[i + 1], st.lenv[i],
+                                                             st.renv[i + 1], st.wave[i], st.wave[i + 1],
+                                                             0.1 * tole, st.M)
+        st.lenv[i + 1] = env
+        st.wave[i], st.wave[i + 1] = nl, nr
+        es.append(e)
+        acc(stats)
+        if bond_hook:
+            bond_hook(True, i, e, stats)
+    for i in range(N - 1, 0, -1):
+        e, env, nl, nr, stats = core.optimize_twosite_merged(ctx, False, st.mpo[i - 1], st.mpo[i], st.lenv[i - 1],
+                                                             st.renv[i], st.wave[i - 1], st.wave[i], 0.1 * tole,
+                                                             st.M)
+        st.renv[i - 1] = env
+        st.wave[i - 1], st.wave[i] = nl, nr
+        es.append(e)
+        acc(stats)
+        if bond_hook:
+            bond_hook(False, i - 1, e, stats)
+    return SweepLog(min(es), es, nsig, flops, time.perf_counter() - t0, times)
+
+
+def dmrg(ctx: Context, mpo_dicts: List[dict], n_elec: int, two_sz: int, M: int, tole: float, max_sweeps: int,
+         min_sweeps: int = 0, verbose: bool = False):
+    """Sweeps until |dE| < tole after at least one iteration (src/dmrg.cpp:37-79)."""
+    mpo = [Tensor.from_dict(ctx, d) for d in mpo_dicts]
+    st = make_initial_state(ctx, mpo, n_elec, two_sz, M)
+    e_prev = 0.0
+    logs = []
+    for it in range(max_sweeps):
+        log = make_sweep(ctx, st, tole)
+        logs.append(log)
+        de = log.energy - e_prev
+        e_prev = log.energy
+        if verbose:
+            print(f"sweep {it}: E = {log.energy:.16f} dE = {de:.2e} ({log.seconds:.2f}s)", flush=True)
+        if it > 0 and abs(de) < tole and it + 1 >= min_sweeps:
+            break
+    return st, logs

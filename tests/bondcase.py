@@ -1,0 +1,38 @@
+"""Shared fixture builder: a consistent two-site bond taken from an oracle sweep."""
+from __future__ import annotations
+
+import functools
+
+from oracle import dmrg as od
+from oracle import from_site_dict
+from oracle import qsd as oq
+from mpsxx_gb300.mpogen import hubbard_mpo
+
+
+@functools.lru_cache(maxsize=None)
+def hubbard_bond(L: int = 10, M: int = 32, bond: int = 4, U: float = 4.0):
+    mpo = [from_site_dict(s) for s in hubbard_mpo(L, -1.0, U)]
+    st = od.make_initial_state(mpo, L, 0, M)
+    od.make_sweep(st, 1e-8)
+    for i in range(bond):
+        res, env, nl, nr = od.optimize_twosite_merged(True, mpo[i], mpo[i + 1], st.lenv[i], st.renv[i + 1],
+                                                      st.wave[i], st.wave[i + 1], 1e-9, M)
+        st.lenv[i + 1] = env
+        st.wave[i] = nl
+        st.wave[i + 1] = nr
+    i = bond
+    mL = od.compute_merged_operator(True, mpo[i], st.lenv[i])
+    mR = od.compute_merged_operator(False, mpo[i + 1], st.renv[i + 1])
+    ql, qr = od.wave_merge_infos(mpo[i], mpo[i + 1], st.lenv[i], st.renv[i + 1])
+    t = oq.QSDArray()
+    oq.gemm("N", "N", 1.0, st.wave[i], st.wave[i + 1], 1.0, t, nc=4)
+    psi = oq.merge_cols(oq.merge_rows(ql, t), qr)
+    full = psi.empty_like()
+    full.allocate(0.0)
+    for k, b in psi.blocks.items():
+        full.blocks[k] = b
+    return dict(mpo=mpo, st=st, i=i, mL=mL, mR=mR, psi=psi, full=full, M=M)
+
+
+def to_dict(a: oq.QSDArray) -> dict:
+    return {"q": a.q, "qshape": a.qshape, "dshape": a.dshape, "blocks": a.blocks}

@@ -1,0 +1,170 @@
+"""CUDA path vs the oracle on the same inputs, through the C ABI (needs a GPU).
+
+Tolerances: FP64 kernels reorder sums relative to the oracle's BLAS, so block
+data is compared at 1e-12 relative to the largest magnitude, energies at 1e-10 Eh.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests.bondcase import hubbard_bond, to_dict
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from mpsxx_gb300 import core
+
+    return core.Context(0)
+
+
+def dev(ctx, a):
+    from mpsxx_gb300 import core
+
+    return core.Tensor.from_dict(ctx, to_dict(a))
+
+
+def max_block_diff(ref_blocks, got_blocks):
+    keys = set(ref_blocks) | set(got_blocks)
+    scale = max([float(np.max(np.abs(b))) for b in ref_blocks.values() if b.size] + [1e-300])
+    err = 0.0
+    for k in keys:
+        r = ref_blocks.get(k)
+        g = got_blocks.get(k)
+        if r is None:
+            r = np.zeros_like(g)
+        if g is None:
+            g = np.zeros_like(r)
+        err = max(err, float(np.max(np.abs(r - g))) if r.size else 0.0)
+    return err / scale
+
+
+def test_sigma_vector_matches_oracle(ctx):
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    L, R, P = dev(ctx, case["mL"]), dev(ctx, case["mR"]), dev(ctx, case["full"])
+    S = P.like()
+    core.compute_sigma_vector(ctx, L, R, P, S)
+    ref = oq.QSDArray()
+    od.compute_sigma_vector(case["mL"], case["mR"], case["full"], ref)
+    assert max_block_diff(ref.blocks, S.to_blocks()) < 1e-12
+    # accumulate semantics (beta = 1): a second call doubles sigma
+    core.compute_sigma_vector(ctx, L, R, P, S)
+    assert max_block_diff({k: 2 * v for k, v in ref.blocks.items()}, S.to_blocks()) < 1e-12
+
+
+def test_diagonal_matches_oracle(ctx):
+    from oracle import dmrg as od
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    L, R, P = dev(ctx, case["mL"]), dev(ctx, case["mR"]), dev(ctx, case["full"])
+    D = P.like()
+    core.compute_diagonal_elements(ctx, L, R, D)
+    ref = case["full"].empty_like()
+    od.compute_diagonal_elements(case["mL"], case["mR"], ref)
+    assert max_block_diff(ref.blocks, D.to_blocks()) < 1e-12
+
+
+@pytest.mark.parametrize("forward", [True, False])
+def test_merged_operator_matches_oracle(ctx, forward):
+    from oracle import dmrg as od
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    st, i = case["st"], case["i"]
+    if forward:
+        mpo, opr = case["mpo"][i], st.lenv[i]
+    else:
+        mpo, opr = case["mpo"][i + 1], st.renv[i + 1]
+    got = core.compute_merged_operator(ctx, forward, dev(ctx, mpo), dev(ctx, opr))
+    ref = od.compute_merged_operator(forward, mpo, opr)
+    q, d = got.shape()
+    assert q == [list(x) for x in ref.qshape] and d == ref.dshape
+    tags, _ = got.blocks()
+    assert list(tags) == sorted(ref.blocks)
+    assert max_block_diff(ref.blocks, got.to_blocks()) < 1e-13
+
+
+@pytest.mark.parametrize("forward", [True, False])
+def test_canonicalize_and_renormalize_match_oracle(ctx, forward):
+    from oracle import dmrg as od
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    M = case["M"]
+    P = dev(ctx, case["psi"])
+    lm, rm = core.canonicalize(ctx, forward, P, M)
+    U, V, kept = od.canonicalize_merged(forward, case["psi"], M)
+    # same new bond (sectors and kept dims)
+    assert lm.shape()[0][1] == U.qshape[1] and lm.shape()[1][1] == U.dshape[1]
+    # the product U (s) V^T is sign-free
+    def prod(a, b):
+        from oracle import qsd as oq
+        c = oq.QSDArray()
+        oq.gemm("N", "N", 1.0, a, b, 1.0, c, nc=2)
+        return c.blocks
+    from oracle import qsd as oq
+    gl = oq.QSDArray(lm.q, *lm.shape())
+    gl.blocks = lm.to_blocks()
+    gr = oq.QSDArray(rm.q, *rm.shape())
+    gr.blocks = rm.to_blocks()
+    assert max_block_diff(prod(U, V), prod(gl, gr)) < 1e-12
+    # renormalised operator from the same (oracle) singular vectors: the kernel
+    # parity does not depend on the SVD's sign gauge
+    if forward:
+        Ud = dev(ctx, U)
+        env = core.renormalize(ctx, True, dev(ctx, case["mL"]), Ud, Ud)
+        ref = od.renormalize_merged(True, case["mL"], U, U)
+    else:
+        Vd = dev(ctx, V)
+        env = core.renormalize(ctx, False, dev(ctx, case["mR"]), Vd, Vd)
+        ref = od.renormalize_merged(False, case["mR"], V, V)
+    tags, _ = env.blocks()
+    assert list(tags) == sorted(ref.blocks)
+    assert max_block_diff(ref.blocks, env.to_blocks()) < 1e-12
+
+
+def test_davidson_matches_oracle(ctx):
+    from oracle import dmrg as od
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    L, R = dev(ctx, case["mL"]), dev(ctx, case["mR"])
+    P = dev(ctx, case["full"])
+    D = P.like()
+    core.compute_diagonal_elements(ctx, L, R, D)
+    e_gpu, st = core.diagonalize(ctx, L, R, D, P, 1e-11)
+    diag = case["full"].empty_like()
+    od.compute_diagonal_elements(case["mL"], case["mR"], diag)
+    psi = case["full"].copy()
+    ost = od.DavidsonStats()
+    e_ref = od.davidson(lambda c, v: od.compute_sigma_vector(case["mL"], case["mR"], c, v), diag, psi, 1e-11, ost)
+    assert abs(e_gpu - e_ref) < 1e-10
+    assert st["converged"] == 1
+
+
+def test_dmrg_hubbard12_energies_match_oracle(ctx):
+    """Hubbard L=12, U=4, half filling, M=64, tole 1e-10: every sweep energy within 1e-10 Eh."""
+    from mpsxx_gb300 import dmrg
+    from mpsxx_gb300.mpogen import hubbard_mpo
+
+    gold = json.load(open(os.path.join(HERE, "golden", "hubbard12_u4_m64.json")))
+    mpo = [__import__("mpsxx_gb300.core", fromlist=["Tensor"]).Tensor.from_dict(ctx, d)
+           for d in hubbard_mpo(12, -1.0, 4.0)]
+    st = dmrg.make_initial_state(ctx, mpo, 12, 0, 64)
+    for k, ref in enumerate(gold["sweeps"]):
+        log = dmrg.make_sweep(ctx, st, gold["tole"])
+        assert abs(log.energy - ref["energy"]) < 1e-10, (k, log.energy, ref["energy"])
+    assert log.energy >= gold["exact"] - 1e-10
