@@ -149,6 +149,24 @@ int mpsxx_gemm(mpsxx_context* ctx, int transa, int transb, double alpha, const m
  * QSTexpand(b, cols_info, a) (include/btas/QSPARSE/QSTmerge.h:297-372). */
 int mpsxx_expand_cols(mpsxx_context* ctx, const mpsxx_tensor* b, const mpsxx_tensor* like, mpsxx_tensor** out);
 
+/* Merged two-site wavefunction psi[A,B] = merge(lwfn[l,n,m] rwfn[m,n',r]) with the
+ * ket merge infos of the bond (src/optimize.hpp:536-557); every allowed block is stored. */
+int mpsxx_merge_wavefunction(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                             const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* lwfn,
+                             const mpsxx_tensor* rwfn, mpsxx_tensor** psi);
+
+/* Split merged lmat[A,m] / rmat[m,B] back into site tensors (QSTexpand of
+ * src/optimize.hpp:611-612) with the same merge infos. */
+int mpsxx_expand_wavefunction(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                              const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* lmat,
+                              const mpsxx_tensor* rmat, mpsxx_tensor** lwfn, mpsxx_tensor** rwfn);
+
+/* Measurement helper (no reference counterpart): average device time in seconds of
+ * `reps` back-to-back sigma applications, bracketed by CUDA events on the
+ * context's stream (sgv accumulates reps times). */
+int mpsxx_sigma_device_time(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                            const mpsxx_tensor* wfn, mpsxx_tensor* sgv, int reps, double* seconds);
+
 /* x /= ||x||_2 (btas::Normalize, include/btas/QSPARSE/QSTBLAS.h:239-243); norm may be NULL. */
 int mpsxx_normalize(mpsxx_context* ctx, mpsxx_tensor* x, double* norm);
 

@@ -47,6 +47,9 @@ SIGNATURES = {
     "mpsxx_gemm": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, vp, vp, C.c_int, vpp]),
     "mpsxx_expand_cols": (C.c_int, [vp, vp, vp, vpp]),
     "mpsxx_normalize": (C.c_int, [vp, vp, c_dbl_p]),
+    "mpsxx_sigma_device_time": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, c_dbl_p]),
+    "mpsxx_merge_wavefunction":(C.c_int, [vp, vp, vp, vp, vp, vp, vp, vpp]),
+    "mpsxx_expand_wavefunction": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vpp, vpp]),
 }
 
 STATUS = {0: "OK", 1: "QSHAPE_MISMATCH", 2: "ALLOC", 3: "NO_CONVERGENCE", 4: "DEVICE_TIMEOUT",

@@ -294,6 +294,21 @@ def normalize(ctx: Context, x: Tensor) -> float:
     return n.value
 
 
+def merge_wavefunction(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor, lwfn: Tensor,
+                       rwfn: Tensor) -> Tensor:
+    o = _out()
+    check(lib().mpsxx_merge_wavefunction(ctx.h, lmpo.h, rmpo.h, lopr.h, ropr.h, lwfn.h, rwfn.h, C.byref(o)))
+    return Tensor(o, ctx)
+
+
+def expand_wavefunction(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor, lmat: Tensor,
+                        rmat: Tensor):
+    lo, ro = _out(), _out()
+    check(lib().mpsxx_expand_wavefunction(ctx.h, lmpo.h, rmpo.h, lopr.h, ropr.h, lmat.h, rmat.h, C.byref(lo),
+                                          C.byref(ro)))
+    return Tensor(lo, ctx), Tensor(ro, ctx)
+
+
 BOND_STAT_KEYS = ("n_sigma", "sigma_flops", "t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "converged")
 
 

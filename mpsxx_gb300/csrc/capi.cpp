@@ -209,7 +209,9 @@ int mpsxx_tensor_upload(mpsxx_tensor* t, const double* host) {
   return guard([&] {
     DTensor& x = ten_mut(t);
     need(host != nullptr || x.nnz == 0, "null host buffer");
-    x.host.assign(host, host + x.nnz);
+    // MPO site tensors (rank 4) keep a host copy: their scalar blocks are the
+    // coefficients of the merged-operator scatter plans
+    if (x.sh.rank == 4 || !x.ctx) x.host.assign(host, host + x.nnz);
     if (x.ctx) {
       need_device(x);
       if (x.nnz)
@@ -411,6 +413,39 @@ int mpsxx_normalize(mpsxx_context* ctx, mpsxx_tensor* x, double* norm) {
     Context& c = ctx_of(ctx);
     const double n = normalize_tensor(c, ten_mut(x));
     if (norm) *norm = n;
+  });
+}
+
+int mpsxx_merge_wavefunction(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                             const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* lwfn,
+                             const mpsxx_tensor* rwfn, mpsxx_tensor** psi) {
+  return guard([&] {
+    need(psi != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    WaveMerge wm = wave_merge_infos(ten(lmpo), ten(rmpo), ten(lopr), ten(ropr));
+    *psi = wrap(merge_wave(c, wm, ten(lwfn), ten(rwfn)), ctx);
+  });
+}
+
+int mpsxx_expand_wavefunction(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                              const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* lmat,
+                              const mpsxx_tensor* rmat, mpsxx_tensor** lwfn, mpsxx_tensor** rwfn) {
+  return guard([&] {
+    need(lwfn && rwfn, "null output");
+    Context& c = ctx_of(ctx);
+    WaveMerge wm = wave_merge_infos(ten(lmpo), ten(rmpo), ten(lopr), ten(ropr));
+    *lwfn = wrap(expand_rows(c, wm.ql, ten(lmat)), ctx);
+    *rwfn = wrap(expand_cols(c, ten(rmat), wm.qr), ctx);
+  });
+}
+
+
+int mpsxx_sigma_device_time(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                            const mpsxx_tensor* wfn, mpsxx_tensor* sgv, int reps, double* seconds) {
+  return guard([&] {
+    need(reps > 0 && seconds != nullptr, "bad arguments");
+    Context& c = ctx_of(ctx);
+    *seconds = sigma_device_time(c, ten(lopr), ten(ropr), ten(wfn), ten_mut(sgv), reps);
   });
 }
 

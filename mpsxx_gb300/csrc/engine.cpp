@@ -277,6 +277,23 @@ void compute_sigma_vector(Context& ctx, const DTensor& L, const DTensor& R, cons
   sigma_run(ctx, p, L, R, psi.d, sigma.d);
 }
 
+double sigma_device_time(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma,
+                         int reps) {
+  SigmaPlan& p = sigma_plan(ctx, L, R, psi);
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "event create");
+  cuda_check(cudaEventCreate(&e1), "event create");
+  cuda_check(cudaEventRecord(e0, ctx.stream), "event record");
+  for (int r = 0; r < reps; ++r) sigma_run(ctx, p, L, R, psi.d, sigma.d);
+  cuda_check(cudaEventRecord(e1, ctx.stream), "event record");
+  cuda_check(cudaEventSynchronize(e1), "event sync");
+  float ms = 0.f;
+  cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event time");
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return double(ms) / 1e3 / reps;
+}
+
 // ---------------------------------------------------------------------------
 // diagonal
 // ---------------------------------------------------------------------------

@@ -123,6 +123,10 @@ struct Context {
 SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi);
 void compute_sigma_vector(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma);
 
+// average device seconds of `reps` sigma applications (CUDA events on ctx.stream)
+double sigma_device_time(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma,
+                         int reps);
+
 // src/compute_diagonal_elements.hpp:65-80
 DiagPlan& diag_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag);
 void compute_diagonal_elements(Context& ctx, const DTensor& L, const DTensor& R, DTensor& diag);

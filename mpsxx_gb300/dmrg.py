@@ -106,6 +106,96 @@ def make_initial_state(ctx: Context, mpo: List[Tensor], n_elec: int, two_sz: int
     return DeviceState(mpo, wave, lenv, renv, M)
 
 
+def _sector_dim(nsites: int, q) -> int:
+    from math import comb
+
+    p, s = q
+    if (p + s) % 2:
+        return 0
+    nu, nd = (p + s) // 2, (p - s) // 2
+    if nu < 0 or nd < 0 or nu > nsites or nd > nsites:
+        return 0
+    return comb(nsites, nu) * comb(nsites, nd)
+
+
+def make_random_state(ctx: Context, mpo: List[Tensor], n_elec: int, two_sz: int, M: int, seed: int = 0,
+                      oversample: float = 2.0) -> DeviceState:
+    """Random MPS of bond dimension M: bond sectors as the initial state, sector dims
+    proportional to the block Hilbert-space dimension (total about oversample*M per
+    bond, each at most its Hilbert dimension), normal random entries, then the same
+    backward canonicalisation with truncation M as ``make_initial_state``."""
+    N = len(mpo)
+    qt = (n_elec, two_sz)
+    qb = generate_quantum_states(N, qt, 0)
+    rng = np.random.default_rng(seed)
+    dims = []
+    for i in range(N - 1):
+        left = i + 1
+        right = N - 1 - i
+        hd = []
+        for q in qb[i]:
+            qr = (qt[0] - q[0], qt[1] - q[1])
+            hd.append(min(_sector_dim(left, q), _sector_dim(right, qr)))
+        tot = float(sum(hd)) or 1.0
+        target = oversample * M
+        dims.append([max(1, min(h, int(np.ceil(target * h / tot)))) if h > 0 else 0 for h in hd])
+    wave: List[Optional[Tensor]] = [None] * N
+    ql, dl = [(0, 0)], [1]
+    for i in range(N):
+        if i < N - 1:
+            qr, dr, q_tot = qb[i], dims[i], (0, 0)
+        else:
+            qr, dr, q_tot = [(0, 0)], [1], qt
+        qshape = [list(ql), list(SITE_QUANTA), [(-q[0], -q[1]) for q in qr]]
+        dshape = [list(dl), [1] * 4, list(dr)]
+        t = Tensor.create(ctx, q_tot, qshape, dshape)
+        t.upload(rng.standard_normal(t.nnz))
+        core.normalize(ctx, t)
+        wave[i] = t
+        ql, dl = qr, dr
+    renv: List[Optional[Tensor]] = [None] * N
+    lenv: List[Optional[Tensor]] = [None] * N
+    renv[N - 1] = _boundary(ctx)
+    wfnc = wave[N - 1]
+    for i in range(N - 1, 0, -1):
+        m2 = core.merge_cols(ctx, wfnc)
+        g, v = core.canonicalize(ctx, False, m2, M)
+        rmps = core.expand_cols(ctx, v, wfnc)
+        lm = core.gemm(ctx, 0, 0, 1.0, wave[i - 1], g, 3)
+        core.normalize(ctx, lm)
+        wfnc = lm
+        wave[i - 1] = lm
+        wave[i] = rmps
+        mR = core.compute_merged_operator(ctx, False, mpo[i], renv[i])
+        vm = core.merge_cols(ctx, rmps)
+        renv[i - 1] = core.renormalize(ctx, False, mR, vm, vm)
+    lenv[0] = _boundary(ctx)
+    return DeviceState(mpo, wave, lenv, renv, M)
+
+
+def bond_operands(ctx: Context, st: DeviceState, i: int):
+    """Merged operators and merged wavefunction of bond (i, i+1) in the state's current gauge."""
+    mL = core.compute_merged_operator(ctx, True, st.mpo[i], st.lenv[i])
+    mR = core.compute_merged_operator(ctx, False, st.mpo[i + 1], st.renv[i + 1])
+    psi = core.merge_wavefunction(ctx, st.mpo[i], st.mpo[i + 1], st.lenv[i], st.renv[i + 1], st.wave[i],
+                                  st.wave[i + 1])
+    return mL, mR, psi
+
+
+def advance_left(ctx: Context, st: DeviceState, stop: int):
+    """Move the orthogonality centre from site 0 to site ``stop`` by forward
+    canonicalisation without optimisation: at each bond U becomes the left site
+    tensor, s V^T joins the next site and the left block operator is renormalised."""
+    for i in range(stop):
+        mL = core.compute_merged_operator(ctx, True, st.mpo[i], st.lenv[i])
+        psi = core.merge_wavefunction(ctx, st.mpo[i], st.mpo[i + 1], st.lenv[i], st.renv[i + 1], st.wave[i],
+                                      st.wave[i + 1])
+        U, sV = core.canonicalize(ctx, True, psi, st.M)
+        st.lenv[i + 1] = core.renormalize(ctx, True, mL, U, U)
+        st.wave[i], st.wave[i + 1] = core.expand_wavefunction(ctx, st.mpo[i], st.mpo[i + 1], st.lenv[i],
+                                                              st.renv[i + 1], U, sV)
+
+
 @dataclass
 class SweepLog:
     energy: float

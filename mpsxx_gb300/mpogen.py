@@ -139,3 +139,312 @@ def hubbard_mpo(L: int, t, U) -> List[dict]:
 
 def mpo_bond_dims(mpo: List[dict]) -> List[int]:
     return [len(s["qshape"][3]) for s in mpo]
+
+
+# ---------------------------------------------------------------------------
+# Generic sum-of-products -> MPO (quantum-chemistry Hamiltonians)
+# ---------------------------------------------------------------------------
+#
+# A term is a product of spin-orbital creation/annihilation operators.  Each term
+# is brought to site order (sign from the fermionic reordering), operators on the
+# same site are fused into one 4x4 site operator, and the MPO is grown from the
+# left: at site k every term is (left bond operator a, site operator o, rest of
+# the string); the bipartite graph between distinct (a, o) and distinct rests is
+# covered by a minimum vertex cover (Konig's theorem).  A covered (a, o) becomes a
+# new bond operator "a * o"; a covered rest r becomes the complementary operator
+# sum_c c (a * o) over its uncovered edges.  Both are exact, so the MPO represents
+# the Hamiltonian exactly; the cover keeps the bond dimension minimal for the cut.
+
+ELEM = {"Ca": _op_matrix("Ca"), "Cb": _op_matrix("Cb"), "Da": _op_matrix("Da"), "Db": _op_matrix("Db")}
+ELEM_Q = {"Ca": (1, 1), "Cb": (1, -1), "Da": (-1, -1), "Db": (-1, 1)}
+
+
+class _SiteOps:
+    """Canonical site operators: matrix normalised so its first non-zero is +1."""
+
+    def __init__(self):
+        self.mats: List[np.ndarray] = [_op_matrix("I")]
+        self.q: List[Tuple[int, int]] = [(0, 0)]
+        self.index: Dict[bytes, int] = {self.mats[0].tobytes(): 0}
+        self.cache: Dict[Tuple[str, ...], Tuple[int, float]] = {(): (0, 1.0)}
+
+    def get(self, seq: Tuple[str, ...]):
+        hit = self.cache.get(seq)
+        if hit is not None:
+            return hit
+        m = np.eye(4)
+        q = (0, 0)
+        for e in seq:
+            m = m @ ELEM[e]
+            q = (q[0] + ELEM_Q[e][0], q[1] + ELEM_Q[e][1])
+        nz = np.flatnonzero(np.abs(m) > 0)
+        if nz.size == 0:
+            self.cache[seq] = (-1, 0.0)
+            return self.cache[seq]
+        scale = float(m.flat[nz[0]])
+        mn = m / scale
+        key = mn.tobytes()
+        idx = self.index.get(key)
+        if idx is None:
+            idx = len(self.mats)
+            self.index[key] = idx
+            self.mats.append(mn)
+            self.q.append(q)
+        self.cache[seq] = (idx, scale)
+        return idx, scale
+
+
+def _site_order(ops):
+    """Stable sort of (site, elem) by site with the fermionic sign of the permutation."""
+    ops = list(ops)
+    sign = 1.0
+    # insertion sort counting transpositions of operators on different sites
+    for i in range(1, len(ops)):
+        j = i
+        while j > 0 and ops[j - 1][0] > ops[j][0]:
+            ops[j - 1], ops[j] = ops[j], ops[j - 1]
+            sign = -sign
+            j -= 1
+    return ops, sign
+
+
+def _fuse(ops, sops: _SiteOps):
+    """Site-ordered elementary ops -> ((site, siteop), ...) and a scale."""
+    out = []
+    scale = 1.0
+    i = 0
+    while i < len(ops):
+        s = ops[i][0]
+        seq = []
+        while i < len(ops) and ops[i][0] == s:
+            seq.append(ops[i][1])
+            i += 1
+        idx, sc = sops.get(tuple(seq))
+        if idx < 0:
+            return None, 0.0
+        scale *= sc
+        if idx != 0:
+            out.append((s, idx))
+    return tuple(out), scale
+
+
+def terms_to_strings(nsite: int, terms, sops: _SiteOps):
+    """[(coef, [(site, elem), ...]), ...] -> {((site, siteop), ...): coef}."""
+    acc: Dict[tuple, float] = {}
+    for coef, ops in terms:
+        if coef == 0.0:
+            continue
+        so, sign = _site_order(ops)
+        key, sc = _fuse(so, sops)
+        if key is None:
+            continue
+        acc[key] = acc.get(key, 0.0) + coef * sign * sc
+    return {k: v for k, v in acc.items() if v != 0.0}
+
+
+def _min_vertex_cover(nl: int, nr: int, edges_l: np.ndarray, edges_r: np.ndarray):
+    """Minimum vertex cover of a bipartite graph (Konig), returns (left mask, right mask)."""
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import maximum_bipartite_matching
+
+    g = sp.csr_matrix((np.ones(edges_l.size, dtype=np.int8), (edges_l, edges_r)), shape=(nl, nr))
+    g.sum_duplicates()
+    match_r = maximum_bipartite_matching(g, perm_type="column")  # left -> right or -1
+    match_l_of_r = np.full(nr, -1, dtype=np.int64)
+    for u, v in enumerate(match_r):
+        if v >= 0:
+            match_l_of_r[v] = u
+    indptr, indices = g.indptr, g.indices
+    visited_l = np.zeros(nl, dtype=bool)
+    visited_r = np.zeros(nr, dtype=bool)
+    stack = [u for u in range(nl) if match_r[u] < 0]
+    for u in stack:
+        visited_l[u] = True
+    while stack:
+        u = stack.pop()
+        for v in indices[indptr[u]:indptr[u + 1]]:
+            if visited_r[v] or match_r[u] == v:
+                continue
+            visited_r[v] = True
+            w = match_l_of_r[v]
+            if w >= 0 and not visited_l[w]:
+                visited_l[w] = True
+                stack.append(w)
+    return ~visited_l, visited_r
+
+
+def mpo_from_strings(nsite: int, strings: Dict[tuple, float], sops: _SiteOps) -> List[dict]:
+    """Exact MPO of sum_s coef_s * prod_k o_{s,k} (site-ordered, fused strings)."""
+    # current terms: (alpha, rest) -> coef, rest = ((site, op), ...) with sites >= k
+    cur: Dict[Tuple[int, tuple], float] = {}
+    for key, c in strings.items():
+        k2 = (0, key)
+        cur[k2] = cur.get(k2, 0.0) + c
+    q_left = [(0, 0)]
+    sites = []
+    for k in range(nsite):
+        lnodes: Dict[Tuple[int, int], int] = {}
+        rnodes: Dict[tuple, int] = {}
+        el, er, ec = [], [], []
+        for (alpha, rest), c in cur.items():
+            if rest and rest[0][0] == k:
+                o, r = rest[0][1], rest[1:]
+            else:
+                o, r = 0, rest
+            lk = (alpha, o)
+            li = lnodes.setdefault(lk, len(lnodes))
+            ri = rnodes.setdefault(r, len(rnodes))
+            el.append(li)
+            er.append(ri)
+            ec.append(c)
+        el = np.asarray(el, dtype=np.int64)
+        er = np.asarray(er, dtype=np.int64)
+        ec = np.asarray(ec, dtype=np.float64)
+        llist = list(lnodes.keys())
+        rlist = list(rnodes.keys())
+        if k == nsite - 1:
+            cover_l = np.zeros(len(llist), dtype=bool)
+            cover_r = np.ones(len(rlist), dtype=bool)
+        else:
+            cover_l, cover_r = _min_vertex_cover(len(llist), len(rlist), el, er)
+        # new bond operators: covered left nodes first (in node order), then covered rests
+        new_ops: List[Tuple[str, object]] = []
+        beta_of_l = {}
+        for li in np.flatnonzero(cover_l):
+            beta_of_l[int(li)] = len(new_ops)
+            new_ops.append(("l", int(li)))
+        beta_of_r = {}
+        for ri in np.flatnonzero(cover_r):
+            beta_of_r[int(ri)] = len(new_ops)
+            new_ops.append(("r", int(ri)))
+        # charges of new operators
+        def lq(li):
+            a, o = llist[li]
+            qa = q_left[a]
+            qo = sops.q[o]
+            return (qa[0] + qo[0], qa[1] + qo[1])
+
+        q_new = []
+        wentries: Dict[Tuple[int, int, int], float] = {}
+        nxt: Dict[Tuple[int, tuple], float] = {}
+        for kind, idx in new_ops:
+            if kind == "l":
+                q_new.append(lq(idx))
+        # covered rests: charge from any incident edge
+        r_charge = {}
+        for e in range(el.size):
+            li, ri = int(el[e]), int(er[e])
+            if li in beta_of_l:
+                b = beta_of_l[li]
+                a, o = llist[li]
+                wentries[(a, o, b)] = 1.0
+                key = (b, rlist[ri])
+                nxt[key] = nxt.get(key, 0.0) + ec[e]
+            else:
+                b = beta_of_r[ri]
+                a, o = llist[li]
+                wentries[(a, o, b)] = wentries.get((a, o, b), 0.0) + ec[e]
+                r_charge[ri] = lq(li)
+                key = (b, rlist[ri])
+                nxt[key] = 1.0
+        for kind, idx in new_ops:
+            if kind == "r":
+                q_new.append(r_charge[idx])
+        W = SiteMPO(q_left, q_new)
+        for (a, o, b), c in wentries.items():
+            if c != 0.0:
+                W.add(a, sops.mats[o], b, c)
+        sites.append(W.to_dict())
+        q_left = q_new
+        cur = {}
+        for (b, r), c in nxt.items():
+            if c != 0.0:
+                cur[(b, r)] = c
+    return sites
+
+
+def qc_terms(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0, tol: float = 0.0):
+    """H = E0 + sum h_pq a+_ps a_qs + 1/2 sum (pq|rs) a+_ps a+_rt a_st a_qs (chemists' notation)."""
+    n = h1.shape[0]
+    C = ("Ca", "Cb")
+    D = ("Da", "Db")
+    terms = []
+    if ecore != 0.0:
+        terms.append((ecore, []))
+    for p in range(n):
+        for q in range(n):
+            v = h1[p, q]
+            if abs(v) <= tol:
+                continue
+            for s in range(2):
+                terms.append((v, [(p, C[s]), (q, D[s])]))
+    nz = np.argwhere(np.abs(eri) > tol)
+    for p, q, r, s in nz:
+        v = 0.5 * eri[p, q, r, s]
+        for a in range(2):
+            for b in range(2):
+                if p == r and a == b:
+                    continue
+                if s == q and a == b:
+                    continue
+                terms.append((v, [(p, C[a]), (r, C[b]), (s, D[b]), (q, D[a])]))
+    return terms
+
+
+def qc_mpo(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0) -> List[dict]:
+    """Exact quantum-chemistry MPO with spatial-orbital sites."""
+    sops = _SiteOps()
+    strings = terms_to_strings(h1.shape[0], qc_terms(h1, eri, ecore), sops)
+    return mpo_from_strings(h1.shape[0], strings, sops)
+
+
+def synthetic_qc_integrals(n: int, K: int, seed: int):
+    """Synthetic integrals: h_pp ~ U(-3,-0.5) sorted ascending, h_pq ~ N(0,0.1^2) e^{-|p-q|/4}
+    symmetrised; (pq|rs) = sum_K L^K_pq L^K_rs with L^K_pq ~ N(0,0.1^2) e^{-|p-q|/4}
+    symmetrised and +0.3 on L^p_pp (p < min(n, K)): 8-fold symmetric and PSD."""
+    rng = np.random.default_rng(seed)
+    idx = np.arange(n)
+    decay = np.exp(-np.abs(idx[:, None] - idx[None, :]) / 4.0)
+    hd = np.sort(rng.uniform(-3.0, -0.5, size=n))
+    off = rng.normal(0.0, 0.1, size=(n, n)) * decay
+    h = 0.5 * (off + off.T)
+    h[idx, idx] = hd
+    Lk = rng.normal(0.0, 0.1, size=(K, n, n)) * decay[None]
+    Lk = 0.5 * (Lk + Lk.transpose(0, 2, 1))
+    for p in range(min(n, K)):
+        Lk[p, p, p] += 0.3
+    eri = np.einsum("kpq,krs->pqrs", Lk, Lk)
+    return h, eri
+
+
+def read_fcidump(path: str):
+    """FCIDUMP reader: unique integrals unfolded with 8-fold symmetry, core energy from
+    the 0 0 0 0 line (same convention as src/parsing_integral.cpp:105-154)."""
+    import re
+
+    with open(path) as f:
+        txt = f.read()
+    head, body = re.split(r"(?:&END|/)\s*\n", txt, maxsplit=1)
+    norb = int(re.search(r"NORB\s*=\s*(\d+)", head).group(1))
+    nelec = int(re.search(r"NELEC\s*=\s*(\d+)", head).group(1))
+    ms2m = re.search(r"MS2\s*=\s*(-?\d+)", head)
+    ms2 = int(ms2m.group(1)) if ms2m else 0
+    h = np.zeros((norb, norb))
+    g = np.zeros((norb, norb, norb, norb))
+    e0 = 0.0
+    for line in body.splitlines():
+        f_ = line.split()
+        if len(f_) < 5:
+            continue
+        v = float(f_[0])
+        i, j, k, l = (int(x) for x in f_[1:5])
+        if i == 0 and j == 0 and k == 0 and l == 0:
+            e0 = v
+        elif k == 0 and l == 0:
+            h[i - 1, j - 1] = h[j - 1, i - 1] = v
+        else:
+            i, j, k, l = i - 1, j - 1, k - 1, l - 1
+            for a, b, c, d in ((i, j, k, l), (j, i, k, l), (i, j, l, k), (j, i, l, k),
+                               (k, l, i, j), (l, k, i, j), (k, l, j, i), (l, k, j, i)):
+                g[a, b, c, d] = v
+    return {"norb": norb, "nelec": nelec, "ms2": ms2, "h1": h, "eri": g, "ecore": e0}
