@@ -108,6 +108,7 @@ static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a,
   plan.h_tiles.clear();
   plan.h_tasks.clear();
   plan.h_pairs.clear();
+  plan.h_reduce.clear();
   plan.flops = 0.0;
   plan.c_elems = 0;
   const int L = a.sh.rank, M = b.sh.rank;
@@ -158,11 +159,49 @@ static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a,
     }
     dt.p1 = static_cast<int>(plan.h_pairs.size());
     if (dt.p1 == dt.p0) continue;
-    const int ti = static_cast<int>(plan.h_tasks.size());
     plan.h_tasks.push_back(dt);
     plan.c_elems += int64_t(c.m) * c.n;
-    for (int tm = 0; tm * kGemmTile < c.m; ++tm)
-      for (int tn = 0; tn * kGemmTile < c.n; ++tn) plan.h_tiles.push_back(DTile{ti, tm, tn, 0});
+  }
+  // tiles; split the pair list of long tasks (split-K) so that the launch fills
+  // the GPU: work of a tile ~ sum of its pairs' k
+  double total = 0.0;
+  for (const auto& dt : plan.h_tasks) {
+    double k = 0.0;
+    for (int p = dt.p0; p < dt.p1; ++p) k += plan.h_pairs[p].k;
+    const double ntile = double((dt.m + kGemmTile - 1) / kGemmTile) * ((dt.n + kGemmTile - 1) / kGemmTile);
+    total += ntile * k;
+  }
+  const double target = std::max(1.0, total / kTargetCtas);
+  plan.nslots = 0;
+  for (int ti = 0; ti < static_cast<int>(plan.h_tasks.size()); ++ti) {
+    const DGemmTask& dt = plan.h_tasks[ti];
+    double k = 0.0;
+    for (int p = dt.p0; p < dt.p1; ++p) k += plan.h_pairs[p].k;
+    const int npair = dt.p1 - dt.p0;
+    int nchunk = static_cast<int>(std::min<double>(npair, std::floor(k / target)));
+    if (nchunk < 2) nchunk = 1;
+    // chunk boundaries with about equal k
+    std::vector<int> bnd{dt.p0};
+    if (nchunk > 1) {
+      double acc = 0.0, step = k / nchunk;
+      for (int p = dt.p0; p < dt.p1 && static_cast<int>(bnd.size()) < nchunk; ++p) {
+        acc += plan.h_pairs[p].k;
+        if (acc >= step * bnd.size() && p + 1 < dt.p1) bnd.push_back(p + 1);
+      }
+    }
+    bnd.push_back(dt.p1);
+    const int nc = static_cast<int>(bnd.size()) - 1;
+    for (int tm = 0; tm * kGemmTile < dt.m; ++tm)
+      for (int tn = 0; tn * kGemmTile < dt.n; ++tn) {
+        if (nc == 1) {
+          plan.h_tiles.push_back(DTile{ti, tm, tn, bnd[0], bnd[1], -1});
+          continue;
+        }
+        const int slot0 = plan.nslots;
+        for (int ch = 0; ch < nc; ++ch) plan.h_tiles.push_back(DTile{ti, tm, tn, bnd[ch], bnd[ch + 1], slot0 + ch});
+        plan.nslots += nc;
+        plan.h_reduce.push_back(DReduce{ti, tm, tn, slot0, nc, 0});
+      }
   }
 }
 
@@ -187,11 +226,22 @@ void GemmPlan::upload(cudaStream_t st) {
   tiles.upload(h_tiles, st);
   dtasks.upload(h_tasks, st);
   pairs.upload(h_pairs, st);
+  reduce.upload(h_reduce, st);
 }
 
-void GemmPlan::run(double alpha, const double* A, const double* B, double* C, cudaStream_t st) const {
+void GemmPlan::run(double alpha, const double* A, const double* B, double* C, double* partial,
+                   cudaStream_t st) const {
+  if (nslots > 0 && partial == nullptr) throw Error(kInternal, "gemm plan: split-K scratch missing");
   launch_gemm_f64(ta, tb, alpha, A, B, C, tiles.get(), static_cast<int>(h_tiles.size()), dtasks.get(), pairs.get(),
-                  st);
+                  partial, st);
+  if (nslots > 0)
+    launch_gemm_reduce(reduce.get(), static_cast<int>(h_reduce.size()), dtasks.get(), alpha, partial, C, st);
+}
+
+static double* gemm_scratch(Context& ctx, const GemmPlan& p) {
+  if (p.nslots == 0) return nullptr;
+  ctx.gemm_part.ensure(p.partial_bytes());
+  return ctx.gemm_part.as<double>();
 }
 
 // Result tensor whose blocks are exactly the task results (a Gemm into an empty array).
@@ -263,8 +313,10 @@ static void sigma_run(Context& ctx, const SigmaPlan& p, const DTensor& L, const 
   ctx.scr1.ensure(std::max<int64_t>(p.scr1.nnz, 1) * sizeof(double));
   double* scr = ctx.scr1.as<double>();
   if (p.scr1.nnz) cuda_check(cudaMemsetAsync(scr, 0, p.scr1.nnz * sizeof(double), ctx.stream), "scr1 zero");
-  p.s1.run(1.0, L.d, psi, scr, ctx.stream);
-  p.s2.run(1.0, scr, R.d, sigma, ctx.stream);
+  ctx.gemm_part.ensure(std::max(p.s1.partial_bytes(), p.s2.partial_bytes()));
+  double* part = ctx.gemm_part.as<double>();
+  p.s1.run(1.0, L.d, psi, scr, part, ctx.stream);
+  p.s2.run(1.0, scr, R.d, sigma, part, ctx.stream);
   ctx.kernel_launches += 2;
   ctx.sigma_flops += p.flops;
   ctx.sigma_calls += 1;
@@ -395,8 +447,9 @@ std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& 
   ctx.scr2.ensure(std::max<int64_t>(scr.nnz, 1) * sizeof(double));
   double* sp = ctx.scr2.as<double>();
   if (scr.nnz) cuda_check(cudaMemsetAsync(sp, 0, scr.nnz * sizeof(double), ctx.stream), "renorm scr zero");
-  p1.run(1.0, bra.d, opr0.d, sp, ctx.stream);
-  p2.run(1.0, sp, ket.d, out->d, ctx.stream);
+  ctx.gemm_part.ensure(std::max(p1.partial_bytes(), p2.partial_bytes()));
+  p1.run(1.0, bra.d, opr0.d, sp, ctx.gemm_part.as<double>(), ctx.stream);
+  p2.run(1.0, sp, ket.d, out->d, ctx.gemm_part.as<double>(), ctx.stream);
   ctx.kernel_launches += 2;
   // plans (device task arrays) must outlive the kernels
   ctx.sync();
@@ -581,7 +634,7 @@ std::unique_ptr<DTensor> merge_wave(Context& ctx, const WaveMerge& wm, const DTe
   plan.upload(ctx.stream);
   psi->ctx = &ctx;
   psi->alloc_device(ctx.stream, true);
-  plan.run(1.0, lwfn.d, rwfn.d, psi->d, ctx.stream);
+  plan.run(1.0, lwfn.d, rwfn.d, psi->d, gemm_scratch(ctx, plan), ctx.stream);
   ctx.kernel_launches += 1;
   ctx.sync();
   return psi;
@@ -766,7 +819,7 @@ std::unique_ptr<DTensor> gemm_new(Context& ctx, Trans ta, Trans tb, double alpha
   plan.upload(ctx.stream);
   c->ctx = &ctx;
   c->alloc_device(ctx.stream, true);
-  plan.run(alpha, a.d, b.d, c->d, ctx.stream);
+  plan.run(alpha, a.d, b.d, c->d, gemm_scratch(ctx, plan), ctx.stream);
   ctx.kernel_launches += 1;
   ctx.sync();
   return c;

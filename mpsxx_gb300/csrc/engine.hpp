@@ -55,14 +55,22 @@ struct GemmPlan {
   std::vector<DTile> h_tiles;
   std::vector<DGemmTask> h_tasks;
   std::vector<DGemmPair> h_pairs;
+  std::vector<DReduce> h_reduce;
   DevArray<DTile> tiles;
   DevArray<DGemmTask> dtasks;
   DevArray<DGemmPair> pairs;
+  DevArray<DReduce> reduce;
+  int nslots = 0;  // split-K partial tiles
   double flops = 0.0;
   int64_t c_elems = 0;  // elements of C touched (for traffic accounting)
   void upload(cudaStream_t st);
-  void run(double alpha, const double* A, const double* B, double* C, cudaStream_t st) const;
+  // partial: nslots * 64 * 64 doubles of scratch (may be null when nslots == 0)
+  void run(double alpha, const double* A, const double* B, double* C, double* partial, cudaStream_t st) const;
+  size_t partial_bytes() const { return size_t(nslots) * kGemmTile * kGemmTile * sizeof(double); }
 };
+
+// target number of CTAs a grouped GEMM is split into (a few waves on 152 SMs)
+constexpr int kTargetCtas = 152 * 8;
 
 // GEMM plan into a C whose layout is `c` (block offsets).  C blocks may be
 // sub-blocks of a larger block when `cmap` is provided (fused merges).
@@ -105,6 +113,7 @@ struct Context {
   DevBuf scalars;    // small device scalars
   DevBuf svd_work;   // solver workspace
   DevBuf svd_mats;   // per-block SVD matrices
+  DevBuf gemm_part;  // split-K partial tiles
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<SigmaPlan>> sigma_plans;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<DiagPlan>> diag_plans;
   // counters for measurement

@@ -18,9 +18,15 @@ struct DGemmPair {
   int64_t a_off, b_off;
   int k, lda, ldb, pad;
 };
-// One output tile of a task.
+// One output tile of a task over the pair range [p0, p1).  slot < 0: the tile
+// adds its result into C; slot >= 0: it writes a 64x64 partial that a fixed-order
+// reduction adds into C (split-K for tasks with long pair lists).
 struct DTile {
-  int task, tm, tn, pad;
+  int task, tm, tn, p0, p1, slot;
+};
+// Reduction of the split partials of one output tile.
+struct DReduce {
+  int task, tm, tn, slot0, nslot, pad;
 };
 
 // Dense 2-D block copy: dst[r*dld + c] (+)= scale * src[r*sld + c].
@@ -52,7 +58,9 @@ constexpr int kGemmTile = 64;
 
 void launch_gemm_f64(int transa, int transb, double alpha, const double* A, const double* B, double* C,
                      const DTile* tiles, int ntiles, const DGemmTask* tasks, const DGemmPair* pairs,
-                     cudaStream_t st);
+                     double* partial, cudaStream_t st);
+void launch_gemm_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
+                        double* C, cudaStream_t st);
 void launch_copy(const DCopy* tasks, int ntasks, const double* src, double* dst, int accumulate,
                  cudaStream_t st);
 void launch_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* src, double* dst,

@@ -22,7 +22,8 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(int transa, int transb, d
                                                        const double* __restrict__ A, const double* __restrict__ B,
                                                        double* __restrict__ C, const DTile* __restrict__ tiles,
                                                        const DGemmTask* __restrict__ tasks,
-                                                       const DGemmPair* __restrict__ pairs) {
+                                                       const DGemmPair* __restrict__ pairs,
+                                                       double* __restrict__ partial) {
   __shared__ double As[TK][TM + 1];
   __shared__ double Bs[TK][TN + 1];
   const DTile t = tiles[blockIdx.x];
@@ -35,7 +36,7 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(int transa, int transb, d
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
 
-  for (int p = task.p0; p < task.p1; ++p) {
+  for (int p = t.p0; p < t.p1; ++p) {
     const DGemmPair pr = pairs[p];
     for (int k0 = 0; k0 < pr.k; k0 += TK) {
       for (int e = threadIdx.x; e < TM * TK; e += 256) {
@@ -84,6 +85,15 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(int transa, int transb, d
       __syncthreads();
     }
   }
+  if (t.slot >= 0) {
+    // split-K partial: the full 64x64 tile, reduced later in chunk order
+    double* part = partial + (int64_t)t.slot * (TM * TN);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) part[(ty + 16 * i) * TN + tx + 16 * j] = acc[i][j];
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int r = m0 + ty + 16 * i;
@@ -95,6 +105,22 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(int transa, int transb, d
       double* dst = C + task.c_off + (int64_t)r * task.ldc + c;
       *dst += alpha * acc[i][j];
     }
+  }
+}
+
+__global__ void __launch_bounds__(256) gemm_reduce_kernel(const DReduce* __restrict__ red,
+                                                          const DGemmTask* __restrict__ tasks, double alpha,
+                                                          const double* __restrict__ partial,
+                                                          double* __restrict__ C) {
+  const DReduce rd = red[blockIdx.x];
+  const DGemmTask task = tasks[rd.task];
+  const int m0 = rd.tm * TM, n0 = rd.tn * TN;
+  for (int e = threadIdx.x; e < TM * TN; e += blockDim.x) {
+    const int r = m0 + e / TN, c = n0 + e % TN;
+    if (r >= task.m || c >= task.n) continue;
+    double s = 0.0;
+    for (int k = 0; k < rd.nslot; ++k) s += partial[(int64_t)(rd.slot0 + k) * (TM * TN) + e];
+    C[task.c_off + (int64_t)r * task.ldc + c] += alpha * s;
   }
 }
 
@@ -275,9 +301,15 @@ inline int grid_for(int64_t n) {
 
 void launch_gemm_f64(int transa, int transb, double alpha, const double* A, const double* B, double* C,
                      const DTile* tiles, int ntiles, const DGemmTask* tasks, const DGemmPair* pairs,
-                     cudaStream_t st) {
+                     double* partial, cudaStream_t st) {
   if (ntiles <= 0) return;
-  gemm_f64_kernel<<<ntiles, 256, 0, st>>>(transa, transb, alpha, A, B, C, tiles, tasks, pairs);
+  gemm_f64_kernel<<<ntiles, 256, 0, st>>>(transa, transb, alpha, A, B, C, tiles, tasks, pairs, partial);
+}
+
+void launch_gemm_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
+                        double* C, cudaStream_t st) {
+  if (nred <= 0) return;
+  gemm_reduce_kernel<<<nred, 256, 0, st>>>(red, tasks, alpha, partial, C);
 }
 
 void launch_copy(const DCopy* tasks, int ntasks, const double* src, double* dst, int accumulate, cudaStream_t st) {
