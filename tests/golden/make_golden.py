@@ -50,6 +50,12 @@ def main():
                                        "energies": sweep_energies_from_log(os.path.join(tests, "twodot.out"))}
         out["INTGEN6_M200"] = {"source": "dmrg/tests/dmrg.out",
                                "energies": sweep_energies_from_log(os.path.join(tests, "dmrg.out"))[-1:]}
+        # integral lines of the 16-orbital FCIDUMP that intgen.cpp wrote (header and core line excluded)
+        import hashlib
+
+        body = open(os.path.join(tests, "FCIDUMP")).read().splitlines()[4:-1]
+        out["INTGEN16_FCIDUMP"] = {"source": "dmrg/tests/FCIDUMP", "lines": len(body),
+                                   "sha256": hashlib.sha256("".join(l + "\n" for l in body).encode()).hexdigest()}
     # HUBBARD12: U=1, h_{i+1,i}=+1, 12 electrons (dmrg/tests/HUBBARD12)
     t0 = time.time()
     mpo = [from_site_dict(s) for s in hubbard_mpo(12, 1.0, 1.0)]
@@ -59,6 +65,8 @@ def main():
     out["HUBBARD12_exact"] = {"energy": float(hubbard_ground_energy(12, 1.0, 1.0, 6, 6)[0])}
     with open(os.path.join(HERE, "reference_energies.json"), "w") as f:
         json.dump(out, f, indent=1)
+    if "--reference-only" in sys.argv:
+        return
     # config: Hubbard L=12, U=4, M=64, 4 sweeps, tole 1e-10
     mpo = [from_site_dict(s) for s in hubbard_mpo(12, -1.0, 4.0)]
     st = od.make_initial_state(mpo, 12, 0, 64)

@@ -1,0 +1,104 @@
+"""The oracle against exact answers and the reference's own golden vectors (CPU)."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def golden(name):
+    return json.load(open(os.path.join(HERE, "golden", name)))
+
+
+def oracle_dmrg(mpo_dicts, n_elec, two_sz, M, tole, sweeps):
+    from oracle import dmrg as od
+    from oracle import from_site_dict
+
+    st, logs = od.dmrg([from_site_dict(s) for s in mpo_dicts], n_elec, two_sz, M, tole, sweeps)
+    return logs[-1].energy
+
+
+def test_hubbard_chain_matches_exact_diagonalisation():
+    from oracle.ed import hubbard_ground_energy
+    from mpsxx_gb300.mpogen import hubbard_mpo
+
+    e = oracle_dmrg(hubbard_mpo(6, -1.0, 4.0), 6, 0, 64, 1e-10, 8)
+    assert abs(e - hubbard_ground_energy(6, -1.0, 4.0, 3, 3)[0]) < 1e-10
+
+
+def test_site_dependent_hubbard_matches_exact_diagonalisation():
+    from oracle.ed import hubbard_ground_energy
+    from mpsxx_gb300.mpogen import hubbard_mpo
+
+    rng = np.random.default_rng(3)
+    t = rng.uniform(0.8, 1.2, 5)
+    U = rng.uniform(2.0, 6.0, 6)
+    e = oracle_dmrg(hubbard_mpo(6, t, U), 6, 0, 64, 1e-10, 8)
+    assert abs(e - hubbard_ground_energy(6, t, U, 3, 3)[0]) < 1e-10
+
+
+@pytest.mark.parametrize("n,nel,two_sz", [(4, 4, 0), (5, 4, 2), (6, 6, 0)])
+def test_qc_hamiltonian_matches_exact_diagonalisation(n, nel, two_sz):
+    from oracle.ed import qc_ground_energy
+    from mpsxx_gb300 import mpogen
+
+    h, eri = mpogen.synthetic_qc_integrals(n, 2 * n, 11 + n)
+    e = oracle_dmrg(mpogen.qc_mpo(h, eri, 0.37), nel, two_sz, 256, 1e-10, 10)
+    ref = qc_ground_energy(h, eri, (nel + two_sz) // 2, (nel - two_sz) // 2, ecore=0.37)[0]
+    assert abs(e - ref) < 1e-9
+
+
+def test_generic_mpo_builder_finds_the_hubbard_bond_dimension():
+    from mpsxx_gb300 import mpogen
+
+    n = 7
+    h = np.zeros((n, n))
+    for i in range(n - 1):
+        h[i, i + 1] = h[i + 1, i] = -1.0
+    eri = np.zeros((n, n, n, n))
+    for i in range(n):
+        eri[i, i, i, i] = 4.0
+    assert mpogen.mpo_bond_dims(mpogen.qc_mpo(h, eri))[:-1] == [6] * (n - 1)
+
+
+def test_hubbard12_reference_golden_energy():
+    """dmrg/tests/HUBBARD12 (U=1, h_{i+1,i}=+1, 12 electrons), M=200: the reference's
+    log holds -11.8406372775523305 (hub12_dmrg.out:15536); the oracle lands within
+    1e-8 of it and both lie above the exact ground state."""
+    from mpsxx_gb300.mpogen import hubbard_mpo
+
+    g = golden("reference_energies.json")
+    ref = float(g["HUBBARD12_M200_roots"]["energies"][0])
+    exact = g["HUBBARD12_exact"]["energy"]
+    e = oracle_dmrg(hubbard_mpo(12, 1.0, 1.0), 12, 0, 200, 1e-8, 10)
+    assert abs(e - ref) < 1e-8
+    assert e >= exact - 1e-12 and ref >= exact - 1e-12
+    assert abs(e - g["HUBBARD12_M200_oracle"]["energy"]) < 1e-10
+
+
+def test_reference_random_integral_generator_is_reproduced():
+    """dmrg/tests/intgen.cpp restated: its 16-orbital FCIDUMP is reproduced bit-exactly
+    (sha256 of the integral lines recorded from the reference's file)."""
+    from tests.golden.intgen import intgen
+
+    g = golden("reference_energies.json")["INTGEN16_FCIDUMP"]
+    _, _, lines = intgen(16)
+    txt = "".join(f"{v:24.16e}{i:4d}{j:4d}{k:4d}{l:4d}\n" for v, i, j, k, l in lines)
+    assert hashlib.sha256(txt.encode()).hexdigest() == g["sha256"]
+    assert len(lines) == g["lines"]
+
+
+def test_hubbard12_u4_m64_fixture_first_sweeps():
+    """Regression: the first two sweeps of the committed L=12, U=4, M=64 fixture."""
+    from oracle import dmrg as od
+    from oracle import from_site_dict
+    from mpsxx_gb300.mpogen import hubbard_mpo
+
+    g = golden("hubbard12_u4_m64.json")
+    st = od.make_initial_state([from_site_dict(s) for s in hubbard_mpo(12, -1.0, 4.0)], 12, 0, 64)
+    for k in range(2):
+        log = od.make_sweep(st, g["tole"])
+        assert abs(log.energy - g["sweeps"][k]["energy"]) < 1e-12
