@@ -53,6 +53,17 @@ const char* mpsxx_last_error(void);
 int mpsxx_context_create(int device, void* stream, mpsxx_context** out);
 int mpsxx_context_destroy(mpsxx_context* ctx);
 int mpsxx_context_sync(mpsxx_context* ctx);
+/* Precision of the bulk contractions of this context (no reference counterpart:
+ * the reference computes in FP64 only).  MPSXX_FP64: every contraction in FP64.
+ * MPSXX_SPLIT_TF32: H_eff*psi runs on the tensor cores with each FP64 operand
+ * split into two TF32 numbers (3 products, FP32 accumulation per block pair,
+ * FP64 across pairs); Davidson subspace algebra, the Rayleigh-Ritz solve and
+ * residual norms stay FP64, and the accepted energy of every diagonalize call is
+ * the Rayleigh quotient of one FP64 H_eff*psi (refinement step). */
+enum mpsxx_precision { MPSXX_FP64 = 0, MPSXX_SPLIT_TF32 = 1 };
+int mpsxx_context_set_precision(mpsxx_context* ctx, int precision);
+int mpsxx_context_get_precision(const mpsxx_context* ctx, int* precision);
+
 /* Kernel launches issued, FP64-equivalent sigma FLOPs and sigma calls so far. */
 int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* sigma_flops, int64_t* sigma_calls);
 
@@ -126,8 +137,10 @@ int mpsxx_canonicalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* wfnc
 
 /* One bond of the two-site sweep (src/optimize.hpp:495-651), single root and one
  * operator group: returns the Ritz value, the renormalised operator of the grown
- * block and the new site tensors.  stats (may be NULL, 8 doubles): n_sigma,
- * sigma FLOPs, t_merge, t_diag, t_davidson, t_svd, t_renorm, converged. */
+ * block and the new site tensors.  stats (may be NULL, 12 doubles): n_sigma,
+ * sigma FLOPs, t_merge, t_diag, t_davidson, t_svd, t_renorm, converged,
+ * Davidson |r|^2, Ritz value before refinement, FP64 |r|^2 after refinement,
+ * FP64 refinement applications (the last three are 0 in FP64 precision). */
 int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_tensor* lmpo,
                                   const mpsxx_tensor* rmpo, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                                   const mpsxx_tensor* lwfn, const mpsxx_tensor* rwfn, double tole, int M,

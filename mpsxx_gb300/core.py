@@ -309,14 +309,29 @@ def expand_wavefunction(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, 
     return Tensor(lo, ctx), Tensor(ro, ctx)
 
 
-BOND_STAT_KEYS = ("n_sigma", "sigma_flops", "t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "converged")
+BOND_STAT_KEYS = ("n_sigma", "sigma_flops", "t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "converged",
+                  "rnorm", "energy_split", "rnorm_fp64", "n_sigma_fp64")
+
+FP64 = 0
+SPLIT_TF32 = 1
+
+
+def set_precision(ctx: Context, precision: int):
+    """Bulk-contraction precision of the context: FP64 or SPLIT_TF32 (tensor cores)."""
+    check(lib().mpsxx_context_set_precision(ctx.h, int(precision)))
+
+
+def get_precision(ctx: Context) -> int:
+    v = C.c_int()
+    check(lib().mpsxx_context_get_precision(ctx.h, C.byref(v)))
+    return v.value
 
 
 def optimize_twosite_merged(ctx: Context, forward: bool, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor,
                             lwfn: Tensor, rwfn: Tensor, tole: float, M: int):
     e = C.c_double()
     env, nl, nr = _out(), _out(), _out()
-    st = (C.c_double * 8)()
+    st = (C.c_double * 12)()
     check(lib().mpsxx_optimize_twosite_merged(ctx.h, int(bool(forward)), lmpo.h, rmpo.h, lopr.h, ropr.h, lwfn.h,
                                               rwfn.h, float(tole), int(M), C.byref(e), C.byref(env), C.byref(nl),
                                               C.byref(nr), st))

@@ -97,6 +97,20 @@ int mpsxx_context_sync(mpsxx_context* ctx) {
   return guard([&] { ctx_of(ctx).sync(); });
 }
 
+int mpsxx_context_set_precision(mpsxx_context* ctx, int precision) {
+  return guard([&] {
+    need(precision == MPSXX_FP64 || precision == MPSXX_SPLIT_TF32, "unknown precision");
+    ctx_of(ctx).precision = precision;
+  });
+}
+
+int mpsxx_context_get_precision(const mpsxx_context* ctx, int* precision) {
+  return guard([&] {
+    need(ctx && ctx->ctx && precision, "null argument");
+    *precision = ctx->ctx->precision;
+  });
+}
+
 int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* sigma_flops, int64_t* sigma_calls) {
   return guard([&] {
     need(ctx && ctx->ctx, "null context");
@@ -285,6 +299,7 @@ int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, con
     need_device(S);
     compute_sigma_vector(c, L, R, P, S);
     c.sync();
+    if (c.precision != kFP64) check_device_error(c);
   });
 }
 
@@ -369,6 +384,10 @@ int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_t
       stats[5] = b.stats.t_svd;
       stats[6] = b.stats.t_renorm;
       stats[7] = b.stats.dav.converged;
+      stats[8] = b.stats.dav.rnorm;
+      stats[9] = b.stats.dav.energy_split;
+      stats[10] = b.stats.dav.rnorm_fp64;
+      stats[11] = b.stats.dav.n_sigma_fp64;
     }
     *env = wrap(std::move(b.env), ctx);
     *new_lwfn = wrap(std::move(b.lwfn), ctx);

@@ -98,6 +98,52 @@ struct CMap {
   int m, n, ldc;
 };
 
+// Output tiles of every task; the pair list of long tasks is split (split-K) so
+// that a launch fills the GPU: the work of a tile ~ the sum of its pairs' k.
+static void make_tiles(const GemmPlan& plan, int tile_m, int tile_n, std::vector<DTile>& tiles,
+                       std::vector<DReduce>& reduce, int& nslots) {
+  tiles.clear();
+  reduce.clear();
+  nslots = 0;
+  double total = 0.0;
+  for (const auto& dt : plan.h_tasks) {
+    double k = 0.0;
+    for (int p = dt.p0; p < dt.p1; ++p) k += plan.h_pairs[p].k;
+    total += double((dt.m + tile_m - 1) / tile_m) * ((dt.n + tile_n - 1) / tile_n) * k;
+  }
+  const double target = std::max(1.0, total / kTargetCtas);
+  for (int ti = 0; ti < static_cast<int>(plan.h_tasks.size()); ++ti) {
+    const DGemmTask& dt = plan.h_tasks[ti];
+    double k = 0.0;
+    for (int p = dt.p0; p < dt.p1; ++p) k += plan.h_pairs[p].k;
+    const int npair = dt.p1 - dt.p0;
+    int nchunk = static_cast<int>(std::min<double>(npair, std::floor(k / target)));
+    if (nchunk < 2) nchunk = 1;
+    // chunk boundaries with about equal k
+    std::vector<int> bnd{dt.p0};
+    if (nchunk > 1) {
+      double acc = 0.0, step = k / nchunk;
+      for (int p = dt.p0; p < dt.p1 && static_cast<int>(bnd.size()) < nchunk; ++p) {
+        acc += plan.h_pairs[p].k;
+        if (acc >= step * bnd.size() && p + 1 < dt.p1) bnd.push_back(p + 1);
+      }
+    }
+    bnd.push_back(dt.p1);
+    const int nc = static_cast<int>(bnd.size()) - 1;
+    for (int tm = 0; tm * tile_m < dt.m; ++tm)
+      for (int tn = 0; tn * tile_n < dt.n; ++tn) {
+        if (nc == 1) {
+          tiles.push_back(DTile{ti, tm, tn, bnd[0], bnd[1], -1});
+          continue;
+        }
+        const int slot0 = nslots;
+        for (int ch = 0; ch < nc; ++ch) tiles.push_back(DTile{ti, tm, tn, bnd[ch], bnd[ch + 1], slot0 + ch});
+        nslots += nc;
+        reduce.push_back(DReduce{ti, tm, tn, slot0, nc, 0});
+      }
+  }
+}
+
 template <class F>
 static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a, const Tensor& b, int K,
                             std::vector<GemmTaskRef>&& tasks, F cmap) {
@@ -162,47 +208,8 @@ static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a,
     plan.h_tasks.push_back(dt);
     plan.c_elems += int64_t(c.m) * c.n;
   }
-  // tiles; split the pair list of long tasks (split-K) so that the launch fills
-  // the GPU: work of a tile ~ sum of its pairs' k
-  double total = 0.0;
-  for (const auto& dt : plan.h_tasks) {
-    double k = 0.0;
-    for (int p = dt.p0; p < dt.p1; ++p) k += plan.h_pairs[p].k;
-    const double ntile = double((dt.m + kGemmTile - 1) / kGemmTile) * ((dt.n + kGemmTile - 1) / kGemmTile);
-    total += ntile * k;
-  }
-  const double target = std::max(1.0, total / kTargetCtas);
-  plan.nslots = 0;
-  for (int ti = 0; ti < static_cast<int>(plan.h_tasks.size()); ++ti) {
-    const DGemmTask& dt = plan.h_tasks[ti];
-    double k = 0.0;
-    for (int p = dt.p0; p < dt.p1; ++p) k += plan.h_pairs[p].k;
-    const int npair = dt.p1 - dt.p0;
-    int nchunk = static_cast<int>(std::min<double>(npair, std::floor(k / target)));
-    if (nchunk < 2) nchunk = 1;
-    // chunk boundaries with about equal k
-    std::vector<int> bnd{dt.p0};
-    if (nchunk > 1) {
-      double acc = 0.0, step = k / nchunk;
-      for (int p = dt.p0; p < dt.p1 && static_cast<int>(bnd.size()) < nchunk; ++p) {
-        acc += plan.h_pairs[p].k;
-        if (acc >= step * bnd.size() && p + 1 < dt.p1) bnd.push_back(p + 1);
-      }
-    }
-    bnd.push_back(dt.p1);
-    const int nc = static_cast<int>(bnd.size()) - 1;
-    for (int tm = 0; tm * kGemmTile < dt.m; ++tm)
-      for (int tn = 0; tn * kGemmTile < dt.n; ++tn) {
-        if (nc == 1) {
-          plan.h_tiles.push_back(DTile{ti, tm, tn, bnd[0], bnd[1], -1});
-          continue;
-        }
-        const int slot0 = plan.nslots;
-        for (int ch = 0; ch < nc; ++ch) plan.h_tiles.push_back(DTile{ti, tm, tn, bnd[ch], bnd[ch + 1], slot0 + ch});
-        plan.nslots += nc;
-        plan.h_reduce.push_back(DReduce{ti, tm, tn, slot0, nc, 0});
-      }
-  }
+  make_tiles(plan, kGemmTile, kGemmTile, plan.h_tiles, plan.h_reduce, plan.nslots);
+  make_tiles(plan, kTcTileM, kTcTileN, plan.h_tiles_tc, plan.h_reduce_tc, plan.nslots_tc);
 }
 
 void build_gemm_plan(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a, const Tensor& b, const Tensor& c, int K,
@@ -227,6 +234,17 @@ void GemmPlan::upload(cudaStream_t st) {
   dtasks.upload(h_tasks, st);
   pairs.upload(h_pairs, st);
   reduce.upload(h_reduce, st);
+  tiles_tc.upload(h_tiles_tc, st);
+  reduce_tc.upload(h_reduce_tc, st);
+}
+
+void GemmPlan::run_tc(double alpha, const double* A, const double* B, double* C, double* partial, int* err,
+                      cudaStream_t st) const {
+  if (nslots_tc > 0 && partial == nullptr) throw Error(kInternal, "gemm plan: split-K scratch missing");
+  launch_gemm_tc(ta, tb, alpha, A, B, C, tiles_tc.get(), static_cast<int>(h_tiles_tc.size()), dtasks.get(),
+                 pairs.get(), partial, err, st);
+  if (nslots_tc > 0)
+    launch_gemm_tc_reduce(reduce_tc.get(), static_cast<int>(h_reduce_tc.size()), dtasks.get(), alpha, partial, C, st);
 }
 
 void GemmPlan::run(double alpha, const double* A, const double* B, double* C, double* partial,
@@ -313,13 +331,43 @@ static void sigma_run(Context& ctx, const SigmaPlan& p, const DTensor& L, const 
   ctx.scr1.ensure(std::max<int64_t>(p.scr1.nnz, 1) * sizeof(double));
   double* scr = ctx.scr1.as<double>();
   if (p.scr1.nnz) cuda_check(cudaMemsetAsync(scr, 0, p.scr1.nnz * sizeof(double), ctx.stream), "scr1 zero");
-  ctx.gemm_part.ensure(std::max(p.s1.partial_bytes(), p.s2.partial_bytes()));
-  double* part = ctx.gemm_part.as<double>();
-  p.s1.run(1.0, L.d, psi, scr, part, ctx.stream);
-  p.s2.run(1.0, scr, R.d, sigma, part, ctx.stream);
-  ctx.kernel_launches += 2;
+  if (ctx.precision == kSplitTF32) {
+    ctx.gemm_part.ensure(std::max(p.s1.partial_bytes_tc(), p.s2.partial_bytes_tc()));
+    double* part = ctx.gemm_part.as<double>();
+    int* err = device_err_flag(ctx);
+    p.s1.run_tc(1.0, L.d, psi, scr, part, err, ctx.stream);
+    p.s2.run_tc(1.0, scr, R.d, sigma, part, err, ctx.stream);
+    ctx.kernel_launches += 2 + (p.s1.nslots_tc > 0) + (p.s2.nslots_tc > 0);
+  } else {
+    ctx.gemm_part.ensure(std::max(p.s1.partial_bytes(), p.s2.partial_bytes()));
+    double* part = ctx.gemm_part.as<double>();
+    p.s1.run(1.0, L.d, psi, scr, part, ctx.stream);
+    p.s2.run(1.0, scr, R.d, sigma, part, ctx.stream);
+    ctx.kernel_launches += 2 + (p.s1.nslots > 0) + (p.s2.nslots > 0);
+  }
   ctx.sigma_flops += p.flops;
   ctx.sigma_calls += 1;
+}
+
+// Device error flag of the tensor-core kernels (zeroed on first use).
+int* device_err_flag(Context& ctx) {
+  if (!ctx.err_flag.p) {
+    ctx.err_flag.ensure(sizeof(int));
+    cuda_check(cudaMemsetAsync(ctx.err_flag.p, 0, sizeof(int), ctx.stream), "err flag zero");
+  }
+  return ctx.err_flag.as<int>();
+}
+
+// Throws DEVICE_TIMEOUT when a tensor-core kernel gave up waiting for its MMAs.
+void check_device_error(Context& ctx) {
+  if (!ctx.err_flag.p) return;
+  int h = 0;
+  cuda_check(cudaMemcpyAsync(&h, ctx.err_flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream), "err d2h");
+  ctx.sync();
+  if (h) {
+    cuda_check(cudaMemsetAsync(ctx.err_flag.p, 0, sizeof(int), ctx.stream), "err flag reset");
+    throw Error(kDeviceTimeout, "tensor-core kernel: MMA completion wait timed out");
+  }
 }
 
 void compute_sigma_vector(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma) {
@@ -937,6 +985,36 @@ double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTens
   launch_copy_vec(wfnc.d, trial, n, st);
   normalize(wfnc.d);
   ctx.sync();
+  if (ctx.precision != kFP64) {
+    check_device_error(ctx);
+    // refinement: the accepted energy is the Rayleigh quotient of one FP64
+    // H_eff*psi of the (normalised) Davidson vector, and the FP64 residual is reported
+    const int saved = ctx.precision;
+    ctx.precision = kFP64;
+    cuda_check(cudaMemsetAsync(sigma, 0, n * sizeof(double), st), "sigma zero");
+    try {
+      sigma_run(ctx, sp, L, R, wfnc.d, sigma);
+    } catch (...) {
+      ctx.precision = saved;
+      throw;
+    }
+    ctx.precision = saved;
+    S.n_sigma_fp64 += 1;
+    launch_multidot(wfnc.d, 1, sigma, 1, n, n, sc + 103, part, nblk, st);
+    double e64 = 0.0;
+    cuda_check(cudaMemcpyAsync(&e64, sc + 103, sizeof(double), cudaMemcpyDeviceToHost, st), "e64 d2h");
+    ctx.sync();
+    launch_copy_vec(errv, sigma, n, st);
+    launch_axpy(errv, wfnc.d, n, -e64, st);
+    launch_multidot(errv, 1, errv, 1, n, n, sc + 104, part, nblk, st);
+    double r64 = 0.0;
+    cuda_check(cudaMemcpyAsync(&r64, sc + 104, sizeof(double), cudaMemcpyDeviceToHost, st), "r64 d2h");
+    ctx.sync();
+    ctx.kernel_launches += 7;
+    S.energy_split = eval;
+    S.rnorm_fp64 = r64;
+    eval = e64;
+  }
   return eval;
 }
 

@@ -61,13 +61,26 @@ struct GemmPlan {
   DevArray<DGemmPair> pairs;
   DevArray<DReduce> reduce;
   int nslots = 0;  // split-K partial tiles
+  // tensor-core (split TF32) tiling of the same tasks: 128 x 64 tiles
+  std::vector<DTile> h_tiles_tc;
+  std::vector<DReduce> h_reduce_tc;
+  DevArray<DTile> tiles_tc;
+  DevArray<DReduce> reduce_tc;
+  int nslots_tc = 0;
   double flops = 0.0;
   int64_t c_elems = 0;  // elements of C touched (for traffic accounting)
   void upload(cudaStream_t st);
   // partial: nslots * 64 * 64 doubles of scratch (may be null when nslots == 0)
   void run(double alpha, const double* A, const double* B, double* C, double* partial, cudaStream_t st) const;
+  // split TF32 tensor-core path; err: device flag set on an MMA wait timeout
+  void run_tc(double alpha, const double* A, const double* B, double* C, double* partial, int* err,
+              cudaStream_t st) const;
   size_t partial_bytes() const { return size_t(nslots) * kGemmTile * kGemmTile * sizeof(double); }
+  size_t partial_bytes_tc() const { return size_t(nslots_tc) * kTcTileM * kTcTileN * sizeof(double); }
 };
+
+// Precision of the bulk contractions (sigma, renormalize).
+enum Precision : int { kFP64 = 0, kSplitTF32 = 1 };
 
 // target number of CTAs a grouped GEMM is split into (a few waves on 152 SMs)
 constexpr int kTargetCtas = 152 * 8;
@@ -99,6 +112,9 @@ struct DavidsonStats {
   int micro = 0;
   double rnorm = 0.0;
   int converged = 0;
+  int n_sigma_fp64 = 0;       // FP64 refinement applications (split precision)
+  double energy_split = 0.0;  // Ritz value before refinement (split precision)
+  double rnorm_fp64 = 0.0;    // |H psi - E psi|^2 with the FP64 operator (split precision)
 };
 
 struct Context {
@@ -114,6 +130,8 @@ struct Context {
   DevBuf svd_work;   // solver workspace
   DevBuf svd_mats;   // per-block SVD matrices
   DevBuf gemm_part;  // split-K partial tiles
+  DevBuf err_flag;   // device error flag of the tensor-core kernels
+  int precision = kFP64;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<SigmaPlan>> sigma_plans;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<DiagPlan>> diag_plans;
   // counters for measurement
@@ -131,6 +149,9 @@ struct Context {
 // src/compute_sigma_vector.hpp:85-96: sigma += L psi R^T over (w, B').
 SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi);
 void compute_sigma_vector(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma);
+
+int* device_err_flag(Context& ctx);
+void check_device_error(Context& ctx);
 
 // average device seconds of `reps` sigma applications (CUDA events on ctx.stream)
 double sigma_device_time(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma,

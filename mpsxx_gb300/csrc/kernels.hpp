@@ -55,6 +55,16 @@ struct DDiagPair {
 };
 
 constexpr int kGemmTile = 64;
+// tensor-core (split TF32) tile: 128 rows x 64 columns
+constexpr int kTcTileM = 128;
+constexpr int kTcTileN = 64;
+
+void launch_gemm_tc(int transa, int transb, double alpha, const double* A, const double* B, double* C,
+                    const DTile* tiles, int ntiles, const DGemmTask* tasks, const DGemmPair* pairs, double* partial,
+                    int* err, cudaStream_t st);
+void launch_gemm_tc_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
+                           double* C, cudaStream_t st);
+int tc_smem_bytes();
 
 void launch_gemm_f64(int transa, int transb, double alpha, const double* A, const double* B, double* C,
                      const DTile* tiles, int ntiles, const DGemmTask* tasks, const DGemmPair* pairs,
