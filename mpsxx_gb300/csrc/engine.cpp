@@ -154,6 +154,9 @@ static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a,
   plan.h_tiles.clear();
   plan.h_tasks.clear();
   plan.h_pairs.clear();
+  plan.pair_a_slot.clear();
+  plan.pair_b_slot.clear();
+  plan.task_ctag.clear();
   plan.h_reduce.clear();
   plan.flops = 0.0;
   plan.c_elems = 0;
@@ -201,15 +204,31 @@ static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a,
       p.ldb = static_cast<int>(ldb);
       p.pad = 0;
       plan.h_pairs.push_back(p);
+      plan.pair_a_slot.push_back(as);
+      plan.pair_b_slot.push_back(bs);
       plan.flops += 2.0 * double(ma) * double(nb) * double(ka);
     }
     dt.p1 = static_cast<int>(plan.h_pairs.size());
     if (dt.p1 == dt.p0) continue;
     plan.h_tasks.push_back(dt);
+    plan.task_ctag.push_back(t.c_tag);
     plan.c_elems += int64_t(c.m) * c.n;
   }
   make_tiles(plan, kGemmTile, kGemmTile, plan.h_tiles, plan.h_reduce, plan.nslots);
   make_tiles(plan, kTcTileM, kTcTileN, plan.h_tiles_tc, plan.h_reduce_tc, plan.nslots_tc);
+  // the tensor-core kernel is persistent (CTA c takes tiles c, c + #SM, ...): heaviest
+  // tiles first gives a longest-processing-time-first balance
+  std::vector<std::pair<int64_t, int>> work(plan.h_tiles_tc.size());
+  for (size_t i = 0; i < plan.h_tiles_tc.size(); ++i) {
+    int64_t w = 0;
+    for (int p = plan.h_tiles_tc[i].p0; p < plan.h_tiles_tc[i].p1; ++p)
+      w += (plan.h_pairs[p].k + kPkTileK - 1) / kPkTileK;
+    work[i] = {-w, static_cast<int>(i)};
+  }
+  std::stable_sort(work.begin(), work.end());
+  std::vector<DTile> sorted(plan.h_tiles_tc.size());
+  for (size_t i = 0; i < work.size(); ++i) sorted[i] = plan.h_tiles_tc[work[i].second];
+  plan.h_tiles_tc.swap(sorted);
 }
 
 void build_gemm_plan(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a, const Tensor& b, const Tensor& c, int K,
@@ -321,24 +340,140 @@ SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DT
   p->s2.upload(ctx.stream);
   p->flops = p->s1.flops + p->s2.flops;
   p->bytes_min = 8 * (L.nnz + R.nnz + 2 * psi.nnz);
+  p->psi_layout = static_cast<const Tensor&>(psi);
+  p->psi_layout.d = nullptr;
   auto& ref = *p;
   ctx.sigma_plans[key] = std::move(p);
   return ref;
 }
 
-static void sigma_run(Context& ctx, const SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi,
+// ---------------------------------------------------------------------------
+// split-TF32 sigma over pre-packed operands
+// ---------------------------------------------------------------------------
+// Orientation of block b of a tensor as a GEMM operand: rows (A rows or B^T rows),
+// K, leading dimension and whether the stored block is K-major (trans = 0) or
+// rows-major along K (trans = 1).
+struct Orient {
+  int rows, k, ld, trans;
+};
+
+template <class F>
+static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t tile_bytes, F orient) {
+  P.base.assign(t.tags.size(), -1);
+  P.nks.assign(t.tags.size(), 0);
+  P.h_packs.clear();
+  int64_t off = 0;
+  for (size_t b = 0; b < t.tags.size(); ++b) {
+    const Orient o = orient(static_cast<int32_t>(b));
+    if (o.rows <= 0 || o.k <= 0) continue;
+    const int ntr = (o.rows + tile_rows - 1) / tile_rows;
+    const int nks = (o.k + kPkTileK - 1) / kPkTileK;
+    P.base[b] = off;
+    P.nks[b] = nks;
+    for (int tr = 0; tr < ntr; ++tr)
+      for (int tk = 0; tk < nks; ++tk)
+        P.h_packs.push_back(DPack{t.offsets[b], off + (int64_t(tr) * nks + tk) * tile_bytes, o.rows, o.k, o.ld,
+                                  o.trans, tile_rows, tr, tk, 0});
+    off += int64_t(ntr) * nks * tile_bytes;
+  }
+  P.bytes = off;
+}
+
+static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R, const Tensor& psi) {
+  auto dims3 = [](const Tensor& t, int32_t b, int* d) { t.block_dims(b, d); };
+  // stage 1: A = L block (dA x dA'), B^T = psi block transposed (dB' x dA')
+  packed_layout(p.pk_L, L, kTcTileM, kPkTileABytes, [&](int32_t b) {
+    int d[kMaxRank];
+    dims3(L, b, d);
+    return Orient{d[0] * d[1], d[2], d[2], 0};
+  });
+  packed_layout(p.pk_psi, psi, kTcTileN, kPkTileBBytes, [&](int32_t b) {
+    int d[kMaxRank];
+    dims3(psi, b, d);
+    return Orient{d[1], d[0], d[1], 1};
+  });
+  // stage-1 output = stage-2 A operand: scr1 block (dA x dB')
+  packed_layout(p.pk_scr1, p.scr1, kTcTileM, kPkTileABytes, [&](int32_t b) {
+    int d[kMaxRank];
+    dims3(p.scr1, b, d);
+    return Orient{d[0] * d[1], d[2], d[2], 0};
+  });
+  // stage 2: B^T = R block (dB x dB')
+  packed_layout(p.pk_R, R, kTcTileN, kPkTileBBytes, [&](int32_t b) {
+    int d[kMaxRank];
+    dims3(R, b, d);
+    return Orient{d[0] * d[1], d[2], d[2], 0};
+  });
+  auto pairs_of = [](const GemmPlan& g, const Packed& A, const Packed& B, std::vector<DPkPair>& out) {
+    out.resize(g.h_pairs.size());
+    for (size_t i = 0; i < g.h_pairs.size(); ++i) {
+      const int32_t as = g.pair_a_slot[i], bs = g.pair_b_slot[i];
+      if (A.base[as] < 0 || B.base[bs] < 0 || A.nks[as] != B.nks[bs])
+        throw Error(kInternal, "packed sigma plan: operand packing mismatch");
+      out[i] = DPkPair{A.base[as], B.base[bs], A.nks[as], 0};
+    }
+  };
+  pairs_of(p.s1, p.pk_L, p.pk_psi, p.h_pk1);
+  pairs_of(p.s2, p.pk_scr1, p.pk_R, p.h_pk2);
+  // stage-1 tasks write packed scr1: c_off = byte base of the block, ldc = its K slices
+  p.h_pk_tasks1 = p.s1.h_tasks;
+  for (size_t ti = 0; ti < p.h_pk_tasks1.size(); ++ti) {
+    const int32_t cs = p.scr1.find(p.s1.task_ctag[ti]);
+    if (cs < 0 || p.pk_scr1.base[cs] < 0) throw Error(kInternal, "packed sigma plan: stage-1 output missing");
+    p.h_pk_tasks1[ti].c_off = p.pk_scr1.base[cs];
+    p.h_pk_tasks1[ti].ldc = p.pk_scr1.nks[cs];
+  }
+  p.pk1.upload(p.h_pk1, ctx.stream);
+  p.pk2.upload(p.h_pk2, ctx.stream);
+  p.pk_tasks1.upload(p.h_pk_tasks1, ctx.stream);
+  p.pk_L.packs.upload(p.pk_L.h_packs, ctx.stream);
+  p.pk_R.packs.upload(p.pk_R.h_packs, ctx.stream);
+  p.pk_psi.packs.upload(p.pk_psi.h_packs, ctx.stream);
+  p.pk_L.buf.ensure(std::max<int64_t>(p.pk_L.bytes, 16));
+  p.pk_R.buf.ensure(std::max<int64_t>(p.pk_R.bytes, 16));
+  p.pk_psi.buf.ensure(std::max<int64_t>(p.pk_psi.bytes, 16));
+  p.pk_scr1.buf.ensure(std::max<int64_t>(p.pk_scr1.bytes, 16));
+  p.pk_built = true;
+}
+
+static void pack_into(Context& ctx, Packed& P, const DTensor& t) {
+  launch_pack(P.packs.get(), static_cast<int>(P.h_packs.size()), t.d, P.buf.as<uint8_t>(), ctx.stream);
+  P.src_layout = t.layout_id;
+  P.src_version = t.data_version;
+  ctx.kernel_launches += 1;
+}
+
+static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi,
+                         double* sigma) {
+  if (!p.pk_built) build_sigma_pk(ctx, p, L, R, p.psi_layout);
+  // operators are packed once per (layout, data version)
+  if (p.pk_L.src_layout != L.layout_id || p.pk_L.src_version != L.data_version) pack_into(ctx, p.pk_L, L);
+  if (p.pk_R.src_layout != R.layout_id || p.pk_R.src_version != R.data_version) pack_into(ctx, p.pk_R, R);
+  launch_pack(p.pk_psi.packs.get(), static_cast<int>(p.pk_psi.h_packs.size()), psi, p.pk_psi.buf.as<uint8_t>(),
+              ctx.stream);
+  int* err = device_err_flag(ctx);
+  launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.pk_scr1.buf.as<uint8_t>(),
+                 p.s1.tiles_tc.get(), static_cast<int>(p.s1.h_tiles_tc.size()), p.pk_tasks1.get(), p.pk1.get(),
+                 nullptr, 1, err, ctx.stream);
+  ctx.gemm_part.ensure(std::max<size_t>(p.s2.partial_bytes_tc(), 16));
+  double* part = ctx.gemm_part.as<double>();
+  launch_gemm_pk(p.pk_scr1.buf.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
+                 p.s2.tiles_tc.get(), static_cast<int>(p.s2.h_tiles_tc.size()), p.s2.dtasks.get(), p.pk2.get(), part,
+                 0, err, ctx.stream);
+  if (p.s2.nslots_tc > 0)
+    launch_gemm_pk_reduce(p.s2.reduce_tc.get(), static_cast<int>(p.s2.h_reduce_tc.size()), p.s2.dtasks.get(), 1.0,
+                          part, sigma, ctx.stream);
+  ctx.kernel_launches += 3 + (p.s2.nslots_tc > 0);
+}
+
+static void sigma_run(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi,
                       double* sigma) {
-  ctx.scr1.ensure(std::max<int64_t>(p.scr1.nnz, 1) * sizeof(double));
-  double* scr = ctx.scr1.as<double>();
-  if (p.scr1.nnz) cuda_check(cudaMemsetAsync(scr, 0, p.scr1.nnz * sizeof(double), ctx.stream), "scr1 zero");
   if (ctx.precision == kSplitTF32) {
-    ctx.gemm_part.ensure(std::max(p.s1.partial_bytes_tc(), p.s2.partial_bytes_tc()));
-    double* part = ctx.gemm_part.as<double>();
-    int* err = device_err_flag(ctx);
-    p.s1.run_tc(1.0, L.d, psi, scr, part, err, ctx.stream);
-    p.s2.run_tc(1.0, scr, R.d, sigma, part, err, ctx.stream);
-    ctx.kernel_launches += 2 + (p.s1.nslots_tc > 0) + (p.s2.nslots_tc > 0);
+    sigma_run_pk(ctx, p, L, R, psi, sigma);
   } else {
+    ctx.scr1.ensure(std::max<int64_t>(p.scr1.nnz, 1) * sizeof(double));
+    double* scr = ctx.scr1.as<double>();
+    if (p.scr1.nnz) cuda_check(cudaMemsetAsync(scr, 0, p.scr1.nnz * sizeof(double), ctx.stream), "scr1 zero");
     ctx.gemm_part.ensure(std::max(p.s1.partial_bytes(), p.s2.partial_bytes()));
     double* part = ctx.gemm_part.as<double>();
     p.s1.run(1.0, L.d, psi, scr, part, ctx.stream);

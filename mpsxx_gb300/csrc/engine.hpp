@@ -55,6 +55,8 @@ struct GemmPlan {
   std::vector<DTile> h_tiles;
   std::vector<DGemmTask> h_tasks;
   std::vector<DGemmPair> h_pairs;
+  std::vector<int32_t> pair_a_slot, pair_b_slot;  // operand block slots of h_pairs
+  std::vector<int64_t> task_ctag;                 // result block tag of each h_tasks entry
   std::vector<DReduce> h_reduce;
   DevArray<DTile> tiles;
   DevArray<DGemmTask> dtasks;
@@ -90,12 +92,31 @@ constexpr int kTargetCtas = 152 * 8;
 void build_gemm_plan(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a, const Tensor& b, const Tensor& c,
                      int K, std::vector<GemmTaskRef>&& tasks);
 
+// Blocks of one tensor packed as split-TF32 tensor-core tiles (one role: A or B).
+struct Packed {
+  DevBuf buf;
+  std::vector<int64_t> base;  // per block slot: byte offset of its tile grid (-1: not packed)
+  std::vector<int> nks;       // per block slot: K slices
+  std::vector<DPack> h_packs;
+  DevArray<DPack> packs;
+  int64_t bytes = 0;
+  uint64_t src_layout = 0, src_version = ~0ull;  // what the buffer currently holds
+};
+
 struct SigmaPlan {
   uint64_t l_id = 0, r_id = 0, psi_id = 0;
   Tensor scr1;  // layout of L*psi
   GemmPlan s1, s2;
   double flops = 0.0;
   int64_t bytes_min = 0;  // 8*(nnz L + nnz R + 2 nnz psi)
+  // split-TF32 path over packed operands
+  Tensor psi_layout;  // the wavefunction layout the plan was built for
+  bool pk_built = false;
+  Packed pk_L, pk_R, pk_psi, pk_scr1;
+  std::vector<DPkPair> h_pk1, h_pk2;
+  std::vector<DGemmTask> h_pk_tasks1;
+  DevArray<DPkPair> pk1, pk2;
+  DevArray<DGemmTask> pk_tasks1;
 };
 
 struct DiagPlan {

@@ -66,6 +66,33 @@ void launch_gemm_tc_reduce(const DReduce* red, int nred, const DGemmTask* tasks,
                            double* C, cudaStream_t st);
 int tc_smem_bytes();
 
+// ---- pre-packed split-TF32 operands -----------------------------------------
+constexpr int kPkTileK = 32;                          // K elements per packed slice
+constexpr uint32_t kPkTileABytes = 128 * 32 * 4 * 2;  // A tile: hi|lo TF32, 128 rows
+constexpr uint32_t kPkTileBBytes = 64 * 32 * 4 * 2;   // B tile: hi|lo TF32, 64 rows
+
+// One (A, B) pair over packed operands: byte offsets of the blocks' tile grids.
+struct DPkPair {
+  int64_t a_pk, b_pk;
+  int nks, pad;
+};
+// One packed tile to produce: element (r, k) of the block is src[src_off + r*ld + k]
+// (trans = 0) or src[src_off + k*ld + r] (trans = 1).
+struct DPack {
+  int64_t src_off, dst_off;
+  int rows, k, ld, trans, tile_rows, tr, tk, pad;
+};
+
+// out_packed: C is written as packed A tiles of the next GEMM (c_off = byte offset of
+// the block's grid, ldc = its K slices per row tile) instead of FP64 C / partials.
+void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
+                    const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
+                    int out_packed, int* err, cudaStream_t st);
+void launch_gemm_pk_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
+                           double* C, cudaStream_t st);
+void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst, cudaStream_t st);
+int pk_smem_bytes();
+
 void launch_gemm_f64(int transa, int transb, double alpha, const double* A, const double* B, double* C,
                      const DTile* tiles, int ntiles, const DGemmTask* tasks, const DGemmPair* pairs,
                      double* partial, cudaStream_t st);

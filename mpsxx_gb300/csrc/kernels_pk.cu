@@ -1,0 +1,406 @@
+// Split-precision grouped block GEMM over pre-packed operands (sm_103a).
+//
+// Operands are packed once into the tensor-core tile format: a block used as the
+// A operand (rows x K) becomes ceil(rows/128) x ceil(K/32) tiles of 32 KB
+// [hi TF32 128x32 | lo TF32 128x32], a block used as B (rows = output columns)
+// becomes ceil(rows/64) x ceil(K/32) tiles of 16 KB, each half in the K-major
+// no-swizzle core-matrix layout the MMA descriptors address (8 rows x 16 bytes per
+// core matrix).  hi = tf32(x), lo = tf32(x - hi); a product is hi*hi + hi*lo + lo*hi.
+//
+// GEMM CTA (256 threads, warp-specialised):
+//   warp 0 lane 0 : producer — per K slice, one bulk copy (TMA engine) of the A tile
+//                   and one of the B tile into a 4-stage shared-memory ring,
+//                   completion counted in bytes on the stage's "full" mbarrier;
+//   warp 1 lane 0 : MMA issuer — 4 K-steps x 3 products of tcgen05.mma kind::tf32
+//                   per slice into one of two TMEM accumulators (one per block pair,
+//                   alternating), commits release the stage ("empty") and, at the end
+//                   of a pair, hand the accumulator to the epilogue ("acc_full");
+//   warps 4-7     : epilogue — per pair, tcgen05.ld of the FP32 accumulator into FP64
+//                   registers (FP32 rounding spans one block pair), then release it
+//                   ("acc_empty"); at the end write FP64 C (+=), an FP64 split-K
+//                   partial, or the packed A tiles of the next GEMM (stage-1 output).
+// Every wait is bounded by a global-timer deadline; a timeout sets a shared abort
+// flag that ends all roles and the device error flag the host checks.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.hpp"
+
+namespace mpsxx {
+
+namespace {
+
+constexpr int BM = kTcTileM;  // 128
+constexpr int BN = kTcTileN;  // 64
+constexpr int BK = kPkTileK;  // 32
+constexpr int NTHREADS = 256;
+constexpr int STAGES = 4;
+constexpr uint32_t A_BYTES = kPkTileABytes;  // 32 KB
+constexpr uint32_t B_BYTES = kPkTileBBytes;  // 16 KB
+constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+constexpr uint32_t TMEM_COLS = 128;  // two 64-column FP32 accumulators
+
+__device__ __forceinline__ uint32_t core_off(int row, int k) {
+  return (uint32_t)(((row >> 3) * (BK / 4) + (k >> 2)) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void split2(double v, uint32_t& h, uint32_t& l) {
+  h = tf32_rna(static_cast<float>(v));
+  l = tf32_rna(static_cast<float>(v - static_cast<double>(__uint_as_float(h))));
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+__host__ __device__ constexpr uint32_t tf32_idesc() {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// bounded wait; false on timeout or when another role aborted
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint64_t deadline,
+                                          volatile int* abort_flag) {
+  while (!mbar_try(mbar, parity)) {
+    if (*abort_flag) return false;
+    if (global_ns() > deadline) {
+      *abort_flag = 1;
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    gemm_pk_kernel(const uint8_t* __restrict__ Apk, const uint8_t* __restrict__ Bpk, double alpha,
+                   double* __restrict__ C, uint8_t* __restrict__ Cpk, const DTile* __restrict__ tiles, int ntiles,
+                   const DGemmTask* __restrict__ tasks, const DPkPair* __restrict__ pairs,
+                   double* __restrict__ partial, int out_packed, int* __restrict__ err, uint64_t timeout_ns) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t accf_bar[2];
+  __shared__ __align__(8) uint64_t acce_bar[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 32) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&accf_bar[b]), 1);
+      mbar_init(smem_u32(&acce_bar[b]), 128);
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_slot;
+  const uint64_t deadline = global_ns() + timeout_ns;
+
+  // Persistent: the CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...; every
+  // role walks the same sequence, so slice and pair counters continue across tiles.
+  if (warp == 0) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      int slice = 0;
+      for (int ti = blockIdx.x; ti < ntiles && !abort_flag; ti += gridDim.x) {
+        const DTile t = tiles[ti];
+        for (int p = t.p0; p < t.p1 && !abort_flag; ++p) {
+          const DPkPair pr = pairs[p];
+          for (int ks = 0; ks < pr.nks; ++ks, ++slice) {
+            const int s = slice % STAGES;
+            const uint32_t round = slice / STAGES;
+            if (!mbar_wait(smem_u32(&empty_bar[s]), (round & 1u) ^ 1u, deadline, &abort_flag)) break;
+            const uint32_t fb = smem_u32(&full_bar[s]);
+            mbar_expect_tx(fb, STAGE_BYTES);
+            const uint32_t dst = smem_u32(ring + s * STAGE_BYTES);
+            bulk_g2s(dst, Apk + pr.a_pk + ((int64_t)t.tm * pr.nks + ks) * A_BYTES, A_BYTES, fb);
+            bulk_g2s(dst + A_BYTES, Bpk + pr.b_pk + ((int64_t)t.tn * pr.nks + ks) * B_BYTES, B_BYTES, fb);
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = tf32_idesc();
+      const uint32_t lbo = 128, sbo = (BK / 4) * 128;
+      int slice = 0, pc = 0;
+      bool ok = true;
+      for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+        const DTile t = tiles[ti];
+        for (int p = t.p0; p < t.p1 && ok; ++p, ++pc) {
+          const DPkPair pr = pairs[p];
+          const int b = pc & 1;
+          // the epilogue must have drained this accumulator (pair pc-2)
+          if (!mbar_wait(smem_u32(&acce_bar[b]), ((pc >> 1) & 1u) ^ 1u, deadline, &abort_flag)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t d = tmem + b * BN;
+          for (int ks = 0; ks < pr.nks; ++ks, ++slice) {
+            const int s = slice % STAGES;
+            const uint32_t round = slice / STAGES;
+            if (!mbar_wait(smem_u32(&full_bar[s]), round & 1u, deadline, &abort_flag)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t a0 = smem_u32(ring + s * STAGE_BYTES);
+            const uint32_t b0 = a0 + A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < BK / 8; ++kk) {
+              const uint32_t koff = kk * 256;
+              const uint64_t ah = smem_desc(a0 + koff, lbo, sbo);
+              const uint64_t al = smem_desc(a0 + A_BYTES / 2 + koff, lbo, sbo);
+              const uint64_t bh = smem_desc(b0 + koff, lbo, sbo);
+              const uint64_t bl = smem_desc(b0 + B_BYTES / 2 + koff, lbo, sbo);
+              mma_tf32(d, ah, bh, idesc, (ks == 0 && kk == 0) ? 0u : 1u);
+              mma_tf32(d, ah, bl, idesc, 1u);
+              mma_tf32(d, al, bh, idesc, 1u);
+            }
+            mma_commit(smem_u32(&empty_bar[s]));  // stage free once these MMAs completed
+          }
+          if (!ok) break;
+          mma_commit(smem_u32(&accf_bar[b]));  // pair accumulated
+        }
+      }
+    }
+  } else if (warp >= 4) {
+    // ---------------- epilogue ----------------
+    const int q = warp - 4;  // TMEM lane quarter
+    int pc = 0;
+    bool ok = true;
+    for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+      const DTile t = tiles[ti];
+      const DGemmTask task = tasks[t.task];
+      double acc[BN];
+#pragma unroll
+      for (int j = 0; j < BN; ++j) acc[j] = 0.0;
+      for (int p = t.p0; p < t.p1; ++p, ++pc) {
+        const int b = pc & 1;
+        if (!mbar_wait(smem_u32(&accf_bar[b]), (pc >> 1) & 1u, deadline, &abort_flag)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * BN;
+#pragma unroll
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+          float v[16];
+          tmem_ld16(taddr + c0, v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+          for (int i = 0; i < 16; ++i) acc[c0 + i] += static_cast<double>(v[i]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        mbar_arrive(smem_u32(&acce_bar[b]));
+      }
+      if (!ok) break;
+      const int row = q * 32 + lane;
+      const int r = t.tm * BM + row;
+      if (out_packed) {
+        // stage-1 output as packed A tiles of the next GEMM: columns [64 tn, 64 tn + 64)
+        // are its K slices 2 tn and 2 tn + 1; ldc carries that GEMM's slices per row tile
+        uint8_t* tile0 = Cpk + task.c_off + ((int64_t)t.tm * task.ldc + 2 * t.tn) * A_BYTES;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (2 * t.tn + h >= task.ldc) break;
+          uint8_t* tile = tile0 + h * A_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < BK; ++kk) {
+            uint32_t hi, lo;
+            split2(alpha * acc[h * BK + kk], hi, lo);
+            *reinterpret_cast<uint32_t*>(tile + core_off(row, kk)) = hi;
+            *reinterpret_cast<uint32_t*>(tile + A_BYTES / 2 + core_off(row, kk)) = lo;
+          }
+        }
+      } else if (t.slot >= 0) {
+        double* part = partial + (int64_t)t.slot * (BM * BN) + (int64_t)row * BN;
+#pragma unroll
+        for (int j = 0; j < BN; ++j) part[j] = acc[j];
+      } else if (r < task.m) {
+        const int n0 = t.tn * BN;
+        double* dst = C + task.c_off + (int64_t)r * task.ldc + n0;
+#pragma unroll
+        for (int j = 0; j < BN; ++j)
+          if (n0 + j < task.n) dst[j] += alpha * acc[j];
+      }
+    }
+  }
+
+  __syncthreads();
+  if (threadIdx.x == 0 && abort_flag) atomicExch(err, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+// Pack FP64 blocks into split-TF32 tiles: one CTA per output tile.
+__global__ void __launch_bounds__(256) pack_kernel(const DPack* __restrict__ packs, const double* __restrict__ src,
+                                                   uint8_t* __restrict__ dst) {
+  const DPack pk = packs[blockIdx.x];
+  const int rows_t = pk.tile_rows;
+  const uint32_t half = (uint32_t)rows_t * BK * 4;
+  uint8_t* tile = dst + pk.dst_off;
+  const int r0 = pk.tr * rows_t, k0 = pk.tk * BK;
+  for (int e = threadIdx.x; e < rows_t * BK; e += blockDim.x) {
+    int r, kk;
+    if (!pk.trans) {
+      r = e / BK;
+      kk = e % BK;
+    } else {
+      kk = e / rows_t;
+      r = e % rows_t;
+    }
+    const int gr = r0 + r, gk = k0 + kk;
+    double v = 0.0;
+    if (gr < pk.rows && gk < pk.k)
+      v = pk.trans ? src[pk.src_off + (int64_t)gk * pk.ld + gr] : src[pk.src_off + (int64_t)gr * pk.ld + gk];
+    uint32_t h, l;
+    split2(v, h, l);
+    *reinterpret_cast<uint32_t*>(tile + core_off(r, kk)) = h;
+    *reinterpret_cast<uint32_t*>(tile + half + core_off(r, kk)) = l;
+  }
+}
+
+__global__ void __launch_bounds__(256) gemm_pk_reduce_kernel(const DReduce* __restrict__ red,
+                                                             const DGemmTask* __restrict__ tasks, double alpha,
+                                                             const double* __restrict__ partial,
+                                                             double* __restrict__ C) {
+  const DReduce rd = red[blockIdx.x];
+  const DGemmTask task = tasks[rd.task];
+  const int m0 = rd.tm * BM, n0 = rd.tn * BN;
+  for (int e = threadIdx.x; e < BM * BN; e += blockDim.x) {
+    const int r = m0 + e / BN, c = n0 + e % BN;
+    if (r >= task.m || c >= task.n) continue;
+    double s = 0.0;
+    for (int k = 0; k < rd.nslot; ++k) s += partial[(int64_t)(rd.slot0 + k) * (BM * BN) + e];
+    C[task.c_off + (int64_t)r * task.ldc + c] += alpha * s;
+  }
+}
+
+}  // namespace
+
+int pk_smem_bytes() { return SMEM_BYTES; }
+
+void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
+                    const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
+                    int out_packed, int* err, cudaStream_t st) {
+  if (ntiles <= 0) return;
+  static int nsm = 0;
+  if (nsm == 0) {
+    cudaFuncSetAttribute(gemm_pk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 152;
+  }
+  // one persistent CTA per SM; the bound covers the whole launch, not one tile
+  const uint64_t timeout_ns = 20000000000ull;  // 20 s
+  const int grid = ntiles < nsm ? ntiles : nsm;
+  gemm_pk_kernel<<<grid, NTHREADS, SMEM_BYTES, st>>>(Apk, Bpk, alpha, C, Cpk, tiles, ntiles, tasks, pairs, partial,
+                                                     out_packed, err, timeout_ns);
+}
+
+void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst, cudaStream_t st) {
+  if (npacks <= 0) return;
+  pack_kernel<<<npacks, 256, 0, st>>>(packs, src, dst);
+}
+
+void launch_gemm_pk_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
+                           double* C, cudaStream_t st) {
+  if (nred <= 0) return;
+  gemm_pk_reduce_kernel<<<nred, 256, 0, st>>>(red, tasks, alpha, partial, C);
+}
+
+}  // namespace mpsxx

@@ -9,12 +9,18 @@
 // output stay FP64.
 //
 // CTA: 128 threads, one 128 x 64 output tile (TMEM: 128 lanes x 64 FP32 columns).
-// Per 32-deep K slice the threads load FP64 operands from global memory, split
-// them and store hi/lo tiles into shared memory in the K-major no-swizzle
-// core-matrix layout (8 rows x 16 bytes per core matrix); thread 0 issues 4 x 3
-// MMAs with shared-memory descriptors and commits them to an mbarrier that all
-// threads wait on (bounded by a global-timer deadline) before the buffers are
-// refilled.  The same task/pair plans as the FP64 kernel drive it.
+// The tile's work is a flat sequence of 32-deep K slices over its (A, B) pairs.
+// Pipeline per slice s:
+//   * raw FP64 operand tiles arrive in shared memory through cp.async, issued two
+//     slices ahead into a double buffer (no register round trip, many bytes in
+//     flight per SM);
+//   * the threads split the raw tiles into TF32 hi/lo tiles in the K-major
+//     no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix);
+//   * thread 0 issues 4 x 3 MMAs with shared-memory descriptors and commits them to
+//     an mbarrier; the wait on it (bounded by a global-timer deadline) happens just
+//     before the next slice overwrites the hi/lo tiles, so loads and the split of
+//     slice s+1 overlap the MMAs of slice s.
+// The same task/pair plans as the FP64 kernel drive it.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -28,12 +34,16 @@ namespace {
 constexpr int BM = kTcTileM;  // 128
 constexpr int BN = kTcTileN;  // 64
 constexpr int BK = 32;        // TF32 elements per K slice (4 MMA steps of K=8)
-constexpr int NTHREADS = 128;
+constexpr int NTHREADS = 256;  // 8 warps: warp w flushes TMEM lanes 32*(w%4).. and columns 32*(w/4)..
+constexpr int CPT = BN / 2;     // accumulator columns per thread
 constexpr uint32_t TMEM_COLS = 64;
 
 constexpr int A_TILE_BYTES = BM * BK * 4;  // 16 KB
 constexpr int B_TILE_BYTES = BN * BK * 4;  // 8 KB
-constexpr int SMEM_BYTES = 2 * A_TILE_BYTES + 2 * B_TILE_BYTES + 1024;
+constexpr int A_RAW_BYTES = BM * BK * 8;   // 32 KB FP64 staging
+constexpr int B_RAW_BYTES = BN * BK * 8;   // 16 KB FP64 staging
+constexpr int RAW_BYTES = A_RAW_BYTES + B_RAW_BYTES;
+constexpr int SMEM_BYTES = 2 * A_TILE_BYTES + 2 * B_TILE_BYTES + 2 * RAW_BYTES + 1024;
 
 // byte offset of element (row, k) in a K-major tile of BK columns made of 8x4 core matrices
 __device__ __forceinline__ uint32_t core_off(int row, int k) {
@@ -109,12 +119,85 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ void split_store(uint8_t* hi_base, uint8_t* lo_base, uint32_t off, double v) {
-  const float x = static_cast<float>(v);
-  const uint32_t h = tf32_rna(x);
-  const uint32_t l = tf32_rna(static_cast<float>(v - static_cast<double>(__uint_as_float(h))));
-  *reinterpret_cast<uint32_t*>(hi_base + off) = h;
-  *reinterpret_cast<uint32_t*>(lo_base + off) = l;
+__device__ __forceinline__ void cp_async8(uint32_t dst, const double* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+struct SliceCursor {
+  int p;   // pair index
+  int k0;  // first K element of the slice inside the pair
+};
+
+__device__ __forceinline__ void advance(SliceCursor& c, const DGemmPair* pairs) {
+  c.k0 += BK;
+  if (c.k0 >= pairs[c.p].k) {
+    ++c.p;
+    c.k0 = 0;
+  }
+}
+
+// Stage one slice of raw FP64 operands (zero outside the block) into shared memory:
+// A as [BM][BK] and B^T as [BN][BK], row-major.
+__device__ __forceinline__ void load_slice(const SliceCursor& c, const DGemmPair* __restrict__ pairs,
+                                           const DGemmTask& task, int m0, int n0, int transa, int transb,
+                                           const double* __restrict__ A, const double* __restrict__ B,
+                                           double* a_raw, double* b_raw) {
+  const DGemmPair pr = pairs[c.p];
+  const int k0 = c.k0;
+  const uint32_t a_s = smem_u32(a_raw), b_s = smem_u32(b_raw);
+  if (!transa) {
+    for (int e = threadIdx.x; e < BM * BK; e += NTHREADS) {
+      const int r = e / BK, kk = e % BK;
+      const int gr = m0 + r, gk = k0 + kk;
+      if (gr < task.m && gk < pr.k)
+        cp_async8(a_s + (uint32_t)(r * BK + kk) * 8, A + pr.a_off + (int64_t)gr * pr.lda + gk);
+      else
+        a_raw[r * BK + kk] = 0.0;
+    }
+  } else {
+    for (int e = threadIdx.x; e < BM * BK; e += NTHREADS) {
+      const int r = e % BM, kk = e / BM;
+      const int gr = m0 + r, gk = k0 + kk;
+      if (gr < task.m && gk < pr.k)
+        cp_async8(a_s + (uint32_t)(r * BK + kk) * 8, A + pr.a_off + (int64_t)gk * pr.lda + gr);
+      else
+        a_raw[r * BK + kk] = 0.0;
+    }
+  }
+  if (!transb) {
+    for (int e = threadIdx.x; e < BN * BK; e += NTHREADS) {
+      const int cc = e % BN, kk = e / BN;
+      const int gc = n0 + cc, gk = k0 + kk;
+      if (gc < task.n && gk < pr.k)
+        cp_async8(b_s + (uint32_t)(cc * BK + kk) * 8, B + pr.b_off + (int64_t)gk * pr.ldb + gc);
+      else
+        b_raw[cc * BK + kk] = 0.0;
+    }
+  } else {
+    for (int e = threadIdx.x; e < BN * BK; e += NTHREADS) {
+      const int cc = e / BK, kk = e % BK;
+      const int gc = n0 + cc, gk = k0 + kk;
+      if (gc < task.n && gk < pr.k)
+        cp_async8(b_s + (uint32_t)(cc * BK + kk) * 8, B + pr.b_off + (int64_t)gc * pr.ldb + gk);
+      else
+        b_raw[cc * BK + kk] = 0.0;
+    }
+  }
+}
+
+__device__ __forceinline__ void split_tile(const double* raw, int rows, uint8_t* hi, uint8_t* lo) {
+  for (int e = threadIdx.x; e < rows * BK; e += NTHREADS) {
+    const int r = e / BK, kk = e % BK;
+    const double v = raw[e];
+    const uint32_t h = tf32_rna(static_cast<float>(v));
+    const uint32_t l = tf32_rna(static_cast<float>(v - static_cast<double>(__uint_as_float(h))));
+    const uint32_t off = core_off(r, kk);
+    *reinterpret_cast<uint32_t*>(hi + off) = h;
+    *reinterpret_cast<uint32_t*>(lo + off) = l;
+  }
 }
 
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -123,12 +206,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                    const DGemmTask* __restrict__ tasks, const DGemmPair* __restrict__ pairs,
                    double* __restrict__ partial, int* __restrict__ err, uint64_t timeout_ns) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  // 1024-aligned operand tiles
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* a_hi = base;
   uint8_t* a_lo = a_hi + A_TILE_BYTES;
   uint8_t* b_hi = a_lo + A_TILE_BYTES;
   uint8_t* b_lo = b_hi + B_TILE_BYTES;
+  double* raw0 = reinterpret_cast<double*>(b_lo + B_TILE_BYTES);
+  double* raw1 = raw0 + RAW_BYTES / 8;
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_slot;
 
@@ -136,6 +220,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const DGemmTask task = tasks[t.task];
   const int m0 = t.tm * BM, n0 = t.tn * BN;
   const int warp = threadIdx.x >> 5;
+
+  // slices of this tile
+  int nslice = 0;
+  for (int p = t.p0; p < t.p1; ++p) nslice += (pairs[p].k + BK - 1) / BK;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -153,102 +241,113 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const uint32_t mb = smem_u32(&mbar);
   const uint32_t idesc = tf32_idesc();
   const uint64_t deadline = global_ns() + timeout_ns;
+  const int quarter = warp & 3, half = warp >> 2;
+  const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(half * CPT);
 
-  double acc[BN];
+  double acc[CPT];
 #pragma unroll
-  for (int j = 0; j < BN; ++j) acc[j] = 0.0;
+  for (int j = 0; j < CPT; ++j) acc[j] = 0.0;
+
+  // prologue: slices 0 and 1 in flight
+  SliceCursor ld{t.p0, 0};
+  for (int s = 0; s < 2; ++s) {
+    if (s < nslice) {
+      double* raw = s ? raw1 : raw0;
+      load_slice(ld, pairs, task, m0, n0, transa, transb, A, B, raw, raw + A_RAW_BYTES / 8);
+      advance(ld, pairs);
+    }
+    cp_async_commit();
+  }
+
   uint32_t phase = 0;
   bool ok = true;
-
-  for (int p = t.p0; p < t.p1 && ok; ++p) {
-    const DGemmPair pr = pairs[p];
-    for (int k0 = 0; k0 < pr.k && ok; k0 += BK) {
-      // A tile: rows m0..m0+BM-1, k0..k0+BK-1 of op(A)
-      if (!transa) {
-        for (int e = threadIdx.x; e < BM * BK; e += NTHREADS) {
-          const int r = e / BK, kk = e % BK;
-          const int gr = m0 + r, gk = k0 + kk;
-          const double v = (gr < task.m && gk < pr.k) ? A[pr.a_off + (int64_t)gr * pr.lda + gk] : 0.0;
-          split_store(a_hi, a_lo, core_off(r, kk), v);
-        }
-      } else {
-        for (int e = threadIdx.x; e < BM * BK; e += NTHREADS) {
-          const int r = e % BM, kk = e / BM;
-          const int gr = m0 + r, gk = k0 + kk;
-          const double v = (gr < task.m && gk < pr.k) ? A[pr.a_off + (int64_t)gk * pr.lda + gr] : 0.0;
-          split_store(a_hi, a_lo, core_off(r, kk), v);
-        }
-      }
-      // B^T tile (N x K, K-major): columns n0..n0+BN-1 of op(B)
-      if (!transb) {
-        for (int e = threadIdx.x; e < BN * BK; e += NTHREADS) {
-          const int c = e % BN, kk = e / BN;
-          const int gc = n0 + c, gk = k0 + kk;
-          const double v = (gc < task.n && gk < pr.k) ? B[pr.b_off + (int64_t)gk * pr.ldb + gc] : 0.0;
-          split_store(b_hi, b_lo, core_off(c, kk), v);
-        }
-      } else {
-        for (int e = threadIdx.x; e < BN * BK; e += NTHREADS) {
-          const int c = e / BK, kk = e % BK;
-          const int gc = n0 + c, gk = k0 + kk;
-          const double v = (gc < task.n && gk < pr.k) ? B[pr.b_off + (int64_t)gc * pr.ldb + gk] : 0.0;
-          split_store(b_hi, b_lo, core_off(c, kk), v);
-        }
-      }
-      // generic-proxy stores -> visible to the tensor core (async proxy)
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t lbo = 128, sbo_a = (BK / 4) * 128, sbo_b = (BK / 4) * 128;
-#pragma unroll
-        for (int ks = 0; ks < BK / 8; ++ks) {
-          const uint32_t koff = ks * 2 * 128;  // two core matrices per K=8 step
-          const uint64_t ah = smem_desc(smem_u32(a_hi) + koff, lbo, sbo_a);
-          const uint64_t al = smem_desc(smem_u32(a_lo) + koff, lbo, sbo_a);
-          const uint64_t bh = smem_desc(smem_u32(b_hi) + koff, lbo, sbo_b);
-          const uint64_t bl = smem_desc(smem_u32(b_lo) + koff, lbo, sbo_b);
-          const uint32_t accum = (k0 == 0 && ks == 0) ? 0u : 1u;
-          mma_tf32(tmem, ah, bh, idesc, accum);
-          mma_tf32(tmem, ah, bl, idesc, 1u);
-          mma_tf32(tmem, al, bh, idesc, 1u);
-        }
-        mma_commit(mb);
-      }
-      // the MMAs read the tiles: wait before the next slice overwrites them; the
-      // verdict is made CTA-uniform so every thread takes the same barriers
+  SliceCursor cv{t.p0, 0};
+  for (int s = 0; s < nslice; ++s) {
+    double* raw = (s & 1) ? raw1 : raw0;
+    cp_async_wait1();  // slice s has landed
+    if (s > 0) {
+      // MMAs of slice s-1 read the hi/lo tiles: they must be complete before the split
       ok = __syncthreads_and(mbar_wait(mb, phase, deadline) ? 1 : 0) != 0;
       phase ^= 1u;
-    }
-    if (!ok) break;
-    // flush this pair's FP32 tile into the FP64 accumulators
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+      if (!ok) break;
+      if (cv.k0 == 0) {
+        // slice s starts a new pair: the accumulator holds the previous pair; flush it to FP64
+        asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      float v[16];
-      tmem_ld16(lane_addr + c0, v);
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
+        for (int c0 = 0; c0 < CPT; c0 += 16) {
+          float v[16];
+          tmem_ld16(lane_addr + c0, v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-      for (int i = 0; i < 16; ++i) acc[c0 + i] += static_cast<double>(v[i]);
+          for (int i = 0; i < 16; ++i) acc[c0 + i] += static_cast<double>(v[i]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+      }
+    } else {
+      __syncthreads();
     }
-    asm volatile("tcgen05.fence::before_thread_sync;");
+    split_tile(raw, BM, a_hi, a_lo);
+    split_tile(raw + A_RAW_BYTES / 8, BN, b_hi, b_lo);
+    // generic-proxy stores -> visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
+    // the raw buffer is free again: stage slice s+2 into it
+    if (s + 2 < nslice) {
+      load_slice(ld, pairs, task, m0, n0, transa, transb, A, B, raw, raw + A_RAW_BYTES / 8);
+      advance(ld, pairs);
+    }
+    cp_async_commit();
+    if (threadIdx.x == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t lbo = 128, sbo = (BK / 4) * 128;
+      const bool first = (cv.k0 == 0);
+#pragma unroll
+      for (int ks = 0; ks < BK / 8; ++ks) {
+        const uint32_t koff = ks * 2 * 128;  // two core matrices per K=8 step
+        const uint64_t ah = smem_desc(smem_u32(a_hi) + koff, lbo, sbo);
+        const uint64_t al = smem_desc(smem_u32(a_lo) + koff, lbo, sbo);
+        const uint64_t bh = smem_desc(smem_u32(b_hi) + koff, lbo, sbo);
+        const uint64_t bl = smem_desc(smem_u32(b_lo) + koff, lbo, sbo);
+        mma_tf32(tmem, ah, bh, idesc, (first && ks == 0) ? 0u : 1u);
+        mma_tf32(tmem, ah, bl, idesc, 1u);
+        mma_tf32(tmem, al, bh, idesc, 1u);
+      }
+      mma_commit(mb);
+    }
+    advance(cv, pairs);
+  }
+  cp_async_wait0();
+  if (ok && nslice > 0) {
+    ok = __syncthreads_and(mbar_wait(mb, phase, deadline) ? 1 : 0) != 0;
+    if (ok) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int c0 = 0; c0 < CPT; c0 += 16) {
+        float v[16];
+        tmem_ld16(lane_addr + c0, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int i = 0; i < 16; ++i) acc[c0 + i] += static_cast<double>(v[i]);
+      }
+    }
   }
 
   if (!ok) {
     if (threadIdx.x == 0) atomicExch(err, 1);
   } else {
-    const int r = m0 + threadIdx.x;  // warp w reads TMEM lanes 32w..32w+31 = tile rows
+    // this thread owns tile row 32*quarter + lane and columns CPT*half .. CPT*half + CPT-1
+    const int row = quarter * 32 + (threadIdx.x & 31);
+    const int col0 = half * CPT;
+    const int r = m0 + row;
     if (t.slot >= 0) {
-      double* part = partial + (int64_t)t.slot * (BM * BN) + (int64_t)threadIdx.x * BN;
+      double* part = partial + (int64_t)t.slot * (BM * BN) + (int64_t)row * BN + col0;
 #pragma unroll
-      for (int j = 0; j < BN; ++j) part[j] = acc[j];
+      for (int j = 0; j < CPT; ++j) part[j] = acc[j];
     } else if (r < task.m) {
-      double* dst = C + task.c_off + (int64_t)r * task.ldc + n0;
+      double* dst = C + task.c_off + (int64_t)r * task.ldc + n0 + col0;
 #pragma unroll
-      for (int j = 0; j < BN; ++j)
-        if (n0 + j < task.n) dst[j] += alpha * acc[j];
+      for (int j = 0; j < CPT; ++j)
+        if (n0 + col0 + j < task.n) dst[j] += alpha * acc[j];
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");

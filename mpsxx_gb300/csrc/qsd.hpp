@@ -98,7 +98,8 @@ struct Tensor {
   int64_t nnz = 0;
   double* d = nullptr;  // device data (nnz doubles), owned when own == true
   bool own = false;
-  uint64_t layout_id = 0;  // changes whenever the block layout changes
+  uint64_t layout_id = 0;     // changes whenever the block layout changes
+  uint64_t data_version = 0;  // bumped whenever the data is replaced from outside a plan
 
   void set_blocks(const std::vector<int64_t>& sorted_tags);
   void allocate_allowed();  // every allowed block of non-zero size (STArray.h:219-237)
