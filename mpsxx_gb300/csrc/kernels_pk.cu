@@ -41,6 +41,15 @@ constexpr uint32_t B_BYTES = kPkTileBBytes;  // 16 KB
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
 constexpr uint32_t TMEM_COLS = 128;  // two 64-column FP32 accumulators
+// Consecutive block pairs of a tile accumulate in the FP32 tensor-memory tile until
+// their summed contraction length reaches FLUSH_K; then the group is flushed into
+// the FP64 accumulators.  This bounds the FP32 accumulation length (rounding ~
+// sqrt(FLUSH_K) * 2^-24, below the TF32 split error) while keeping FP64 work —
+// GB300's narrowest pipe — off the per-pair path.
+constexpr int FLUSH_K = 1024;
+
+// group boundary: after pair p (with running contraction length kacc) of a tile
+__device__ __forceinline__ bool group_ends(int kacc, int p, int p_last) { return kacc >= FLUSH_K || p == p_last; }
 
 __device__ __forceinline__ uint32_t core_off(int row, int k) {
   return (uint32_t)(((row >> 3) * (BK / 4) + (k >> 2)) * 128 + (row & 7) * 16 + (k & 3) * 4);
@@ -212,19 +221,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     if (lane == 0) {
       const uint32_t idesc = tf32_idesc();
       const uint32_t lbo = 128, sbo = (BK / 4) * 128;
-      int slice = 0, pc = 0;
+      int slice = 0, gc = 0;
       bool ok = true;
       for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
         const DTile t = tiles[ti];
-        for (int p = t.p0; p < t.p1 && ok; ++p, ++pc) {
+        int kacc = 0;
+        for (int p = t.p0; p < t.p1 && ok; ++p) {
           const DPkPair pr = pairs[p];
-          const int b = pc & 1;
-          // the epilogue must have drained this accumulator (pair pc-2)
-          if (!mbar_wait(smem_u32(&acce_bar[b]), ((pc >> 1) & 1u) ^ 1u, deadline, &abort_flag)) {
-            ok = false;
-            break;
+          const int b = gc & 1;
+          const bool group_start = (kacc == 0);
+          if (group_start) {
+            // the epilogue must have drained this accumulator (group gc-2)
+            if (!mbar_wait(smem_u32(&acce_bar[b]), ((gc >> 1) & 1u) ^ 1u, deadline, &abort_flag)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
           }
-          asm volatile("tcgen05.fence::after_thread_sync;");
           const uint32_t d = tmem + b * BN;
           for (int ks = 0; ks < pr.nks; ++ks, ++slice) {
             const int s = slice % STAGES;
@@ -243,31 +256,83 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const uint64_t al = smem_desc(a0 + A_BYTES / 2 + koff, lbo, sbo);
               const uint64_t bh = smem_desc(b0 + koff, lbo, sbo);
               const uint64_t bl = smem_desc(b0 + B_BYTES / 2 + koff, lbo, sbo);
-              mma_tf32(d, ah, bh, idesc, (ks == 0 && kk == 0) ? 0u : 1u);
+              mma_tf32(d, ah, bh, idesc, (group_start && ks == 0 && kk == 0) ? 0u : 1u);
               mma_tf32(d, ah, bl, idesc, 1u);
               mma_tf32(d, al, bh, idesc, 1u);
             }
             mma_commit(smem_u32(&empty_bar[s]));  // stage free once these MMAs completed
           }
           if (!ok) break;
-          mma_commit(smem_u32(&accf_bar[b]));  // pair accumulated
+          kacc += pr.nks * BK;
+          if (group_ends(kacc, p, t.p1 - 1)) {
+            mma_commit(smem_u32(&accf_bar[b]));  // group accumulated
+            ++gc;
+            kacc = 0;
+          }
         }
       }
     }
   } else if (warp >= 4) {
     // ---------------- epilogue ----------------
     const int q = warp - 4;  // TMEM lane quarter
-    int pc = 0;
+    const int row = q * 32 + lane;
+    int gc = 0;
     bool ok = true;
     for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
       const DTile t = tiles[ti];
       const DGemmTask task = tasks[t.task];
+      const int r = t.tm * BM + row;
+      if (out_packed) {
+        // stage-1 output (one group): FP32 straight from tensor memory, re-split into
+        // the packed A tiles of the next GEMM; columns [64 tn, 64 tn + 64) are its K
+        // slices 2 tn and 2 tn + 1, ldc carries that GEMM's slices per row tile
+        int kacc = 0;
+        for (int p = t.p0; p < t.p1 && ok; ++p) {
+          kacc += pairs[p].nks * BK;
+          if (!group_ends(kacc, p, t.p1 - 1)) continue;
+          kacc = 0;
+          const int b = gc & 1;
+          if (!mbar_wait(smem_u32(&accf_bar[b]), (gc >> 1) & 1u, deadline, &abort_flag)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * BN;
+          uint8_t* tile0 = Cpk + task.c_off + ((int64_t)t.tm * task.ldc + 2 * t.tn) * A_BYTES;
+          const float fa = static_cast<float>(alpha);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            float v[BK];
+            tmem_ld16(taddr + h * BK, v);
+            tmem_ld16(taddr + h * BK + 16, v + 16);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            if (2 * t.tn + h >= task.ldc) continue;
+            uint8_t* tile = tile0 + h * A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < BK; ++kk) {
+              const float x = fa * v[kk];
+              const uint32_t hi = tf32_rna(x);
+              const uint32_t lo = tf32_rna(x - __uint_as_float(hi));
+              *reinterpret_cast<uint32_t*>(tile + core_off(row, kk)) = hi;
+              *reinterpret_cast<uint32_t*>(tile + A_BYTES / 2 + core_off(row, kk)) = lo;
+            }
+          }
+          asm volatile("tcgen05.fence::before_thread_sync;");
+          mbar_arrive(smem_u32(&acce_bar[b]));
+          ++gc;
+        }
+        continue;
+      }
       double acc[BN];
 #pragma unroll
       for (int j = 0; j < BN; ++j) acc[j] = 0.0;
-      for (int p = t.p0; p < t.p1; ++p, ++pc) {
-        const int b = pc & 1;
-        if (!mbar_wait(smem_u32(&accf_bar[b]), (pc >> 1) & 1u, deadline, &abort_flag)) {
+      int kacc = 0;
+      for (int p = t.p0; p < t.p1; ++p) {
+        kacc += pairs[p].nks * BK;
+        if (!group_ends(kacc, p, t.p1 - 1)) continue;
+        kacc = 0;
+        const int b = gc & 1;
+        if (!mbar_wait(smem_u32(&accf_bar[b]), (gc >> 1) & 1u, deadline, &abort_flag)) {
           ok = false;
           break;
         }
@@ -283,27 +348,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
         mbar_arrive(smem_u32(&acce_bar[b]));
+        ++gc;
       }
       if (!ok) break;
-      const int row = q * 32 + lane;
-      const int r = t.tm * BM + row;
-      if (out_packed) {
-        // stage-1 output as packed A tiles of the next GEMM: columns [64 tn, 64 tn + 64)
-        // are its K slices 2 tn and 2 tn + 1; ldc carries that GEMM's slices per row tile
-        uint8_t* tile0 = Cpk + task.c_off + ((int64_t)t.tm * task.ldc + 2 * t.tn) * A_BYTES;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          if (2 * t.tn + h >= task.ldc) break;
-          uint8_t* tile = tile0 + h * A_BYTES;
-#pragma unroll
-          for (int kk = 0; kk < BK; ++kk) {
-            uint32_t hi, lo;
-            split2(alpha * acc[h * BK + kk], hi, lo);
-            *reinterpret_cast<uint32_t*>(tile + core_off(row, kk)) = hi;
-            *reinterpret_cast<uint32_t*>(tile + A_BYTES / 2 + core_off(row, kk)) = lo;
-          }
-        }
-      } else if (t.slot >= 0) {
+      if (t.slot >= 0) {
         double* part = partial + (int64_t)t.slot * (BM * BN) + (int64_t)row * BN;
 #pragma unroll
         for (int j = 0; j < BN; ++j) part[j] = acc[j];
@@ -360,7 +408,10 @@ __global__ void __launch_bounds__(256) gemm_pk_reduce_kernel(const DReduce* __re
   const DReduce rd = red[blockIdx.x];
   const DGemmTask task = tasks[rd.task];
   const int m0 = rd.tm * BM, n0 = rd.tn * BN;
-  for (int e = threadIdx.x; e < BM * BN; e += blockDim.x) {
+  // blockIdx.y takes one of gridDim.y contiguous element ranges of the tile
+  const int per = (BM * BN) / gridDim.y;
+  const int e0 = blockIdx.y * per;
+  for (int e = e0 + threadIdx.x; e < e0 + per; e += blockDim.x) {
     const int r = m0 + e / BN, c = n0 + e % BN;
     if (r >= task.m || c >= task.n) continue;
     double s = 0.0;
@@ -400,7 +451,7 @@ void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst
 void launch_gemm_pk_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
                            double* C, cudaStream_t st) {
   if (nred <= 0) return;
-  gemm_pk_reduce_kernel<<<nred, 256, 0, st>>>(red, tasks, alpha, partial, C);
+  gemm_pk_reduce_kernel<<<dim3(nred, 16), 256, 0, st>>>(red, tasks, alpha, partial, C);
 }
 
 }  // namespace mpsxx
