@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="split", choices=["split", "fp64"])
+    ap.add_argument("--tole", type=float, default=1e-8, help="sweep tolerance (Davidson |r|^2 < 0.1 tole)")
+    ap.add_argument("--no-bond", action="store_true", help="skip the FP64-vs-split bond step")
     return ap.parse_args()
 
 
@@ -138,7 +140,32 @@ def build_workload(args, ctx):
     bond = args.bond if args.bond >= 0 else args.norb // 2 - 1
     dmrg.advance_left(ctx, st, bond)
     mL, mR, psi = dmrg.bond_operands(ctx, st, bond)
-    return dict(mpo_d=mpo_d, mL=mL, mR=mR, psi=psi, bond=bond, W=mpogen.mpo_bond_dims(mpo_d)[bond])
+    return dict(mpo_d=mpo_d, mL=mL, mR=mR, psi=psi, bond=bond, W=mpogen.mpo_bond_dims(mpo_d)[bond], st=st)
+
+
+def bond_compare(ctx, wl, M, tole):
+    """One full two-site step (merged operators, diagonal, Davidson, SVD, renormalise,
+    expand) on the bench bond, FP64 and split precision from identical inputs."""
+    from mpsxx_gb300 import core
+
+    st, i = wl["st"], wl["bond"]
+    out = {}
+    for name, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
+        core.set_precision(ctx, prec)
+        ctx.sync()
+        t0 = time.perf_counter()
+        e, env, nl, nr, s = core.optimize_twosite_merged(ctx, True, st.mpo[i], st.mpo[i + 1], st.lenv[i],
+                                                         st.renv[i + 1], st.wave[i], st.wave[i + 1], 0.1 * tole, M)
+        dt = time.perf_counter() - t0
+        out[name] = {"seconds": dt, "energy": e, "n_sigma": int(s["n_sigma"]),
+                     "n_sigma_fp64": int(s["n_sigma_fp64"]) if prec != core.FP64 else int(s["n_sigma"]),
+                     "t_davidson": s["t_davidson"], "t_renorm": s["t_renorm"], "t_svd": s["t_svd"],
+                     "t_merge": s["t_merge"], "converged": int(s["converged"])}
+    core.set_precision(ctx, core.FP64)
+    out["abs_dE"] = abs(out["split"]["energy"] - out["fp64"]["energy"])
+    out["speedup"] = out["fp64"]["seconds"] / out["split"]["seconds"]
+    out["tole"] = tole
+    return out
 
 
 def roofline_peaks():
@@ -331,6 +358,7 @@ def main():
 
     peaks, src = roofline_peaks()
     fp64_peak = measure_fp64_peak(torch)
+    bond = bond_compare(ctx, wl, args.M, args.tole) if not args.no_bond else None
     out = None
     if rank == 0:
         achieved = fl_per_step / kt["sigma_kernels_s"] / 1e12
@@ -366,6 +394,7 @@ def main():
                           "peak": fp64_peak, "frac": fl_per_step / fp64_s / 1e12 / fp64_peak,
                           "speedup_of_headline": fp64_s / kt["sigma_kernels_s"]},
             "accuracy": {"max_rel_err_vs_fp64": rel},
+            "bond_step": bond,
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline:

@@ -257,14 +257,6 @@ void GemmPlan::upload(cudaStream_t st) {
   reduce_tc.upload(h_reduce_tc, st);
 }
 
-void GemmPlan::run_tc(double alpha, const double* A, const double* B, double* C, double* partial, int* err,
-                      cudaStream_t st) const {
-  if (nslots_tc > 0 && partial == nullptr) throw Error(kInternal, "gemm plan: split-K scratch missing");
-  launch_gemm_tc(ta, tb, alpha, A, B, C, tiles_tc.get(), static_cast<int>(h_tiles_tc.size()), dtasks.get(),
-                 pairs.get(), partial, err, st);
-  if (nslots_tc > 0)
-    launch_gemm_tc_reduce(reduce_tc.get(), static_cast<int>(h_reduce_tc.size()), dtasks.get(), alpha, partial, C, st);
-}
 
 void GemmPlan::run(double alpha, const double* A, const double* B, double* C, double* partial,
                    cudaStream_t st) const {
@@ -1027,8 +1019,11 @@ double normalize_tensor(Context& ctx, DTensor& x) {
 // ---------------------------------------------------------------------------
 // Davidson (single root)
 // ---------------------------------------------------------------------------
-double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag, DTensor& wfnc, double tol,
-                   DavidsonStats* stats) {
+// The Davidson loop of src/diagonalize.hpp:310-449 in the context's current
+// precision.  Stops when |r|^2 < tol, or — with rel_floor > 0 — when |r|^2 falls
+// below (rel_floor * E)^2, the resolution of an inexact operator.
+static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag, DTensor& wfnc,
+                           double tol, double rel_floor, int max_macro, DavidsonStats& S) {
   const int max_ritz = 10;
   const int64_t n = wfnc.nnz;
   if (diag.nnz != wfnc.nnz)
@@ -1045,9 +1040,6 @@ double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTens
   double* part = ctx.partial.as<double>();
   double* sc = ctx.scalars.as<double>();  // [0..99] dots, [100] norm, [101] dot, [128..227] rvec
   double* rvec_d = sc + 128;
-  DavidsonStats local;
-  DavidsonStats& S = stats ? *stats : local;
-  S = DavidsonStats{};
 
   auto sigma_of = [&](int k) {
     cuda_check(cudaMemsetAsync(sigma + k * n, 0, n * sizeof(double), st), "sigma zero");
@@ -1064,7 +1056,7 @@ double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTens
   double eval = 0.0;
   int niter = 0, iconv = 0;
   std::vector<double> hdots(100), heff, rvec, rval;
-  while (iconv < 1 && niter < 4) {
+  while (iconv < 1 && niter < max_macro) {
     normalize(trial);
     sigma_of(0);
     for (int m = 1; m <= max_ritz; ++m) {
@@ -1094,7 +1086,7 @@ double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTens
       cuda_check(cudaMemcpyAsync(&rnorm, sc + 101, sizeof(double), cudaMemcpyDeviceToHost, st), "rnorm d2h");
       ctx.sync();
       S.rnorm = rnorm;
-      if (rnorm < tol) {
+      if (rnorm < tol || (rel_floor > 0.0 && rnorm < rel_floor * rel_floor * eval * eval)) {
         ++iconv;
         break;
       }
@@ -1115,42 +1107,50 @@ double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTens
     }
     ++niter;
   }
-  S.macro = niter;
+  S.macro += niter;
   S.converged = iconv;
   launch_copy_vec(wfnc.d, trial, n, st);
   normalize(wfnc.d);
   ctx.sync();
-  if (ctx.precision != kFP64) {
-    check_device_error(ctx);
-    // refinement: the accepted energy is the Rayleigh quotient of one FP64
-    // H_eff*psi of the (normalised) Davidson vector, and the FP64 residual is reported
-    const int saved = ctx.precision;
-    ctx.precision = kFP64;
-    cuda_check(cudaMemsetAsync(sigma, 0, n * sizeof(double), st), "sigma zero");
-    try {
-      sigma_run(ctx, sp, L, R, wfnc.d, sigma);
-    } catch (...) {
-      ctx.precision = saved;
-      throw;
-    }
-    ctx.precision = saved;
-    S.n_sigma_fp64 += 1;
-    launch_multidot(wfnc.d, 1, sigma, 1, n, n, sc + 103, part, nblk, st);
-    double e64 = 0.0;
-    cuda_check(cudaMemcpyAsync(&e64, sc + 103, sizeof(double), cudaMemcpyDeviceToHost, st), "e64 d2h");
-    ctx.sync();
-    launch_copy_vec(errv, sigma, n, st);
-    launch_axpy(errv, wfnc.d, n, -e64, st);
-    launch_multidot(errv, 1, errv, 1, n, n, sc + 104, part, nblk, st);
-    double r64 = 0.0;
-    cuda_check(cudaMemcpyAsync(&r64, sc + 104, sizeof(double), cudaMemcpyDeviceToHost, st), "r64 d2h");
-    ctx.sync();
-    ctx.kernel_launches += 7;
-    S.energy_split = eval;
-    S.rnorm_fp64 = r64;
-    eval = e64;
-  }
   return eval;
+}
+
+// Relative resolution of the split-TF32 operator: |H_split psi - H psi| stays
+// below ~1e-5 |H psi| (measured a few 1e-6), so a residual under (1e-5 E)^2 is
+// as converged as that operator allows.
+constexpr double kSplitResidualFloor = 1.0e-5;
+
+double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag, DTensor& wfnc, double tol,
+                   DavidsonStats* stats) {
+  DavidsonStats local;
+  DavidsonStats& S = stats ? *stats : local;
+  S = DavidsonStats{};
+  if (ctx.precision == kFP64) return davidson_run(ctx, L, R, diag, wfnc, tol, 0.0, 4, S);
+  // split precision: the bulk of the iterations with the tensor-core operator ...
+  const double e_split = davidson_run(ctx, L, R, diag, wfnc, tol, kSplitResidualFloor, 4, S);
+  check_device_error(ctx);
+  S.energy_split = e_split;
+  // ... then the refinement: the same Davidson from the split vector with the FP64
+  // operator.  Its first FP64 H_eff*psi gives the accepted Rayleigh quotient and the
+  // FP64 residual; when that residual already meets the tolerance this is the only
+  // FP64 application, otherwise the FP64 iterations continue to the tolerance.
+  DavidsonStats R64;
+  const int saved = ctx.precision;
+  ctx.precision = kFP64;
+  double e = 0.0;
+  try {
+    e = davidson_run(ctx, L, R, diag, wfnc, tol, 0.0, 2, R64);
+  } catch (...) {
+    ctx.precision = saved;
+    throw;
+  }
+  ctx.precision = saved;
+  S.n_sigma_fp64 = R64.n_sigma;
+  S.n_sigma += R64.n_sigma;
+  S.micro += R64.micro;
+  S.rnorm_fp64 = R64.rnorm;
+  S.converged = R64.converged;
+  return e;
 }
 
 // ---------------------------------------------------------------------------

@@ -74,9 +74,6 @@ struct GemmPlan {
   void upload(cudaStream_t st);
   // partial: nslots * 64 * 64 doubles of scratch (may be null when nslots == 0)
   void run(double alpha, const double* A, const double* B, double* C, double* partial, cudaStream_t st) const;
-  // split TF32 tensor-core path; err: device flag set on an MMA wait timeout
-  void run_tc(double alpha, const double* A, const double* B, double* C, double* partial, int* err,
-              cudaStream_t st) const;
   size_t partial_bytes() const { return size_t(nslots) * kGemmTile * kGemmTile * sizeof(double); }
   size_t partial_bytes_tc() const { return size_t(nslots_tc) * kTcTileM * kTcTileN * sizeof(double); }
 };

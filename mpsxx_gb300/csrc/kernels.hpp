@@ -59,13 +59,6 @@ constexpr int kGemmTile = 64;
 constexpr int kTcTileM = 128;
 constexpr int kTcTileN = 64;
 
-void launch_gemm_tc(int transa, int transb, double alpha, const double* A, const double* B, double* C,
-                    const DTile* tiles, int ntiles, const DGemmTask* tasks, const DGemmPair* pairs, double* partial,
-                    int* err, cudaStream_t st);
-void launch_gemm_tc_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
-                           double* C, cudaStream_t st);
-int tc_smem_bytes();
-
 // ---- pre-packed split-TF32 operands -----------------------------------------
 constexpr int kPkTileK = 32;                          // K elements per packed slice
 constexpr uint32_t kPkTileABytes = 128 * 32 * 4 * 2;  // A tile: hi|lo TF32, 128 rows

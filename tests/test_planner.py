@@ -155,6 +155,54 @@ def test_qshape_mismatch_raises_reference_message(lib):
     assert "gemm_contract_qshape contraction of quantum numbers failed" in str(ei.value)
 
 
+CPP_PROGRAM = r"""
+#include <cstdio>
+#include "mpsxx_gb300.hpp"
+using namespace mpsxx::gb300;
+int main() {
+  // L[A,w,A'] (3 sectors, w: 2 operators) x psi[A',B] with host-only descriptors
+  std::vector<std::vector<Sector>> ls = {{{0,0,2},{1,1,3},{2,0,1}}, {{0,0,1},{1,1,1}}, {{0,0,2},{-1,-1,3},{-2,0,1}}};
+  std::vector<std::vector<Sector>> ps = {{{0,0,2},{1,1,3},{2,0,1}}, {{2,0,4},{1,-1,2},{0,0,3}}};
+  QSDArray L(nullptr, 0, 0, ls), P(nullptr, 2, 0, ps);
+  auto tasks = gemm_tasks(MPSXX_NOTRANS, MPSXX_NOTRANS, L, P, 3);
+  size_t np = 0;
+  for (auto& t : tasks) np += t.second.size();
+  std::printf("%zu %zu %lld %lld\n", tasks.size(), np, (long long)L.nblocks(), (long long)P.nblocks());
+  try {
+    QSDArray bad(nullptr, 0, 0, ls, nullptr);
+    gemm_tasks(MPSXX_NOTRANS, MPSXX_NOTRANS, bad, bad, 5);
+  } catch (const std::runtime_error& e) {
+    std::printf("error: %s\n", e.what());
+  }
+  return 0;
+}
+"""
+
+
+def test_cpp_dropin_header_compiles_and_plans(lib, tmp_path):
+    """The C++ drop-in header (reference names over gb300::QSDArray) builds against the
+    library and reproduces the Python binding's enumeration; errors become exceptions."""
+    import subprocess
+
+    from mpsxx_gb300 import core
+    from mpsxx_gb300._lib import LIB_PATH
+
+    src = tmp_path / "dropin.cpp"
+    src.write_text(CPP_PROGRAM)
+    exe = tmp_path / "dropin"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                    "-L", str(LIB_PATH.parent), "-lmpsxx_gb300", f"-Wl,-rpath,{LIB_PATH.parent}"], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    ntask, npair, nbl, nbp = (int(x) for x in out[0].split())
+    L = core.Tensor.create(None, (0, 0), [[(0, 0), (1, 1), (2, 0)], [(0, 0), (1, 1)], [(0, 0), (-1, -1), (-2, 0)]],
+                           [[2, 3, 1], [1, 1], [2, 3, 1]])
+    P = core.Tensor.create(None, (2, 0), [[(0, 0), (1, 1), (2, 0)], [(2, 0), (1, -1), (0, 0)]], [[2, 3, 1], [4, 2, 3]])
+    ref = core.gemm_tasks(0, 0, L, P, 3)
+    assert (ntask, npair) == (len(ref), sum(len(p) for _, p in ref)) and ntask > 0
+    assert nbl == L.info()[2] and nbp == P.info()[2]
+    assert out[1].startswith("error: ") and "rank" in out[1]
+
+
 def test_invalid_tensor_arguments_are_rejected(lib):
     from mpsxx_gb300 import core
     from mpsxx_gb300._lib import MpsxxError
