@@ -183,6 +183,23 @@ int mpsxx_sigma_device_time(mpsxx_context* ctx, const mpsxx_tensor* lopr, const 
 /* x /= ||x||_2 (btas::Normalize, include/btas/QSPARSE/QSTBLAS.h:239-243); norm may be NULL. */
 int mpsxx_normalize(mpsxx_context* ctx, mpsxx_tensor* x, double* norm);
 
+/* Allocation-free multi-dot; this entry point has no counterpart in the reference.
+ * out[i*ny + j] = dot(X + i*stride, Y + j*stride) over n doubles (all device
+ * pointers), 1 <= nx, ny <= 10: the Rayleigh-Ritz products of the Davidson solver.
+ * It is for callers that must not allocate device memory while they run — code
+ * being recorded into a CUDA graph, a host framework that owns the device memory
+ * through its own pool, or a loop that cannot afford the synchronisation an
+ * allocation may cause.  It needs no context and calls no allocator: its reduction
+ * scratch is a fixed array of 304 x 100 doubles (243 KB) built into the library,
+ * which every device that loads the library holds until the process exits.  The
+ * first call on a device resolves the array's address for that device, so make it
+ * before any stream capture.  All calls on a device share the array: calls whose
+ * kernels overlap on the GPU race.  Larger requests (nx or ny > 10) are rejected
+ * with MPSXX_INVALID_ARGUMENT.  The work is enqueued on `stream` (NULL: the default
+ * stream) and the call returns without waiting for it. */
+int mpsxx_multidot_noalloc(const double* X, int nx, const double* Y, int ny, int64_t n, int64_t stride,
+                           double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -50,6 +50,7 @@ SIGNATURES = {
     "mpsxx_expand_cols": (C.c_int, [vp, vp, vp, vpp]),
     "mpsxx_normalize": (C.c_int, [vp, vp, c_dbl_p]),
     "mpsxx_sigma_device_time": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, c_dbl_p]),
+    "mpsxx_multidot_noalloc": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int64, C.c_int64, vp, vp]),
     "mpsxx_merge_wavefunction":(C.c_int, [vp, vp, vp, vp, vp, vp, vp, vpp]),
     "mpsxx_expand_wavefunction": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vpp, vpp]),
 }

@@ -69,6 +69,10 @@ mpsxx_tensor* wrap(std::unique_ptr<DTensor> t, mpsxx_context* owner) {
 }
 }  // namespace
 
+namespace mpsxx {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace mpsxx
+
 extern "C" {
 
 int mpsxx_version(void) { return 100; }
