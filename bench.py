@@ -44,7 +44,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="split", choices=["split", "fp64"])
     ap.add_argument("--tole", type=float, default=1e-8, help="sweep tolerance (Davidson |r|^2 < 0.1 tole)")
-    ap.add_argument("--no-bond", action="store_true", help="skip the FP64-vs-split bond step")
+    ap.add_argument("--bond-step", action="store_true", help="also time one full bond step at the bench bond")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the FP64-vs-split sweep comparison")
+    ap.add_argument("--sweep-norb", type=int, default=12)
+    ap.add_argument("--sweep-M", type=int, default=128)
+    ap.add_argument("--sweep-max", type=int, default=12)
     return ap.parse_args()
 
 
@@ -141,6 +145,40 @@ def build_workload(args, ctx):
     dmrg.advance_left(ctx, st, bond)
     mL, mR, psi = dmrg.bond_operands(ctx, st, bond)
     return dict(mpo_d=mpo_d, mL=mL, mR=mR, psi=psi, bond=bond, W=mpogen.mpo_bond_dims(mpo_d)[bond], st=st)
+
+
+def sweep_compare(args, device: int):
+    """Two-site DMRG to convergence (|dE| < tole after >= 2 sweeps), FP64 and split
+    precision, from the reference's initial state on a smaller synthetic QC system."""
+    from mpsxx_gb300 import core, dmrg, mpogen
+
+    n, M = args.sweep_norb, args.sweep_M
+    h1, eri = mpogen.synthetic_qc_integrals(n, 2 * n, args.seed)
+    mpo_d = mpogen.qc_mpo(h1, eri)
+    res = {"workload": f"qc n={n} K={2 * n} seed={args.seed} M={M} tole={args.tole}"}
+    for name, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
+        ctx = core.Context(device)
+        core.set_precision(ctx, prec)
+        mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
+        st = dmrg.make_initial_state(ctx, mpo, n, 0, M)
+        sweeps, e_prev = [], 0.0
+        for it in range(args.sweep_max):
+            log = dmrg.make_sweep(ctx, st, args.tole)
+            sweeps.append({"seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma})
+            de = log.energy - e_prev
+            e_prev = log.energy
+            if it > 0 and abs(de) < args.tole:
+                break
+        res[name] = {"sweeps": len(sweeps), "energy": sweeps[-1]["energy"],
+                     "seconds_total": sum(s["seconds"] for s in sweeps),
+                     "seconds_last_sweep": sweeps[-1]["seconds"],
+                     "n_sigma_total": sum(s["n_sigma"] for s in sweeps), "per_sweep": sweeps}
+        del st, mpo
+        ctx.close()
+    res["abs_dE"] = abs(res["split"]["energy"] - res["fp64"]["energy"])
+    res["speedup_last_sweep"] = res["fp64"]["seconds_last_sweep"] / res["split"]["seconds_last_sweep"]
+    res["speedup_total"] = res["fp64"]["seconds_total"] / res["split"]["seconds_total"]
+    return res
 
 
 def bond_compare(ctx, wl, M, tole):
@@ -358,7 +396,8 @@ def main():
 
     peaks, src = roofline_peaks()
     fp64_peak = measure_fp64_peak(torch)
-    bond = bond_compare(ctx, wl, args.M, args.tole) if not args.no_bond else None
+    bond = bond_compare(ctx, wl, args.M, args.tole) if args.bond_step else None
+    sweep = sweep_compare(args, local) if not args.no_sweep else None
     out = None
     if rank == 0:
         achieved = fl_per_step / kt["sigma_kernels_s"] / 1e12
@@ -395,6 +434,7 @@ def main():
                           "speedup_of_headline": fp64_s / kt["sigma_kernels_s"]},
             "accuracy": {"max_rel_err_vs_fp64": rel},
             "bond_step": bond,
+            "sweeps": sweep,
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline:
