@@ -148,34 +148,42 @@ def build_workload(args, ctx):
 
 
 def sweep_compare(args, device: int):
-    """Two-site DMRG to convergence (|dE| < tole after >= 2 sweeps), FP64 and split
-    precision, from the reference's initial state on a smaller synthetic QC system."""
+    """Two-site DMRG from the reference's initial state on a smaller synthetic QC
+    system: FP64 until |dE| < tole after >= 2 sweeps, then split precision for the
+    same number of sweeps, so that the energies are compared sweep by sweep."""
     from mpsxx_gb300 import core, dmrg, mpogen
 
     n, M = args.sweep_norb, args.sweep_M
     h1, eri = mpogen.synthetic_qc_integrals(n, 2 * n, args.seed)
     mpo_d = mpogen.qc_mpo(h1, eri)
     res = {"workload": f"qc n={n} K={2 * n} seed={args.seed} M={M} tole={args.tole}"}
+    nsweeps = args.sweep_max
     for name, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
         ctx = core.Context(device)
         core.set_precision(ctx, prec)
         mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
         st = dmrg.make_initial_state(ctx, mpo, n, 0, M)
         sweeps, e_prev = [], 0.0
-        for it in range(args.sweep_max):
+        for it in range(nsweeps):
             log = dmrg.make_sweep(ctx, st, args.tole)
-            sweeps.append({"seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma})
+            sweeps.append({"seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma,
+                           "sigma_flops": log.sigma_flops, **{k: round(v, 4) for k, v in log.times.items()}})
             de = log.energy - e_prev
             e_prev = log.energy
-            if it > 0 and abs(de) < args.tole:
+            if prec == core.FP64 and it > 0 and abs(de) < args.tole:
+                nsweeps = it + 1
                 break
         res[name] = {"sweeps": len(sweeps), "energy": sweeps[-1]["energy"],
                      "seconds_total": sum(s["seconds"] for s in sweeps),
                      "seconds_last_sweep": sweeps[-1]["seconds"],
-                     "n_sigma_total": sum(s["n_sigma"] for s in sweeps), "per_sweep": sweeps}
+                     "n_sigma_total": sum(s["n_sigma"] for s in sweeps),
+                     "sigma_tflops_last_sweep": sweeps[-1]["sigma_flops"] / sweeps[-1]["seconds"] / 1e12,
+                     "per_sweep": sweeps}
         del st, mpo
         ctx.close()
-    res["abs_dE"] = abs(res["split"]["energy"] - res["fp64"]["energy"])
+    de = [abs(a["energy"] - b["energy"]) for a, b in zip(res["split"]["per_sweep"], res["fp64"]["per_sweep"])]
+    res["abs_dE"] = de[-1]
+    res["abs_dE_max_over_sweeps"] = max(de)
     res["speedup_last_sweep"] = res["fp64"]["seconds_last_sweep"] / res["split"]["seconds_last_sweep"]
     res["speedup_total"] = res["fp64"]["seconds_total"] / res["split"]["seconds_total"]
     return res

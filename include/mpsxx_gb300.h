@@ -56,16 +56,36 @@ int mpsxx_context_sync(mpsxx_context* ctx);
 /* Precision of the bulk contractions of this context (no reference counterpart:
  * the reference computes in FP64 only).  MPSXX_FP64: every contraction in FP64.
  * MPSXX_SPLIT_TF32: H_eff*psi runs on the tensor cores with each FP64 operand
- * split into two TF32 numbers (3 products, FP32 accumulation per block pair,
- * FP64 across pairs); Davidson subspace algebra, the Rayleigh-Ritz solve and
- * residual norms stay FP64, and the accepted energy of every diagonalize call is
- * the Rayleigh quotient of one FP64 H_eff*psi (refinement step). */
-enum mpsxx_precision { MPSXX_FP64 = 0, MPSXX_SPLIT_TF32 = 1 };
+ * split into two TF32 numbers (3 products, FP32 accumulation within groups of
+ * 1024 products, FP64 across groups); Davidson subspace algebra, the Rayleigh-Ritz
+ * solve and residual norms stay FP64.  Every diagonalize call ends with a
+ * refinement anchored on one FP64 H_eff*psi: the converged split vector's FP64
+ * product fixes all subspace entries that involve it, and the remaining
+ * corrections use the split operator (a second anchor only when that continuation
+ * does not converge).  The returned value is that refined Ritz value; when the
+ * split vector already meets the tolerance it is the FP64 Rayleigh quotient. */
+enum mpsxx_precision { MPSXX_FP64 = 0, MPSXX_SPLIT_TF32 = 1, MPSXX_SPLIT_TF32_ALL = 2 };
 int mpsxx_context_set_precision(mpsxx_context* ctx, int precision);
 int mpsxx_context_get_precision(const mpsxx_context* ctx, int* precision);
 
+/* Truncation tie window of canonicalize: singular values s with
+ * s >= cutoff * (1 - tie_rtol) are kept together with the cutoff value (the
+ * reference keeps s >= cutoff, include/btas/QSPARSE/QSTLAPACK.h:217-232), so that
+ * symmetry-degenerate values that differ by rounding stay together.
+ * tie_rtol < 0 restores the default, 1e-10. */
+int mpsxx_context_set_truncation(mpsxx_context* ctx, double tie_rtol);
+
 /* Kernel launches issued, FP64-equivalent sigma FLOPs and sigma calls so far. */
 int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* sigma_flops, int64_t* sigma_calls);
+
+/* Phase timers of the bond step, in seconds.  enable = 1 starts accumulating (each
+ * phase then ends with a stream synchronisation), 0 stops, -1 leaves the setting;
+ * reset = 1 zeroes them after they are read.  Up to n timers are written to t, in
+ * the order of MPSXX_PHASE_NAMES; *count receives the number of phases. */
+#define MPSXX_PHASE_NAMES                                                                                    \
+  "merge_plan", "merge_alloc", "merge_run", "wave_merge", "sigma_plan", "sigma", "davidson_rest", "svd_solve", \
+      "svd_select", "svd_post", "renorm_plan", "renorm_run"
+int mpsxx_context_profile(mpsxx_context* ctx, int enable, int reset, double* t, int n, int* count);
 
 /* ---- tensors ------------------------------------------------------------- */
 /* Create a block-sparse tensor.  qn holds 2*sum(nsec) ints (p, 2Sz per sector,

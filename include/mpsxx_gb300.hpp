@@ -37,6 +37,7 @@ class Context {
   Context& operator=(const Context&) = delete;
   mpsxx_context* get() const { return h_; }
   void set_precision(int p) { check(mpsxx_context_set_precision(h_, p)); }
+  void set_truncation(double tie_rtol) { check(mpsxx_context_set_truncation(h_, tie_rtol)); }
 
  private:
   mpsxx_context* h_ = nullptr;

@@ -41,6 +41,18 @@ class Context:
         check(lib().mpsxx_context_counters(self.h, C.byref(la), C.byref(fl), C.byref(ca)))
         return {"launches": la.value, "sigma_flops": fl.value, "sigma_calls": ca.value}
 
+    def set_truncation(self, tie_rtol: float = -1.0):
+        """Relative tie window at the truncation cutoff (< 0: the precision's default)."""
+        check(lib().mpsxx_context_set_truncation(self.h, float(tie_rtol)))
+
+    def profile(self, enable=-1, reset=False):
+        """Phase timers in seconds (PHASE_NAMES); enable=1/0 switches timing on/off."""
+        t = (C.c_double * len(PHASE_NAMES))()
+        cnt = C.c_int()
+        check(lib().mpsxx_context_profile(self.h, int(enable), int(bool(reset)), t, len(PHASE_NAMES), C.byref(cnt)))
+        assert cnt.value == len(PHASE_NAMES)
+        return dict(zip(PHASE_NAMES, list(t)))
+
     def close(self):
         if getattr(self, "h", None):
             lib().mpsxx_context_destroy(self.h)
@@ -309,11 +321,15 @@ def expand_wavefunction(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, 
     return Tensor(lo, ctx), Tensor(ro, ctx)
 
 
+PHASE_NAMES = ("merge_plan", "merge_alloc", "merge_run", "wave_merge", "sigma_plan", "sigma", "davidson_rest",
+               "svd_solve", "svd_select", "svd_post", "renorm_plan", "renorm_run")
+
 BOND_STAT_KEYS = ("n_sigma", "sigma_flops", "t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "converged",
                   "rnorm", "energy_split", "rnorm_fp64", "n_sigma_fp64")
 
 FP64 = 0
 SPLIT_TF32 = 1
+SPLIT_TF32_ALL = 2  # H_eff*psi and the renormalisation contractions
 
 
 def set_precision(ctx: Context, precision: int):

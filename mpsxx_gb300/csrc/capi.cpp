@@ -103,7 +103,8 @@ int mpsxx_context_sync(mpsxx_context* ctx) {
 
 int mpsxx_context_set_precision(mpsxx_context* ctx, int precision) {
   return guard([&] {
-    need(precision == MPSXX_FP64 || precision == MPSXX_SPLIT_TF32, "unknown precision");
+    need(precision == MPSXX_FP64 || precision == MPSXX_SPLIT_TF32 || precision == MPSXX_SPLIT_TF32_ALL,
+         "unknown precision");
     ctx_of(ctx).precision = precision;
   });
 }
@@ -115,12 +116,31 @@ int mpsxx_context_get_precision(const mpsxx_context* ctx, int* precision) {
   });
 }
 
+int mpsxx_context_set_truncation(mpsxx_context* ctx, double tie_rtol) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    ctx->ctx->tie_rtol = tie_rtol;
+  });
+}
+
 int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* sigma_flops, int64_t* sigma_calls) {
   return guard([&] {
     need(ctx && ctx->ctx, "null context");
     if (launches) *launches = ctx->ctx->kernel_launches;
     if (sigma_flops) *sigma_flops = ctx->ctx->sigma_flops;
     if (sigma_calls) *sigma_calls = ctx->ctx->sigma_calls;
+  });
+}
+
+int mpsxx_context_profile(mpsxx_context* ctx, int enable, int reset, double* t, int n, int* count) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    mpsxx::Context& c = *ctx->ctx;
+    if (count) *count = mpsxx::kNumPhases;
+    for (int i = 0; t && i < n && i < mpsxx::kNumPhases; ++i) t[i] = c.timers[i];
+    if (reset)
+      for (double& x : c.timers) x = 0.0;
+    if (enable >= 0) c.profile = enable != 0;
   });
 }
 
@@ -328,6 +348,7 @@ int mpsxx_renormalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* opr0,
     need(opr1 != nullptr, "null output");
     Context& c = ctx_of(ctx);
     auto r = renormalize(c, forward != 0, ten(opr0), ten(bra), ten(ket));
+    c.sync();
     *opr1 = wrap(std::move(r), ctx);
   });
 }
@@ -338,6 +359,7 @@ int mpsxx_compute_merged_operator(mpsxx_context* ctx, int forward, const mpsxx_t
     need(out != nullptr, "null output");
     Context& c = ctx_of(ctx);
     auto r = compute_merged_operator(c, forward != 0, ten(mpo), ten(opr));
+    c.sync();
     *out = wrap(std::move(r), ctx);
   });
 }
@@ -364,6 +386,7 @@ int mpsxx_canonicalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* wfnc
     need(lmat && rmat, "null output");
     Context& c = ctx_of(ctx);
     CanonResult r = canonicalize(c, forward != 0, ten(wfnc), M, noise);
+    c.sync();
     *lmat = wrap(std::move(r.lmat), ctx);
     *rmat = wrap(std::move(r.rmat), ctx);
   });
@@ -379,6 +402,7 @@ int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_t
     Context& c = ctx_of(ctx);
     BondOut b = optimize_twosite_merged(c, forward != 0, ten(lmpo), ten(rmpo), ten(lopr), ten(ropr), ten(lwfn),
                                         ten(rwfn), tole, M);
+    c.sync();
     if (energy) *energy = b.stats.energy;
     if (stats) {
       stats[0] = b.stats.dav.n_sigma;
@@ -408,6 +432,7 @@ int mpsxx_merge_cols(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** o
     need(A.sh.rank == 3, "merge_cols: expects a 3-index tensor");
     MergeInfo info({A.sh.qshape[1], A.sh.qshape[2]}, {A.sh.dshape[1], A.sh.dshape[2]});
     *out = wrap(merge_cols(c, A, info), ctx);
+    c.sync();
   });
 }
 
@@ -418,6 +443,7 @@ int mpsxx_gemm(mpsxx_context* ctx, int transa, int transb, double alpha, const m
     Context& cx = ctx_of(ctx);
     *c = wrap(gemm_new(cx, transa ? kTrans : kNoTrans, transb ? kTrans : kNoTrans, alpha, ten(a), ten(b), c_rank),
               ctx);
+    cx.sync();
   });
 }
 
@@ -429,6 +455,7 @@ int mpsxx_expand_cols(mpsxx_context* ctx, const mpsxx_tensor* b, const mpsxx_ten
     need(L.sh.rank == 3, "expand_cols: `like` must be a 3-index tensor");
     MergeInfo info({L.sh.qshape[1], L.sh.qshape[2]}, {L.sh.dshape[1], L.sh.dshape[2]});
     *out = wrap(expand_cols(c, ten(b), info), ctx);
+    c.sync();
   });
 }
 
@@ -448,6 +475,7 @@ int mpsxx_merge_wavefunction(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const
     Context& c = ctx_of(ctx);
     WaveMerge wm = wave_merge_infos(ten(lmpo), ten(rmpo), ten(lopr), ten(ropr));
     *psi = wrap(merge_wave(c, wm, ten(lwfn), ten(rwfn)), ctx);
+    c.sync();
   });
 }
 
@@ -460,6 +488,7 @@ int mpsxx_expand_wavefunction(mpsxx_context* ctx, const mpsxx_tensor* lmpo, cons
     WaveMerge wm = wave_merge_infos(ten(lmpo), ten(rmpo), ten(lopr), ten(ropr));
     *lwfn = wrap(expand_rows(c, wm.ql, ten(lmat)), ctx);
     *rwfn = wrap(expand_cols(c, ten(rmat), wm.qr), ctx);
+    c.sync();
   });
 }
 

@@ -3,10 +3,15 @@
 #include "engine.hpp"
 
 #include <algorithm>
+#include <array>
+#include <atomic>
+#include <exception>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <thread>
+#include <tuple>
 
 #include "jacobi.hpp"
 
@@ -20,23 +25,152 @@ static void solver_check(cusolverStatus_t s, const char* what) {
   if (s != CUSOLVER_STATUS_SUCCESS) throw Error(kSolver, std::string(what) + ": cusolver status " + std::to_string(s));
 }
 
-void DevBuf::ensure(size_t bytes) {
-  if (bytes <= cap) return;
-  release();
-  const size_t nb = std::max<size_t>(bytes, 256);
-  void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, nb);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    throw Error(kAlloc, std::string("device allocation of ") + std::to_string(nb) + " bytes failed: " +
-                            cudaGetErrorString(e));
+// ---------------------------------------------------------------------------
+// device block cache
+// ---------------------------------------------------------------------------
+namespace {
+struct CachedBlock {
+  void* p;
+  int device;
+  cudaStream_t st;    // stream of the last owner
+  cudaEvent_t ready;  // recorded on st at release: the last owner's work is queued before it
+};
+
+class BlockCache {
+ public:
+  // Rounded allocation size: powers of two below 2 MiB, multiples of 2 MiB above.
+  static size_t round(size_t bytes) {
+    bytes = std::max<size_t>(bytes, 512);
+    if (bytes < (size_t(2) << 20)) {
+      size_t r = 512;
+      while (r < bytes) r <<= 1;
+      return r;
+    }
+    const size_t g = size_t(2) << 20;
+    return (bytes + g - 1) / g * g;
   }
-  p = q;
-  cap = nb;
+
+  void* get(size_t bytes, cudaStream_t st, size_t* got) {
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    const size_t want = round(bytes);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      // best fit among blocks of at most 5/4 of the request
+      for (auto it = free_.lower_bound(want); it != free_.end() && it->first <= want + want / 4; ++it) {
+        if (it->second.device != dev) continue;
+        CachedBlock b = it->second;
+        *got = it->first;
+        cached_ -= it->first;
+        free_.erase(it);
+        if (b.ready) {
+          if (b.st != st) cuda_check(cudaStreamWaitEvent(st, b.ready, 0), "block cache wait");
+          cudaEventDestroy(b.ready);
+        }
+        return b.p;
+      }
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      trim();  // give the cached blocks back and try once more
+      e = cudaMalloc(&p, want);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(kAlloc, std::string("device allocation of ") + std::to_string(want) + " bytes failed: " +
+                                cudaGetErrorString(e));
+      }
+    }
+    *got = want;
+    return p;
+  }
+
+  void put(void* p, size_t bytes, cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    bool live = false;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      live = live_.count(st) > 0;
+    }
+    // A stream that is no longer registered belonged to a context that drained it
+    // before going away: the block is idle and needs no event.
+    cudaEvent_t ev = nullptr;
+    if (live && (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess ||
+                 cudaEventRecord(ev, st) != cudaSuccess)) {
+      // the context is failing: return the block for good
+      cudaGetLastError();
+      if (ev) cudaEventDestroy(ev);
+      cudaFree(p);
+      return;
+    }
+    std::lock_guard<std::mutex> lk(mu_);
+    free_.emplace(bytes, CachedBlock{p, dev, live ? st : nullptr, ev});
+    cached_ += bytes;
+  }
+
+  void register_stream(cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(mu_);
+    live_[st] += 1;
+  }
+  void unregister_stream(cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = live_.find(st);
+    if (it != live_.end() && --it->second == 0) live_.erase(it);
+  }
+
+  // Free every cached block (waits for its last owner's work first).
+  void trim() {
+    std::multimap<size_t, CachedBlock> blocks;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      blocks.swap(free_);
+      cached_ = 0;
+    }
+    for (auto& kv : blocks) {
+      if (kv.second.ready) {
+        cudaEventSynchronize(kv.second.ready);
+        cudaEventDestroy(kv.second.ready);
+      }
+      cudaFree(kv.second.p);
+    }
+  }
+
+  size_t cached_bytes() {
+    std::lock_guard<std::mutex> lk(mu_);
+    return cached_;
+  }
+
+ private:
+  std::mutex mu_;
+  std::multimap<size_t, CachedBlock> free_;
+  std::map<cudaStream_t, int> live_;  // streams of live contexts
+  size_t cached_ = 0;
+};
+
+// Never destroyed: blocks may be released during static destruction, after the
+// CUDA runtime has begun shutting down.
+BlockCache& block_cache() {
+  static BlockCache* c = new BlockCache;
+  return *c;
+}
+}  // namespace
+
+void trim_block_cache() { block_cache().trim(); }
+size_t block_cache_bytes() { return block_cache().cached_bytes(); }
+
+void DevBuf::ensure(size_t bytes, cudaStream_t stream) {
+  if (bytes <= cap && stream == st) return;
+  release();
+  size_t got = 0;
+  p = block_cache().get(bytes, stream, &got);
+  cap = got;
+  st = stream;
 }
 
 void DevBuf::release() {
-  if (p) cudaFree(p);
+  if (p) block_cache().put(p, cap, st);
   p = nullptr;
   cap = 0;
 }
@@ -44,7 +178,7 @@ void DevBuf::release() {
 template <class T>
 void DevArray<T>::upload(const std::vector<T>& h, cudaStream_t st) {
   n = h.size();
-  buf.ensure(std::max<size_t>(1, n) * sizeof(T));
+  buf.ensure(std::max<size_t>(1, n) * sizeof(T), st);
   if (n) cuda_check(cudaMemcpyAsync(buf.p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice, st), "plan upload");
 }
 template struct DevArray<DTile>;
@@ -60,7 +194,7 @@ template struct DevArray<int64_t>;
 template struct DevArray<int>;
 
 void DTensor::alloc_device(cudaStream_t st, bool zero) {
-  store.ensure(std::max<int64_t>(nnz, 1) * sizeof(double));
+  store.ensure(std::max<int64_t>(nnz, 1) * sizeof(double), st);
   d = store.as<double>();
   if (zero && nnz) cuda_check(cudaMemsetAsync(d, 0, nnz * sizeof(double), st), "tensor zero");
 }
@@ -75,14 +209,46 @@ Context::Context(int dev, cudaStream_t st) : device(dev) {
   }
   solver_check(cusolverDnCreate(&solver), "cusolverDnCreate");
   solver_check(cusolverDnSetStream(solver, stream), "cusolverDnSetStream");
+  block_cache().register_stream(stream);
 }
 
 Context::~Context() {
+  // drain the stream and hand the context's buffers back while it is registered
+  cudaStreamSynchronize(stream);
+  sigma_plans.clear();
+  diag_plans.clear();
+  for (DevBuf* b : {&scr1, &scr2, &work, &partial, &scalars, &svd_work, &svd_mats, &gemm_part, &err_flag})
+    b->release();
+  for (auto& l : svd_lanes) {
+    cudaStreamSynchronize(l->stream);
+    l->work.release();
+    block_cache().unregister_stream(l->stream);
+    if (l->solver) cusolverDnDestroy(l->solver);
+    if (l->done) cudaEventDestroy(l->done);
+    cudaStreamDestroy(l->stream);
+  }
+  if (svd_ready) cudaEventDestroy(svd_ready);
+  block_cache().unregister_stream(stream);
   if (solver) cusolverDnDestroy(solver);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
 void Context::sync() { cuda_check(cudaStreamSynchronize(stream), "stream sync"); }
+
+static double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+PhaseTimer::PhaseTimer(Context& c, int ph) : ctx(c), phase(ph), t0(c.profile ? now() : 0.0) {}
+
+void PhaseTimer::stop() {
+  if (!open) return;
+  open = false;
+  if (!ctx.profile) return;
+  cudaStreamSynchronize(ctx.stream);
+  dt = now() - t0;
+  ctx.timers[phase] += dt;
+}
 
 // ---------------------------------------------------------------------------
 // grouped GEMM plans
@@ -269,7 +435,7 @@ void GemmPlan::run(double alpha, const double* A, const double* B, double* C, do
 
 static double* gemm_scratch(Context& ctx, const GemmPlan& p) {
   if (p.nslots == 0) return nullptr;
-  ctx.gemm_part.ensure(p.partial_bytes());
+  ctx.gemm_part.ensure(p.partial_bytes(), ctx.stream);
   return ctx.gemm_part.as<double>();
 }
 
@@ -312,6 +478,7 @@ SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DT
   auto key = std::make_tuple(L.layout_id, R.layout_id, psi.layout_id);
   auto it = ctx.sigma_plans.find(key);
   if (it != ctx.sigma_plans.end()) return *it->second;
+  PhaseTimer tm(ctx, kPhSigmaPlan);
   if (L.sh.rank != 3 || R.sh.rank != 3 || psi.sh.rank != 2)
     throw Error(kInvalidArgument, "compute_sigma_vector: expects 3-index operators and a 2-index wavefunction");
   auto p = std::make_unique<SigmaPlan>();
@@ -421,10 +588,10 @@ static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Te
   p.pk_L.packs.upload(p.pk_L.h_packs, ctx.stream);
   p.pk_R.packs.upload(p.pk_R.h_packs, ctx.stream);
   p.pk_psi.packs.upload(p.pk_psi.h_packs, ctx.stream);
-  p.pk_L.buf.ensure(std::max<int64_t>(p.pk_L.bytes, 16));
-  p.pk_R.buf.ensure(std::max<int64_t>(p.pk_R.bytes, 16));
-  p.pk_psi.buf.ensure(std::max<int64_t>(p.pk_psi.bytes, 16));
-  p.pk_scr1.buf.ensure(std::max<int64_t>(p.pk_scr1.bytes, 16));
+  p.pk_L.buf.ensure(std::max<int64_t>(p.pk_L.bytes, 16), ctx.stream);
+  p.pk_R.buf.ensure(std::max<int64_t>(p.pk_R.bytes, 16), ctx.stream);
+  p.pk_psi.buf.ensure(std::max<int64_t>(p.pk_psi.bytes, 16), ctx.stream);
+  p.pk_scr1.buf.ensure(std::max<int64_t>(p.pk_scr1.bytes, 16), ctx.stream);
   p.pk_built = true;
 }
 
@@ -435,19 +602,68 @@ static void pack_into(Context& ctx, Packed& P, const DTensor& t) {
   ctx.kernel_launches += 1;
 }
 
+static void build_split_gemm(Context& ctx, SplitGemm& sg, const GemmPlan& g, const Tensor& a, const Tensor& b) {
+  // operand orientation from the plan: A tiles hold rows m with K inner, B tiles rows n
+  std::vector<Orient> oa(a.tags.size(), Orient{0, 0, 0, 0}), ob(b.tags.size(), Orient{0, 0, 0, 0});
+  for (size_t t = 0; t < g.h_tasks.size(); ++t) {
+    const DGemmTask& tk = g.h_tasks[t];
+    for (int p = tk.p0; p < tk.p1; ++p) {
+      const DGemmPair& pr = g.h_pairs[p];
+      oa[g.pair_a_slot[p]] = Orient{tk.m, pr.k, pr.lda, g.ta == kTrans ? 1 : 0};
+      ob[g.pair_b_slot[p]] = Orient{tk.n, pr.k, pr.ldb, g.tb == kTrans ? 0 : 1};
+    }
+  }
+  packed_layout(sg.pa, a, kTcTileM, kPkTileABytes, [&](int32_t s) { return oa[s]; });
+  packed_layout(sg.pb, b, kTcTileN, kPkTileBBytes, [&](int32_t s) { return ob[s]; });
+  sg.h_pk.resize(g.h_pairs.size());
+  for (size_t i = 0; i < g.h_pairs.size(); ++i) {
+    const int32_t as = g.pair_a_slot[i], bs = g.pair_b_slot[i];
+    if (sg.pa.base[as] < 0 || sg.pb.base[bs] < 0 || sg.pa.nks[as] != sg.pb.nks[bs])
+      throw Error(kInternal, "split gemm plan: operand packing mismatch");
+    sg.h_pk[i] = DPkPair{sg.pa.base[as], sg.pb.base[bs], sg.pa.nks[as], 0};
+  }
+  sg.pk.upload(sg.h_pk, ctx.stream);
+  sg.pa.packs.upload(sg.pa.h_packs, ctx.stream);
+  sg.pb.packs.upload(sg.pb.h_packs, ctx.stream);
+  sg.pa.buf.ensure(std::max<int64_t>(sg.pa.bytes, 16), ctx.stream);
+  sg.pb.buf.ensure(std::max<int64_t>(sg.pb.bytes, 16), ctx.stream);
+}
+
+// C += alpha * op(A) op(B) over the plan's tasks, in split TF32 (g uploaded).
+static void run_split_gemm(Context& ctx, SplitGemm& sg, const GemmPlan& g, double alpha, const double* A,
+                           const double* B, double* C) {
+  if (g.h_tasks.empty()) return;
+  launch_pack(sg.pa.packs.get(), static_cast<int>(sg.pa.h_packs.size()), A, sg.pa.buf.as<uint8_t>(), ctx.stream);
+  launch_pack(sg.pb.packs.get(), static_cast<int>(sg.pb.h_packs.size()), B, sg.pb.buf.as<uint8_t>(), ctx.stream);
+  ctx.gemm_part.ensure(std::max<size_t>(g.partial_bytes_tc(), 16), ctx.stream);
+  double* part = ctx.gemm_part.as<double>();
+  int* err = device_err_flag(ctx);
+  launch_gemm_pk(sg.pa.buf.as<uint8_t>(), sg.pb.buf.as<uint8_t>(), alpha, C, nullptr, g.tiles_tc.get(),
+                 static_cast<int>(g.h_tiles_tc.size()), g.dtasks.get(), sg.pk.get(), part, 0, err, ctx.stream);
+  if (g.nslots_tc > 0)
+    launch_gemm_pk_reduce(g.reduce_tc.get(), static_cast<int>(g.h_reduce_tc.size()), g.dtasks.get(), alpha, part, C,
+                          ctx.stream);
+  ctx.kernel_launches += 3 + (g.nslots_tc > 0);
+}
+
 static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi,
                          double* sigma) {
-  if (!p.pk_built) build_sigma_pk(ctx, p, L, R, p.psi_layout);
-  // operators are packed once per (layout, data version)
-  if (p.pk_L.src_layout != L.layout_id || p.pk_L.src_version != L.data_version) pack_into(ctx, p.pk_L, L);
-  if (p.pk_R.src_layout != R.layout_id || p.pk_R.src_version != R.data_version) pack_into(ctx, p.pk_R, R);
+  {
+    PhaseTimer tm(ctx, kPhSigmaPlan);
+    if (!p.pk_built) build_sigma_pk(ctx, p, L, R, p.psi_layout);
+    // operators are packed once per (layout, data version)
+    if (p.pk_L.src_layout != L.layout_id || p.pk_L.src_version != L.data_version) pack_into(ctx, p.pk_L, L);
+    if (p.pk_R.src_layout != R.layout_id || p.pk_R.src_version != R.data_version) pack_into(ctx, p.pk_R, R);
+    tm.stop();
+    ctx.timers[kPhSigma] -= tm.dt;  // counted as planning, not as H_eff * psi
+  }
   launch_pack(p.pk_psi.packs.get(), static_cast<int>(p.pk_psi.h_packs.size()), psi, p.pk_psi.buf.as<uint8_t>(),
               ctx.stream);
   int* err = device_err_flag(ctx);
   launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.pk_scr1.buf.as<uint8_t>(),
                  p.s1.tiles_tc.get(), static_cast<int>(p.s1.h_tiles_tc.size()), p.pk_tasks1.get(), p.pk1.get(),
                  nullptr, 1, err, ctx.stream);
-  ctx.gemm_part.ensure(std::max<size_t>(p.s2.partial_bytes_tc(), 16));
+  ctx.gemm_part.ensure(std::max<size_t>(p.s2.partial_bytes_tc(), 16), ctx.stream);
   double* part = ctx.gemm_part.as<double>();
   launch_gemm_pk(p.pk_scr1.buf.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
                  p.s2.tiles_tc.get(), static_cast<int>(p.s2.h_tiles_tc.size()), p.s2.dtasks.get(), p.pk2.get(), part,
@@ -459,14 +675,14 @@ static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTe
 }
 
 static void sigma_run(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi,
-                      double* sigma) {
-  if (ctx.precision == kSplitTF32) {
+                      double* sigma, int precision) {
+  if (precision != kFP64) {
     sigma_run_pk(ctx, p, L, R, psi, sigma);
   } else {
-    ctx.scr1.ensure(std::max<int64_t>(p.scr1.nnz, 1) * sizeof(double));
+    ctx.scr1.ensure(std::max<int64_t>(p.scr1.nnz, 1) * sizeof(double), ctx.stream);
     double* scr = ctx.scr1.as<double>();
     if (p.scr1.nnz) cuda_check(cudaMemsetAsync(scr, 0, p.scr1.nnz * sizeof(double), ctx.stream), "scr1 zero");
-    ctx.gemm_part.ensure(std::max(p.s1.partial_bytes(), p.s2.partial_bytes()));
+    ctx.gemm_part.ensure(std::max(p.s1.partial_bytes(), p.s2.partial_bytes()), ctx.stream);
     double* part = ctx.gemm_part.as<double>();
     p.s1.run(1.0, L.d, psi, scr, part, ctx.stream);
     p.s2.run(1.0, scr, R.d, sigma, part, ctx.stream);
@@ -479,7 +695,7 @@ static void sigma_run(Context& ctx, SigmaPlan& p, const DTensor& L, const DTenso
 // Device error flag of the tensor-core kernels (zeroed on first use).
 int* device_err_flag(Context& ctx) {
   if (!ctx.err_flag.p) {
-    ctx.err_flag.ensure(sizeof(int));
+    ctx.err_flag.ensure(sizeof(int), ctx.stream);
     cuda_check(cudaMemsetAsync(ctx.err_flag.p, 0, sizeof(int), ctx.stream), "err flag zero");
   }
   return ctx.err_flag.as<int>();
@@ -501,7 +717,7 @@ void compute_sigma_vector(Context& ctx, const DTensor& L, const DTensor& R, cons
   if (sigma.nnz != psi.nnz || sigma.tags != psi.tags)
     throw Error(kInvalidArgument, "compute_sigma_vector: sigma must have the wavefunction's block layout");
   SigmaPlan& p = sigma_plan(ctx, L, R, psi);
-  sigma_run(ctx, p, L, R, psi.d, sigma.d);
+  sigma_run(ctx, p, L, R, psi.d, sigma.d, ctx.precision);
 }
 
 double sigma_device_time(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma,
@@ -511,7 +727,7 @@ double sigma_device_time(Context& ctx, const DTensor& L, const DTensor& R, const
   cuda_check(cudaEventCreate(&e0), "event create");
   cuda_check(cudaEventCreate(&e1), "event create");
   cuda_check(cudaEventRecord(e0, ctx.stream), "event record");
-  for (int r = 0; r < reps; ++r) sigma_run(ctx, p, L, R, psi.d, sigma.d);
+  for (int r = 0; r < reps; ++r) sigma_run(ctx, p, L, R, psi.d, sigma.d, ctx.precision);
   cuda_check(cudaEventRecord(e1, ctx.stream), "event record");
   cuda_check(cudaEventSynchronize(e1), "event sync");
   float ms = 0.f;
@@ -528,6 +744,7 @@ DiagPlan& diag_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTen
   auto key = std::make_tuple(L.layout_id, R.layout_id, diag.layout_id);
   auto it = ctx.diag_plans.find(key);
   if (it != ctx.diag_plans.end()) return *it->second;
+  PhaseTimer tm(ctx, kPhSigmaPlan);
   auto p = std::make_unique<DiagPlan>();
   // tied arrays: row sector -> [(w, block slot)] for blocks (i, w, i), ascending w
   auto tied = [](const Tensor& t) {
@@ -592,6 +809,7 @@ void compute_diagonal_elements(Context& ctx, const DTensor& L, const DTensor& R,
 // ---------------------------------------------------------------------------
 std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& opr0, const DTensor& bra,
                                      const DTensor& ket) {
+  PhaseTimer tplan(ctx, kPhRenormPlan);
   Tensor cbra = conj_view(bra);
   int K1 = 0, K2 = 0;
   GemmPlan p1, p2;
@@ -615,19 +833,31 @@ std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& 
   auto out = std::make_unique<DTensor>();
   layout_from_tasks(*out, s2, t2);
   build_gemm_plan(p2, kNoTrans, tb2, scr, ket, *out, K2, std::move(t2));
+  const bool split = ctx.precision == kSplitTF32All;
+  SplitGemm g1, g2;
   p1.upload(ctx.stream);
   p2.upload(ctx.stream);
+  if (split) {
+    build_split_gemm(ctx, g1, p1, cbra, opr0);
+    build_split_gemm(ctx, g2, p2, scr, ket);
+  }
+  tplan.stop();
+  PhaseTimer trun(ctx, kPhRenormRun);
   out->ctx = &ctx;
   out->alloc_device(ctx.stream, true);
-  ctx.scr2.ensure(std::max<int64_t>(scr.nnz, 1) * sizeof(double));
+  ctx.scr2.ensure(std::max<int64_t>(scr.nnz, 1) * sizeof(double), ctx.stream);
   double* sp = ctx.scr2.as<double>();
   if (scr.nnz) cuda_check(cudaMemsetAsync(sp, 0, scr.nnz * sizeof(double), ctx.stream), "renorm scr zero");
-  ctx.gemm_part.ensure(std::max(p1.partial_bytes(), p2.partial_bytes()));
-  p1.run(1.0, bra.d, opr0.d, sp, ctx.gemm_part.as<double>(), ctx.stream);
-  p2.run(1.0, sp, ket.d, out->d, ctx.gemm_part.as<double>(), ctx.stream);
-  ctx.kernel_launches += 2;
-  // plans (device task arrays) must outlive the kernels
-  ctx.sync();
+  if (split) {
+    run_split_gemm(ctx, g1, p1, 1.0, bra.d, opr0.d, sp);
+    run_split_gemm(ctx, g2, p2, 1.0, sp, ket.d, out->d);
+    check_device_error(ctx);
+  } else {
+    ctx.gemm_part.ensure(std::max(p1.partial_bytes(), p2.partial_bytes()), ctx.stream);
+    p1.run(1.0, bra.d, opr0.d, sp, ctx.gemm_part.as<double>(), ctx.stream);
+    p2.run(1.0, sp, ket.d, out->d, ctx.gemm_part.as<double>(), ctx.stream);
+    ctx.kernel_launches += 2;
+  }
   return out;
 }
 
@@ -639,126 +869,174 @@ std::unique_ptr<DTensor> compute_merged_operator(Context& ctx, bool forward, con
   if (mpo.sh.rank != 4 || opr.sh.rank != 3) throw Error(kInvalidArgument, "merged operator: bad ranks");
   if (static_cast<int64_t>(mpo.host.size()) != mpo.nnz)
     throw Error(kInvalidArgument, "merged operator: MPO coefficients must be available on the host");
-  // MPO block lookup by left/right bond index
-  int idx[kMaxRank];
+  PhaseTimer tplan(ctx, kPhMergePlan);
+  for (size_t b = 0; b < mpo.tags.size(); ++b)
+    if ((b + 1 < mpo.tags.size() ? mpo.offsets[b + 1] : mpo.nnz) - mpo.offsets[b] != 1)
+      throw Error(kInvalidArgument, "merged operator: MPO blocks must be scalars (1x1x1x1)");
+  // Forward:  mL[A=(a,s), v, A'=(x,t)] = sum_w W[w,s,t,v] L[a,w,x]
+  // Backward: mR[B=(s,b), w, B'=(t,y)] = sum_v W[w,s,t,v] R[b,v,y]
+  // Every environment block (a,c,x) (c = w forward, v backward) meets the MPO
+  // entries that share c; a destination sub-block is fixed by the environment's
+  // outer pair (a,x) and the entry's column (s,t,u) (u = v forward, w backward).
+  // The plan is built group by group over (a,x) with a dense column stamp, so its
+  // cost is linear in the number of contributions (no sorting, no hashing).
+  const int ns = mpo.sh.nsec(1), nt = mpo.sh.nsec(2);
+  const int c_axis = forward ? 0 : 3, u_axis = forward ? 3 : 0;
+  const int nu = mpo.sh.nsec(u_axis);
   MergeInfo mb, mk;
   auto out = std::make_unique<DTensor>();
   out->sh.rank = 3;
   out->sh.q = opr.sh.q + mpo.sh.q;
-  struct Contrib {
-    int64_t src_off;
-    int sld;
-    double coef;
-  };
-  struct DstKey {
-    int64_t otag;
-    int ipr, ipc;
-    bool operator<(const DstKey& o) const {
-      if (otag != o.otag) return otag < o.otag;
-      if (ipr != o.ipr) return ipr < o.ipr;
-      return ipc < o.ipc;
-    }
-  };
-  std::map<DstKey, std::pair<std::pair<int, int>, std::vector<Contrib>>> dst;
-  const int ns = mpo.sh.nsec(1);
   if (forward) {
-    // mL[A=(a,s), v, A'=(x,t)] += W[w,s,t,v] * L[a,w,x]
     mb = MergeInfo({opr.sh.qshape[0], mpo.sh.qshape[1]}, {opr.sh.dshape[0], mpo.sh.dshape[1]});
     mk = MergeInfo({opr.sh.qshape[2], mpo.sh.qshape[2]}, {opr.sh.dshape[2], mpo.sh.dshape[2]});
-    out->sh.qshape = {mb.q_merged, mpo.sh.qshape[3], mk.q_merged};
-    out->sh.dshape = {mb.d_merged, mpo.sh.dshape[3], mk.d_merged};
-    out->sh.finalize();
-    std::map<int, std::vector<int32_t>> wblocks;  // w -> mpo block slots
-    for (size_t b = 0; b < mpo.tags.size(); ++b) {
-      mpo.sh.index(mpo.tags[b], idx);
-      wblocks[idx[0]].push_back(static_cast<int32_t>(b));
-    }
-    const int nt = mpo.sh.nsec(2);
-    for (size_t lb = 0; lb < opr.tags.size(); ++lb) {
-      opr.sh.index(opr.tags[lb], idx);
-      const int a = idx[0], w = idx[1], x = idx[2];
-      auto wi = wblocks.find(w);
-      if (wi == wblocks.end()) continue;
-      const int da = opr.sh.dshape[0][a], dx = opr.sh.dshape[2][x];
-      for (int32_t mbk : wi->second) {
-        int mi[kMaxRank];
-        mpo.sh.index(mpo.tags[mbk], mi);
-        const int s = mi[1], t = mi[2], v = mi[3];
-        const int ipr = a * ns + s, ipc = x * nt + t;
-        const int A = mb.merged_of[ipr], Ap = mk.merged_of[ipc];
-        int oi[3] = {A, v, Ap};
-        if (!out->sh.allowed(oi)) throw Error(kQShapeMismatch, "merged operator: contribution not allowed");
-        DstKey key{out->sh.tag(oi), ipr, ipc};
-        auto& e = dst[key];
-        e.first = {da * mpo.sh.dshape[1][s], dx * mpo.sh.dshape[2][t]};
-        e.second.push_back({opr.offsets[lb], dx, mpo.host[mpo.offsets[mbk]]});
-      }
-    }
   } else {
-    // mR[B=(s,b), w, B'=(t,y)] += W[w,s,t,v] * R[b,v,y]
     mb = MergeInfo({mpo.sh.qshape[1], opr.sh.qshape[0]}, {mpo.sh.dshape[1], opr.sh.dshape[0]});
-    mk = MergeInfo({mpo.sh.qshape[2], opr.sh.qshape[2]}, {mpo.sh.dshape[1], opr.sh.dshape[0]});
-    out->sh.qshape = {mb.q_merged, mpo.sh.qshape[0], mk.q_merged};
-    out->sh.dshape = {mb.d_merged, mpo.sh.dshape[0], mk.d_merged};
-    out->sh.finalize();
-    std::map<int, std::vector<int32_t>> vblocks;  // v -> mpo block slots
+    mk = MergeInfo({mpo.sh.qshape[2], opr.sh.qshape[2]}, {mpo.sh.dshape[2], opr.sh.dshape[2]});
+  }
+  out->sh.qshape = {mb.q_merged, mpo.sh.qshape[u_axis], mk.q_merged};
+  out->sh.dshape = {mb.d_merged, mpo.sh.dshape[u_axis], mk.d_merged};
+  out->sh.finalize();
+  // MPO entries by contracted index c, in block order: column id (s*nt + t)*nu + u
+  const int nc = mpo.sh.nsec(c_axis);
+  std::vector<int32_t> row_ptr(nc + 1, 0), ent_col, ent_st;
+  std::vector<double> ent_coef;
+  {
+    std::vector<std::array<int, 4>> mi(mpo.tags.size());
     for (size_t b = 0; b < mpo.tags.size(); ++b) {
-      mpo.sh.index(mpo.tags[b], idx);
-      vblocks[idx[3]].push_back(static_cast<int32_t>(b));
+      mpo.sh.index(mpo.tags[b], mi[b].data());
+      row_ptr[mi[b][c_axis] + 1]++;
     }
-    const int nb = opr.sh.nsec(0), ny = opr.sh.nsec(2);
-    for (size_t rb = 0; rb < opr.tags.size(); ++rb) {
-      opr.sh.index(opr.tags[rb], idx);
-      const int b = idx[0], v = idx[1], y = idx[2];
-      auto vi = vblocks.find(v);
-      if (vi == vblocks.end()) continue;
-      const int db = opr.sh.dshape[0][b], dy = opr.sh.dshape[2][y];
-      for (int32_t mbk : vi->second) {
-        int mi[kMaxRank];
-        mpo.sh.index(mpo.tags[mbk], mi);
-        const int w = mi[0], s = mi[1], t = mi[2];
-        const int ipr = s * nb + b, ipc = t * ny + y;
-        const int B = mb.merged_of[ipr], Bp = mk.merged_of[ipc];
-        int oi[3] = {B, w, Bp};
-        if (!out->sh.allowed(oi)) throw Error(kQShapeMismatch, "merged operator: contribution not allowed");
-        DstKey key{out->sh.tag(oi), ipr, ipc};
-        auto& e = dst[key];
-        e.first = {db * mpo.sh.dshape[1][s], dy * mpo.sh.dshape[2][t]};
-        e.second.push_back({opr.offsets[rb], dy, mpo.host[mpo.offsets[mbk]]});
-      }
+    for (int c = 0; c < nc; ++c) row_ptr[c + 1] += row_ptr[c];
+    ent_col.resize(mpo.tags.size());
+    ent_coef.resize(mpo.tags.size());
+    std::vector<int32_t> fill(row_ptr.begin(), row_ptr.end() - 1);
+    for (size_t b = 0; b < mpo.tags.size(); ++b) {
+      const int e = fill[mi[b][c_axis]]++;
+      ent_col[e] = (mi[b][1] * nt + mi[b][2]) * nu + mi[b][u_axis];
+      ent_coef[e] = mpo.host[mpo.offsets[b]];
     }
   }
+  // environment blocks grouped by outer pair (a,x), contracted index ascending
+  const int nx = opr.sh.nsec(2);
+  std::vector<std::array<int, 3>> oi(opr.tags.size());
+  std::vector<int32_t> order(opr.tags.size());
+  for (size_t b = 0; b < opr.tags.size(); ++b) {
+    opr.sh.index(opr.tags[b], oi[b].data());
+    order[b] = static_cast<int32_t>(b);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+    return int64_t(oi[x][0]) * nx + oi[x][2] < int64_t(oi[y][0]) * nx + oi[y][2];
+  });
+  // pass 1: destinations of every group, with their contribution counts
+  struct Dst {
+    int32_t col, cnt;
+    int64_t otag;
+  };
+  std::vector<Dst> dsts;
+  std::vector<int64_t> group_first;  // [g] -> first destination of group g
+  std::vector<int32_t> group_src;    // [g] -> first entry of order[] in group g
+  const int ncols_all = ns * nt * nu;
+  std::vector<int32_t> stamp(ncols_all, -1), where(ncols_all, 0);
+  const int64_t nsparse = out->sh.nsparse;
+  std::vector<uint64_t> present((nsparse + 63) / 64, 0);
+  for (size_t o = 0; o < order.size();) {
+    const int a = oi[order[o]][0], x = oi[order[o]][2];
+    size_t o1 = o;
+    while (o1 < order.size() && oi[order[o1]][0] == a && oi[order[o1]][2] == x) ++o1;
+    const int g = static_cast<int>(group_first.size());
+    group_first.push_back(static_cast<int64_t>(dsts.size()));
+    group_src.push_back(static_cast<int32_t>(o));
+    for (size_t q = o; q < o1; ++q) {
+      const int c = oi[order[q]][1];
+      for (int e = row_ptr[c]; e < row_ptr[c + 1]; ++e) {
+        const int col = ent_col[e];
+        if (stamp[col] != g) {
+          stamp[col] = g;
+          where[col] = static_cast<int32_t>(dsts.size());
+          const int u = col % nu, st = col / nu, sidx = st / nt, tidx = st % nt;
+          const int ipr = forward ? a * ns + sidx : sidx * opr.sh.nsec(0) + a;
+          const int ipc = forward ? x * nt + tidx : tidx * nx + x;
+          int ti[3] = {mb.merged_of[ipr], u, mk.merged_of[ipc]};
+          if (!out->sh.allowed(ti)) throw Error(kQShapeMismatch, "merged operator: contribution not allowed");
+          const int64_t otag = out->sh.tag(ti);
+          present[otag >> 6] |= uint64_t(1) << (otag & 63);
+          dsts.push_back(Dst{col, 0, otag});
+        }
+        dsts[where[col]].cnt++;
+      }
+    }
+    o = o1;
+  }
+  group_first.push_back(static_cast<int64_t>(dsts.size()));
+  group_src.push_back(static_cast<int32_t>(order.size()));
+  // output blocks: the marked tags in ascending order; slot of a tag by rank
   std::vector<int64_t> tags;
-  for (const auto& kv : dst)
-    if (tags.empty() || tags.back() != kv.first.otag) tags.push_back(kv.first.otag);
+  std::vector<int32_t> rank_before(present.size() + 1, 0);
+  for (size_t w = 0; w < present.size(); ++w) {
+    rank_before[w + 1] = rank_before[w] + __builtin_popcountll(present[w]);
+    for (uint64_t bits = present[w]; bits; bits &= bits - 1)
+      tags.push_back(int64_t(w) * 64 + __builtin_ctzll(bits));
+  }
   out->set_blocks(tags);
+  auto slot_of = [&](int64_t t) {
+    return rank_before[t >> 6] + __builtin_popcountll(present[t >> 6] & ((uint64_t(1) << (t & 63)) - 1));
+  };
+  // pass 2: destination records and their sources (ascending contracted index)
   std::vector<DScatterDst> hd;
   std::vector<DScatterSrc> hs;
-  hd.reserve(dst.size());
-  for (const auto& kv : dst) {
-    const int32_t os = out->find(kv.first.otag);
-    out->sh.index(kv.first.otag, idx);
-    const int dcols = out->sh.dshape[2][idx[2]];
-    DScatterDst d;
-    d.dst_off = out->offsets[os] + int64_t(mb.offset_packed[kv.first.ipr]) * dcols + mk.offset_packed[kv.first.ipc];
-    d.rows = kv.second.first.first;
-    d.cols = kv.second.first.second;
-    d.dld = dcols;
-    d.s0 = static_cast<int>(hs.size());
-    for (const auto& c : kv.second.second) hs.push_back(DScatterSrc{c.src_off, c.sld, 0, c.coef});
-    d.s1 = static_cast<int>(hs.size());
-    d.pad = 0;
-    if (d.rows > 0 && d.cols > 0) hd.push_back(d);
+  hd.reserve(dsts.size());
+  {
+    int64_t total = 0;
+    for (const Dst& d : dsts) total += d.cnt;
+    hs.resize(total);
   }
+  std::vector<int32_t> fill(ncols_all, 0);
+  int64_t next_src = 0;
+  for (size_t g = 0; g + 1 < group_first.size(); ++g) {
+    for (int64_t di = group_first[g]; di < group_first[g + 1]; ++di) {
+      const Dst& d = dsts[di];
+      fill[d.col] = static_cast<int32_t>(next_src);
+      const int st = d.col / nu, sidx = st / nt, tidx = st % nt;
+      const int32_t first = group_src[g];
+      const int a = oi[order[first]][0], x = oi[order[first]][2];
+      const int da = opr.sh.dshape[0][a], dx = opr.sh.dshape[2][x];
+      const int ipr = forward ? a * ns + sidx : sidx * opr.sh.nsec(0) + a;
+      const int ipc = forward ? x * nt + tidx : tidx * nx + x;
+      int ti[3];
+      out->sh.index(d.otag, ti);
+      const int dcols = out->sh.dshape[2][ti[2]];
+      DScatterDst r;
+      r.dst_off = out->offsets[slot_of(d.otag)] + int64_t(mb.offset_packed[ipr]) * dcols + mk.offset_packed[ipc];
+      r.rows = da * mpo.sh.dshape[1][sidx];
+      r.cols = dx * mpo.sh.dshape[2][tidx];
+      r.dld = dcols;
+      r.s0 = static_cast<int>(next_src);
+      r.s1 = static_cast<int>(next_src + d.cnt);
+      r.pad = 0;
+      next_src += d.cnt;
+      if (r.rows > 0 && r.cols > 0) hd.push_back(r);
+    }
+    for (int32_t q = group_src[g]; q < group_src[g + 1]; ++q) {
+      const int32_t ob = order[q];
+      const int c = oi[ob][1];
+      const int sld = opr.sh.dshape[2][oi[ob][2]];
+      for (int e = row_ptr[c]; e < row_ptr[c + 1]; ++e)
+        hs[fill[ent_col[e]]++] = DScatterSrc{opr.offsets[ob], sld, 0, ent_coef[e]};
+    }
+  }
+  tplan.stop();
+  PhaseTimer talloc(ctx, kPhMergeAlloc);
   out->ctx = &ctx;
   out->alloc_device(ctx.stream, true);
+  talloc.stop();
+  PhaseTimer trun(ctx, kPhMergeRun);
   DevArray<DScatterDst> dd;
   DevArray<DScatterSrc> ds;
   dd.upload(hd, ctx.stream);
   ds.upload(hs, ctx.stream);
   launch_scatter(dd.get(), static_cast<int>(hd.size()), ds.get(), opr.d, out->d, ctx.stream);
   ctx.kernel_launches += 1;
-  ctx.sync();
   return out;
 }
 
@@ -778,6 +1056,7 @@ WaveMerge wave_merge_infos(const DTensor& lmpo, const DTensor& rmpo, const DTens
 }
 
 std::unique_ptr<DTensor> merge_wave(Context& ctx, const WaveMerge& wm, const DTensor& lwfn, const DTensor& rwfn) {
+  PhaseTimer tm(ctx, kPhWaveMerge);
   int K = 0;
   Shape t4 = gemm_result_shape(kNoTrans, kNoTrans, lwfn.sh, rwfn.sh, 4, &K);
   auto tasks = enumerate_gemm(kNoTrans, kNoTrans, lwfn, rwfn, t4, K);
@@ -811,7 +1090,6 @@ std::unique_ptr<DTensor> merge_wave(Context& ctx, const WaveMerge& wm, const DTe
   psi->alloc_device(ctx.stream, true);
   plan.run(1.0, lwfn.d, rwfn.d, psi->d, gemm_scratch(ctx, plan), ctx.stream);
   ctx.kernel_launches += 1;
-  ctx.sync();
   return psi;
 }
 
@@ -867,7 +1145,6 @@ std::unique_ptr<DTensor> expand_rows(Context& ctx, const MergeInfo& info, const 
   dc.upload(cp, ctx.stream);
   launch_copy(dc.get(), static_cast<int>(cp.size()), b.d, a->d, 0, ctx.stream);
   ctx.kernel_launches += 1;
-  ctx.sync();
   return a;
 }
 
@@ -924,7 +1201,6 @@ std::unique_ptr<DTensor> expand_cols(Context& ctx, const DTensor& b, const Merge
   dc.upload(cp, ctx.stream);
   launch_copy(dc.get(), static_cast<int>(cp.size()), b.d, a->d, 0, ctx.stream);
   ctx.kernel_launches += 1;
-  ctx.sync();
   return a;
 }
 
@@ -978,7 +1254,6 @@ std::unique_ptr<DTensor> merge_cols(Context& ctx, const DTensor& a, const MergeI
   dc.upload(cp, ctx.stream);
   launch_copy(dc.get(), static_cast<int>(cp.size()), a.d, b->d, 0, ctx.stream);
   ctx.kernel_launches += 1;
-  ctx.sync();
   return b;
 }
 
@@ -996,7 +1271,6 @@ std::unique_ptr<DTensor> gemm_new(Context& ctx, Trans ta, Trans tb, double alpha
   c->alloc_device(ctx.stream, true);
   plan.run(alpha, a.d, b.d, c->d, gemm_scratch(ctx, plan), ctx.stream);
   ctx.kernel_launches += 1;
-  ctx.sync();
   return c;
 }
 
@@ -1004,8 +1278,8 @@ double normalize_tensor(Context& ctx, DTensor& x) {
   const int64_t n = x.nnz;
   if (n == 0) return 0.0;
   const int nblk = multidot_blocks(n);
-  ctx.partial.ensure(size_t(nblk) * 100 * sizeof(double));
-  ctx.scalars.ensure(256 * sizeof(double));
+  ctx.partial.ensure(size_t(nblk) * 100 * sizeof(double), ctx.stream);
+  ctx.scalars.ensure(256 * sizeof(double), ctx.stream);
   double* sc = ctx.scalars.as<double>();
   launch_multidot(x.d, 1, x.d, 1, n, n, sc + 100, ctx.partial.as<double>(), nblk, ctx.stream);
   launch_scal_dev(x.d, n, sc + 100, 1, ctx.stream);
@@ -1021,30 +1295,37 @@ double normalize_tensor(Context& ctx, DTensor& x) {
 // ---------------------------------------------------------------------------
 // The Davidson loop of src/diagonalize.hpp:310-449 in the context's current
 // precision.  Stops when |r|^2 < tol, or — with rel_floor > 0 — when |r|^2 falls
-// below (rel_floor * E)^2, the resolution of an inexact operator.
+// below (rel_floor * E)^2, the resolution of an inexact operator.  With anchor set,
+// the first H_eff * psi (of the start vector) is applied in FP64 and the rest in the
+// context's precision; S.rnorm_fp64 then holds the start vector's FP64 residual.
 static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag, DTensor& wfnc,
-                           double tol, double rel_floor, int max_macro, DavidsonStats& S) {
+                           double tol, double rel_floor, int max_macro, DavidsonStats& S, bool anchor = false) {
   const int max_ritz = 10;
   const int64_t n = wfnc.nnz;
   if (diag.nnz != wfnc.nnz)
     throw Error(kInvalidArgument, "diagonalize: diag and wavefunction layouts differ");
   cudaStream_t st = ctx.stream;
   SigmaPlan& sp = sigma_plan(ctx, L, R, wfnc);
-  ctx.work.ensure(size_t(2 * max_ritz + 1) * std::max<int64_t>(n, 1) * sizeof(double));
+  ctx.work.ensure(size_t(2 * max_ritz + 1) * std::max<int64_t>(n, 1) * sizeof(double), ctx.stream);
   double* trial = ctx.work.as<double>();
   double* sigma = trial + int64_t(max_ritz) * n;
   double* errv = sigma + int64_t(max_ritz) * n;
   const int nblk = multidot_blocks(n);
-  ctx.partial.ensure(size_t(nblk) * 100 * sizeof(double));
-  ctx.scalars.ensure(256 * sizeof(double));
+  ctx.partial.ensure(size_t(nblk) * 100 * sizeof(double), ctx.stream);
+  ctx.scalars.ensure(256 * sizeof(double), ctx.stream);
   double* part = ctx.partial.as<double>();
   double* sc = ctx.scalars.as<double>();  // [0..99] dots, [100] norm, [101] dot, [128..227] rvec
   double* rvec_d = sc + 128;
 
-  auto sigma_of = [&](int k) {
+  PhaseTimer trest(ctx, kPhDavidsonRest);
+  auto sigma_of = [&](int k, int precision) {
+    PhaseTimer tm(ctx, kPhSigma);
     cuda_check(cudaMemsetAsync(sigma + k * n, 0, n * sizeof(double), st), "sigma zero");
-    sigma_run(ctx, sp, L, R, trial + k * n, sigma + k * n);
+    sigma_run(ctx, sp, L, R, trial + k * n, sigma + k * n, precision);
     S.n_sigma += 1;
+    if (precision == kFP64) S.n_sigma_fp64 += 1;
+    tm.stop();
+    ctx.timers[kPhDavidsonRest] -= tm.dt;  // H_eff * psi is not part of the rest
   };
   auto normalize = [&](double* x) {
     launch_multidot(x, 1, x, 1, n, n, sc + 100, part, nblk, st);
@@ -1058,7 +1339,7 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
   std::vector<double> hdots(100), heff, rvec, rval;
   while (iconv < 1 && niter < max_macro) {
     normalize(trial);
-    sigma_of(0);
+    sigma_of(0, anchor && niter == 0 ? kFP64 : ctx.precision);
     for (int m = 1; m <= max_ritz; ++m) {
       launch_multidot(trial, m, sigma, m, n, n, sc, part, nblk, st);
       ctx.kernel_launches += 2;
@@ -1086,6 +1367,7 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
       cuda_check(cudaMemcpyAsync(&rnorm, sc + 101, sizeof(double), cudaMemcpyDeviceToHost, st), "rnorm d2h");
       ctx.sync();
       S.rnorm = rnorm;
+      if (anchor && niter == 0 && m == 1) S.rnorm_fp64 = rnorm;
       if (rnorm < tol || (rel_floor > 0.0 && rnorm < rel_floor * rel_floor * eval * eval)) {
         ++iconv;
         break;
@@ -1102,7 +1384,7 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
         normalize(errv);
         launch_copy_vec(trial + m * n, errv, n, st);
         ctx.kernel_launches += 1;
-        sigma_of(m);
+        sigma_of(m, ctx.precision);
       }
     }
     ++niter;
@@ -1119,6 +1401,8 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
 // below ~1e-5 |H psi| (measured a few 1e-6), so a residual under (1e-5 E)^2 is
 // as converged as that operator allows.
 constexpr double kSplitResidualFloor = 1.0e-5;
+// FP64-anchored refinement rounds of a split-precision diagonalisation
+constexpr int kRefineRounds = 2;
 
 double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag, DTensor& wfnc, double tol,
                    DavidsonStats* stats) {
@@ -1126,30 +1410,31 @@ double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTens
   DavidsonStats& S = stats ? *stats : local;
   S = DavidsonStats{};
   if (ctx.precision == kFP64) return davidson_run(ctx, L, R, diag, wfnc, tol, 0.0, 4, S);
-  // split precision: the bulk of the iterations with the tensor-core operator ...
+  // Split precision.  (1) The Davidson iterations with the tensor-core operator, to
+  // its resolution.  (2) Refinement: one FP64 H_eff * psi of that vector anchors a
+  // continuation of the Davidson run in which only the new correction vectors are
+  // applied in split precision.  Subspace entries that involve the anchor are FP64
+  // (<t_i|H|psi> = <t_i|sigma_FP64>), so the split error enters the Ritz value only
+  // through the small correction components, at second order; with a start vector
+  // already within the tolerance the accepted value is the FP64 Rayleigh quotient.
+  // A continuation that ends unconverged (subspace full) is anchored once more.
   const double e_split = davidson_run(ctx, L, R, diag, wfnc, tol, kSplitResidualFloor, 4, S);
   check_device_error(ctx);
   S.energy_split = e_split;
-  // ... then the refinement: the same Davidson from the split vector with the FP64
-  // operator.  Its first FP64 H_eff*psi gives the accepted Rayleigh quotient and the
-  // FP64 residual; when that residual already meets the tolerance this is the only
-  // FP64 application, otherwise the FP64 iterations continue to the tolerance.
-  DavidsonStats R64;
-  const int saved = ctx.precision;
-  ctx.precision = kFP64;
-  double e = 0.0;
-  try {
-    e = davidson_run(ctx, L, R, diag, wfnc, tol, 0.0, 2, R64);
-  } catch (...) {
-    ctx.precision = saved;
-    throw;
+  double e = e_split;
+  for (int round = 0; round < kRefineRounds; ++round) {
+    DavidsonStats R1;
+    e = davidson_run(ctx, L, R, diag, wfnc, tol, 0.0, 1, R1, /*anchor=*/true);
+    check_device_error(ctx);
+    S.n_sigma += R1.n_sigma;
+    S.n_sigma_fp64 += R1.n_sigma_fp64;
+    S.micro += R1.micro;
+    S.macro += R1.macro;
+    S.rnorm = R1.rnorm;
+    S.rnorm_fp64 = R1.rnorm_fp64;
+    S.converged = R1.converged;
+    if (R1.converged) break;
   }
-  ctx.precision = saved;
-  S.n_sigma_fp64 = R64.n_sigma;
-  S.n_sigma += R64.n_sigma;
-  S.micro += R64.micro;
-  S.rnorm_fp64 = R64.rnorm;
-  S.converged = R64.converged;
   return e;
 }
 
@@ -1175,10 +1460,18 @@ std::vector<int> select_kept(const std::vector<std::vector<double>>& svals, int 
   return kept;
 }
 
+// Default tie window of the truncation cutoff: symmetry-related singular values
+// (e.g. of the (N, Sz) and (N, -Sz) sectors of an Sz = 0 state) agree to rounding
+// and are kept or dropped together.
+constexpr double kTieRtolDefault = 1.0e-10;
+// concurrent SVD lanes of canonicalize
+constexpr int kSvdLanes = 8;
+
 CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise) {
   if (noise >= 1.0e-8) throw Error(kInvalidArgument, "canonicalize: noise injection is not supported");
   if (wfnc.sh.rank != 2) throw Error(kInvalidArgument, "canonicalize: expects a merged (2-index) wavefunction");
   cudaStream_t st = ctx.stream;
+  PhaseTimer tsolve(ctx, kPhSvdSolve);
   const int ncols = wfnc.sh.nsec(1);
   struct Blk {
     int32_t slot;
@@ -1186,7 +1479,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     int64_t u_off, s_off, v_off;  // inside svd_mats
   };
   std::vector<Blk> blks;
-  int64_t tot = 0;
+  int64_t nsv = 0;  // singular values first (one contiguous read-back), then U and V^T
   int64_t maxmn = 0;
   for (size_t b = 0; b < wfnc.tags.size(); ++b) {
     const int i = static_cast<int>(wfnc.tags[b] / ncols), j = static_cast<int>(wfnc.tags[b] % ncols);
@@ -1194,63 +1487,123 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     if (m == 0 || n == 0) continue;
     const int k = std::min(m, n);
     Blk x{static_cast<int32_t>(b), i, j, m, n, k, 0, 0, 0};
-    x.u_off = tot;
-    tot += int64_t(m) * k;
-    x.s_off = tot;
-    tot += k;
-    x.v_off = tot;
-    tot += int64_t(k) * n;
+    x.s_off = nsv;
+    nsv += k;
     maxmn = std::max<int64_t>(maxmn, int64_t(m) * n);
     blks.push_back(x);
   }
-  // workspace: matrices + one transposed copy + per-call solver buffers
+  // Device layout (doubles): singular values | gesvd info per block (two ints per
+  // double) | U and V^T per block.  The head (values and infos) is read back.
+  const int64_t info_off = (nsv + 1) & ~int64_t(1);
+  const int64_t head = info_off + (static_cast<int64_t>(blks.size()) + 1) / 2 + 1;
+  int64_t tot = head;
+  for (auto& x : blks) {
+    x.u_off = tot;
+    tot += int64_t(x.m) * x.k;
+    x.v_off = tot;
+    tot += int64_t(x.k) * x.n;
+  }
+  // Lanes take blocks largest first; each lane has its own workspace.
+  ctx.svd_mats.ensure(size_t(tot) * sizeof(double), ctx.stream);
+  double* mats = ctx.svd_mats.as<double>();
+  int* infos = reinterpret_cast<int*>(mats + info_off);
   int lwork = 0;
   for (const auto& x : blks) {
-    const int M_ = std::max(x.m, x.n), N_ = std::min(x.m, x.n);
     int lw = 0;
-    solver_check(cusolverDnDgesvd_bufferSize(ctx.solver, M_, N_, &lw), "gesvd bufferSize");
+    solver_check(cusolverDnDgesvd_bufferSize(ctx.solver, std::max(x.m, x.n), std::min(x.m, x.n), &lw),
+                 "gesvd bufferSize");
     lwork = std::max(lwork, lw);
   }
-  const int64_t tmp_elems = 3 * maxmn + 16;
-  ctx.svd_mats.ensure(size_t(tot + tmp_elems) * sizeof(double));
-  ctx.svd_work.ensure(size_t(lwork + 64) * sizeof(double) + size_t(std::max<int64_t>(maxmn, 1)) * sizeof(double) +
-                      64);
-  double* mats = ctx.svd_mats.as<double>();
-  double* tA = mats + tot;                // col-major working copy of the block
-  double* tU = tA + maxmn;                // col-major U when transposes are needed
-  double* tV = tU + maxmn;                // col-major VT when transposes are needed
-  double* work = ctx.svd_work.as<double>();
-  double* rwork = work + lwork + 8;
-  int* info = reinterpret_cast<int*>(rwork + std::max<int64_t>(maxmn, 1));
-  for (const auto& x : blks) {
-    const double* a = wfnc.d + wfnc.offsets[x.slot];
-    double* U = mats + x.u_off;
-    double* S = mats + x.s_off;
-    double* V = mats + x.v_off;
-    if (x.n >= x.m) {
-      // row-major A (m x n) is col-major A^T (n x m): A^T = Ux S VxT, so U_A = VxT buffer, Vt_A = Ux buffer
-      cuda_check(cudaMemcpyAsync(tA, a, int64_t(x.m) * x.n * sizeof(double), cudaMemcpyDeviceToDevice, st),
-                 "svd copy");
-      solver_check(cusolverDnDgesvd(ctx.solver, 'S', 'S', x.n, x.m, tA, x.n, S, V, x.n, U, x.m, work, lwork, rwork,
-                                    info),
-                   "gesvd");
-    } else {
-      // col-major copy of A (m x n) = row-major A^T (n x m)
-      launch_transpose(a, tA, x.m, x.n, st);
-      solver_check(cusolverDnDgesvd(ctx.solver, 'S', 'S', x.m, x.n, tA, x.m, S, tU, x.m, tV, x.n, work, lwork, rwork,
-                                    info),
-                   "gesvd");
-      // tU col-major (m x k) == row-major (k x m): transpose into row-major U (m x k)
-      launch_transpose(tU, U, x.k, x.m, st);
-      // tV col-major (k x n) == row-major (n x k): transpose into row-major Vt (k x n)
-      launch_transpose(tV, V, x.n, x.k, st);
-      ctx.kernel_launches += 3;
-    }
+  // per lane: gesvd work | rwork | col-major copy of A | col-major U | col-major V^T
+  const size_t lane_doubles = size_t(lwork) + 8 + 4 * size_t(std::max<int64_t>(maxmn, 1)) + 8;
+  std::vector<int> by_cost(blks.size());
+  std::iota(by_cost.begin(), by_cost.end(), 0);
+  std::stable_sort(by_cost.begin(), by_cost.end(), [&](int p, int q) {
+    return double(blks[p].m) * blks[p].n * blks[p].k > double(blks[q].m) * blks[q].n * blks[q].k;
+  });
+  const int hw = std::max(1, static_cast<int>(std::thread::hardware_concurrency()));
+  const int nlanes = std::max(1, std::min({kSvdLanes, hw, static_cast<int>(blks.size())}));
+  while (static_cast<int>(ctx.svd_lanes.size()) < nlanes) {
+    auto l = std::make_unique<Context::SvdLane>();
+    cuda_check(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking), "svd lane stream");
+    cuda_check(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming), "svd lane event");
+    solver_check(cusolverDnCreate(&l->solver), "cusolverDnCreate");
+    solver_check(cusolverDnSetStream(l->solver, l->stream), "cusolverDnSetStream");
+    block_cache().register_stream(l->stream);
+    ctx.svd_lanes.push_back(std::move(l));
   }
-  // singular values to the host
-  std::vector<double> hmats(tot);
-  if (tot) cuda_check(cudaMemcpyAsync(hmats.data(), mats, tot * sizeof(double), cudaMemcpyDeviceToHost, st), "s d2h");
+  if (!ctx.svd_ready) cuda_check(cudaEventCreateWithFlags(&ctx.svd_ready, cudaEventDisableTiming), "svd event");
+  cuda_check(cudaEventRecord(ctx.svd_ready, st), "svd ready");
+  std::atomic<int> next{0};
+  std::vector<std::exception_ptr> errs(nlanes);
+  std::vector<int64_t> lane_launches(nlanes, 0);
+  auto lane_fn = [&](int li) {
+    try {
+      cuda_check(cudaSetDevice(ctx.device), "cudaSetDevice");
+      Context::SvdLane& ln = *ctx.svd_lanes[li];
+      cudaStream_t ls = ln.stream;
+      cuda_check(cudaStreamWaitEvent(ls, ctx.svd_ready, 0), "svd lane wait");
+      ln.work.ensure(lane_doubles * sizeof(double), ls);
+      double* work = ln.work.as<double>();
+      double* rwork = work + lwork + 8;
+      double* tA = rwork + std::max<int64_t>(maxmn, 1);  // col-major working copy of the block
+      double* tU = tA + maxmn;                           // col-major U when transposes are needed
+      double* tV = tU + maxmn;                           // col-major VT when transposes are needed
+      for (int i = next.fetch_add(1); i < static_cast<int>(blks.size()); i = next.fetch_add(1)) {
+        const Blk& x = blks[by_cost[i]];
+        const double* a = wfnc.d + wfnc.offsets[x.slot];
+        double* U = mats + x.u_off;
+        double* S = mats + x.s_off;
+        double* V = mats + x.v_off;
+        int* info = infos + by_cost[i];
+        if (x.n >= x.m) {
+          // row-major A (m x n) is col-major A^T (n x m): A^T = Ux S VxT, so U_A = VxT buffer, Vt_A = Ux buffer
+          cuda_check(cudaMemcpyAsync(tA, a, int64_t(x.m) * x.n * sizeof(double), cudaMemcpyDeviceToDevice, ls),
+                     "svd copy");
+          solver_check(cusolverDnDgesvd(ln.solver, 'S', 'S', x.n, x.m, tA, x.n, S, V, x.n, U, x.m, work, lwork,
+                                        rwork, info),
+                       "gesvd");
+        } else {
+          // col-major copy of A (m x n) = row-major A^T (n x m)
+          launch_transpose(a, tA, x.m, x.n, ls);
+          solver_check(cusolverDnDgesvd(ln.solver, 'S', 'S', x.m, x.n, tA, x.m, S, tU, x.m, tV, x.n, work, lwork,
+                                        rwork, info),
+                       "gesvd");
+          // tU col-major (m x k) == row-major (k x m): transpose into row-major U (m x k)
+          launch_transpose(tU, U, x.k, x.m, ls);
+          // tV col-major (k x n) == row-major (n x k): transpose into row-major Vt (k x n)
+          launch_transpose(tV, V, x.n, x.k, ls);
+          lane_launches[li] += 3;
+        }
+      }
+      cuda_check(cudaEventRecord(ln.done, ls), "svd lane done");
+    } catch (...) {
+      errs[li] = std::current_exception();
+    }
+  };
+  {
+    std::vector<std::thread> pool;
+    for (int li = 1; li < nlanes; ++li) pool.emplace_back(lane_fn, li);
+    lane_fn(0);
+    for (auto& t : pool) t.join();
+  }
+  for (int li = 0; li < nlanes; ++li) {
+    if (errs[li]) std::rethrow_exception(errs[li]);
+    cuda_check(cudaStreamWaitEvent(st, ctx.svd_lanes[li]->done, 0), "svd join");
+    ctx.kernel_launches += lane_launches[li];
+  }
+  // singular values and solver statuses to the host
+  std::vector<double> hmats(head);
+  cuda_check(cudaMemcpyAsync(hmats.data(), mats, head * sizeof(double), cudaMemcpyDeviceToHost, st), "s d2h");
   ctx.sync();
+  {
+    const int* hinfo = reinterpret_cast<const int*>(hmats.data() + info_off);
+    for (size_t b = 0; b < blks.size(); ++b)
+      if (hinfo[b] != 0)
+        throw Error(kSolver, "canonicalize: gesvd did not converge (info " + std::to_string(hinfo[b]) + ")");
+  }
+  tsolve.stop();
+  PhaseTimer tselect(ctx, kPhSvdSelect);
   // sector of each block's singular values: row sector (LeftArrow) or column sector (RightArrow)
   std::map<int, size_t> sec_of;
   std::vector<std::vector<double>> svals;
@@ -1268,7 +1621,8 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     blk_sv[kv.second] = static_cast<int>(svals.size() - 1);
   }
   CanonResult res;
-  std::vector<int> kept = select_kept(svals, M, 1e-10, &res.discarded);
+  const double tie = ctx.tie_rtol >= 0.0 ? ctx.tie_rtol : kTieRtolDefault;
+  std::vector<int> kept = select_kept(svals, M, tie, &res.discarded);
   // new bond sectors in ascending sector order
   std::vector<Qn> q_nz;
   std::vector<int> d_nz;
@@ -1345,6 +1699,8 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
       bcol.push_back(k);
     }
   }
+  tselect.stop();
+  PhaseTimer tpost(ctx, kPhSvdPost);
   DevArray<DCopy> dcu, dcv;
   DevArray<double> ds;
   DevArray<int64_t> dso, dbo;
@@ -1365,7 +1721,6 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     launch_scale_blocks_cols(U->d, dbo.get(), dbr.get(), dbc.get(), dso.get(), static_cast<int>(boff.size()),
                              ds.get(), st);
   ctx.kernel_launches += 3;
-  ctx.sync();
   res.lmat = std::move(U);
   res.rmat = std::move(V);
   return res;
@@ -1374,9 +1729,6 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
 // ---------------------------------------------------------------------------
 // one bond
 // ---------------------------------------------------------------------------
-static double now() {
-  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
-}
 
 BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo, const DTensor& rmpo,
                                 const DTensor& lopr, const DTensor& ropr, const DTensor& lwfn, const DTensor& rwfn,

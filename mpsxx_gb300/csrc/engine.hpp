@@ -5,6 +5,7 @@
 #include <cusolverDn.h>
 
 #include <map>
+#include <mutex>
 #include <memory>
 #include <string>
 #include <vector>
@@ -16,11 +17,16 @@ namespace mpsxx {
 
 void cuda_check(cudaError_t e, const char* what);
 
-// Grow-only device buffer.
+// Grow-only device buffer.  Storage comes from the process-wide block cache:
+// released blocks are kept for reuse instead of being returned with cudaFree, which
+// would synchronise the device.  A buffer is used on the stream it was allocated on;
+// its release records an event there, and a later owner on another stream waits for
+// that event on the GPU before touching the block.
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
-  void ensure(size_t bytes);
+  cudaStream_t st = nullptr;
+  void ensure(size_t bytes, cudaStream_t stream);
   void release();
   ~DevBuf() { release(); }
   template <class T>
@@ -33,7 +39,7 @@ template <class T>
 struct DevArray {
   DevBuf buf;
   size_t n = 0;
-  void upload(const std::vector<T>& h, cudaStream_t st);
+  void upload(const std::vector<T>& h, cudaStream_t st);  // allocates on st
   T* get() const { return buf.as<T>(); }
 };
 
@@ -78,8 +84,9 @@ struct GemmPlan {
   size_t partial_bytes_tc() const { return size_t(nslots_tc) * kTcTileM * kTcTileN * sizeof(double); }
 };
 
-// Precision of the bulk contractions (sigma, renormalize).
-enum Precision : int { kFP64 = 0, kSplitTF32 = 1 };
+// Precision of the bulk contractions: kSplitTF32 runs H_eff * psi on the tensor
+// cores, kSplitTF32All also the renormalisation contractions.
+enum Precision : int { kFP64 = 0, kSplitTF32 = 1, kSplitTF32All = 2 };
 
 // target number of CTAs a grouped GEMM is split into (a few waves on 152 SMs)
 constexpr int kTargetCtas = 152 * 8;
@@ -98,6 +105,15 @@ struct Packed {
   DevArray<DPack> packs;
   int64_t bytes = 0;
   uint64_t src_layout = 0, src_version = ~0ull;  // what the buffer currently holds
+};
+
+// Split-TF32 execution of one GemmPlan: the operand blocks the plan touches are
+// packed as tensor-core tiles from their FP64 storage, and the persistent kernel
+// accumulates into the FP64 result (split-K partials reduced in a fixed order).
+struct SplitGemm {
+  Packed pa, pb;
+  std::vector<DPkPair> h_pk;
+  DevArray<DPkPair> pk;
 };
 
 struct SigmaPlan {
@@ -130,9 +146,26 @@ struct DavidsonStats {
   int micro = 0;
   double rnorm = 0.0;
   int converged = 0;
-  int n_sigma_fp64 = 0;       // FP64 refinement applications (split precision)
+  int n_sigma_fp64 = 0;       // applications in FP64 (all of them in FP64 precision)
   double energy_split = 0.0;  // Ritz value before refinement (split precision)
   double rnorm_fp64 = 0.0;    // |H psi - E psi|^2 with the FP64 operator (split precision)
+};
+
+// Phases of one bond step timed by Context::timers.
+enum Phase {
+  kPhMergePlan = 0,   // merged operators: host plan
+  kPhMergeAlloc,      // merged operators: device allocation
+  kPhMergeRun,        // merged operators: plan upload + scatter kernel
+  kPhWaveMerge,       // two-site wavefunction merge
+  kPhSigmaPlan,       // sigma / diagonal plans (host) and operand packing
+  kPhSigma,           // H_eff * psi applications
+  kPhDavidsonRest,    // Davidson without H_eff * psi
+  kPhSvdSolve,        // per-block SVDs
+  kPhSvdSelect,       // truncation and result layout (host)
+  kPhSvdPost,         // U / sV^T copies and scaling
+  kPhRenormPlan,      // renormalisation plans (host)
+  kPhRenormRun,       // renormalisation contractions
+  kNumPhases
 };
 
 struct Context {
@@ -149,17 +182,47 @@ struct Context {
   DevBuf svd_mats;   // per-block SVD matrices
   DevBuf gemm_part;  // split-K partial tiles
   DevBuf err_flag;   // device error flag of the tensor-core kernels
+  // canonicalize: independent per-block SVDs run on these lanes concurrently, each
+  // driven by its own host thread (the solver's launches are host-bound)
+  struct SvdLane {
+    cusolverDnHandle_t solver = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    DevBuf work;
+  };
+  std::vector<std::unique_ptr<SvdLane>> svd_lanes;
+  cudaEvent_t svd_ready = nullptr;
   int precision = kFP64;
+  // truncation: singular values within this relative window of the cutoff count as
+  // equal to it and are kept together; < 0 selects the default (1e-10)
+  double tie_rtol = -1.0;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<SigmaPlan>> sigma_plans;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<DiagPlan>> diag_plans;
   // counters for measurement
   int64_t kernel_launches = 0;
   double sigma_flops = 0.0;
   int64_t sigma_calls = 0;
+  // phase timers in seconds (enum Phase); accumulated only while profile is on,
+  // each phase closing with a stream synchronisation
+  bool profile = false;
+  double timers[kNumPhases] = {};
 
   explicit Context(int dev, cudaStream_t st);
   ~Context();
   void sync();
+};
+
+// Accumulates the time to its destruction (or stop()) into ctx.timers[phase] when
+// profiling is on; the stream is synchronised first so device work is included.
+struct PhaseTimer {
+  Context& ctx;
+  int phase;
+  double t0;
+  double dt = 0.0;  // measured duration (0 when profiling is off)
+  bool open = true;
+  PhaseTimer(Context& c, int ph);
+  void stop();
+  ~PhaseTimer() { stop(); }
 };
 
 // --- hot-path operations (reference names) ---------------------------------

@@ -220,7 +220,7 @@ def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None) -> Sw
         nonlocal nsig, flops
         nsig += int(stats["n_sigma"])
         flops += stats["sigma_flops"]
-        for k in ("t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm"):
+        for k in ("t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "n_sigma_fp64"):
             times[k] = times.get(k, 0.0) + stats[k]
 
     for i in range(N - 1):

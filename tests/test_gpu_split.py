@@ -107,3 +107,58 @@ def test_split_dmrg_hubbard12_matches_fp64(ctx):
         core.set_precision(ctx, core.FP64)
     print("split sweep energies - fp64 oracle:", [e - g["energy"] for e, g in zip(es, gold["sweeps"])])
     assert abs(es[-1] - gold["sweeps"][-1]["energy"]) < 1e-8
+
+
+def test_split_bond_step_refines_with_few_fp64_products(ctx):
+    """One bond of a converged QC n=8 sweep from identical inputs: the split step's
+    refined energy matches the FP64 step within 1e-9 Eh with at most two FP64
+    H_eff*psi (the anchor, and a second one only if the continuation fills up)."""
+    from mpsxx_gb300 import core, dmrg, mpogen
+
+    h, eri = mpogen.synthetic_qc_integrals(8, 16, 3)
+    mpo = [core.Tensor.from_dict(ctx, d) for d in mpogen.qc_mpo(h, eri)]
+    core.set_precision(ctx, core.FP64)
+    st = dmrg.make_initial_state(ctx, mpo, 8, 0, 64)
+    for _ in range(3):
+        dmrg.make_sweep(ctx, st, 1e-9)
+    i = 3
+    dmrg.advance_left(ctx, st, i)  # orthogonality centre from site 0 to the bond
+    res = {}
+    try:
+        for name, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
+            core.set_precision(ctx, prec)
+            e, _, _, _, s = core.optimize_twosite_merged(ctx, True, st.mpo[i], st.mpo[i + 1], st.lenv[i],
+                                                         st.renv[i + 1], st.wave[i], st.wave[i + 1], 1e-11, 64)
+            res[name] = (e, s)
+    finally:
+        core.set_precision(ctx, core.FP64)
+    (e64, s64), (e32, s32) = res["fp64"], res["split"]
+    print("bond step fp64", e64, s64["n_sigma"], "split", e32, s32["n_sigma"], s32["n_sigma_fp64"], s32["rnorm"])
+    assert abs(e32 - e64) < 1e-9
+    assert 1 <= s32["n_sigma_fp64"] <= 2
+    assert s32["converged"] == 1
+
+
+def test_split_renormalize_matches_fp64_qc_bond(ctx):
+    """Renormalisation contractions (U^T mL U forward, V mR V^T backward) in split
+    precision within 2e-6 of FP64, relative to the largest magnitude."""
+    from mpsxx_gb300 import core, dmrg, mpogen
+
+    h, eri = mpogen.synthetic_qc_integrals(8, 16, 5)
+    mpo = [core.Tensor.from_dict(ctx, d) for d in mpogen.qc_mpo(h, eri)]
+    st = dmrg.make_random_state(ctx, mpo, 8, 0, 128, seed=4)
+    dmrg.advance_left(ctx, st, 3)
+    mL, mR, psi = dmrg.bond_operands(ctx, st, 3)
+    for forward in (True, False):
+        U, V = core.canonicalize(ctx, forward, psi, 128)
+        op, bra = (mL, U) if forward else (mR, V)
+        out = {}
+        try:
+            for prec in (core.FP64, core.SPLIT_TF32_ALL):
+                core.set_precision(ctx, prec)
+                out[prec] = core.renormalize(ctx, forward, op, bra, bra).download()
+        finally:
+            core.set_precision(ctx, core.FP64)
+        err = rel_err(out[core.SPLIT_TF32_ALL], out[core.FP64])
+        print("renormalize forward" if forward else "renormalize backward", "split rel err", err)
+        assert err < 2e-6
