@@ -43,12 +43,14 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="split", choices=["split", "fp64"])
-    ap.add_argument("--tole", type=float, default=1e-8, help="sweep tolerance (Davidson |r|^2 < 0.1 tole)")
+    ap.add_argument("--tole", type=float, default=1e-9, help="sweep tolerance (Davidson |r|^2 < 0.1 tole)")
     ap.add_argument("--bond-step", action="store_true", help="also time one full bond step at the bench bond")
     ap.add_argument("--no-sweep", action="store_true", help="skip the FP64-vs-split sweep comparison")
-    ap.add_argument("--sweep-norb", type=int, default=12)
-    ap.add_argument("--sweep-M", type=int, default=128)
+    ap.add_argument("--sweep-norb", type=int, default=16)
+    ap.add_argument("--sweep-M", type=int, default=256)
     ap.add_argument("--sweep-max", type=int, default=12)
+    ap.add_argument("--sweep-split-all", action="store_true",
+                    help="also sweep with the renormalisation contractions in split precision")
     return ap.parse_args()
 
 
@@ -158,7 +160,10 @@ def sweep_compare(args, device: int):
     mpo_d = mpogen.qc_mpo(h1, eri)
     res = {"workload": f"qc n={n} K={2 * n} seed={args.seed} M={M} tole={args.tole}"}
     nsweeps = args.sweep_max
-    for name, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
+    arms = [("fp64", core.FP64), ("split", core.SPLIT_TF32)]
+    if args.sweep_split_all:
+        arms.append(("split_all", core.SPLIT_TF32_ALL))
+    for name, prec in arms:
         ctx = core.Context(device)
         core.set_precision(ctx, prec)
         mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
@@ -181,6 +186,10 @@ def sweep_compare(args, device: int):
                      "per_sweep": sweeps}
         del st, mpo
         ctx.close()
+    if "split_all" in res:
+        res["split_all"]["abs_dE"] = abs(res["split_all"]["energy"] - res["fp64"]["energy"])
+        res["split_all"]["speedup_last_sweep"] = (res["fp64"]["seconds_last_sweep"] /
+                                                  res["split_all"]["seconds_last_sweep"])
     de = [abs(a["energy"] - b["energy"]) for a, b in zip(res["split"]["per_sweep"], res["fp64"]["per_sweep"])]
     res["abs_dE"] = de[-1]
     res["abs_dE_max_over_sweeps"] = max(de)

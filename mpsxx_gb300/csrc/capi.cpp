@@ -250,7 +250,7 @@ int mpsxx_tensor_upload(mpsxx_tensor* t, const double* host) {
     // MPO site tensors (rank 4) keep a host copy: their scalar blocks are the
     // coefficients of the merged-operator scatter plans
     if (x.sh.rank == 4 || !x.ctx) x.host.assign(host, host + x.nnz);
-    x.data_version += 1;  // device copies derived from the old data (packed operands) are stale
+    x.data_version = next_data_version();  // device copies of the old data (packed operands) are stale
     if (x.ctx) {
       need_device(x);
       if (x.nnz)

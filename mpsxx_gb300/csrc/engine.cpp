@@ -196,6 +196,7 @@ template struct DevArray<int>;
 void DTensor::alloc_device(cudaStream_t st, bool zero) {
   store.ensure(std::max<int64_t>(nnz, 1) * sizeof(double), st);
   d = store.as<double>();
+  data_version = next_data_version();
   if (zero && nnz) cuda_check(cudaMemsetAsync(d, 0, nnz * sizeof(double), st), "tensor zero");
 }
 
@@ -217,6 +218,8 @@ Context::~Context() {
   cudaStreamSynchronize(stream);
   sigma_plans.clear();
   diag_plans.clear();
+  merge_plans.clear();
+  renorm_plans.clear();
   for (DevBuf* b : {&scr1, &scr2, &work, &partial, &scalars, &svd_work, &svd_mats, &gemm_part, &err_flag})
     b->release();
   for (auto& l : svd_lanes) {
@@ -502,6 +505,7 @@ SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DT
   p->psi_layout = static_cast<const Tensor&>(psi);
   p->psi_layout.d = nullptr;
   auto& ref = *p;
+  if (ctx.sigma_plans.size() >= kMaxCachedPlans) ctx.sigma_plans.clear();
   ctx.sigma_plans[key] = std::move(p);
   return ref;
 }
@@ -625,14 +629,14 @@ static void build_split_gemm(Context& ctx, SplitGemm& sg, const GemmPlan& g, con
   sg.pk.upload(sg.h_pk, ctx.stream);
   sg.pa.packs.upload(sg.pa.h_packs, ctx.stream);
   sg.pb.packs.upload(sg.pb.h_packs, ctx.stream);
-  sg.pa.buf.ensure(std::max<int64_t>(sg.pa.bytes, 16), ctx.stream);
-  sg.pb.buf.ensure(std::max<int64_t>(sg.pb.bytes, 16), ctx.stream);
 }
 
 // C += alpha * op(A) op(B) over the plan's tasks, in split TF32 (g uploaded).
 static void run_split_gemm(Context& ctx, SplitGemm& sg, const GemmPlan& g, double alpha, const double* A,
                            const double* B, double* C) {
   if (g.h_tasks.empty()) return;
+  sg.pa.buf.ensure(std::max<int64_t>(sg.pa.bytes, 16), ctx.stream);
+  sg.pb.buf.ensure(std::max<int64_t>(sg.pb.bytes, 16), ctx.stream);
   launch_pack(sg.pa.packs.get(), static_cast<int>(sg.pa.h_packs.size()), A, sg.pa.buf.as<uint8_t>(), ctx.stream);
   launch_pack(sg.pb.packs.get(), static_cast<int>(sg.pb.h_packs.size()), B, sg.pb.buf.as<uint8_t>(), ctx.stream);
   ctx.gemm_part.ensure(std::max<size_t>(g.partial_bytes_tc(), 16), ctx.stream);
@@ -651,6 +655,9 @@ static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTe
   {
     PhaseTimer tm(ctx, kPhSigmaPlan);
     if (!p.pk_built) build_sigma_pk(ctx, p, L, R, p.psi_layout);
+    // packed buffers are handed back between bonds; the plan itself is kept
+    for (Packed* P : {&p.pk_L, &p.pk_R, &p.pk_psi, &p.pk_scr1})
+      P->buf.ensure(std::max<int64_t>(P->bytes, 16), ctx.stream);
     // operators are packed once per (layout, data version)
     if (p.pk_L.src_layout != L.layout_id || p.pk_L.src_version != L.data_version) pack_into(ctx, p.pk_L, L);
     if (p.pk_R.src_layout != R.layout_id || p.pk_R.src_version != R.data_version) pack_into(ctx, p.pk_R, R);
@@ -794,6 +801,7 @@ DiagPlan& diag_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTen
   p->tasks.upload(p->h_tasks, ctx.stream);
   p->pairs.upload(p->h_pairs, ctx.stream);
   auto& ref = *p;
+  if (ctx.diag_plans.size() >= kMaxCachedPlans) ctx.diag_plans.clear();
   ctx.diag_plans[key] = std::move(p);
   return ref;
 }
@@ -807,55 +815,69 @@ void compute_diagonal_elements(Context& ctx, const DTensor& L, const DTensor& R,
 // ---------------------------------------------------------------------------
 // renormalize (merged operator)
 // ---------------------------------------------------------------------------
-std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& opr0, const DTensor& bra,
-                                     const DTensor& ket) {
-  PhaseTimer tplan(ctx, kPhRenormPlan);
+static std::unique_ptr<RenormPlan> build_renorm_plan(Context& ctx, bool forward, const Tensor& opr0,
+                                                     const Tensor& bra, const Tensor& ket) {
+  auto rp = std::make_unique<RenormPlan>();
   Tensor cbra = conj_view(bra);
   int K1 = 0, K2 = 0;
-  GemmPlan p1, p2;
-  Tensor scr;
   Shape s2;
   if (forward) {
     Shape s1 = gemm_result_shape(kTrans, kNoTrans, cbra.sh, opr0.sh, 3, &K1);
     auto t1 = enumerate_gemm(kTrans, kNoTrans, cbra, opr0, s1, K1);
-    layout_from_tasks(scr, s1, t1);
-    build_gemm_plan(p1, kTrans, kNoTrans, cbra, opr0, scr, K1, std::move(t1));
-    s2 = gemm_result_shape(kNoTrans, kNoTrans, scr.sh, ket.sh, 3, &K2);
+    layout_from_tasks(rp->scr, s1, t1);
+    build_gemm_plan(rp->p1, kTrans, kNoTrans, cbra, opr0, rp->scr, K1, std::move(t1));
+    s2 = gemm_result_shape(kNoTrans, kNoTrans, rp->scr.sh, ket.sh, 3, &K2);
   } else {
     Shape s1 = gemm_result_shape(kNoTrans, kNoTrans, cbra.sh, opr0.sh, 3, &K1);
     auto t1 = enumerate_gemm(kNoTrans, kNoTrans, cbra, opr0, s1, K1);
-    layout_from_tasks(scr, s1, t1);
-    build_gemm_plan(p1, kNoTrans, kNoTrans, cbra, opr0, scr, K1, std::move(t1));
-    s2 = gemm_result_shape(kNoTrans, kTrans, scr.sh, ket.sh, 3, &K2);
+    layout_from_tasks(rp->scr, s1, t1);
+    build_gemm_plan(rp->p1, kNoTrans, kNoTrans, cbra, opr0, rp->scr, K1, std::move(t1));
+    s2 = gemm_result_shape(kNoTrans, kTrans, rp->scr.sh, ket.sh, 3, &K2);
   }
   const Trans tb2 = forward ? kNoTrans : kTrans;
-  auto t2 = enumerate_gemm(kNoTrans, tb2, scr, ket, s2, K2);
-  auto out = std::make_unique<DTensor>();
-  layout_from_tasks(*out, s2, t2);
-  build_gemm_plan(p2, kNoTrans, tb2, scr, ket, *out, K2, std::move(t2));
-  const bool split = ctx.precision == kSplitTF32All;
-  SplitGemm g1, g2;
-  p1.upload(ctx.stream);
-  p2.upload(ctx.stream);
-  if (split) {
-    build_split_gemm(ctx, g1, p1, cbra, opr0);
-    build_split_gemm(ctx, g2, p2, scr, ket);
+  auto t2 = enumerate_gemm(kNoTrans, tb2, rp->scr, ket, s2, K2);
+  layout_from_tasks(rp->out, s2, t2);
+  build_gemm_plan(rp->p2, kNoTrans, tb2, rp->scr, ket, rp->out, K2, std::move(t2));
+  rp->p1.upload(ctx.stream);
+  rp->p2.upload(ctx.stream);
+  return rp;
+}
+
+std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& opr0, const DTensor& bra,
+                                     const DTensor& ket) {
+  PhaseTimer tplan(ctx, kPhRenormPlan);
+  const auto key = std::make_tuple(forward ? 1 : 0, opr0.layout_id, bra.layout_id, ket.layout_id);
+  auto it = ctx.renorm_plans.find(key);
+  if (it == ctx.renorm_plans.end()) {
+    if (ctx.renorm_plans.size() >= kMaxCachedPlans) ctx.renorm_plans.clear();
+    it = ctx.renorm_plans.emplace(key, build_renorm_plan(ctx, forward, opr0, bra, ket)).first;
   }
+  RenormPlan& rp = *it->second;
+  const bool split = ctx.precision == kSplitTF32All;
+  if (split && !rp.split_built) {
+    build_split_gemm(ctx, rp.g1, rp.p1, conj_view(bra), opr0);
+    build_split_gemm(ctx, rp.g2, rp.p2, rp.scr, ket);
+    rp.split_built = true;
+  }
+  auto out = std::make_unique<DTensor>();
+  static_cast<Tensor&>(*out) = rp.out;
   tplan.stop();
   PhaseTimer trun(ctx, kPhRenormRun);
   out->ctx = &ctx;
   out->alloc_device(ctx.stream, true);
-  ctx.scr2.ensure(std::max<int64_t>(scr.nnz, 1) * sizeof(double), ctx.stream);
+  const int64_t scr_nnz = rp.scr.nnz;
+  ctx.scr2.ensure(std::max<int64_t>(scr_nnz, 1) * sizeof(double), ctx.stream);
   double* sp = ctx.scr2.as<double>();
-  if (scr.nnz) cuda_check(cudaMemsetAsync(sp, 0, scr.nnz * sizeof(double), ctx.stream), "renorm scr zero");
+  if (scr_nnz) cuda_check(cudaMemsetAsync(sp, 0, scr_nnz * sizeof(double), ctx.stream), "renorm scr zero");
   if (split) {
-    run_split_gemm(ctx, g1, p1, 1.0, bra.d, opr0.d, sp);
-    run_split_gemm(ctx, g2, p2, 1.0, sp, ket.d, out->d);
+    run_split_gemm(ctx, rp.g1, rp.p1, 1.0, bra.d, opr0.d, sp);
+    run_split_gemm(ctx, rp.g2, rp.p2, 1.0, sp, ket.d, out->d);
+    for (Packed* P : {&rp.g1.pa, &rp.g1.pb, &rp.g2.pa, &rp.g2.pb}) P->buf.release();
     check_device_error(ctx);
   } else {
-    ctx.gemm_part.ensure(std::max(p1.partial_bytes(), p2.partial_bytes()), ctx.stream);
-    p1.run(1.0, bra.d, opr0.d, sp, ctx.gemm_part.as<double>(), ctx.stream);
-    p2.run(1.0, sp, ket.d, out->d, ctx.gemm_part.as<double>(), ctx.stream);
+    ctx.gemm_part.ensure(std::max(rp.p1.partial_bytes(), rp.p2.partial_bytes()), ctx.stream);
+    rp.p1.run(1.0, bra.d, opr0.d, sp, ctx.gemm_part.as<double>(), ctx.stream);
+    rp.p2.run(1.0, sp, ket.d, out->d, ctx.gemm_part.as<double>(), ctx.stream);
     ctx.kernel_launches += 2;
   }
   return out;
@@ -864,12 +886,8 @@ std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& 
 // ---------------------------------------------------------------------------
 // merged super-block operators (scatter of scalar MPO blocks)
 // ---------------------------------------------------------------------------
-std::unique_ptr<DTensor> compute_merged_operator(Context& ctx, bool forward, const DTensor& mpo,
-                                                 const DTensor& opr) {
-  if (mpo.sh.rank != 4 || opr.sh.rank != 3) throw Error(kInvalidArgument, "merged operator: bad ranks");
-  if (static_cast<int64_t>(mpo.host.size()) != mpo.nnz)
-    throw Error(kInvalidArgument, "merged operator: MPO coefficients must be available on the host");
-  PhaseTimer tplan(ctx, kPhMergePlan);
+static std::unique_ptr<MergePlan> build_merge_plan(Context& ctx, bool forward, const DTensor& mpo,
+                                                   const DTensor& opr) {
   for (size_t b = 0; b < mpo.tags.size(); ++b)
     if ((b + 1 < mpo.tags.size() ? mpo.offsets[b + 1] : mpo.nnz) - mpo.offsets[b] != 1)
       throw Error(kInvalidArgument, "merged operator: MPO blocks must be scalars (1x1x1x1)");
@@ -1025,17 +1043,37 @@ std::unique_ptr<DTensor> compute_merged_operator(Context& ctx, bool forward, con
         hs[fill[ent_col[e]]++] = DScatterSrc{opr.offsets[ob], sld, 0, ent_coef[e]};
     }
   }
+  auto plan = std::make_unique<MergePlan>();
+  plan->layout = static_cast<const Tensor&>(*out);
+  plan->dst.upload(hd, ctx.stream);
+  plan->src.upload(hs, ctx.stream);
+  plan->ndst = static_cast<int>(hd.size());
+  return plan;
+}
+
+std::unique_ptr<DTensor> compute_merged_operator(Context& ctx, bool forward, const DTensor& mpo,
+                                                 const DTensor& opr) {
+  if (mpo.sh.rank != 4 || opr.sh.rank != 3) throw Error(kInvalidArgument, "merged operator: bad ranks");
+  if (static_cast<int64_t>(mpo.host.size()) != mpo.nnz)
+    throw Error(kInvalidArgument, "merged operator: MPO coefficients must be available on the host");
+  PhaseTimer tplan(ctx, kPhMergePlan);
+  // the plan depends on the layouts and on the MPO coefficients (data version)
+  const auto key = std::make_tuple(forward ? 1 : 0, mpo.layout_id, mpo.data_version, opr.layout_id);
+  auto it = ctx.merge_plans.find(key);
+  if (it == ctx.merge_plans.end()) {
+    if (ctx.merge_plans.size() >= kMaxCachedPlans) ctx.merge_plans.clear();
+    it = ctx.merge_plans.emplace(key, build_merge_plan(ctx, forward, mpo, opr)).first;
+  }
+  const MergePlan& plan = *it->second;
+  auto out = std::make_unique<DTensor>();
+  static_cast<Tensor&>(*out) = plan.layout;
   tplan.stop();
   PhaseTimer talloc(ctx, kPhMergeAlloc);
   out->ctx = &ctx;
   out->alloc_device(ctx.stream, true);
   talloc.stop();
   PhaseTimer trun(ctx, kPhMergeRun);
-  DevArray<DScatterDst> dd;
-  DevArray<DScatterSrc> ds;
-  dd.upload(hd, ctx.stream);
-  ds.upload(hs, ctx.stream);
-  launch_scatter(dd.get(), static_cast<int>(hd.size()), ds.get(), opr.d, out->d, ctx.stream);
+  launch_scatter(plan.dst.get(), plan.ndst, plan.src.get(), opr.d, out->d, ctx.stream);
   ctx.kernel_launches += 1;
   return out;
 }
@@ -1730,6 +1768,22 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
 // one bond
 // ---------------------------------------------------------------------------
 
+// Plans are keyed by structural layout ids and kept across bonds and sweeps (a
+// converged sweep repeats the layouts of the previous one); the large packed
+// operand buffers go back to the block cache after every bond.
+void release_bond_buffers(Context& ctx) {
+  for (auto& kv : ctx.sigma_plans)
+    for (Packed* P : {&kv.second->pk_L, &kv.second->pk_R, &kv.second->pk_psi, &kv.second->pk_scr1}) {
+      P->buf.release();
+      P->src_layout = 0;
+      P->src_version = ~0ull;
+    }
+  if (ctx.sigma_plans.size() > kMaxCachedPlans) ctx.sigma_plans.clear();
+  if (ctx.diag_plans.size() > kMaxCachedPlans) ctx.diag_plans.clear();
+  if (ctx.merge_plans.size() > kMaxCachedPlans) ctx.merge_plans.clear();
+  if (ctx.renorm_plans.size() > kMaxCachedPlans) ctx.renorm_plans.clear();
+}
+
 BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo, const DTensor& rmpo,
                                 const DTensor& lopr, const DTensor& ropr, const DTensor& lwfn, const DTensor& rwfn,
                                 double tole, int M) {
@@ -1766,9 +1820,7 @@ BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo,
   out.stats.t_renorm = t5 - t4;
   out.lwfn = expand_rows(ctx, wm.ql, *cr.lmat);
   out.rwfn = expand_cols(ctx, *cr.rmat, wm.qr);
-  // the plans keyed by these layouts die with the tensors
-  ctx.sigma_plans.clear();
-  ctx.diag_plans.clear();
+  release_bond_buffers(ctx);
   return out;
 }
 

@@ -91,6 +91,9 @@ enum Precision : int { kFP64 = 0, kSplitTF32 = 1, kSplitTF32All = 2 };
 // target number of CTAs a grouped GEMM is split into (a few waves on 152 SMs)
 constexpr int kTargetCtas = 152 * 8;
 
+// plans kept per kind in a context before the cache is emptied
+constexpr size_t kMaxCachedPlans = 512;
+
 // GEMM plan into a C whose layout is `c` (block offsets).  C blocks may be
 // sub-blocks of a larger block when `cmap` is provided (fused merges).
 void build_gemm_plan(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a, const Tensor& b, const Tensor& c,
@@ -130,6 +133,22 @@ struct SigmaPlan {
   std::vector<DGemmTask> h_pk_tasks1;
   DevArray<DPkPair> pk1, pk2;
   DevArray<DGemmTask> pk_tasks1;
+};
+
+// Merged-operator scatter plan (result layout + destination/source records).
+struct MergePlan {
+  Tensor layout;
+  DevArray<DScatterDst> dst;
+  DevArray<DScatterSrc> src;
+  int ndst = 0;
+};
+
+// Renormalisation plan: both Gemm stages and the layouts they produce.
+struct RenormPlan {
+  Tensor scr, out;
+  GemmPlan p1, p2;
+  bool split_built = false;
+  SplitGemm g1, g2;
 };
 
 struct DiagPlan {
@@ -198,6 +217,8 @@ struct Context {
   double tie_rtol = -1.0;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<SigmaPlan>> sigma_plans;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<DiagPlan>> diag_plans;
+  std::map<std::tuple<int, uint64_t, uint64_t, uint64_t>, std::unique_ptr<MergePlan>> merge_plans;
+  std::map<std::tuple<int, uint64_t, uint64_t, uint64_t>, std::unique_ptr<RenormPlan>> renorm_plans;
   // counters for measurement
   int64_t kernel_launches = 0;
   double sigma_flops = 0.0;
@@ -224,6 +245,9 @@ struct PhaseTimer {
   void stop();
   ~PhaseTimer() { stop(); }
 };
+
+// Hand the packed-operand buffers of the cached plans back to the block cache.
+void release_bond_buffers(Context& ctx);
 
 // --- hot-path operations (reference names) ---------------------------------
 

@@ -7,9 +7,36 @@
 
 namespace mpsxx {
 
-uint64_t next_layout_id() {
+uint64_t next_data_version() {
   static std::atomic<uint64_t> counter{1};
   return counter.fetch_add(1);
+}
+
+namespace {
+uint64_t mix(uint64_t h, uint64_t v) {
+  // splitmix64 finaliser over the running state
+  uint64_t z = h ^ (v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2));
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+}  // namespace
+
+uint64_t structure_hash(const Shape& sh, const std::vector<int64_t>& tags) {
+  uint64_t h = mix(0x6d707378ull, static_cast<uint64_t>(sh.rank));
+  h = mix(h, static_cast<uint32_t>(sh.q.p));
+  h = mix(h, static_cast<uint32_t>(sh.q.s));
+  for (int i = 0; i < sh.rank; ++i) {
+    h = mix(h, sh.qshape[i].size());
+    for (size_t j = 0; j < sh.qshape[i].size(); ++j) {
+      h = mix(h, static_cast<uint32_t>(sh.qshape[i][j].p));
+      h = mix(h, static_cast<uint32_t>(sh.qshape[i][j].s));
+      h = mix(h, static_cast<uint32_t>(sh.dshape[i][j]));
+    }
+  }
+  h = mix(h, tags.size());
+  for (int64_t t : tags) h = mix(h, static_cast<uint64_t>(t));
+  return h ? h : 1;
 }
 
 void Shape::finalize() {
@@ -52,7 +79,7 @@ void Tensor::set_blocks(const std::vector<int64_t>& sorted_tags) {
     off += sh.block_size(idx);
   }
   nnz = off;
-  layout_id = next_layout_id();
+  layout_id = structure_hash(sh, tags);
 }
 
 void Tensor::allocate_allowed() {

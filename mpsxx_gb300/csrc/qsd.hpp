@@ -98,8 +98,13 @@ struct Tensor {
   int64_t nnz = 0;
   double* d = nullptr;  // device data (nnz doubles), owned when own == true
   bool own = false;
-  uint64_t layout_id = 0;     // changes whenever the block layout changes
-  uint64_t data_version = 0;  // bumped whenever the data is replaced from outside a plan
+  // Structural identity of the block layout (a hash of shape and stored tags):
+  // tensors with equal layouts share it, so plans keyed by it are reused across
+  // bonds and sweeps.
+  uint64_t layout_id = 0;
+  // Process-wide unique identity of the current data (new storage or an upload);
+  // copies derived from the data (packed operands) are keyed by it.
+  uint64_t data_version = 0;
 
   void set_blocks(const std::vector<int64_t>& sorted_tags);
   void allocate_allowed();  // every allowed block of non-zero size (STArray.h:219-237)
@@ -119,7 +124,8 @@ struct Tensor {
   }
 };
 
-uint64_t next_layout_id();
+uint64_t next_data_version();
+uint64_t structure_hash(const Shape& sh, const std::vector<int64_t>& tags);
 
 // ---------------------------------------------------------------------------
 // Block-task enumeration of ST_Gemm_thread (include/btas/SPARSE/STBLAS.h:297-359)
