@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--sweep-norb", type=int, default=16)
     ap.add_argument("--sweep-M", type=int, default=256)
     ap.add_argument("--sweep-max", type=int, default=12)
+    ap.add_argument("--warm-sweeps", type=int, default=3,
+                    help="sweeps in each precision from the FP64-converged state")
     ap.add_argument("--sweep-split-all", action="store_true",
                     help="also sweep with the renormalisation contractions in split precision")
     return ap.parse_args()
@@ -163,6 +165,7 @@ def sweep_compare(args, device: int):
     arms = [("fp64", core.FP64), ("split", core.SPLIT_TF32)]
     if args.sweep_split_all:
         arms.append(("split_all", core.SPLIT_TF32_ALL))
+    warm = None
     for name, prec in arms:
         ctx = core.Context(device)
         core.set_precision(ctx, prec)
@@ -184,18 +187,49 @@ def sweep_compare(args, device: int):
                      "n_sigma_total": sum(s["n_sigma"] for s in sweeps),
                      "sigma_tflops_last_sweep": sweeps[-1]["sigma_flops"] / sweeps[-1]["seconds"] / 1e12,
                      "per_sweep": sweeps}
+        if prec == core.FP64 and args.warm_sweeps > 0:
+            warm = warm_compare(args, ctx, st)
         del st, mpo
         ctx.close()
     if "split_all" in res:
         res["split_all"]["abs_dE"] = abs(res["split_all"]["energy"] - res["fp64"]["energy"])
         res["split_all"]["speedup_last_sweep"] = (res["fp64"]["seconds_last_sweep"] /
                                                   res["split_all"]["seconds_last_sweep"])
+    res["warm"] = warm
     de = [abs(a["energy"] - b["energy"]) for a, b in zip(res["split"]["per_sweep"], res["fp64"]["per_sweep"])]
     res["abs_dE"] = de[-1]
     res["abs_dE_max_over_sweeps"] = max(de)
     res["speedup_last_sweep"] = res["fp64"]["seconds_last_sweep"] / res["split"]["seconds_last_sweep"]
     res["speedup_total"] = res["fp64"]["seconds_total"] / res["split"]["seconds_total"]
     return res
+
+
+def warm_compare(args, ctx, st):
+    """From the FP64-converged state, the same number of further sweeps in FP64 and
+    in split precision (identical start, same fixed point): energies sweep by sweep
+    and sweep times at convergence."""
+    from mpsxx_gb300 import core, dmrg
+
+    out = {}
+    for name, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
+        core.set_precision(ctx, prec)
+        s2 = dmrg.DeviceState(st.mpo, list(st.wave), list(st.lenv), list(st.renv), st.M)
+        rows = []
+        for _ in range(args.warm_sweeps):
+            log = dmrg.make_sweep(ctx, s2, args.tole)
+            rows.append({"seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma,
+                         "n_sigma_fp64": int(log.times.get("n_sigma_fp64", 0)), "sigma_flops": log.sigma_flops})
+        out[name] = rows
+    core.set_precision(ctx, core.FP64)
+    de = [abs(a["energy"] - b["energy"]) for a, b in zip(out["split"], out["fp64"])]
+    t64 = sum(r["seconds"] for r in out["fp64"])
+    t32 = sum(r["seconds"] for r in out["split"])
+    out["abs_dE_per_sweep"] = de
+    out["abs_dE_max"] = max(de)
+    out["seconds_per_sweep_fp64"] = t64 / len(out["fp64"])
+    out["seconds_per_sweep_split"] = t32 / len(out["split"])
+    out["speedup"] = t64 / t32
+    return out
 
 
 def bond_compare(ctx, wl, M, tole):

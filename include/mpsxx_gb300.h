@@ -167,6 +167,20 @@ int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_t
                                   double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
                                   mpsxx_tensor** new_rwfn, double* stats);
 
+/* Adjoint of the bond energy with respect to the MPO: for the normalised merged
+ * two-site wavefunction psi[A,B] of the bond between lmpo and rmpo,
+ * E = <psi| H_eff |psi>, and grad_l[b] = dE/d(block b of lmpo), grad_r likewise
+ * (arrays of nnz(lmpo) and nnz(rmpo) doubles, block order; MPO blocks are 1x1x1x1).
+ * dE/d(merged operator) is contracted on the tensor cores in split precision when
+ * the context's precision is not MPSXX_FP64, then pulled back through the merged-
+ * operator scatter by a deterministic adjoint kernel.  E is linear in each site
+ * MPO, so sum_b W_l[b] grad_l[b] = E.  No reference counterpart (the reference has
+ * no derivatives); it differentiates mpsxx::compute_merged_operator
+ * (src/optimize.hpp:273-368) and compute_sigma_vector. */
+int mpsxx_mpo_gradient(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                       const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* psi, double* grad_l,
+                       double* grad_r);
+
 /* Merge the last two indices of a 3-index site tensor in place of the
  * reference's QSTmerge(a, cols_info, b) (include/btas/QSPARSE/QSTmerge.h:85-140). */
 int mpsxx_merge_cols(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** out);

@@ -288,6 +288,17 @@ def gemm(ctx: Context, transa: int, transb: int, alpha: float, a: Tensor, b: Ten
     return Tensor(o, ctx)
 
 
+def mpo_gradient(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor, psi: Tensor):
+    """dE/dW for both site MPOs of a bond, E = <psi|H_eff|psi> (psi normalised,
+    merged two-site form); arrays in the MPOs' block order."""
+    gl = np.zeros(lmpo.nnz)
+    gr = np.zeros(rmpo.nnz)
+    dp = C.POINTER(C.c_double)
+    check(lib().mpsxx_mpo_gradient(ctx.h, lmpo.h, rmpo.h, lopr.h, ropr.h, psi.h, gl.ctypes.data_as(dp),
+                                   gr.ctypes.data_as(dp)))
+    return gl, gr
+
+
 def merge_cols(ctx: Context, a: Tensor) -> Tensor:
     o = _out()
     check(lib().mpsxx_merge_cols(ctx.h, a.h, C.byref(o)))

@@ -424,6 +424,19 @@ int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_t
   });
 }
 
+int mpsxx_mpo_gradient(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                       const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* psi, double* grad_l,
+                       double* grad_r) {
+  return guard([&] {
+    need(grad_l && grad_r, "null output");
+    Context& c = ctx_of(ctx);
+    std::vector<double> gl, gr;
+    bond_mpo_gradient(c, ten(lmpo), ten(rmpo), ten(lopr), ten(ropr), ten(psi), gl, gr);
+    std::memcpy(grad_l, gl.data(), gl.size() * sizeof(double));
+    std::memcpy(grad_r, gr.data(), gr.size() * sizeof(double));
+  });
+}
+
 int mpsxx_merge_cols(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** out) {
   return guard([&] {
     need(out != nullptr, "null output");

@@ -928,11 +928,13 @@ static std::unique_ptr<MergePlan> build_merge_plan(Context& ctx, bool forward, c
     for (int c = 0; c < nc; ++c) row_ptr[c + 1] += row_ptr[c];
     ent_col.resize(mpo.tags.size());
     ent_coef.resize(mpo.tags.size());
+    ent_st.resize(mpo.tags.size());
     std::vector<int32_t> fill(row_ptr.begin(), row_ptr.end() - 1);
     for (size_t b = 0; b < mpo.tags.size(); ++b) {
       const int e = fill[mi[b][c_axis]]++;
       ent_col[e] = (mi[b][1] * nt + mi[b][2]) * nu + mi[b][u_axis];
       ent_coef[e] = mpo.host[mpo.offsets[b]];
+      ent_st[e] = static_cast<int32_t>(b);  // MPO block slot of the entry
     }
   }
   // environment blocks grouped by outer pair (a,x), contracted index ascending
@@ -1031,7 +1033,7 @@ static std::unique_ptr<MergePlan> build_merge_plan(Context& ctx, bool forward, c
       r.dld = dcols;
       r.s0 = static_cast<int>(next_src);
       r.s1 = static_cast<int>(next_src + d.cnt);
-      r.pad = 0;
+      r.pad = slot_of(d.otag);
       next_src += d.cnt;
       if (r.rows > 0 && r.cols > 0) hd.push_back(r);
     }
@@ -1040,7 +1042,7 @@ static std::unique_ptr<MergePlan> build_merge_plan(Context& ctx, bool forward, c
       const int c = oi[ob][1];
       const int sld = opr.sh.dshape[2][oi[ob][2]];
       for (int e = row_ptr[c]; e < row_ptr[c + 1]; ++e)
-        hs[fill[ent_col[e]]++] = DScatterSrc{opr.offsets[ob], sld, 0, ent_coef[e]};
+        hs[fill[ent_col[e]]++] = DScatterSrc{opr.offsets[ob], sld, ent_st[e], ent_coef[e]};
     }
   }
   auto plan = std::make_unique<MergePlan>();
@@ -1048,7 +1050,92 @@ static std::unique_ptr<MergePlan> build_merge_plan(Context& ctx, bool forward, c
   plan->dst.upload(hd, ctx.stream);
   plan->src.upload(hs, ctx.stream);
   plan->ndst = static_cast<int>(hd.size());
+  plan->h_dst = std::move(hd);
+  plan->src_entry.resize(hs.size());
+  for (size_t i = 0; i < hs.size(); ++i) plan->src_entry[i] = hs[i].pad;
+  plan->nentries = static_cast<int>(mpo.tags.size());
   return plan;
+}
+
+static MergePlan& merge_plan(Context& ctx, bool forward, const DTensor& mpo, const DTensor& opr) {
+  const auto key = std::make_tuple(forward ? 1 : 0, mpo.layout_id, mpo.data_version, opr.layout_id);
+  auto it = ctx.merge_plans.find(key);
+  if (it == ctx.merge_plans.end()) {
+    if (ctx.merge_plans.size() >= kMaxCachedPlans) ctx.merge_plans.clear();
+    it = ctx.merge_plans.emplace(key, build_merge_plan(ctx, forward, mpo, opr)).first;
+  }
+  return *it->second;
+}
+
+// dE/dW[e] = sum over the scatter records of MPO block e of <Y_sub, env_block>,
+// with Y = dE/d(merged operator) laid out as any tensor whose blocks carry the
+// merged operator's sector indices (the adjoint of compute_merged_operator).
+std::vector<double> mpo_gradient(Context& ctx, bool forward, const DTensor& mpo, const DTensor& opr,
+                                 const DTensor& Y) {
+  MergePlan& plan = merge_plan(ctx, forward, mpo, opr);
+  if (Y.sh.rank != 3) throw Error(kInvalidArgument, "mpo gradient: adjoint operator must have 3 indices");
+  for (int i = 0; i < 3; ++i)
+    if (Y.sh.dshape[i] != plan.layout.sh.dshape[i])
+      throw Error(kInvalidArgument, "mpo gradient: adjoint operator sectors differ from the merged operator's");
+  if (!plan.adj_built) {
+    std::vector<int> ptr(plan.nentries + 1, 0), idx(plan.src_entry.size());
+    for (int32_t e : plan.src_entry) ptr[e + 1]++;
+    for (int e = 0; e < plan.nentries; ++e) ptr[e + 1] += ptr[e];
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (size_t s = 0; s < plan.src_entry.size(); ++s) idx[fill[plan.src_entry[s]]++] = static_cast<int>(s);
+    plan.adj_ptr.upload(ptr, ctx.stream);
+    plan.adj_idx.upload(idx, ctx.stream);
+    plan.adj_built = true;
+  }
+  // destinations rebased onto Y's blocks (absent blocks: Y = 0 there)
+  std::vector<DScatterDst> yd(plan.h_dst);
+  for (DScatterDst& d : yd) {
+    const int64_t tag = plan.layout.tags[d.pad];
+    const int32_t ys = Y.find(tag);
+    d.dst_off = ys < 0 ? -1 : Y.offsets[ys] + (d.dst_off - plan.layout.offsets[d.pad]);
+  }
+  DevArray<DScatterDst> dyd;
+  dyd.upload(yd, ctx.stream);
+  DevBuf g, G;
+  g.ensure(std::max<size_t>(plan.src_entry.size(), 1) * sizeof(double), ctx.stream);
+  G.ensure(std::max(plan.nentries, 1) * sizeof(double), ctx.stream);
+  cuda_check(cudaMemsetAsync(g.p, 0, std::max<size_t>(plan.src_entry.size(), 1) * sizeof(double), ctx.stream),
+             "gradient zero");
+  launch_adjoint_scatter(dyd.get(), static_cast<int>(yd.size()), plan.src.get(), Y.d, opr.d, g.as<double>(),
+                         ctx.stream);
+  launch_segment_sum(plan.adj_ptr.get(), plan.adj_idx.get(), g.as<double>(), plan.nentries, G.as<double>(),
+                     ctx.stream);
+  ctx.kernel_launches += 2;
+  std::vector<double> out(plan.nentries);
+  if (plan.nentries)
+    cuda_check(cudaMemcpyAsync(out.data(), G.p, plan.nentries * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream),
+               "gradient d2h");
+  ctx.sync();
+  return out;
+}
+
+// Gradient of E = <psi| H_eff |psi> (psi normalised, merged two-site form) with
+// respect to the scalar blocks of both site MPOs of the bond.
+void bond_mpo_gradient(Context& ctx, const DTensor& lmpo, const DTensor& rmpo, const DTensor& lopr,
+                       const DTensor& ropr, const DTensor& psi, std::vector<double>& gl, std::vector<double>& gr) {
+  auto mL = compute_merged_operator(ctx, true, lmpo, lopr);
+  auto mR = compute_merged_operator(ctx, false, rmpo, ropr);
+  // dE/dmL[A,w,A'] = sum psi[A,B] mR[B,w,B'] psi[A',B'] (a backward renormalisation
+  // with psi as bra and ket); dE/dmR likewise forward.  These contractions follow
+  // the context's precision (split when H_eff * psi is split).
+  const int saved = ctx.precision;
+  if (ctx.precision != kFP64) ctx.precision = kSplitTF32All;
+  std::unique_ptr<DTensor> Y, Z;
+  try {
+    Y = renormalize(ctx, false, *mR, psi, psi);
+    Z = renormalize(ctx, true, *mL, psi, psi);
+  } catch (...) {
+    ctx.precision = saved;
+    throw;
+  }
+  ctx.precision = saved;
+  gl = mpo_gradient(ctx, true, lmpo, lopr, *Y);
+  gr = mpo_gradient(ctx, false, rmpo, ropr, *Z);
 }
 
 std::unique_ptr<DTensor> compute_merged_operator(Context& ctx, bool forward, const DTensor& mpo,
@@ -1058,13 +1145,7 @@ std::unique_ptr<DTensor> compute_merged_operator(Context& ctx, bool forward, con
     throw Error(kInvalidArgument, "merged operator: MPO coefficients must be available on the host");
   PhaseTimer tplan(ctx, kPhMergePlan);
   // the plan depends on the layouts and on the MPO coefficients (data version)
-  const auto key = std::make_tuple(forward ? 1 : 0, mpo.layout_id, mpo.data_version, opr.layout_id);
-  auto it = ctx.merge_plans.find(key);
-  if (it == ctx.merge_plans.end()) {
-    if (ctx.merge_plans.size() >= kMaxCachedPlans) ctx.merge_plans.clear();
-    it = ctx.merge_plans.emplace(key, build_merge_plan(ctx, forward, mpo, opr)).first;
-  }
-  const MergePlan& plan = *it->second;
+  const MergePlan& plan = merge_plan(ctx, forward, mpo, opr);
   auto out = std::make_unique<DTensor>();
   static_cast<Tensor&>(*out) = plan.layout;
   tplan.stop();

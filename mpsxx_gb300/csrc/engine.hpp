@@ -141,6 +141,13 @@ struct MergePlan {
   DevArray<DScatterDst> dst;
   DevArray<DScatterSrc> src;
   int ndst = 0;
+  // adjoint (MPO gradient): host copies of the destinations (pad = result block
+  // slot), the MPO block of every source, and the sources grouped by MPO block
+  std::vector<DScatterDst> h_dst;
+  std::vector<int32_t> src_entry;
+  int nentries = 0;
+  bool adj_built = false;
+  DevArray<int> adj_ptr, adj_idx;
 };
 
 // Renormalisation plan: both Gemm stages and the layouts they produce.
@@ -245,6 +252,13 @@ struct PhaseTimer {
   void stop();
   ~PhaseTimer() { stop(); }
 };
+
+// Adjoint of compute_merged_operator: dE/dW for the MPO blocks given
+// Y = dE/d(merged operator); and both site gradients of one bond's energy.
+std::vector<double> mpo_gradient(Context& ctx, bool forward, const DTensor& mpo, const DTensor& opr,
+                                 const DTensor& Y);
+void bond_mpo_gradient(Context& ctx, const DTensor& lmpo, const DTensor& rmpo, const DTensor& lopr,
+                       const DTensor& ropr, const DTensor& psi, std::vector<double>& gl, std::vector<double>& gr);
 
 // Hand the packed-operand buffers of the cached plans back to the block cache.
 void release_bond_buffers(Context& ctx);

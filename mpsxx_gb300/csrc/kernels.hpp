@@ -95,6 +95,13 @@ void launch_copy(const DCopy* tasks, int ntasks, const double* src, double* dst,
                  cudaStream_t st);
 void launch_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* src, double* dst,
                     cudaStream_t st);
+// Adjoint of launch_scatter: for every source record s of destination d,
+// g[s] = sum_{r,c} Y[d.dst_off + r*d.dld + c] * src[s.src_off + r*s.sld + c]
+// (destinations with dst_off < 0 are skipped and leave their g untouched).
+void launch_adjoint_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* Y,
+                            const double* src, double* g, cudaStream_t st);
+// G[e] = sum_{k = ptr[e]}^{ptr[e+1]-1} g[idx[k]], summed in index order.
+void launch_segment_sum(const int* ptr, const int* idx, const double* g, int ne, double* G, cudaStream_t st);
 void launch_diag(const DDiagTask* tasks, int ntasks, const DDiagPair* pairs, const double* L, const double* R,
                  double* out, cudaStream_t st);
 

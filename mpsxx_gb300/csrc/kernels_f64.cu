@@ -154,6 +154,44 @@ __global__ void scatter_kernel(const DScatterDst* __restrict__ dsts, const DScat
   }
 }
 
+// One CTA per destination sub-block; for each of its sources a block-wide dot
+// product with a fixed reduction tree (warp shuffles, then the warp totals in order).
+__global__ void adjoint_scatter_kernel(const DScatterDst* __restrict__ dsts, const DScatterSrc* __restrict__ srcs,
+                                       const double* __restrict__ Y, const double* __restrict__ src,
+                                       double* __restrict__ g) {
+  __shared__ double warp_part[8];
+  const DScatterDst t = dsts[blockIdx.x];
+  if (t.dst_off < 0) return;
+  const int64_t n = (int64_t)t.rows * t.cols;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int s = t.s0; s < t.s1; ++s) {
+    const DScatterSrc q = srcs[s];
+    double acc = 0.0;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+      const int r = static_cast<int>(e / t.cols), c = static_cast<int>(e % t.cols);
+      acc = fma(Y[t.dst_off + (int64_t)r * t.dld + c], src[q.src_off + (int64_t)r * q.sld + c], acc);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) warp_part[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0.0;
+      for (int w = 0; w < nwarps; ++w) tot += warp_part[w];
+      g[s] = tot;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void segment_sum_kernel(const int* __restrict__ ptr, const int* __restrict__ idx,
+                                   const double* __restrict__ g, int ne, double* __restrict__ G) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  double acc = 0.0;
+  for (int k = ptr[e]; k < ptr[e + 1]; ++k) acc += g[idx[k]];
+  G[e] = acc;
+}
+
 __global__ void diag_kernel(const DDiagTask* __restrict__ tasks, const DDiagPair* __restrict__ pairs,
                             const double* __restrict__ L, const double* __restrict__ R, double* __restrict__ out) {
   const DDiagTask t = tasks[blockIdx.x];
@@ -321,6 +359,17 @@ void launch_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, 
                     cudaStream_t st) {
   if (ndst <= 0) return;
   scatter_kernel<<<ndst, 256, 0, st>>>(dsts, srcs, src, dst);
+}
+
+void launch_adjoint_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* Y,
+                            const double* src, double* g, cudaStream_t st) {
+  if (ndst <= 0) return;
+  adjoint_scatter_kernel<<<ndst, 256, 0, st>>>(dsts, srcs, Y, src, g);
+}
+
+void launch_segment_sum(const int* ptr, const int* idx, const double* g, int ne, double* G, cudaStream_t st) {
+  if (ne <= 0) return;
+  segment_sum_kernel<<<(ne + 255) / 256, 256, 0, st>>>(ptr, idx, g, ne, G);
 }
 
 void launch_diag(const DDiagTask* tasks, int ntasks, const DDiagPair* pairs, const double* L, const double* R,

@@ -263,3 +263,111 @@ def dmrg(ctx: Context, mpo_dicts: List[dict], n_elec: int, two_sz: int, M: int, 
         if it > 0 and abs(de) < tole and it + 1 >= min_sweeps:
             break
     return st, logs
+
+
+# ---------------------------------------------------------------------------
+# energy gradient with respect to the MPO and the Hamiltonian parameters
+# ---------------------------------------------------------------------------
+def _right_env_step(ctx: Context, st: DeviceState, R: Tensor, k: int) -> Tensor:
+    """R_{k-1} from R_k and the right-canonical site tensor k."""
+    mR = core.compute_merged_operator(ctx, False, st.mpo[k], R)
+    vm = core.merge_cols(ctx, st.wave[k])
+    return core.renormalize(ctx, False, mR, vm, vm)
+
+
+@dataclass
+class GradientLog:
+    energy: float                 # <psi|H|psi> of the (unchanged) state
+    bond_energies: List[float]    # the same value measured at every bond
+    site_grads: List[np.ndarray]  # dE/dW per site, in the MPO's block order
+    env_recomputed: int           # right environments rebuilt from checkpoints
+    env_peak: int                 # right environments held at once
+    seconds: float
+
+
+def gradient_sweep(ctx: Context, st: DeviceState, checkpoint: int = 4) -> GradientLog:
+    """dE/dW for every site MPO of a state whose orthogonality centre is at site 0
+    (as a backward sweep leaves it).
+
+    One forward pass: at bond (i, i+1) the merged two-site wavefunction gives
+    dE/dW_i (and dE/dW_{i+1} at the last bond) through the adjoint of the merged
+    operator; the centre then moves on by an SVD that keeps every non-zero singular
+    value, so the state and its energy do not change.  Right block operators are
+    kept only at every ``checkpoint``-th site; the others are recomputed from the
+    nearest checkpoint to the right when the pass reaches them and dropped once used.
+    The state's own list of right environments is not modified."""
+    t0 = time.perf_counter()
+    N = len(st.mpo)
+    ckpt = {j: st.renv[j] for j in range(N) if j % checkpoint == 0 or j == N - 1}
+    pending: Dict[int, Tensor] = {}
+    recomputed = 0
+    peak = len(ckpt)
+    wave = list(st.wave)
+    work = DeviceState(st.mpo, wave, [None] * N, [None] * N, st.M)
+
+    def right_env(j: int) -> Tensor:
+        nonlocal recomputed, peak
+        if j in ckpt:
+            return ckpt[j]
+        if j in pending:
+            return pending.pop(j)
+        c = min(k for k in ckpt if k > j)
+        R = ckpt[c]
+        for k in range(c, j, -1):
+            R = _right_env_step(ctx, work, R, k)
+            recomputed += 1
+            if k - 1 > j:
+                pending[k - 1] = R
+        peak = max(peak, len(ckpt) + len(pending) + 1)
+        return R
+
+    L = st.lenv[0]
+    grads: List[Optional[np.ndarray]] = [None] * N
+    energies = []
+    for i in range(N - 1):
+        R = right_env(i + 1)
+        psi = core.merge_wavefunction(ctx, st.mpo[i], st.mpo[i + 1], L, R, wave[i], wave[i + 1])
+        core.normalize(ctx, psi)
+        gl, gr = core.mpo_gradient(ctx, st.mpo[i], st.mpo[i + 1], L, R, psi)
+        grads[i] = gl
+        if i == N - 2:
+            grads[i + 1] = gr
+        # E is linear in W_i: E = sum_b W_i[b] dE/dW_i[b]
+        energies.append(float(np.dot(st.mpo[i].download(), gl)))
+        if i < N - 2:
+            # move the centre: psi has rank <= M, so keeping M singular values is exact
+            mL = core.compute_merged_operator(ctx, True, st.mpo[i], L)
+            U, sV = core.canonicalize(ctx, True, psi, st.M)
+            wave[i], wave[i + 1] = core.expand_wavefunction(ctx, st.mpo[i], st.mpo[i + 1], L, R, U, sV)
+            L = core.renormalize(ctx, True, mL, U, U)
+    return GradientLog(float(np.mean(energies)), energies, grads, recomputed, peak, time.perf_counter() - t0)
+
+
+def parameter_gradient(site_grads: List[np.ndarray], mpo_tags: List[np.ndarray],
+                       jacobians: List[Dict[int, Dict[object, float]]]) -> Dict[object, float]:
+    """Chain rule through the MPO generator: dE/dtheta = sum over sites and blocks of
+    dE/dW[b] * dW[b]/dtheta, with the generator's per-site {tag: {theta: dW/dtheta}}."""
+    out: Dict[object, float] = {}
+    for g, tags, jac in zip(site_grads, mpo_tags, jacobians):
+        for b, tag in enumerate(tags):
+            d = jac.get(int(tag))
+            if not d:
+                continue
+            for par, f in d.items():
+                out[par] = out.get(par, 0.0) + float(g[b]) * f
+    return out
+
+
+def restart_state(ctx: Context, mpo: List[Tensor], st: DeviceState) -> DeviceState:
+    """The MPS of ``st`` (orthogonality centre at site 0) with a new Hamiltonian of
+    the same MPO block structure: right block operators rebuilt for ``mpo``."""
+    N = len(mpo)
+    wave = list(st.wave)
+    renv: List[Optional[Tensor]] = [None] * N
+    lenv: List[Optional[Tensor]] = [None] * N
+    renv[N - 1] = _boundary(ctx)
+    new = DeviceState(mpo, wave, lenv, renv, st.M)
+    for k in range(N - 1, 0, -1):
+        renv[k - 1] = _right_env_step(ctx, new, renv[k], k)
+    lenv[0] = _boundary(ctx)
+    return new

@@ -18,7 +18,7 @@ tag), the neutral exchange format both the device path and the oracle consume.
 """
 from __future__ import annotations
 
-from typing import Dict, List, Sequence, Tuple
+from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -61,9 +61,12 @@ class SiteMPO:
         # right bond quantum shape is minus the charge of the next left operators
         self.qr = [_neg(tuple(q)) for q in q_right_ops]
         self.entries: Dict[Tuple[int, int, int, int], float] = {}
+        # d(entry)/d(parameter) of the Hamiltonian parameters the entries depend on
+        self.jac: Dict[Tuple[int, int, int, int], Dict[object, float]] = {}
 
-    def add(self, w: int, mat: np.ndarray, w2: int, coef: float = 1.0):
-        """W[w,:,:,w2] += coef * (sign-adjusted) mat."""
+    def add(self, w: int, mat: np.ndarray, w2: int, coef: float = 1.0, dcoef: Optional[Dict[object, float]] = None):
+        """W[w,:,:,w2] += coef * (sign-adjusted) mat.  ``dcoef`` maps parameters to
+        d(coef)/d(parameter); the entries' derivatives are accumulated alongside."""
         if coef == 0.0:
             return
         lpar = self.ql[w][0] & 1
@@ -76,6 +79,10 @@ class SiteMPO:
                     v = -v
                 key = (w, s, sp, w2)
                 self.entries[key] = self.entries.get(key, 0.0) + coef * v
+                if dcoef:
+                    jk = self.jac.setdefault(key, {})
+                    for par, dv in dcoef.items():
+                        jk[par] = jk.get(par, 0.0) + dv * v
 
     def to_dict(self) -> dict:
         nl, nr = len(self.ql), len(self.qr)
@@ -94,14 +101,31 @@ class SiteMPO:
             blocks[tag] = np.full((1, 1, 1, 1), v)
         return {"q": (0, 0), "qshape": qshape, "dshape": dshape, "blocks": blocks}
 
+    def jacobian(self) -> Dict[int, Dict[object, float]]:
+        """{block tag: {parameter: d(block)/d(parameter)}} over the stored blocks."""
+        nr = len(self.qr)
+        strides = (4 * 4 * nr, 4 * nr, nr, 1)
+        out = {}
+        for key, d in self.jac.items():
+            if self.entries.get(key, 0.0) == 0.0:
+                continue
+            w, s, sp, w2 = key
+            tag = w * strides[0] + s * strides[1] + sp * strides[2] + w2
+            nz = {par: v for par, v in d.items() if v != 0.0}
+            if nz:
+                out[tag] = nz
+        return out
 
-def hubbard_mpo(L: int, t, U) -> List[dict]:
+
+def hubbard_mpo(L: int, t, U, jacobian: bool = False):
     """Open-chain Hubbard MPO.
 
     H = sum_i t_i sum_s (c+_{i s} c_{i+1 s} + h.c.) + sum_i U_i n_{i up} n_{i dn}
     (``t_i`` is the one-electron integral h_{i,i+1}; scalars broadcast).
     Left-block operators at an inner bond: I, H, c+_a, c+_b, c_a, c_b of the last
-    site, so the bond dimension is 6.
+    site, so the bond dimension is 6.  With ``jacobian`` also returns, per site,
+    {block tag: {("t", i) or ("U", i): d(block)/d(parameter)}} (the MPO is linear in
+    the parameters; a parameter that is exactly zero has no block to carry it).
     """
     tt = np.broadcast_to(np.asarray(t, dtype=np.float64), (max(L - 1, 1),)).copy()
     uu = np.broadcast_to(np.asarray(U, dtype=np.float64), (L,)).copy()
@@ -119,22 +143,26 @@ def hubbard_mpo(L: int, t, U) -> List[dict]:
             W.add(0, I, 0)
         if k > 0:
             W.add(1, I, iH_r)  # H * 1
-        W.add(0, NN, iH_r, uu[k])  # on-site U
+        W.add(0, NN, iH_r, uu[k], {("U", k): 1.0})  # on-site U
         if k > 0:
             h = tt[k - 1]
+            dt = {("t", k - 1): 1.0}
+            dmt = {("t", k - 1): -1.0}
             # c+_{k-1 s} c_{k s}
-            W.add(2, Da, iH_r, h)
-            W.add(3, Db, iH_r, h)
+            W.add(2, Da, iH_r, h, dt)
+            W.add(3, Db, iH_r, h, dt)
             # c+_{k s} c_{k-1 s} = - c_{k-1 s} c+_{k s}
-            W.add(4, Ca, iH_r, -h)
-            W.add(5, Cb, iH_r, -h)
+            W.add(4, Ca, iH_r, -h, dmt)
+            W.add(5, Cb, iH_r, -h, dmt)
         if not last:
             W.add(0, Ca, 2)
             W.add(0, Cb, 3)
             W.add(0, Da, 4)
             W.add(0, Db, 5)
-        sites.append(W.to_dict())
-    return sites
+        sites.append(W)
+    if jacobian:
+        return [W.to_dict() for W in sites], [W.jacobian() for W in sites]
+    return [W.to_dict() for W in sites]
 
 
 def mpo_bond_dims(mpo: List[dict]) -> List[int]:
@@ -228,10 +256,20 @@ def _fuse(ops, sops: _SiteOps):
     return tuple(out), scale
 
 
-def terms_to_strings(nsite: int, terms, sops: _SiteOps):
-    """[(coef, [(site, elem), ...]), ...] -> {((site, siteop), ...): coef}."""
+def _lin_add(acc: Dict[object, float], lin: Optional[Dict[object, float]], f: float = 1.0):
+    if lin:
+        for par, v in lin.items():
+            acc[par] = acc.get(par, 0.0) + f * v
+
+
+def terms_to_strings(nsite: int, terms, sops: _SiteOps, track: bool = False):
+    """[(coef, [(site, elem), ...][, dcoef]), ...] -> {((site, siteop), ...): coef}.
+    With ``track`` also {string: {parameter: d(coef)/d(parameter)}} from the terms'
+    optional third element {parameter: d(coef)/d(parameter)}."""
     acc: Dict[tuple, float] = {}
-    for coef, ops in terms:
+    lins: Dict[tuple, Dict[object, float]] = {}
+    for term in terms:
+        coef, ops = term[0], term[1]
         if coef == 0.0:
             continue
         so, sign = _site_order(ops)
@@ -239,7 +277,12 @@ def terms_to_strings(nsite: int, terms, sops: _SiteOps):
         if key is None:
             continue
         acc[key] = acc.get(key, 0.0) + coef * sign * sc
-    return {k: v for k, v in acc.items() if v != 0.0}
+        if track and len(term) > 2:
+            _lin_add(lins.setdefault(key, {}), term[2], sign * sc)
+    strings = {k: v for k, v in acc.items() if v != 0.0}
+    if track:
+        return strings, {k: lins[k] for k in strings if k in lins}
+    return strings
 
 
 def _min_vertex_cover(nl: int, nr: int, edges_l: np.ndarray, edges_r: np.ndarray):
@@ -273,19 +316,29 @@ def _min_vertex_cover(nl: int, nr: int, edges_l: np.ndarray, edges_r: np.ndarray
     return ~visited_l, visited_r
 
 
-def mpo_from_strings(nsite: int, strings: Dict[tuple, float], sops: _SiteOps) -> List[dict]:
-    """Exact MPO of sum_s coef_s * prod_k o_{s,k} (site-ordered, fused strings)."""
+def mpo_from_strings(nsite: int, strings: Dict[tuple, float], sops: _SiteOps,
+                     lins: Optional[Dict[tuple, Dict[object, float]]] = None):
+    """Exact MPO of sum_s coef_s * prod_k o_{s,k} (site-ordered, fused strings).
+    With ``lins`` ({string: {parameter: d(coef)/d(parameter)}}) the parameter
+    derivatives are carried through the construction (every coefficient lands in
+    exactly one MPO entry, the rest of its path being identity-like 1's) and the
+    per-site {block tag: {parameter: derivative}} maps are returned as well."""
+    track = lins is not None
     # current terms: (alpha, rest) -> coef, rest = ((site, op), ...) with sites >= k
     cur: Dict[Tuple[int, tuple], float] = {}
+    curlin: Dict[Tuple[int, tuple], Dict[object, float]] = {}
     for key, c in strings.items():
         k2 = (0, key)
         cur[k2] = cur.get(k2, 0.0) + c
+        if track and key in lins:
+            _lin_add(curlin.setdefault(k2, {}), lins[key])
+    jacs = []
     q_left = [(0, 0)]
     sites = []
     for k in range(nsite):
         lnodes: Dict[Tuple[int, int], int] = {}
         rnodes: Dict[tuple, int] = {}
-        el, er, ec = [], [], []
+        el, er, ec, elin = [], [], [], []
         for (alpha, rest), c in cur.items():
             if rest and rest[0][0] == k:
                 o, r = rest[0][1], rest[1:]
@@ -297,6 +350,8 @@ def mpo_from_strings(nsite: int, strings: Dict[tuple, float], sops: _SiteOps) ->
             el.append(li)
             er.append(ri)
             ec.append(c)
+            if track:
+                elin.append(curlin.get((alpha, rest)))
         el = np.asarray(el, dtype=np.int64)
         er = np.asarray(er, dtype=np.int64)
         ec = np.asarray(ec, dtype=np.float64)
@@ -326,7 +381,9 @@ def mpo_from_strings(nsite: int, strings: Dict[tuple, float], sops: _SiteOps) ->
 
         q_new = []
         wentries: Dict[Tuple[int, int, int], float] = {}
+        wlin: Dict[Tuple[int, int, int], Dict[object, float]] = {}
         nxt: Dict[Tuple[int, tuple], float] = {}
+        nxtlin: Dict[Tuple[int, tuple], Dict[object, float]] = {}
         for kind, idx in new_ops:
             if kind == "l":
                 q_new.append(lq(idx))
@@ -340,10 +397,14 @@ def mpo_from_strings(nsite: int, strings: Dict[tuple, float], sops: _SiteOps) ->
                 wentries[(a, o, b)] = 1.0
                 key = (b, rlist[ri])
                 nxt[key] = nxt.get(key, 0.0) + ec[e]
+                if track and elin[e]:
+                    _lin_add(nxtlin.setdefault(key, {}), elin[e])
             else:
                 b = beta_of_r[ri]
                 a, o = llist[li]
                 wentries[(a, o, b)] = wentries.get((a, o, b), 0.0) + ec[e]
+                if track and elin[e]:
+                    _lin_add(wlin.setdefault((a, o, b), {}), elin[e])
                 r_charge[ri] = lq(li)
                 key = (b, rlist[ri])
                 nxt[key] = 1.0
@@ -353,18 +414,27 @@ def mpo_from_strings(nsite: int, strings: Dict[tuple, float], sops: _SiteOps) ->
         W = SiteMPO(q_left, q_new)
         for (a, o, b), c in wentries.items():
             if c != 0.0:
-                W.add(a, sops.mats[o], b, c)
+                W.add(a, sops.mats[o], b, c, wlin.get((a, o, b)))
         sites.append(W.to_dict())
+        if track:
+            jacs.append(W.jacobian())
         q_left = q_new
         cur = {}
+        curlin = {}
         for (b, r), c in nxt.items():
             if c != 0.0:
                 cur[(b, r)] = c
+                if track and (b, r) in nxtlin:
+                    curlin[(b, r)] = nxtlin[(b, r)]
+    if track:
+        return sites, jacs
     return sites
 
 
-def qc_terms(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0, tol: float = 0.0):
-    """H = E0 + sum h_pq a+_ps a_qs + 1/2 sum (pq|rs) a+_ps a+_rt a_st a_qs (chemists' notation)."""
+def qc_terms(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0, tol: float = 0.0, track_h: bool = False):
+    """H = E0 + sum h_pq a+_ps a_qs + 1/2 sum (pq|rs) a+_ps a+_rt a_st a_qs (chemists' notation).
+    With ``track_h`` the one-electron terms carry {("h", p, q): 1} (derivative of
+    their coefficient with respect to the matrix element h1[p, q])."""
     n = h1.shape[0]
     C = ("Ca", "Cb")
     D = ("Da", "Db")
@@ -377,7 +447,10 @@ def qc_terms(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0, tol: float = 0
             if abs(v) <= tol:
                 continue
             for s in range(2):
-                terms.append((v, [(p, C[s]), (q, D[s])]))
+                if track_h:
+                    terms.append((v, [(p, C[s]), (q, D[s])], {("h", p, q): 1.0}))
+                else:
+                    terms.append((v, [(p, C[s]), (q, D[s])]))
     nz = np.argwhere(np.abs(eri) > tol)
     for p, q, r, s in nz:
         v = 0.5 * eri[p, q, r, s]
@@ -391,9 +464,13 @@ def qc_terms(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0, tol: float = 0
     return terms
 
 
-def qc_mpo(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0) -> List[dict]:
-    """Exact quantum-chemistry MPO with spatial-orbital sites."""
+def qc_mpo(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0, jacobian: bool = False):
+    """Exact quantum-chemistry MPO with spatial-orbital sites.  With ``jacobian``
+    also the per-site {block tag: {("h", p, q): d(block)/d(h1[p, q])}} maps."""
     sops = _SiteOps()
+    if jacobian:
+        strings, lins = terms_to_strings(h1.shape[0], qc_terms(h1, eri, ecore, track_h=True), sops, track=True)
+        return mpo_from_strings(h1.shape[0], strings, sops, lins)
     strings = terms_to_strings(h1.shape[0], qc_terms(h1, eri, ecore), sops)
     return mpo_from_strings(h1.shape[0], strings, sops)
 
