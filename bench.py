@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--sweep-norb", type=int, default=16)
     ap.add_argument("--sweep-M", type=int, default=256)
     ap.add_argument("--sweep-max", type=int, default=12)
+    ap.add_argument("--gradient", action="store_true",
+                    help="also run the energy-gradient workloads (site-dependent Hubbard L=32 M=512, QC n=16 M=256)")
+    ap.add_argument("--grad-fd", type=int, default=2, help="parameters checked by central differences per workload")
     ap.add_argument("--warm-sweeps", type=int, default=3,
                     help="sweeps in each precision from the FP64-converged state")
     ap.add_argument("--sweep-split-all", action="store_true",
@@ -202,6 +205,97 @@ def sweep_compare(args, device: int):
     res["speedup_last_sweep"] = res["fp64"]["seconds_last_sweep"] / res["split"]["seconds_last_sweep"]
     res["speedup_total"] = res["fp64"]["seconds_total"] / res["split"]["seconds_total"]
     return res
+
+
+def _converge(ctx, mpo, n_elec, M, tole, max_sweeps, st=None):
+    from mpsxx_gb300 import dmrg
+
+    if st is None:
+        st = dmrg.make_initial_state(ctx, mpo, n_elec, 0, M)
+    e_prev, n = None, 0
+    for n in range(1, max_sweeps + 1):
+        log = dmrg.make_sweep(ctx, st, tole)
+        if e_prev is not None and abs(log.energy - e_prev) < tole:
+            break
+        e_prev = log.energy
+    return st, log.energy, n
+
+
+def gradient_bench(args, device: int):
+    """Adjoint energy gradients: dE/dU_i, dE/dt_i of a site-dependent Hubbard chain
+    (L=32, U_i ~ U(2,6), |t_i| ~ U(0.8,1.2), half filling, M=512) and dE/dh_pq of the
+    n=16 synthetic QC Hamiltonian (M=256).  Gradient in FP64 and split precision on
+    the same converged state, environments checkpointed every 4 sites; a few
+    parameters checked by central differences (step 1e-4) of warm-restarted DMRG."""
+    import numpy as np
+
+    from mpsxx_gb300 import core, dmrg, mpogen
+
+    out = {}
+    rng = np.random.default_rng(args.seed)
+    L = 32
+    U = rng.uniform(2.0, 6.0, L)
+    t = -rng.uniform(0.8, 1.2, L - 1)
+    n = 16
+    h1, eri = mpogen.synthetic_qc_integrals(n, 2 * n, args.seed)
+    cases = [
+        ("hubbard_L32_M512", lambda th: mpogen.hubbard_mpo(L, th[0], th[1], jacobian=True), (t, U), L, 512,
+         [("U", 0), ("U", L // 2), ("t", L // 2)]),
+        ("qc_n16_M256", lambda th: mpogen.qc_mpo(th[0], eri, jacobian=True), (h1,), n, 256,
+         [("h", 0, 0), ("h", 3, 5), ("h", 7, 8)]),
+    ]
+    tole = 1e-10
+    for name, build, theta, nel, M, checks in cases:
+        ctx = core.Context(device)
+        sites, jacs = build(theta)
+        mpo = [core.Tensor.from_dict(ctx, d) for d in sites]
+        t0 = time.perf_counter()
+        st, e0, nsw = _converge(ctx, mpo, nel, M, tole, 20)
+        t_dmrg = time.perf_counter() - t0
+        tags = [m.blocks()[0] for m in st.mpo]
+        res = {"energy": e0, "sweeps": nsw, "dmrg_seconds": t_dmrg, "checkpoint": 4}
+        grads = {}
+        for pname, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
+            core.set_precision(ctx, prec)
+            g = dmrg.gradient_sweep(ctx, st, checkpoint=4)
+            core.set_precision(ctx, core.FP64)
+            grads[pname] = dmrg.parameter_gradient(g.site_grads, tags, jacs)
+            res[pname] = {"seconds": g.seconds, "state_energy": g.energy, "env_recomputed": g.env_recomputed,
+                          "env_peak": g.env_peak, "env_all": len(st.mpo)}
+        keys = sorted(grads["fp64"], key=str)
+        res["n_parameters"] = len(keys)
+        res["split_vs_fp64_max_rel"] = max(abs(grads["split"][k] - grads["fp64"][k]) / max(1.0, abs(grads["fp64"][k]))
+                                          for k in keys)
+        fd_rows = []
+        for par in checks[: args.grad_fd]:
+            vals = []
+            for sgn in (1.0, -1.0):
+                th = [np.array(x, copy=True) for x in theta]
+                if par[0] == "U":
+                    th[1][par[1]] += sgn * 1e-4
+                elif par[0] == "t":
+                    th[0][par[1]] += sgn * 1e-4
+                else:  # symmetric step of h_pq and h_qp
+                    p, q = par[1], par[2]
+                    th[0][p, q] += sgn * 1e-4
+                    if p != q:
+                        th[0][q, p] += sgn * 1e-4
+                sites2, _ = build(th)
+                mpo2 = [core.Tensor.from_dict(ctx, d) for d in sites2]
+                st2 = dmrg.restart_state(ctx, mpo2, st)
+                st2, _, _ = _converge(ctx, mpo2, nel, M, tole * 0.1, 8, st2)
+                vals.append(dmrg.gradient_sweep(ctx, st2, checkpoint=4).energy)
+            fd = (vals[0] - vals[1]) / 2e-4
+            adj = grads["fp64"].get(par, 0.0)
+            if par[0] == "h" and par[1] != par[2]:
+                adj += grads["fp64"].get(("h", par[2], par[1]), 0.0)
+            fd_rows.append({"param": list(map(str, par)), "adjoint": adj, "fd": fd,
+                            "rel": abs(adj - fd) / max(1.0, abs(fd))})
+        res["fd_checks"] = fd_rows
+        out[name] = res
+        del st, mpo
+        ctx.close()
+    return out
 
 
 def warm_compare(args, ctx, st):
@@ -449,6 +543,7 @@ def main():
     fp64_peak = measure_fp64_peak(torch)
     bond = bond_compare(ctx, wl, args.M, args.tole) if args.bond_step else None
     sweep = sweep_compare(args, local) if not args.no_sweep else None
+    grad = gradient_bench(args, local) if args.gradient else None
     out = None
     if rank == 0:
         achieved = fl_per_step / kt["sigma_kernels_s"] / 1e12
@@ -486,6 +581,7 @@ def main():
             "accuracy": {"max_rel_err_vs_fp64": rel},
             "bond_step": bond,
             "sweeps": sweep,
+            "gradient": grad,
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline:

@@ -181,6 +181,12 @@ int mpsxx_mpo_gradient(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx
                        const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* psi, double* grad_l,
                        double* grad_r);
 
+/* a[i, j, k] -> out[(i, j), k] and its inverse (QSTmerge / QSTexpand over the
+ * leading two indices, include/btas/QSPARSE/QSTmerge.h:31-120,218-295) for the
+ * one-site algorithm; `like` supplies the unmerged sectors. */
+int mpsxx_merge_rows(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** out);
+int mpsxx_expand_rows(mpsxx_context* ctx, const mpsxx_tensor* b, const mpsxx_tensor* like, mpsxx_tensor** out);
+
 /* Merge the last two indices of a 3-index site tensor in place of the
  * reference's QSTmerge(a, cols_info, b) (include/btas/QSPARSE/QSTmerge.h:85-140). */
 int mpsxx_merge_cols(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** out);

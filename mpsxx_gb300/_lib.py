@@ -26,6 +26,8 @@ SIGNATURES = {
     "mpsxx_context_counters": (C.c_int, [vp, c_i64_p, c_dbl_p, c_i64_p]),
     "mpsxx_context_set_truncation": (C.c_int, [vp, C.c_double]),
     "mpsxx_mpo_gradient": (C.c_int, [vp, vp, vp, vp, vp, vp, c_dbl_p, c_dbl_p]),
+    "mpsxx_merge_rows": (C.c_int, [vp, vp, vpp]),
+    "mpsxx_expand_rows": (C.c_int, [vp, vp, vp, vpp]),
     "mpsxx_context_profile": (C.c_int, [vp, C.c_int, C.c_int, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_context_set_precision": (C.c_int, [vp, C.c_int]),
     "mpsxx_context_get_precision": (C.c_int, [vp, c_int_p]),

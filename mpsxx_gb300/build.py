@@ -51,7 +51,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     if force or not out.exists() or out.stat().st_mtime < max(o.stat().st_mtime for o in objs):
-        cmd = [nvcc(), ARCH, "-shared", "-o", str(out)] + [str(o) for o in objs] + ["-lcusolver", "-lcudart", "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+        cmd = [nvcc(), ARCH, "-shared", "-o", str(out)] + [str(o) for o in objs] + ["-lcusolver", "-lcublas", "-lcudart", "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -299,6 +299,18 @@ def mpo_gradient(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: T
     return gl, gr
 
 
+def merge_rows(ctx: Context, a: Tensor) -> Tensor:
+    o = _out()
+    check(lib().mpsxx_merge_rows(ctx.h, a.h, C.byref(o)))
+    return Tensor(o, ctx)
+
+
+def expand_rows(ctx: Context, b: Tensor, like: Tensor) -> Tensor:
+    o = _out()
+    check(lib().mpsxx_expand_rows(ctx.h, b.h, like.h, C.byref(o)))
+    return Tensor(o, ctx)
+
+
 def merge_cols(ctx: Context, a: Tensor) -> Tensor:
     o = _out()
     check(lib().mpsxx_merge_cols(ctx.h, a.h, C.byref(o)))

@@ -449,6 +449,30 @@ int mpsxx_merge_cols(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** o
   });
 }
 
+int mpsxx_merge_rows(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    const DTensor& A = ten(a);
+    need(A.sh.rank == 3, "merge_rows: expects a 3-index tensor");
+    MergeInfo info({A.sh.qshape[0], A.sh.qshape[1]}, {A.sh.dshape[0], A.sh.dshape[1]});
+    *out = wrap(merge_rows(c, info, A), ctx);
+    c.sync();
+  });
+}
+
+int mpsxx_expand_rows(mpsxx_context* ctx, const mpsxx_tensor* b, const mpsxx_tensor* like, mpsxx_tensor** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    const DTensor& L = ten(like);
+    need(L.sh.rank == 3, "expand_rows: `like` must be a 3-index tensor");
+    MergeInfo info({L.sh.qshape[0], L.sh.qshape[1]}, {L.sh.dshape[0], L.sh.dshape[1]});
+    *out = wrap(expand_rows(c, info, ten(b)), ctx);
+    c.sync();
+  });
+}
+
 int mpsxx_gemm(mpsxx_context* ctx, int transa, int transb, double alpha, const mpsxx_tensor* a,
                const mpsxx_tensor* b, int c_rank, mpsxx_tensor** c) {
   return guard([&] {

@@ -227,6 +227,7 @@ Context::~Context() {
     l->work.release();
     block_cache().unregister_stream(l->stream);
     if (l->solver) cusolverDnDestroy(l->solver);
+    if (l->blas) cublasDestroy(l->blas);
     if (l->done) cudaEventDestroy(l->done);
     cudaStreamDestroy(l->stream);
   }
@@ -1323,6 +1324,59 @@ std::unique_ptr<DTensor> expand_cols(Context& ctx, const DTensor& b, const Merge
   return a;
 }
 
+std::unique_ptr<DTensor> merge_rows(Context& ctx, const MergeInfo& info, const DTensor& a) {
+  // a[(i,j), x...] -> b[A, x...]  (QSTmerge over the leading indices,
+  // include/btas/QSPARSE/QSTmerge.h:31-120): every block is a contiguous row range
+  const int MR = static_cast<int>(info.qshape.size());
+  const int MC = a.sh.rank - MR;
+  if (MC < 1) throw Error(kInvalidArgument, "merge_rows: nothing left to keep as columns");
+  auto b = std::make_unique<DTensor>();
+  b->sh.rank = MC + 1;
+  b->sh.q = a.sh.q;
+  b->sh.qshape.push_back(info.q_merged);
+  b->sh.dshape.push_back(info.d_merged);
+  for (int i = MR; i < a.sh.rank; ++i) {
+    b->sh.qshape.push_back(a.sh.qshape[i]);
+    b->sh.dshape.push_back(a.sh.dshape[i]);
+  }
+  b->sh.finalize();
+  const int64_t a_stride = a.sh.stride[MR - 1];  // tag = packed_row * a_stride + rest
+  const int64_t b_stride = b->sh.stride[0];
+  struct Pend {
+    int64_t btag, src_off;
+    int rows, cols, roff;
+  };
+  std::vector<Pend> pend;
+  int idx[kMaxRank];
+  for (size_t ab = 0; ab < a.tags.size(); ++ab) {
+    const int64_t ip = a.tags[ab] / a_stride, rest = a.tags[ab] % a_stride;
+    const int A = info.merged_of[ip];
+    const int64_t bt = A * b_stride + rest;
+    if (!b->sh.allowed_tag(bt)) continue;
+    a.sh.index(a.tags[ab], idx);
+    int64_t cols = 1;
+    for (int k = MR; k < a.sh.rank; ++k) cols *= a.sh.dshape[k][idx[k]];
+    pend.push_back({bt, a.offsets[ab], info.d_packed[ip], static_cast<int>(cols), info.offset_packed[ip]});
+  }
+  std::vector<int64_t> tags;
+  for (auto& p : pend) tags.push_back(p.btag);
+  std::sort(tags.begin(), tags.end());
+  tags.erase(std::unique(tags.begin(), tags.end()), tags.end());
+  b->set_blocks(tags);
+  std::vector<DCopy> cp;
+  for (auto& p : pend) {
+    const int32_t s = b->find(p.btag);
+    cp.push_back(DCopy{b->offsets[s] + int64_t(p.roff) * p.cols, p.src_off, p.rows, p.cols, p.cols, p.cols, 1.0});
+  }
+  b->ctx = &ctx;
+  b->alloc_device(ctx.stream, true);
+  DevArray<DCopy> dc;
+  dc.upload(cp, ctx.stream);
+  launch_copy(dc.get(), static_cast<int>(cp.size()), a.d, b->d, 0, ctx.stream);
+  ctx.kernel_launches += 1;
+  return b;
+}
+
 std::unique_ptr<DTensor> merge_cols(Context& ctx, const DTensor& a, const MergeInfo& info) {
   const int MC = static_cast<int>(info.qshape.size());
   const int MR = a.sh.rank - MC;
@@ -1585,6 +1639,8 @@ std::vector<int> select_kept(const std::vector<std::vector<double>>& svals, int 
 constexpr double kTieRtolDefault = 1.0e-10;
 // concurrent SVD lanes of canonicalize
 constexpr int kSvdLanes = 8;
+// smallest min(m, n) of a block that takes the reduced-density-matrix route
+constexpr int kEighMin = 96;
 
 CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise) {
   if (noise >= 1.0e-8) throw Error(kInvalidArgument, "canonicalize: noise injection is not supported");
@@ -1596,6 +1652,8 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     int32_t slot;
     int i, j, m, n, k;
     int64_t u_off, s_off, v_off;  // inside svd_mats
+    bool eigh = false;            // density-matrix route: U (forward) or V (backward) from eigh,
+                                  // the other factor stored already multiplied by s
   };
   std::vector<Blk> blks;
   int64_t nsv = 0;  // singular values first (one contiguous read-back), then U and V^T
@@ -1626,15 +1684,29 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   ctx.svd_mats.ensure(size_t(tot) * sizeof(double), ctx.stream);
   double* mats = ctx.svd_mats.as<double>();
   int* infos = reinterpret_cast<int*>(mats + info_off);
+  // Blocks with min(m, n) >= kEighMin take the reduced-density-matrix route: the
+  // eigenvectors of A A^T (forward) or A^T A (backward) give the kept factor, the
+  // other one is a projection of A (cuSOLVER's gesvd is latency-bound at these
+  // sizes); smaller blocks take gesvd.
   int lwork = 0;
-  for (const auto& x : blks) {
+  int64_t max_gram = 1;
+  for (auto& x : blks) {
     int lw = 0;
-    solver_check(cusolverDnDgesvd_bufferSize(ctx.solver, std::max(x.m, x.n), std::min(x.m, x.n), &lw),
-                 "gesvd bufferSize");
+    x.eigh = x.k >= kEighMin;
+    if (x.eigh) {
+      const int d = forward ? x.m : x.n;
+      solver_check(cusolverDnDsyevd_bufferSize(ctx.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, d,
+                                               nullptr, d, nullptr, &lw),
+                   "syevd bufferSize");
+      max_gram = std::max<int64_t>(max_gram, int64_t(d) * d + d);
+    } else {
+      solver_check(cusolverDnDgesvd_bufferSize(ctx.solver, std::max(x.m, x.n), std::min(x.m, x.n), &lw),
+                   "gesvd bufferSize");
+    }
     lwork = std::max(lwork, lw);
   }
-  // per lane: gesvd work | rwork | col-major copy of A | col-major U | col-major V^T
-  const size_t lane_doubles = size_t(lwork) + 8 + 4 * size_t(std::max<int64_t>(maxmn, 1)) + 8;
+  // per lane: solver work | rwork | col-major copy of A | col-major U | col-major V^T | Gram + eigenvalues
+  const size_t lane_doubles = size_t(lwork) + 8 + 4 * size_t(std::max<int64_t>(maxmn, 1)) + 8 + size_t(max_gram);
   std::vector<int> by_cost(blks.size());
   std::iota(by_cost.begin(), by_cost.end(), 0);
   std::stable_sort(by_cost.begin(), by_cost.end(), [&](int p, int q) {
@@ -1648,6 +1720,8 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     cuda_check(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming), "svd lane event");
     solver_check(cusolverDnCreate(&l->solver), "cusolverDnCreate");
     solver_check(cusolverDnSetStream(l->solver, l->stream), "cusolverDnSetStream");
+    if (cublasCreate(&l->blas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(l->blas, l->stream) != CUBLAS_STATUS_SUCCESS)
+      throw Error(kCuda, "cublas handle for the SVD lanes");
     block_cache().register_stream(l->stream);
     ctx.svd_lanes.push_back(std::move(l));
   }
@@ -1675,7 +1749,30 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
         double* S = mats + x.s_off;
         double* V = mats + x.v_off;
         int* info = infos + by_cost[i];
-        if (x.n >= x.m) {
+        if (x.eigh) {
+          double* G = tV + maxmn;
+          const double one = 1.0, zero = 0.0;
+          const int d = forward ? x.m : x.n;
+          double* W = G + int64_t(d) * d;
+          // a: row-major m x n == column-major n x m (ld n)
+          cublasStatus_t bs =
+              forward ? cublasDgemm(ln.blas, CUBLAS_OP_T, CUBLAS_OP_N, x.m, x.m, x.n, &one, a, x.n, a, x.n, &zero, G,
+                                    x.m)
+                      : cublasDgemm(ln.blas, CUBLAS_OP_N, CUBLAS_OP_T, x.n, x.n, x.m, &one, a, x.n, a, x.n, &zero, G,
+                                    x.n);
+          if (bs != CUBLAS_STATUS_SUCCESS) throw Error(kCuda, "canonicalize: Gram matrix dgemm failed");
+          solver_check(cusolverDnDsyevd(ln.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, d, G, d, W, work,
+                                        lwork, info),
+                       "syevd");
+          // forward: U (row-major m x k) and s V^T = U^T A; backward: V^T (row-major k x n) and U s = A V
+          launch_eig_factors(G, W, d, x.k, forward ? 0 : 1, forward ? U : V, tU, S, ls);
+          bs = forward ? cublasDgemm(ln.blas, CUBLAS_OP_N, CUBLAS_OP_N, x.n, x.k, x.m, &one, a, x.n, tU, x.m, &zero,
+                                     V, x.n)
+                       : cublasDgemm(ln.blas, CUBLAS_OP_T, CUBLAS_OP_N, x.k, x.m, x.n, &one, tU, x.n, a, x.n, &zero,
+                                     U, x.k);
+          if (bs != CUBLAS_STATUS_SUCCESS) throw Error(kCuda, "canonicalize: projection dgemm failed");
+          lane_launches[li] += 1;
+        } else if (x.n >= x.m) {
           // row-major A (m x n) is col-major A^T (n x m): A^T = Ux S VxT, so U_A = VxT buffer, Vt_A = Ux buffer
           cuda_check(cudaMemcpyAsync(tA, a, int64_t(x.m) * x.n * sizeof(double), cudaMemcpyDeviceToDevice, ls),
                      "svd copy");
@@ -1807,7 +1904,10 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     cu.push_back(DCopy{U->offsets[us], x.u_off, x.m, k, k, x.k, 1.0});
     cv.push_back(DCopy{V->offsets[vs], x.v_off, k, x.n, x.n, x.n, 1.0});
     soff.push_back(static_cast<int64_t>(s_kept.size()));
-    s_kept.insert(s_kept.end(), hmats.begin() + x.s_off, hmats.begin() + x.s_off + k);
+    if (x.eigh)
+      s_kept.insert(s_kept.end(), k, 1.0);  // the projected factor already carries s
+    else
+      s_kept.insert(s_kept.end(), hmats.begin() + x.s_off, hmats.begin() + x.s_off + k);
     if (forward) {
       boff.push_back(V->offsets[vs]);
       brow.push_back(k);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <map>
@@ -212,6 +213,7 @@ struct Context {
   // driven by its own host thread (the solver's launches are host-bound)
   struct SvdLane {
     cusolverDnHandle_t solver = nullptr;
+    cublasHandle_t blas = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     DevBuf work;
@@ -314,6 +316,7 @@ std::unique_ptr<DTensor> expand_rows(Context& ctx, const MergeInfo& info, const 
 std::unique_ptr<DTensor> expand_cols(Context& ctx, const DTensor& b, const MergeInfo& info);
 // QSTmerge column merge of the trailing indices (include/btas/QSPARSE/QSTmerge.h:85-140)
 std::unique_ptr<DTensor> merge_cols(Context& ctx, const DTensor& a, const MergeInfo& info);
+std::unique_ptr<DTensor> merge_rows(Context& ctx, const MergeInfo& info, const DTensor& a);
 
 // btas::Gemm into an empty result (QSTBLAS.h:182-226)
 std::unique_ptr<DTensor> gemm_new(Context& ctx, Trans ta, Trans tb, double alpha, const DTensor& a, const DTensor& b,

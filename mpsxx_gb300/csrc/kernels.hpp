@@ -98,6 +98,12 @@ void launch_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, 
 // Adjoint of launch_scatter: for every source record s of destination d,
 // g[s] = sum_{r,c} Y[d.dst_off + r*d.dld + c] * src[s.src_off + r*s.sld + c]
 // (destinations with dst_off < 0 are skipped and leave their g untouched).
+// Eigenvectors G (d x d, column-major, eigenvalues w ascending) of a Gram matrix ->
+// the k leading ones in descending order: out (row-major d x k, or its transpose
+// k x d when transposed != 0), xcm (column-major d x k) and s_j = sqrt(w) with
+// eigenvalues under 64 eps * w_max set to zero.
+void launch_eig_factors(const double* G, const double* w, int d, int k, int transposed, double* out, double* xcm,
+                        double* s, cudaStream_t st);
 void launch_adjoint_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* Y,
                             const double* src, double* g, cudaStream_t st);
 // G[e] = sum_{k = ptr[e]}^{ptr[e+1]-1} g[idx[k]], summed in index order.

@@ -8,6 +8,8 @@
 // order, so results are deterministic run to run.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.hpp"
 
 namespace mpsxx {
@@ -180,6 +182,25 @@ __global__ void adjoint_scatter_kernel(const DScatterDst* __restrict__ dsts, con
       g[s] = tot;
     }
     __syncthreads();
+  }
+}
+
+__global__ void eig_factors_kernel(const double* __restrict__ G, const double* __restrict__ w, int d, int k,
+                                   int transposed, double* __restrict__ out, double* __restrict__ xcm,
+                                   double* __restrict__ s) {
+  const int64_t n = (int64_t)d * k;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = static_cast<int>(e % d), j = static_cast<int>(e / d);
+    const double v = G[r + (int64_t)(d - 1 - j) * d];
+    xcm[r + (int64_t)j * d] = v;
+    if (transposed)
+      out[(int64_t)j * d + r] = v;
+    else
+      out[(int64_t)r * k + j] = v;
+    if (r == 0) {
+      const double lam = w[d - 1 - j], top = w[d - 1];
+      s[j] = lam > 64.0 * 2.220446049250313e-16 * top ? sqrt(lam) : 0.0;
+    }
   }
 }
 
@@ -365,6 +386,14 @@ void launch_adjoint_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc
                             const double* src, double* g, cudaStream_t st) {
   if (ndst <= 0) return;
   adjoint_scatter_kernel<<<ndst, 256, 0, st>>>(dsts, srcs, Y, src, g);
+}
+
+void launch_eig_factors(const double* G, const double* w, int d, int k, int transposed, double* out, double* xcm,
+                        double* s, cudaStream_t st) {
+  const int64_t n = (int64_t)d * k;
+  if (n <= 0) return;
+  const int grid = static_cast<int>(std::min<int64_t>((n + 255) / 256, 4096));
+  eig_factors_kernel<<<grid, 256, 0, st>>>(G, w, d, k, transposed, out, xcm, s);
 }
 
 void launch_segment_sum(const int* ptr, const int* idx, const double* g, int ne, double* G, cudaStream_t st) {

@@ -204,6 +204,7 @@ class SweepLog:
     sigma_flops: float
     seconds: float
     times: Dict[str, float] = field(default_factory=dict)
+    kind: str = "twosite"
 
 
 def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None) -> SweepLog:
@@ -246,22 +247,77 @@ def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None) -> Sw
     return SweepLog(min(es), es, nsig, flops, time.perf_counter() - t0, times)
 
 
+def optimize_onesite(ctx: Context, forward: bool, st: DeviceState, i: int, tole: float):
+    """One-site step at site i (src/optimize.hpp:37-145) through the merged hot path:
+    forward, psi[(l,n), r] with mL = merge(L_i, W_i) and the unmerged R_i; backward,
+    psi[l, (n,r)] with the unmerged L_i and mR = merge(R_i, W_i).  Davidson, truncated
+    SVD (M kept), s V^T (or U s) moved into the neighbouring site, and the block
+    operator renormalised past site i.  Returns (energy, diagonalize stats)."""
+    wf = st.wave[i]
+    if forward:
+        op = core.compute_merged_operator(ctx, True, st.mpo[i], st.lenv[i])
+        L, R = op, st.renv[i]
+        psi = core.merge_rows(ctx, wf)
+    else:
+        op = core.compute_merged_operator(ctx, False, st.mpo[i], st.renv[i])
+        L, R = st.lenv[i], op
+        psi = core.merge_cols(ctx, wf)
+    diag = psi.like()
+    core.compute_diagonal_elements(ctx, L, R, diag)
+    e, stats = core.diagonalize(ctx, L, R, diag, psi, tole)
+    if forward:
+        U, sV = core.canonicalize(ctx, True, psi, st.M)
+        st.wave[i] = core.expand_rows(ctx, U, wf)
+        nxt = core.gemm(ctx, 0, 0, 1.0, sV, st.wave[i + 1], 3)
+        st.wave[i + 1] = nxt
+        st.lenv[i + 1] = core.renormalize(ctx, True, op, U, U)
+    else:
+        Us, V = core.canonicalize(ctx, False, psi, st.M)
+        st.wave[i] = core.expand_cols(ctx, V, wf)
+        prv = core.gemm(ctx, 0, 0, 1.0, st.wave[i - 1], Us, 3)
+        st.wave[i - 1] = prv
+        st.renv[i - 1] = core.renormalize(ctx, False, op, V, V)
+    return e, stats
+
+
+def make_sweep_onesite(ctx: Context, st: DeviceState, tole: float) -> SweepLog:
+    """One-site forward then backward sweep (sites 0..N-2, then N-1..1); Davidson
+    tolerance 0.1*tole; sweep energy = minimum over sites."""
+    N = len(st.mpo)
+    t0 = time.perf_counter()
+    es: List[float] = []
+    nsig = 0
+    for i in range(N - 1):
+        e, s = optimize_onesite(ctx, True, st, i, 0.1 * tole)
+        es.append(e)
+        nsig += s["n_sigma"]
+    for i in range(N - 1, 0, -1):
+        e, s = optimize_onesite(ctx, False, st, i, 0.1 * tole)
+        es.append(e)
+        nsig += s["n_sigma"]
+    return SweepLog(min(es), es, nsig, 0.0, time.perf_counter() - t0, kind="onesite")
+
+
 def dmrg(ctx: Context, mpo_dicts: List[dict], n_elec: int, two_sz: int, M: int, tole: float, max_sweeps: int,
-         min_sweeps: int = 0, verbose: bool = False):
-    """Sweeps until |dE| < tole after at least one iteration (src/dmrg.cpp:37-79)."""
+         min_sweeps: int = 0, verbose: bool = False, onesite: bool = False):
+    """Sweeps until |dE| < tole after at least one iteration (src/dmrg.cpp:37-79); with
+    ``onesite``, the reference's second stage follows: one-site sweeps from the
+    converged two-site state until |dE| < tole again (src/dmrg.cpp:80-115)."""
     mpo = [Tensor.from_dict(ctx, d) for d in mpo_dicts]
     st = make_initial_state(ctx, mpo, n_elec, two_sz, M)
     e_prev = 0.0
     logs = []
-    for it in range(max_sweeps):
-        log = make_sweep(ctx, st, tole)
-        logs.append(log)
-        de = log.energy - e_prev
-        e_prev = log.energy
-        if verbose:
-            print(f"sweep {it}: E = {log.energy:.16f} dE = {de:.2e} ({log.seconds:.2f}s)", flush=True)
-        if it > 0 and abs(de) < tole and it + 1 >= min_sweeps:
-            break
+    stages = [make_sweep] + ([make_sweep_onesite] if onesite else [])
+    for stage in stages:
+        for it in range(max_sweeps):
+            log = stage(ctx, st, tole)
+            logs.append(log)
+            de = log.energy - e_prev
+            e_prev = log.energy
+            if verbose:
+                print(f"{stage.__name__} {it}: E = {log.energy:.16f} dE = {de:.2e} ({log.seconds:.2f}s)", flush=True)
+            if it > 0 and abs(de) < tole and it + 1 >= min_sweeps:
+                break
     return st, logs
 
 
