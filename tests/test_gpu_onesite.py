@@ -1,7 +1,7 @@
 """One-site stage (src/optimize.hpp:37-145, src/dmrg.cpp:80-115) on the merged
 hot path (needs a GPU): after the two-site stage, one-site sweeps reproduce the
-exact energy when M is exact, stay variational and move the energy by less than
-the truncation scale when M truncates."""
+exact energy when M is exact, and stay variational, above the two-site sweep energy
+by at most the truncation scale, when M truncates."""
 import numpy as np
 import pytest
 
@@ -39,4 +39,6 @@ def test_two_then_one_site_stages(ctx, M):
     if M == 256:
         assert abs(e1 - exact) < 1e-9 and abs(e2 - exact) < 1e-9
     else:
-        assert abs(e1 - e2) < 1e-4
+        # the two-site sweep energy is taken before truncation (4M states at the bond),
+        # the one-site one inside M states: apart by the truncation error
+        assert e2 - 1e-9 <= e1 < e2 + 1e-3
