@@ -503,6 +503,7 @@ def main():
     core.set_precision(ctx, core.SPLIT_TF32 if args.precision == "split" else core.FP64)
     for _ in range(args.warmup):
         core.compute_sigma_vector(ctx, mL, mR, psi, sig)
+    tuning = ctx.tuning()
     barrier(ws)
     torch.cuda.synchronize()
     launches0 = ctx.counters()["launches"]
@@ -579,6 +580,7 @@ def main():
                           "peak": fp64_peak, "frac": fl_per_step / fp64_s / 1e12 / fp64_peak,
                           "speedup_of_headline": fp64_s / kt["sigma_kernels_s"]},
             "accuracy": {"max_rel_err_vs_fp64": rel},
+            "sigma_tuning": [{"w_scratch_mb": b / 2**20, "target_tiles": tt, "ms": ms} for b, tt, ms in tuning],
             "bond_step": bond,
             "sweeps": sweep,
             "gradient": grad,

@@ -87,6 +87,14 @@ int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* 
       "svd_select", "svd_post", "renorm_plan", "renorm_run"
 int mpsxx_context_profile(mpsxx_context* ctx, int enable, int reset, double* t, int n, int* count);
 
+/* The split-precision H_eff*psi plan of a bond is autotuned on first use: candidate
+ * schedules (stage-2 split-K sized for a target number of tensor-core tiles, and for
+ * very large L*psi intermediates the MPO index w processed in groups that fit a
+ * scratch budget) are timed and the fastest is kept with the plan.  The last
+ * tuning's (budget bytes, target tiles, milliseconds) triples are written to out (up
+ * to n values); *count receives their number. */
+int mpsxx_context_tuning(const mpsxx_context* ctx, double* out, int n, int* count);
+
 /* ---- tensors ------------------------------------------------------------- */
 /* Create a block-sparse tensor.  qn holds 2*sum(nsec) ints (p, 2Sz per sector,
  * index by index), dims holds sum(nsec) ints.  nblocks < 0 allocates every

@@ -25,6 +25,7 @@ SIGNATURES = {
     "mpsxx_context_sync": (C.c_int, [vp]),
     "mpsxx_context_counters": (C.c_int, [vp, c_i64_p, c_dbl_p, c_i64_p]),
     "mpsxx_context_set_truncation": (C.c_int, [vp, C.c_double]),
+    "mpsxx_context_tuning": (C.c_int, [vp, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_mpo_gradient": (C.c_int, [vp, vp, vp, vp, vp, vp, c_dbl_p, c_dbl_p]),
     "mpsxx_merge_rows": (C.c_int, [vp, vp, vpp]),
     "mpsxx_expand_rows": (C.c_int, [vp, vp, vp, vpp]),

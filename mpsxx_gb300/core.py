@@ -45,6 +45,14 @@ class Context:
         """Relative tie window at the truncation cutoff (< 0: the precision's default)."""
         check(lib().mpsxx_context_set_truncation(self.h, float(tie_rtol)))
 
+    def tuning(self):
+        """Last sigma autotuning: [(w scratch budget bytes, target tiles, milliseconds), ...]."""
+        buf = (C.c_double * 64)()
+        cnt = C.c_int()
+        check(lib().mpsxx_context_tuning(self.h, buf, 64, C.byref(cnt)))
+        v = list(buf)[: cnt.value]
+        return [(int(v[i]), int(v[i + 1]), v[i + 2]) for i in range(0, len(v), 3)]
+
     def profile(self, enable=-1, reset=False):
         """Phase timers in seconds (PHASE_NAMES); enable=1/0 switches timing on/off."""
         t = (C.c_double * len(PHASE_NAMES))()

@@ -144,6 +144,15 @@ int mpsxx_context_profile(mpsxx_context* ctx, int enable, int reset, double* t, 
   });
 }
 
+int mpsxx_context_tuning(const mpsxx_context* ctx, double* out, int n, int* count) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    const auto& t = ctx->ctx->last_tuning;
+    if (count) *count = static_cast<int>(t.size());
+    for (int i = 0; out && i < n && i < static_cast<int>(t.size()); ++i) out[i] = t[i];
+  });
+}
+
 int mpsxx_tensor_create(mpsxx_context* ctx, int rank, const int* q, const int* nsec, const int* qn, const int* dims,
                         int64_t nblocks, const int64_t* tags, mpsxx_tensor** out) {
   return guard([&] {

@@ -271,7 +271,7 @@ struct CMap {
 // Output tiles of every task; the pair list of long tasks is split (split-K) so
 // that a launch fills the GPU: the work of a tile ~ the sum of its pairs' k.
 static void make_tiles(const GemmPlan& plan, int tile_m, int tile_n, std::vector<DTile>& tiles,
-                       std::vector<DReduce>& reduce, int& nslots) {
+                       std::vector<DReduce>& reduce, int& nslots, int target_ctas = kTargetCtas) {
   tiles.clear();
   reduce.clear();
   nslots = 0;
@@ -281,7 +281,7 @@ static void make_tiles(const GemmPlan& plan, int tile_m, int tile_n, std::vector
     for (int p = dt.p0; p < dt.p1; ++p) k += plan.h_pairs[p].k;
     total += double((dt.m + tile_m - 1) / tile_m) * ((dt.n + tile_n - 1) / tile_n) * k;
   }
-  const double target = std::max(1.0, total / kTargetCtas);
+  const double target = std::max(1.0, total / target_ctas);
   for (int ti = 0; ti < static_cast<int>(plan.h_tasks.size()); ++ti) {
     const DGemmTask& dt = plan.h_tasks[ti];
     double k = 0.0;
@@ -313,6 +313,8 @@ static void make_tiles(const GemmPlan& plan, int tile_m, int tile_n, std::vector
       }
   }
 }
+
+static void tile_tc(GemmPlan& plan, int target_ctas);
 
 template <class F>
 static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a, const Tensor& b, int K,
@@ -385,9 +387,14 @@ static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a,
     plan.c_elems += int64_t(c.m) * c.n;
   }
   make_tiles(plan, kGemmTile, kGemmTile, plan.h_tiles, plan.h_reduce, plan.nslots);
-  make_tiles(plan, kTcTileM, kTcTileN, plan.h_tiles_tc, plan.h_reduce_tc, plan.nslots_tc);
-  // the tensor-core kernel is persistent (CTA c takes tiles c, c + #SM, ...): heaviest
-  // tiles first gives a longest-processing-time-first balance
+  tile_tc(plan, kTargetCtas);
+}
+
+// Tensor-core (128 x 64) tiling of a plan's tasks with split-K chunks sized for about
+// target_ctas tiles, heaviest first: the kernel is persistent (CTA c takes tiles c,
+// c + #SM, ...), so this is a longest-processing-time-first balance.
+static void tile_tc(GemmPlan& plan, int target_ctas) {
+  make_tiles(plan, kTcTileM, kTcTileN, plan.h_tiles_tc, plan.h_reduce_tc, plan.nslots_tc, target_ctas);
   std::vector<std::pair<int64_t, int>> work(plan.h_tiles_tc.size());
   for (size_t i = 0; i < plan.h_tiles_tc.size(); ++i) {
     int64_t w = 0;
@@ -651,14 +658,288 @@ static void run_split_gemm(Context& ctx, SplitGemm& sg, const GemmPlan& g, doubl
   ctx.kernel_launches += 3 + (g.nslots_tc > 0);
 }
 
+// w-groups of a sigma plan for a scratch budget (bytes of packed L*psi per group).
+static void build_sigma_groups(Context& ctx, SigmaPlan& p, int64_t budget) {
+  p.groups.clear();
+  p.group_scr_bytes = 0;
+  p.group_slots = 0;
+  const Tensor& s = p.scr1;
+  const int nw = s.sh.nsec(1);
+  // packed bytes of every L*psi block and its w
+  std::vector<int64_t> blk_bytes(s.tags.size(), 0), w_bytes(nw, 0);
+  std::vector<int> blk_w(s.tags.size(), 0);
+  for (size_t b = 0; b < s.tags.size(); ++b) {
+    int d[kMaxRank], idx[kMaxRank];
+    s.block_dims(static_cast<int32_t>(b), d);
+    s.sh.index(s.tags[b], idx);
+    blk_w[b] = idx[1];
+    if (p.pk_scr1.base[b] < 0) continue;
+    const int64_t ntr = (int64_t(d[0]) * d[1] + kTcTileM - 1) / kTcTileM;
+    blk_bytes[b] = ntr * p.pk_scr1.nks[b] * kPkTileABytes;
+    w_bytes[idx[1]] += blk_bytes[b];
+  }
+  std::vector<int> group_of_w(nw, 0);
+  int ng = 0;
+  int64_t cur = 0;
+  for (int w = 0; w < nw; ++w) {
+    if (w_bytes[w] == 0) {
+      group_of_w[w] = std::max(ng - 1, 0);
+      continue;
+    }
+    if (ng == 0 || (budget > 0 && cur > 0 && cur + w_bytes[w] > budget)) {
+      ++ng;
+      cur = 0;
+    }
+    group_of_w[w] = ng - 1;
+    cur += w_bytes[w];
+  }
+  ng = std::max(ng, 1);
+  // group-local packed bases of the L*psi blocks
+  std::vector<int64_t> local(s.tags.size(), -1), fill(ng, 0);
+  for (size_t b = 0; b < s.tags.size(); ++b) {
+    if (blk_bytes[b] == 0) continue;
+    const int g = group_of_w[blk_w[b]];
+    local[b] = fill[g];
+    fill[g] += blk_bytes[b];
+  }
+  for (int g = 0; g < ng; ++g) p.group_scr_bytes = std::max(p.group_scr_bytes, fill[g]);
+  // stage 1: tasks rebased, tiles bucketed by group
+  std::vector<DGemmTask> tasks1 = p.h_pk_tasks1;
+  std::vector<int> task1_group(tasks1.size(), 0);
+  for (size_t ti = 0; ti < tasks1.size(); ++ti) {
+    const int32_t cs = s.find(p.s1.task_ctag[ti]);
+    if (cs < 0 || local[cs] < 0) throw Error(kInternal, "grouped sigma plan: stage-1 output missing");
+    tasks1[ti].c_off = local[cs];
+    task1_group[ti] = group_of_w[blk_w[cs]];
+  }
+  std::vector<std::vector<DTile>> t1(ng), t2(ng);
+  std::vector<std::vector<DReduce>> red(ng);
+  std::vector<int> slots(ng, 0);
+  for (const DTile& t : p.s1.h_tiles_tc) {
+    if (t.slot >= 0) throw Error(kInternal, "grouped sigma plan: stage 1 is not split along K");
+    t1[task1_group[t.task]].push_back(t);
+  }
+  // stage 2: pairs rebased; per task the runs of consecutive pairs in one group
+  std::vector<DPkPair> pairs2 = p.h_pk2;
+  std::vector<int> pair_group(pairs2.size(), 0);
+  for (size_t i = 0; i < pairs2.size(); ++i) {
+    const int32_t as = p.s2.pair_a_slot[i];
+    pairs2[i].a_pk = local[as];
+    pair_group[i] = group_of_w[blk_w[as]];
+  }
+  struct Run {
+    int task, p0, p1;
+    double k;
+  };
+  std::vector<std::vector<Run>> runs(ng);
+  std::vector<double> gwork(ng, 0.0);
+  for (int ti = 0; ti < static_cast<int>(p.s2.h_tasks.size()); ++ti) {
+    const DGemmTask& dt = p.s2.h_tasks[ti];
+    const double tiles = double((dt.m + kTcTileM - 1) / kTcTileM) * ((dt.n + kTcTileN - 1) / kTcTileN);
+    for (int a = dt.p0; a < dt.p1;) {
+      int b = a;
+      double k = 0.0;
+      while (b < dt.p1 && pair_group[b] == pair_group[a]) k += p.s2.h_pairs[b++].k;
+      runs[pair_group[a]].push_back(Run{ti, a, b, k});
+      gwork[pair_group[a]] += tiles * k;
+      a = b;
+    }
+  }
+  for (int g = 0; g < ng; ++g) {
+    const double target = std::max(1.0, gwork[g] / kTargetCtas);
+    for (const Run& r : runs[g]) {
+      const DGemmTask& dt = p.s2.h_tasks[r.task];
+      int nchunk = static_cast<int>(std::min<double>(r.p1 - r.p0, std::floor(r.k / target)));
+      if (nchunk < 2) nchunk = 1;
+      std::vector<int> bnd{r.p0};
+      if (nchunk > 1) {
+        double acc = 0.0, step = r.k / nchunk;
+        for (int q = r.p0; q < r.p1 && static_cast<int>(bnd.size()) < nchunk; ++q) {
+          acc += p.s2.h_pairs[q].k;
+          if (acc >= step * bnd.size() && q + 1 < r.p1) bnd.push_back(q + 1);
+        }
+      }
+      bnd.push_back(r.p1);
+      const int nc = static_cast<int>(bnd.size()) - 1;
+      for (int tm = 0; tm * kTcTileM < dt.m; ++tm)
+        for (int tn = 0; tn * kTcTileN < dt.n; ++tn) {
+          if (nc == 1) {
+            t2[g].push_back(DTile{r.task, tm, tn, bnd[0], bnd[1], -1});
+            continue;
+          }
+          for (int ch = 0; ch < nc; ++ch) t2[g].push_back(DTile{r.task, tm, tn, bnd[ch], bnd[ch + 1], slots[g] + ch});
+          red[g].push_back(DReduce{r.task, tm, tn, slots[g], nc, 0});
+          slots[g] += nc;
+        }
+    }
+  }
+  // heaviest tiles first within each launch (persistent CTAs take tiles round-robin)
+  auto tile_work = [&](const DTile& t, const std::vector<DGemmPair>& pr) {
+    int64_t w = 0;
+    for (int q = t.p0; q < t.p1; ++q) w += (pr[q].k + kPkTileK - 1) / kPkTileK;
+    return w;
+  };
+  std::vector<DTile> all1, all2;
+  std::vector<DReduce> allr;
+  for (int g = 0; g < ng; ++g) {
+    std::stable_sort(t1[g].begin(), t1[g].end(),
+                     [&](const DTile& a, const DTile& b) { return tile_work(a, p.s1.h_pairs) > tile_work(b, p.s1.h_pairs); });
+    std::stable_sort(t2[g].begin(), t2[g].end(),
+                     [&](const DTile& a, const DTile& b) { return tile_work(a, p.s2.h_pairs) > tile_work(b, p.s2.h_pairs); });
+    SigmaPlan::Group G;
+    G.t1_begin = static_cast<int>(all1.size());
+    G.t1_count = static_cast<int>(t1[g].size());
+    G.t2_begin = static_cast<int>(all2.size());
+    G.t2_count = static_cast<int>(t2[g].size());
+    G.r_begin = static_cast<int>(allr.size());
+    G.r_count = static_cast<int>(red[g].size());
+    G.nslots = slots[g];
+    p.group_slots = std::max(p.group_slots, slots[g]);
+    all1.insert(all1.end(), t1[g].begin(), t1[g].end());
+    all2.insert(all2.end(), t2[g].begin(), t2[g].end());
+    allr.insert(allr.end(), red[g].begin(), red[g].end());
+    p.groups.push_back(G);
+  }
+  p.gt1.upload(all1, ctx.stream);
+  p.gt2.upload(all2, ctx.stream);
+  p.gred.upload(allr, ctx.stream);
+  p.gtasks1.upload(tasks1, ctx.stream);
+  p.gpk2.upload(pairs2, ctx.stream);
+  p.group_budget = budget;
+}
+
+static void sigma_run_pk_whole(Context& ctx, SigmaPlan& p, double* sigma);
+static void sigma_groups_run(Context& ctx, SigmaPlan& p, double* sigma);
+
+// sigma += H psi over the w-groups through the plan's CUDA graph (captured on first
+// use, and again whenever a buffer it refers to has moved): the graph zeroes the
+// staged result and runs every group's launches; one axpy adds it to sigma.
+static void sigma_groups_graph(Context& ctx, SigmaPlan& p, double* sigma) {
+  const int64_t n = std::max<int64_t>(p.psi_layout.nnz, 1);
+  p.staged.ensure(size_t(n) * sizeof(double), ctx.stream);
+  p.group_scr.ensure(std::max<int64_t>(p.group_scr_bytes, 16), ctx.stream);
+  ctx.gemm_part.ensure(std::max<size_t>(size_t(p.group_slots) * kTcTileM * kTcTileN * sizeof(double), 16),
+                       ctx.stream);
+  int* err = device_err_flag(ctx);
+  const std::vector<const void*> ptrs = {p.pk_L.buf.p, p.pk_R.buf.p, p.pk_psi.buf.p, p.group_scr.p,
+                                         ctx.gemm_part.p,  p.staged.p,   err};
+  if (!p.graph || ptrs != p.graph_ptrs) {
+    p.drop_graph();
+    cudaGraph_t g = nullptr;
+    cuda_check(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
+    cuda_check(cudaMemsetAsync(p.staged.p, 0, size_t(n) * sizeof(double), ctx.stream), "staged zero");
+    sigma_groups_run(ctx, p, p.staged.as<double>());
+    cuda_check(cudaStreamEndCapture(ctx.stream, &g), "graph capture end");
+    cudaError_t e = cudaGraphInstantiate(&p.graph, g, 0);
+    cudaGraphDestroy(g);
+    cuda_check(e, "graph instantiate");
+    p.graph_ptrs = ptrs;
+  }
+  cuda_check(cudaGraphLaunch(p.graph, ctx.stream), "graph launch");
+  launch_axpy(sigma, p.staged.as<double>(), n, 1.0, ctx.stream);
+  ctx.kernel_launches += 1;
+}
+
+// sigma += H psi over the w-groups of the plan (packed operators and psi in place).
+static void sigma_groups_run(Context& ctx, SigmaPlan& p, double* sigma) {
+  p.group_scr.ensure(std::max<int64_t>(p.group_scr_bytes, 16), ctx.stream);
+  ctx.gemm_part.ensure(std::max<size_t>(size_t(p.group_slots) * kTcTileM * kTcTileN * sizeof(double), 16),
+                       ctx.stream);
+  double* part = ctx.gemm_part.as<double>();
+  int* err = device_err_flag(ctx);
+  for (const SigmaPlan::Group& G : p.groups) {
+    if (G.t1_count)
+      launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.group_scr.as<uint8_t>(),
+                     p.gt1.get() + G.t1_begin, G.t1_count, p.gtasks1.get(), p.pk1.get(), nullptr, 1, err,
+                     ctx.stream);
+    if (G.t2_count)
+      launch_gemm_pk(p.group_scr.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
+                     p.gt2.get() + G.t2_begin, G.t2_count, p.s2.dtasks.get(), p.gpk2.get(), part, 0, err,
+                     ctx.stream);
+    if (G.r_count)
+      launch_gemm_pk_reduce(p.gred.get() + G.r_begin, G.r_count, p.s2.dtasks.get(), 1.0, part, sigma, ctx.stream);
+    ctx.kernel_launches += (G.t1_count > 0) + (G.t2_count > 0) + (G.r_count > 0);
+  }
+}
+
+// Autotuner of the tensor-core schedule: times one H_eff*psi (psi already packed) into
+// a scratch result for a few stage-2 split-K granularities (and, for very large
+// intermediates, w blocking) and keeps the fastest.  Runs once per plan; plans are
+// kept across bonds and sweeps.
+static void tune_sigma_groups(Context& ctx, SigmaPlan& p) {
+  const int64_t n = std::max<int64_t>(p.psi_layout.nnz, 1);
+  DevBuf out;
+  out.ensure(size_t(n) * sizeof(double), ctx.stream);
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "tune event");
+  cuda_check(cudaEventCreate(&e1), "tune event");
+  const int64_t mb = int64_t(1) << 20;
+  // candidates: (w budget, stage-2 CTA target); budget 0 = all of w at once.  w
+  // blocking pays per-group pipeline fill and tail costs (measured 2x slower than one
+  // pass when the intermediate fits), so it is tried only when the whole-w
+  // intermediate is large enough to matter for memory.
+  std::vector<std::pair<int64_t, int>> cands = {{0, 152 * 4}, {0, 152 * 8}, {0, 152 * 16}};
+  if (p.pk_scr1.bytes > (int64_t(8) << 30)) cands.push_back({128 * mb, 152 * 8});
+  std::pair<int64_t, int> best = cands[0];
+  float best_ms = 0.0f;
+  ctx.last_tuning.clear();
+  for (const auto& cand : cands) {
+    const int64_t b = cand.first;
+    if (b > 0) {
+      build_sigma_groups(ctx, p, b);
+      p.drop_graph();
+      if (p.groups.size() < 2) continue;  // no blocking at this budget
+    } else {
+      tile_tc(p.s2, cand.second);
+      p.s2.tiles_tc.upload(p.s2.h_tiles_tc, ctx.stream);
+      p.s2.reduce_tc.upload(p.s2.h_reduce_tc, ctx.stream);
+    }
+    float ms = 0.0f;
+    for (int rep = 0; rep < 2; ++rep) {
+      cuda_check(cudaMemsetAsync(out.p, 0, size_t(n) * sizeof(double), ctx.stream), "tune zero");
+      cuda_check(cudaEventRecord(e0, ctx.stream), "tune record");
+      if (b > 0)
+        sigma_groups_graph(ctx, p, out.as<double>());
+      else
+        sigma_run_pk_whole(ctx, p, out.as<double>());
+      cuda_check(cudaEventRecord(e1, ctx.stream), "tune record");
+      cuda_check(cudaEventSynchronize(e1), "tune sync");
+      cuda_check(cudaEventElapsedTime(&ms, e0, e1), "tune time");
+    }
+    ctx.last_tuning.push_back(double(b));
+    ctx.last_tuning.push_back(double(cand.second));
+    ctx.last_tuning.push_back(ms);
+    if (best_ms == 0.0f || ms < best_ms) {
+      best = cand;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  p.drop_graph();
+  if (best.first > 0) {
+    build_sigma_groups(ctx, p, best.first);
+    p.pk_scr1.buf.release();
+  } else {
+    p.groups.clear();
+    tile_tc(p.s2, best.second);
+    p.s2.tiles_tc.upload(p.s2.h_tiles_tc, ctx.stream);
+    p.s2.reduce_tc.upload(p.s2.h_reduce_tc, ctx.stream);
+  }
+  p.group_budget = best.first;
+  p.tuned_ms = best_ms;
+}
+
 static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi,
                          double* sigma) {
   {
     PhaseTimer tm(ctx, kPhSigmaPlan);
     if (!p.pk_built) build_sigma_pk(ctx, p, L, R, p.psi_layout);
     // packed buffers are handed back between bonds; the plan itself is kept
-    for (Packed* P : {&p.pk_L, &p.pk_R, &p.pk_psi, &p.pk_scr1})
+    for (Packed* P : {&p.pk_L, &p.pk_R, &p.pk_psi})
       P->buf.ensure(std::max<int64_t>(P->bytes, 16), ctx.stream);
+    // the whole-w intermediate is only needed when w is not blocked (or while tuning)
+    if (p.group_budget <= 0) p.pk_scr1.buf.ensure(std::max<int64_t>(p.pk_scr1.bytes, 16), ctx.stream);
     // operators are packed once per (layout, data version)
     if (p.pk_L.src_layout != L.layout_id || p.pk_L.src_version != L.data_version) pack_into(ctx, p.pk_L, L);
     if (p.pk_R.src_layout != R.layout_id || p.pk_R.src_version != R.data_version) pack_into(ctx, p.pk_R, R);
@@ -667,6 +948,17 @@ static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTe
   }
   launch_pack(p.pk_psi.packs.get(), static_cast<int>(p.pk_psi.h_packs.size()), psi, p.pk_psi.buf.as<uint8_t>(),
               ctx.stream);
+  if (p.group_budget < 0) tune_sigma_groups(ctx, p);
+  if (p.group_budget > 0) {
+    sigma_groups_graph(ctx, p, sigma);
+    ctx.kernel_launches += 1;
+    return;
+  }
+  sigma_run_pk_whole(ctx, p, sigma);
+}
+
+// Both stages over all of w at once (the packed L*psi intermediate in HBM).
+static void sigma_run_pk_whole(Context& ctx, SigmaPlan& p, double* sigma) {
   int* err = device_err_flag(ctx);
   launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.pk_scr1.buf.as<uint8_t>(),
                  p.s1.tiles_tc.get(), static_cast<int>(p.s1.h_tiles_tc.size()), p.pk_tasks1.get(), p.pk1.get(),
@@ -1953,12 +2245,16 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
 // converged sweep repeats the layouts of the previous one); the large packed
 // operand buffers go back to the block cache after every bond.
 void release_bond_buffers(Context& ctx) {
-  for (auto& kv : ctx.sigma_plans)
+  for (auto& kv : ctx.sigma_plans) {
     for (Packed* P : {&kv.second->pk_L, &kv.second->pk_R, &kv.second->pk_psi, &kv.second->pk_scr1}) {
       P->buf.release();
       P->src_layout = 0;
       P->src_version = ~0ull;
     }
+    kv.second->group_scr.release();
+    kv.second->staged.release();
+    kv.second->drop_graph();
+  }
   if (ctx.sigma_plans.size() > kMaxCachedPlans) ctx.sigma_plans.clear();
   if (ctx.diag_plans.size() > kMaxCachedPlans) ctx.diag_plans.clear();
   if (ctx.merge_plans.size() > kMaxCachedPlans) ctx.merge_plans.clear();

@@ -134,6 +134,36 @@ struct SigmaPlan {
   std::vector<DGemmTask> h_pk_tasks1;
   DevArray<DPkPair> pk1, pk2;
   DevArray<DGemmTask> pk_tasks1;
+  // w-blocked execution: the MPO index w is cut into groups whose packed L*psi
+  // intermediates fit a scratch of group_budget bytes; each group runs stage 1 then
+  // stage 2 out of that scratch, which stays in L2 instead of going to HBM and back
+  struct Group {
+    int t1_begin = 0, t1_count = 0;  // stage-1 tiles (gt1)
+    int t2_begin = 0, t2_count = 0;  // stage-2 tiles (gt2)
+    int r_begin = 0, r_count = 0;    // split-K reductions (gred)
+    int nslots = 0;
+  };
+  int64_t group_budget = -1;  // < 0: not tuned yet; 0: one pass over all of w (no groups)
+  std::vector<Group> groups;
+  int64_t group_scr_bytes = 0;
+  int group_slots = 0;
+  DevArray<DTile> gt1, gt2;
+  DevArray<DGemmTask> gtasks1;  // stage-1 tasks with group-local packed output bases
+  DevArray<DPkPair> gpk2;       // stage-2 pairs with group-local L*psi bases
+  DevArray<DReduce> gred;
+  DevBuf group_scr;
+  double tuned_ms = 0.0;        // sigma time of the chosen budget when it was tuned
+  // the grouped launch sequence captured as one CUDA graph, writing into `staged`;
+  // valid while the buffers it was captured with stay where they are
+  cudaGraphExec_t graph = nullptr;
+  DevBuf staged;
+  std::vector<const void*> graph_ptrs;
+  void drop_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    graph_ptrs.clear();
+  }
+  ~SigmaPlan() { drop_graph(); }
 };
 
 // Merged-operator scatter plan (result layout + destination/source records).
@@ -236,6 +266,8 @@ struct Context {
   // each phase closing with a stream synchronisation
   bool profile = false;
   double timers[kNumPhases] = {};
+  // last autotuning of a sigma plan: (scratch budget in bytes, milliseconds) pairs
+  std::vector<double> last_tuning;
 
   explicit Context(int dev, cudaStream_t st);
   ~Context();

@@ -54,6 +54,15 @@ struct DDiagPair {
   int64_t l_off, r_off;
 };
 
+// Davidson subspace size: multi-dot and rotation kernels handle up to 10 vectors
+constexpr int kMaxDot = 10;
+
+// One problem of the batched Davidson: its slice of the vector arena.
+struct DBatchProb {
+  int64_t off, n;
+};
+constexpr int kBatchBlocks = 16;  // blocks per problem in the batched reductions
+
 constexpr int kGemmTile = 64;
 // tensor-core (split TF32) tile: 128 rows x 64 columns
 constexpr int kTcTileM = 128;
@@ -102,6 +111,21 @@ void launch_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, 
 // the k leading ones in descending order: out (row-major d x k, or its transpose
 // k x d when transposed != 0), xcm (column-major d x k) and s_j = sqrt(w) with
 // eigenvalues under 64 eps * w_max set to zero.
+// Batched Davidson level-1 operations over problems[0..nprob) (see kernels_batch.cu
+// for the slot layout); nmax = the largest problem size; partial holds
+// nprob * kBatchBlocks * 100 doubles.
+void launch_bcopy(const DBatchProb* probs, int nprob, int64_t nmax, double* A, int from, int to, cudaStream_t st);
+void launch_bzero(const DBatchProb* probs, int nprob, int64_t nmax, double* A, int slot, cudaStream_t st);
+void launch_bmultidot(const DBatchProb* probs, int nprob, const double* A, int m, double* partial, double* out,
+                      cudaStream_t st);
+void launch_brotate(const DBatchProb* probs, int nprob, int64_t nmax, double* A, int m, const double* R,
+                    cudaStream_t st);
+void launch_bresidual(const DBatchProb* probs, int nprob, double* A, const double* eval, double* partial,
+                      double* rnorm, cudaStream_t st);
+void launch_bprecondition(const DBatchProb* probs, int nprob, int64_t nmax, double* A, const double* eval,
+                          cudaStream_t st);
+void launch_bproject(const DBatchProb* probs, int nprob, int64_t nmax, double* A, int t, double* partial,
+                     double* sums, cudaStream_t st);
 void launch_eig_factors(const double* G, const double* w, int d, int k, int transposed, double* out, double* xcm,
                         double* s, cudaStream_t st);
 void launch_adjoint_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* Y,

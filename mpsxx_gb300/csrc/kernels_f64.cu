@@ -256,7 +256,6 @@ __global__ void copy_vec_kernel(double* y, const double* x, int64_t n) {
     y[i] = x[i];
 }
 
-constexpr int kMaxDot = 10;
 
 // Each CTA reduces a contiguous chunk into partial[blk][i*ny+j]; a fixed-order
 // second pass makes the sum deterministic.
