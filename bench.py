@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--gradient", action="store_true",
                     help="also run the energy-gradient workloads (site-dependent Hubbard L=32 M=512, QC n=16 M=256)")
     ap.add_argument("--grad-fd", type=int, default=2, help="parameters checked by central differences per workload")
+    ap.add_argument("--scan", action="store_true",
+                    help="also run the batched scan: 64 Hubbard chains, L ~ U{16..32}, U ~ U(0,8), M 64->256 over 6 sweeps")
+    ap.add_argument("--scan-chains", type=int, default=64)
+    ap.add_argument("--scan-compare", type=int, default=8, help="chains also swept one by one for comparison")
     ap.add_argument("--warm-sweeps", type=int, default=3,
                     help="sweeps in each precision from the FP64-converged state")
     ap.add_argument("--sweep-split-all", action="store_true",
@@ -296,6 +300,40 @@ def gradient_bench(args, device: int):
         del st, mpo
         ctx.close()
     return out
+
+
+def scan_bench(args, device: int):
+    """Batched parameter scan: all chains' bond steps in lockstep (one grouped tensor-core
+    H_eff*psi launch per stage for all unconverged chains), split precision with the
+    FP64 refinement; a subset of the chains is also swept one by one for timing and
+    energy comparison."""
+    from mpsxx_gb300 import core, scan
+
+    specs = scan.random_specs(args.scan_chains, args.seed)
+    sched = scan.m_schedule(64, 256, 6)
+    ctx = core.Context(device)
+    core.set_precision(ctx, core.SPLIT_TF32)
+    chains = scan.make_chains(ctx, specs, sched[0])
+    rows = []
+    for M in sched:
+        r = scan.sweep_batched(ctx, chains, M, args.tole)
+        rows.append({"M": M, "seconds": r["seconds"], "n_sigma": r["n_sigma"], "bond_steps": r["bond_steps"]})
+    t_batched = sum(r["seconds"] for r in rows)
+    k = min(args.scan_compare, len(specs))
+    single = scan.make_chains(ctx, specs[:k], sched[0])
+    t_single = 0.0
+    for M in sched:
+        t_single += scan.sweep_sequential(ctx, single, M, args.tole)["seconds"]
+    de = [abs(a.energies[-1] - b.energies[-1]) for a, b in zip(chains[:k], single)]
+    ctx.close()
+    per_chain_batched = t_batched / len(specs)
+    per_chain_single = t_single / k
+    return {"chains": len(specs), "lengths": [s[0] for s in specs], "M_schedule": sched, "tole": args.tole,
+            "precision": "split", "per_sweep": rows, "seconds_batched_all": t_batched,
+            "seconds_per_chain_batched": per_chain_batched, "compared_chains": k,
+            "seconds_per_chain_one_by_one": per_chain_single, "speedup_per_chain": per_chain_single / per_chain_batched,
+            "abs_dE_max_vs_one_by_one": max(de),
+            "final_energies": [c.energies[-1] for c in chains]}
 
 
 def warm_compare(args, ctx, st):
@@ -545,6 +583,7 @@ def main():
     bond = bond_compare(ctx, wl, args.M, args.tole) if args.bond_step else None
     sweep = sweep_compare(args, local) if not args.no_sweep else None
     grad = gradient_bench(args, local) if args.gradient else None
+    scan_res = scan_bench(args, local) if args.scan else None
     out = None
     if rank == 0:
         achieved = fl_per_step / kt["sigma_kernels_s"] / 1e12
@@ -584,6 +623,7 @@ def main():
             "bond_step": bond,
             "sweeps": sweep,
             "gradient": grad,
+            "scan": scan_res,
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline:

@@ -175,6 +175,21 @@ int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_t
                                   double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
                                   mpsxx_tensor** new_rwfn, double* stats);
 
+/* optimize_twosite_merged for n independent bonds at once (e.g. the chains of a
+ * parameter scan), arrays of n entries each.  The Davidson iterations of all bonds
+ * run in lockstep: in split precision every H_eff*psi of the unconverged bonds is
+ * one grouped tensor-core launch per stage (captured with its packing as a CUDA
+ * graph) and the vector algebra is one batched launch per operation; the results
+ * equal n separate mpsxx_optimize_twosite_merged calls up to rounding.  stats:
+ * 6 doubles per bond (n_sigma, n_sigma_fp64, micro iterations, converged,
+ * |r|^2, energy before refinement). */
+int mpsxx_optimize_twosite_merged_batch(mpsxx_context* ctx, int n, const int* forward,
+                                        const mpsxx_tensor* const* lmpo, const mpsxx_tensor* const* rmpo,
+                                        const mpsxx_tensor* const* lopr, const mpsxx_tensor* const* ropr,
+                                        const mpsxx_tensor* const* lwfn, const mpsxx_tensor* const* rwfn, double tole,
+                                        const int* M, double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
+                                        mpsxx_tensor** new_rwfn, double* stats);
+
 /* Adjoint of the bond energy with respect to the MPO: for the normalised merged
  * two-site wavefunction psi[A,B] of the bond between lmpo and rmpo,
  * E = <psi| H_eff |psi>, and grad_l[b] = dE/d(block b of lmpo), grad_r likewise

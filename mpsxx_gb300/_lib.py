@@ -28,6 +28,9 @@ SIGNATURES = {
     "mpsxx_context_tuning": (C.c_int, [vp, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_mpo_gradient": (C.c_int, [vp, vp, vp, vp, vp, vp, c_dbl_p, c_dbl_p]),
     "mpsxx_merge_rows": (C.c_int, [vp, vp, vpp]),
+    "mpsxx_optimize_twosite_merged_batch": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), vpp, vpp, vpp, vpp, vpp, vpp,
+                                                      C.c_double, C.POINTER(C.c_int), c_dbl_p, vpp, vpp, vpp,
+                                                      c_dbl_p]),
     "mpsxx_expand_rows": (C.c_int, [vp, vp, vp, vpp]),
     "mpsxx_context_profile": (C.c_int, [vp, C.c_int, C.c_int, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_context_set_precision": (C.c_int, [vp, C.c_int]),

@@ -296,6 +296,31 @@ def gemm(ctx: Context, transa: int, transb: int, alpha: float, a: Tensor, b: Ten
     return Tensor(o, ctx)
 
 
+BATCH_STAT_KEYS = ("n_sigma", "n_sigma_fp64", "micro", "converged", "rnorm", "energy_split")
+
+
+def optimize_twosite_merged_batch(ctx: Context, forward, lmpo, rmpo, lopr, ropr, lwfn, rwfn, tole: float, M):
+    """optimize_twosite_merged for n independent bonds at once (lists of n entries;
+    forward and M may be scalars).  Returns (energies, envs, new_lwfns, new_rwfns, stats)."""
+    n = len(lmpo)
+    fw = [int(bool(forward))] * n if isinstance(forward, (bool, int)) else [int(bool(f)) for f in forward]
+    Ms = [int(M)] * n if isinstance(M, int) else [int(m) for m in M]
+
+    def handles(ts):
+        return (C.c_void_p * n)(*[t.h.value if isinstance(t.h, C.c_void_p) else t.h for t in ts])
+
+    e = np.zeros(n)
+    st = np.zeros(6 * max(n, 1))
+    env, nl, nr = (C.c_void_p * n)(), (C.c_void_p * n)(), (C.c_void_p * n)()
+    dp = C.POINTER(C.c_double)
+    check(lib().mpsxx_optimize_twosite_merged_batch(
+        ctx.h, n, (C.c_int * n)(*fw), handles(lmpo), handles(rmpo), handles(lopr), handles(ropr), handles(lwfn),
+        handles(rwfn), float(tole), (C.c_int * n)(*Ms), e.ctypes.data_as(dp), env, nl, nr, st.ctypes.data_as(dp)))
+    wrap = lambda arr: [Tensor(C.c_void_p(arr[i]), ctx) for i in range(n)]  # noqa: E731
+    stats = [dict(zip(BATCH_STAT_KEYS, st[6 * i:6 * i + 6])) for i in range(n)]
+    return e, wrap(env), wrap(nl), wrap(nr), stats
+
+
 def mpo_gradient(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor, psi: Tensor):
     """dE/dW for both site MPOs of a bond, E = <psi|H_eff|psi> (psi normalised,
     merged two-site form); arrays in the MPOs' block order."""

@@ -433,6 +433,49 @@ int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_t
   });
 }
 
+int mpsxx_optimize_twosite_merged_batch(mpsxx_context* ctx, int n, const int* forward,
+                                        const mpsxx_tensor* const* lmpo, const mpsxx_tensor* const* rmpo,
+                                        const mpsxx_tensor* const* lopr, const mpsxx_tensor* const* ropr,
+                                        const mpsxx_tensor* const* lwfn, const mpsxx_tensor* const* rwfn, double tole,
+                                        const int* M, double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
+                                        mpsxx_tensor** new_rwfn, double* stats) {
+  return guard([&] {
+    need(n >= 0, "negative batch size");
+    need(n == 0 || (forward && lmpo && rmpo && lopr && ropr && lwfn && rwfn && M && energy && env && new_lwfn &&
+                    new_rwfn),
+         "null argument");
+    Context& c = ctx_of(ctx);
+    std::vector<BondArgs> args(n);
+    for (int i = 0; i < n; ++i) {
+      args[i].forward = forward[i] != 0;
+      args[i].lmpo = &ten(lmpo[i]);
+      args[i].rmpo = &ten(rmpo[i]);
+      args[i].lopr = &ten(lopr[i]);
+      args[i].ropr = &ten(ropr[i]);
+      args[i].lwfn = &ten(lwfn[i]);
+      args[i].rwfn = &ten(rwfn[i]);
+      args[i].M = M[i];
+    }
+    std::vector<BondOut> out = optimize_twosite_merged_batch(c, args, tole);
+    for (int i = 0; i < n; ++i) {
+      energy[i] = out[i].stats.energy;
+      env[i] = wrap(std::move(out[i].env), ctx);
+      new_lwfn[i] = wrap(std::move(out[i].lwfn), ctx);
+      new_rwfn[i] = wrap(std::move(out[i].rwfn), ctx);
+      if (stats) {
+        const DavidsonStats& d = out[i].stats.dav;
+        double* s = stats + 6 * i;
+        s[0] = d.n_sigma;
+        s[1] = d.n_sigma_fp64;
+        s[2] = d.micro;
+        s[3] = d.converged;
+        s[4] = d.rnorm;
+        s[5] = d.energy_split;
+      }
+    }
+  });
+}
+
 int mpsxx_mpo_gradient(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
                        const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* psi, double* grad_l,
                        double* grad_r) {

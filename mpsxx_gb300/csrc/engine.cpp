@@ -182,6 +182,10 @@ void DevArray<T>::upload(const std::vector<T>& h, cudaStream_t st) {
   if (n) cuda_check(cudaMemcpyAsync(buf.p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice, st), "plan upload");
 }
 template struct DevArray<DTile>;
+template struct DevArray<DPkPair>;
+template struct DevArray<DPack>;
+template struct DevArray<DReduce>;
+template struct DevArray<DBatchProb>;
 template struct DevArray<DGemmTask>;
 template struct DevArray<DGemmPair>;
 template struct DevArray<DDiagTask>;
@@ -600,10 +604,6 @@ static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Te
   p.pk_L.packs.upload(p.pk_L.h_packs, ctx.stream);
   p.pk_R.packs.upload(p.pk_R.h_packs, ctx.stream);
   p.pk_psi.packs.upload(p.pk_psi.h_packs, ctx.stream);
-  p.pk_L.buf.ensure(std::max<int64_t>(p.pk_L.bytes, 16), ctx.stream);
-  p.pk_R.buf.ensure(std::max<int64_t>(p.pk_R.bytes, 16), ctx.stream);
-  p.pk_psi.buf.ensure(std::max<int64_t>(p.pk_psi.bytes, 16), ctx.stream);
-  p.pk_scr1.buf.ensure(std::max<int64_t>(p.pk_scr1.bytes, 16), ctx.stream);
   p.pk_built = true;
 }
 
@@ -990,6 +990,15 @@ static void sigma_run(Context& ctx, SigmaPlan& p, const DTensor& L, const DTenso
   }
   ctx.sigma_flops += p.flops;
   ctx.sigma_calls += 1;
+}
+
+void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R) {
+  if (!p.pk_built) build_sigma_pk(ctx, p, L, R, p.psi_layout);
+}
+
+void apply_sigma(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi, double* sigma,
+                 int precision) {
+  sigma_run(ctx, p, L, R, psi, sigma, precision);
 }
 
 // Device error flag of the tensor-core kernels (zeroed on first use).

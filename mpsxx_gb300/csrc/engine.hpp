@@ -287,6 +287,12 @@ struct PhaseTimer {
   ~PhaseTimer() { stop(); }
 };
 
+// Packed-operand layouts of a sigma plan (built once), and one H_eff*psi of the plan
+// in the given precision (sigma += H psi) — the building blocks of batched steps.
+void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R);
+void apply_sigma(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi, double* sigma,
+                 int precision);
+
 // Adjoint of compute_merged_operator: dE/dW for the MPO blocks given
 // Y = dE/d(merged operator); and both site gradients of one bond's energy.
 std::vector<double> mpo_gradient(Context& ctx, bool forward, const DTensor& mpo, const DTensor& opr,
@@ -370,5 +376,21 @@ struct BondOut {
 BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo, const DTensor& rmpo,
                                 const DTensor& lopr, const DTensor& ropr, const DTensor& lwfn,
                                 const DTensor& rwfn, double tole, int M);
+
+// --- batched steps over independent problems (batch.cpp) --------------------
+// Lowest eigenpairs of independent effective Hamiltonians, Davidson in lockstep with
+// one grouped tensor-core H_eff*psi launch (split precision) for all of them.
+std::vector<double> diagonalize_batch(Context& ctx, const std::vector<const DTensor*>& L,
+                                      const std::vector<const DTensor*>& R, const std::vector<const DTensor*>& diag,
+                                      const std::vector<DTensor*>& psi, double tol, std::vector<DavidsonStats>& stats);
+struct BondArgs {
+  bool forward = true;
+  const DTensor *lmpo = nullptr, *rmpo = nullptr, *lopr = nullptr, *ropr = nullptr, *lwfn = nullptr,
+                *rwfn = nullptr;
+  int M = 0;
+};
+// optimize_twosite_merged for every bond of `args` (independent problems), their
+// Davidson iterations batched.
+std::vector<BondOut> optimize_twosite_merged_batch(Context& ctx, const std::vector<BondArgs>& args, double tole);
 
 }  // namespace mpsxx

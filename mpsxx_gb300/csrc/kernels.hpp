@@ -124,7 +124,8 @@ void launch_bresidual(const DBatchProb* probs, int nprob, double* A, const doubl
                       double* rnorm, cudaStream_t st);
 void launch_bprecondition(const DBatchProb* probs, int nprob, int64_t nmax, double* A, const double* eval,
                           cudaStream_t st);
-void launch_bproject(const DBatchProb* probs, int nprob, int64_t nmax, double* A, int t, double* partial,
+// r = slot rs: r <- (r/|r| - (trial_t . r/|r|) trial_t), or r <- r/|r| when t < 0
+void launch_bproject(const DBatchProb* probs, int nprob, int64_t nmax, double* A, int rs, int t, double* partial,
                      double* sums, cudaStream_t st);
 void launch_eig_factors(const double* G, const double* w, int d, int k, int transposed, double* out, double* xcm,
                         double* s, cudaStream_t st);

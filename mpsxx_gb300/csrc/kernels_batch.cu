@@ -148,12 +148,12 @@ __global__ void bprecondition_kernel(const DBatchProb* __restrict__ probs, doubl
   }
 }
 
-// partial sums of |r|^2 and (when t >= 0) trial_t . r
-__global__ void bnorm_dot_kernel(const DBatchProb* __restrict__ probs, const double* __restrict__ A, int t,
+// partial sums of |r|^2 and (when t >= 0) trial_t . r, r = slot rs
+__global__ void bnorm_dot_kernel(const DBatchProb* __restrict__ probs, const double* __restrict__ A, int rs, int t,
                                  double* __restrict__ partial) {
   __shared__ double red[kBt / 32][2];
   const DBatchProb p = probs[blockIdx.y];
-  const double* r = A + p.off + 20 * p.n;
+  const double* r = A + p.off + (int64_t)rs * p.n;
   const double* v = t >= 0 ? A + p.off + (int64_t)t * p.n : nullptr;
   const int64_t chunk = (p.n + gridDim.x - 1) / gridDim.x;
   const int64_t lo = blockIdx.x * chunk, hi = min(lo + chunk, p.n);
@@ -192,12 +192,13 @@ __global__ void bsum_kernel(const double* __restrict__ partial, int nblk, int np
 }
 
 // r <- (r - d * trial_t) / |r| with (|r|^2, d) from s[2c]; t < 0: r <- r / |r|
-__global__ void bproject_kernel(const DBatchProb* __restrict__ probs, double* A, int t, const double* __restrict__ s) {
+__global__ void bproject_kernel(const DBatchProb* __restrict__ probs, double* A, int rs, int t,
+                                const double* __restrict__ s) {
   const DBatchProb p = probs[blockIdx.y];
   const double nrm = sqrt(s[2 * blockIdx.y]);
   const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
   const double d = s[2 * blockIdx.y + 1] * inv;  // trial_t . (r / |r|)
-  double* r = A + p.off + 20 * p.n;
+  double* r = A + p.off + (int64_t)rs * p.n;
   const double* v = t >= 0 ? A + p.off + (int64_t)t * p.n : nullptr;
   for (int64_t i = blockIdx.x * (int64_t)kBt + threadIdx.x; i < p.n; i += (int64_t)gridDim.x * kBt) {
     const double x = r[i] * inv;
@@ -245,12 +246,12 @@ void launch_bprecondition(const DBatchProb* probs, int nprob, int64_t nmax, doub
   bprecondition_kernel<<<dim3(grid_x(nmax), nprob), kBt, 0, st>>>(probs, A, eval);
 }
 
-void launch_bproject(const DBatchProb* probs, int nprob, int64_t nmax, double* A, int t, double* partial,
+void launch_bproject(const DBatchProb* probs, int nprob, int64_t nmax, double* A, int rs, int t, double* partial,
                      double* sums, cudaStream_t st) {
   if (nprob <= 0) return;
-  bnorm_dot_kernel<<<dim3(kBatchBlocks, nprob), kBt, 0, st>>>(probs, A, t, partial);
+  bnorm_dot_kernel<<<dim3(kBatchBlocks, nprob), kBt, 0, st>>>(probs, A, rs, t, partial);
   bsum_pairs_kernel<<<(nprob + 127) / 128, 128, 0, st>>>(partial, kBatchBlocks, nprob, sums);
-  bproject_kernel<<<dim3(grid_x(nmax), nprob), kBt, 0, st>>>(probs, A, t, sums);
+  bproject_kernel<<<dim3(grid_x(nmax), nprob), kBt, 0, st>>>(probs, A, rs, t, sums);
 }
 
 }  // namespace mpsxx
