@@ -28,6 +28,11 @@ sys.path.insert(0, ROOT)
 
 L2_BYTES = 129 * 1024 * 1024
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per H_eff*psi of the default
+# workload (QC n=20, K=40, seed 1, M=512, bond (9,10)), summed over the launches of one
+# step, from one ncu capture of the launch list (one pass); None for other workloads.
+MEASURED_TRAFFIC = {("split", 20, 40, 1, 512): 10.06e9, }
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -590,8 +595,12 @@ def main():
         if args.precision == "split":
             # TF32 dense rate = half the measured BF16 rate; 3 products per FP64-equivalent product
             tf32 = peaks["bf16_tflops"] / 2.0
+            traffic = MEASURED_TRAFFIC.get((args.precision, args.norb, args.nchol, args.seed, args.M))
             roof = {"bound": "tensor", "achieved": achieved, "peak": tf32 / 3.0, "unit": "TFLOP/s",
-                    "frac": achieved / (tf32 / 3.0), "traffic": None,
+                    "frac": achieved / (tf32 / 3.0), "traffic": traffic,
+                    "traffic_note": "DRAM bytes per H_eff*psi (all launches of the step) from ncu; algorithmic "
+                                    "bytes are hbm_algorithmic_bytes" if traffic else None,
+                    "hbm_algorithmic_bytes": bytes_alg,
                     "peak_source": f"{src} bf16_tflops/2 (TF32 dense) /3 (3-product split), FP64-equivalent"}
         else:
             roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
