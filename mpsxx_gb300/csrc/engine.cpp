@@ -1942,6 +1942,11 @@ constexpr double kTieRtolDefault = 1.0e-10;
 constexpr int kSvdLanes = 8;
 // smallest min(m, n) of a block that takes the reduced-density-matrix route
 constexpr int kEighMin = 96;
+// largest min(m, n) of a block given to the Jacobi kernel: its cost grows as
+// min(m,n)^2 max(m,n) per sweep on the FP64 pipe of one SM, which on this GPU is
+// ~8 GFLOP/s; measured on the 64-chain scan, limits of 64 and 128 columns made the
+// canonicalize phase 2.7x slower than the solver lanes, so only tiny blocks go there
+constexpr int kJacobiUseCols = 24;
 
 CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise) {
   if (noise >= 1.0e-8) throw Error(kInvalidArgument, "canonicalize: noise injection is not supported");
@@ -1955,6 +1960,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     int64_t u_off, s_off, v_off;  // inside svd_mats
     bool eigh = false;            // density-matrix route: U (forward) or V (backward) from eigh,
                                   // the other factor stored already multiplied by s
+    bool jacobi = false;          // batched one-sided Jacobi kernel (small blocks)
   };
   std::vector<Blk> blks;
   int64_t nsv = 0;  // singular values first (one contiguous read-back), then U and V^T
@@ -1985,13 +1991,25 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   ctx.svd_mats.ensure(size_t(tot) * sizeof(double), ctx.stream);
   double* mats = ctx.svd_mats.as<double>();
   int* infos = reinterpret_cast<int*>(mats + info_off);
-  // Blocks with min(m, n) >= kEighMin take the reduced-density-matrix route: the
-  // eigenvectors of A A^T (forward) or A^T A (backward) give the kept factor, the
-  // other one is a projection of A (cuSOLVER's gesvd is latency-bound at these
-  // sizes); smaller blocks take gesvd.
+  // Blocks whose working copy fits in shared memory go to one launch of the batched
+  // Jacobi SVD kernel.  Of the rest, blocks with min(m, n) >= kEighMin take the
+  // reduced-density-matrix route: the eigenvectors of A A^T (forward) or A^T A
+  // (backward) give the kept factor, the other one is a projection of A (cuSOLVER's
+  // gesvd is latency-bound at these sizes); the others take gesvd.
   int lwork = 0;
   int64_t max_gram = 1;
+  std::vector<DSvdBlock> jac;
+  size_t jac_smem = 0;
+  for (size_t bi = 0; bi < blks.size(); ++bi) {
+    Blk& x = blks[bi];
+    if (x.k <= kJacobiUseCols && jacobi_svd_smem(x.m, x.n) <= kJacobiMaxSmem) {
+      x.jacobi = true;
+      jac.push_back(DSvdBlock{wfnc.offsets[x.slot], x.u_off, x.s_off, x.v_off, x.m, x.n, static_cast<int>(bi), 0});
+      jac_smem = std::max(jac_smem, jacobi_svd_smem(x.m, x.n));
+    }
+  }
   for (auto& x : blks) {
+    if (x.jacobi) continue;
     int lw = 0;
     x.eigh = x.k >= kEighMin;
     if (x.eigh) {
@@ -2008,13 +2026,14 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   }
   // per lane: solver work | rwork | col-major copy of A | col-major U | col-major V^T | Gram + eigenvalues
   const size_t lane_doubles = size_t(lwork) + 8 + 4 * size_t(std::max<int64_t>(maxmn, 1)) + 8 + size_t(max_gram);
-  std::vector<int> by_cost(blks.size());
-  std::iota(by_cost.begin(), by_cost.end(), 0);
+  std::vector<int> by_cost;
+  for (size_t bi = 0; bi < blks.size(); ++bi)
+    if (!blks[bi].jacobi) by_cost.push_back(static_cast<int>(bi));
   std::stable_sort(by_cost.begin(), by_cost.end(), [&](int p, int q) {
     return double(blks[p].m) * blks[p].n * blks[p].k > double(blks[q].m) * blks[q].n * blks[q].k;
   });
   const int hw = std::max(1, static_cast<int>(std::thread::hardware_concurrency()));
-  const int nlanes = std::max(1, std::min({kSvdLanes, hw, static_cast<int>(blks.size())}));
+  const int nlanes = std::min({kSvdLanes, hw, static_cast<int>(by_cost.size())});
   while (static_cast<int>(ctx.svd_lanes.size()) < nlanes) {
     auto l = std::make_unique<Context::SvdLane>();
     cuda_check(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking), "svd lane stream");
@@ -2028,6 +2047,13 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   }
   if (!ctx.svd_ready) cuda_check(cudaEventCreateWithFlags(&ctx.svd_ready, cudaEventDisableTiming), "svd event");
   cuda_check(cudaEventRecord(ctx.svd_ready, st), "svd ready");
+  // the small blocks on the context's stream, concurrently with the lanes
+  DevArray<DSvdBlock> djac;
+  if (!jac.empty()) {
+    djac.upload(jac, st);
+    launch_jacobi_svd(djac.get(), static_cast<int>(jac.size()), jac_smem, wfnc.d, mats, infos, st);
+    ctx.kernel_launches += 1;
+  }
   std::atomic<int> next{0};
   std::vector<std::exception_ptr> errs(nlanes);
   std::vector<int64_t> lane_launches(nlanes, 0);
@@ -2043,7 +2069,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
       double* tA = rwork + std::max<int64_t>(maxmn, 1);  // col-major working copy of the block
       double* tU = tA + maxmn;                           // col-major U when transposes are needed
       double* tV = tU + maxmn;                           // col-major VT when transposes are needed
-      for (int i = next.fetch_add(1); i < static_cast<int>(blks.size()); i = next.fetch_add(1)) {
+      for (int i = next.fetch_add(1); i < static_cast<int>(by_cost.size()); i = next.fetch_add(1)) {
         const Blk& x = blks[by_cost[i]];
         const double* a = wfnc.d + wfnc.offsets[x.slot];
         double* U = mats + x.u_off;
@@ -2101,7 +2127,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   {
     std::vector<std::thread> pool;
     for (int li = 1; li < nlanes; ++li) pool.emplace_back(lane_fn, li);
-    lane_fn(0);
+    if (nlanes > 0) lane_fn(0);
     for (auto& t : pool) t.join();
   }
   for (int li = 0; li < nlanes; ++li) {
@@ -2117,7 +2143,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     const int* hinfo = reinterpret_cast<const int*>(hmats.data() + info_off);
     for (size_t b = 0; b < blks.size(); ++b)
       if (hinfo[b] != 0)
-        throw Error(kSolver, "canonicalize: gesvd did not converge (info " + std::to_string(hinfo[b]) + ")");
+        throw Error(kSolver, "canonicalize: block SVD did not converge (info " + std::to_string(hinfo[b]) + ")");
   }
   tsolve.stop();
   PhaseTimer tselect(ctx, kPhSvdSelect);

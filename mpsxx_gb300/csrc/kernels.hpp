@@ -29,6 +29,15 @@ struct DReduce {
   int task, tm, tn, slot0, nslot, pad;
 };
 
+// One block of a batched Jacobi SVD: row-major m x n at src_off; outputs U (row-major
+// m x k), s (k) and V^T (row-major k x n), k = min(m, n), descending s.
+struct DSvdBlock {
+  int64_t src_off, u_off, s_off, v_off;
+  int m, n, info_slot, pad;
+};
+constexpr int kJacobiMaxCols = 128;                  // min(m, n) limit of the Jacobi kernel
+constexpr size_t kJacobiMaxSmem = 200 * 1024;        // its shared-memory limit per block
+
 // Dense 2-D block copy: dst[r*dld + c] (+)= scale * src[r*sld + c].
 struct DCopy {
   int64_t dst_off, src_off;
@@ -104,13 +113,6 @@ void launch_copy(const DCopy* tasks, int ntasks, const double* src, double* dst,
                  cudaStream_t st);
 void launch_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* src, double* dst,
                     cudaStream_t st);
-// Adjoint of launch_scatter: for every source record s of destination d,
-// g[s] = sum_{r,c} Y[d.dst_off + r*d.dld + c] * src[s.src_off + r*s.sld + c]
-// (destinations with dst_off < 0 are skipped and leave their g untouched).
-// Eigenvectors G (d x d, column-major, eigenvalues w ascending) of a Gram matrix ->
-// the k leading ones in descending order: out (row-major d x k, or its transpose
-// k x d when transposed != 0), xcm (column-major d x k) and s_j = sqrt(w) with
-// eigenvalues under 64 eps * w_max set to zero.
 // Batched Davidson level-1 operations over problems[0..nprob) (see kernels_batch.cu
 // for the slot layout); nmax = the largest problem size; partial holds
 // nprob * kBatchBlocks * 100 doubles.
@@ -127,8 +129,20 @@ void launch_bprecondition(const DBatchProb* probs, int nprob, int64_t nmax, doub
 // r = slot rs: r <- (r/|r| - (trial_t . r/|r|) trial_t), or r <- r/|r| when t < 0
 void launch_bproject(const DBatchProb* probs, int nprob, int64_t nmax, double* A, int rs, int t, double* partial,
                      double* sums, cudaStream_t st);
+// Batched one-sided Jacobi SVD (kernels_svd.cu); smem_bytes >= jacobi_svd_smem of
+// every block; info[info_slot] = 1 when a block did not converge.
+size_t jacobi_svd_smem(int m, int n);
+void launch_jacobi_svd(const DSvdBlock* blocks, int nblocks, size_t smem_bytes, const double* src, double* out,
+                       int* info, cudaStream_t st);
+// Eigenvectors G (d x d, column-major, eigenvalues w ascending) of a Gram matrix ->
+// the k leading ones in descending order: out (row-major d x k, or its transpose
+// k x d when transposed != 0), xcm (column-major d x k) and s_j = sqrt(w) with
+// eigenvalues under 64 eps * w_max set to zero.
 void launch_eig_factors(const double* G, const double* w, int d, int k, int transposed, double* out, double* xcm,
                         double* s, cudaStream_t st);
+// Adjoint of launch_scatter: for every source record s of destination d,
+// g[s] = sum_{r,c} Y[d.dst_off + r*d.dld + c] * src[s.src_off + r*s.sld + c]
+// (destinations with dst_off < 0 are skipped and leave their g untouched).
 void launch_adjoint_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc* srcs, const double* Y,
                             const double* src, double* g, cudaStream_t st);
 // G[e] = sum_{k = ptr[e]}^{ptr[e+1]-1} g[idx[k]], summed in index order.
