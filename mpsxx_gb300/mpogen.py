@@ -494,6 +494,31 @@ def synthetic_qc_integrals(n: int, K: int, seed: int):
     return h, eri
 
 
+def write_fcidump(path: str, h1: np.ndarray, eri: np.ndarray, nelec: int, ms2: int = 0, ecore: float = 0.0,
+                  tol: float = 0.0):
+    """FCIDUMP writer: the unique 8-fold entries (i >= j, k >= l, ij >= kl, 1-based),
+    one-electron entries with k = l = 0 and the core energy on the 0 0 0 0 line."""
+    n = h1.shape[0]
+    lines = [f" &FCI NORB={n},NELEC={nelec},MS2={ms2},", "  ORBSYM=" + "1," * n, "  ISYM=1,", " &END"]
+    for i in range(n):
+        for j in range(i + 1):
+            ij = i * (i + 1) // 2 + j
+            for k in range(n):
+                for l in range(k + 1):
+                    if k * (k + 1) // 2 + l > ij:
+                        continue
+                    v = eri[i, j, k, l]
+                    if abs(v) > tol:
+                        lines.append(f"{v:28.20e} {i + 1:4d} {j + 1:4d} {k + 1:4d} {l + 1:4d}")
+    for i in range(n):
+        for j in range(i + 1):
+            if abs(h1[i, j]) > tol:
+                lines.append(f"{h1[i, j]:28.20e} {i + 1:4d} {j + 1:4d} {0:4d} {0:4d}")
+    lines.append(f"{ecore:28.20e} {0:4d} {0:4d} {0:4d} {0:4d}")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
 def read_fcidump(path: str):
     """FCIDUMP reader: unique integrals unfolded with 8-fold symmetry, core energy from
     the 0 0 0 0 line (same convention as src/parsing_integral.cpp:105-154)."""
