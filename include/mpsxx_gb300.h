@@ -157,6 +157,21 @@ int mpsxx_compute_merged_operator(mpsxx_context* ctx, int forward, const mpsxx_t
 int mpsxx_diagonalize(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                       const mpsxx_tensor* diag, mpsxx_tensor* wfnc, double tol, double* energy, int* stats);
 
+/* diagonalize with lower roots projected out (state-specific multi-root targeting,
+ * the projected Functor of src/diagonalize.hpp:200-277): for every lower root j, S[j]
+ * is its wavefunction and H[j] its H_eff product expressed in this bond's basis
+ * (tensors with wfnc's block layout), E[j] its energy; the operator applied is
+ * H c - S_j <H_j|c> - H_j <S_j|c> + E_j S_j <S_j|c>, and the start vector and the
+ * result are orthogonalised against the S_j (at most 12 roots). */
+int mpsxx_diagonalize_projected(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                                const mpsxx_tensor* diag, mpsxx_tensor* wfnc, double tol, int nproj,
+                                const mpsxx_tensor* const* S, const mpsxx_tensor* const* H, const double* E,
+                                double* energy, int* stats);
+
+/* y += alpha x for tensors of the same sectors; every block of x must be stored in y
+ * (btas::Axpy over the blocks of x, include/btas/SPARSE/STBLAS.h). */
+int mpsxx_tensor_accumulate(mpsxx_context* ctx, double alpha, const mpsxx_tensor* x, mpsxx_tensor* y);
+
 /* Truncated SVD of a merged wavefunction; forward: lmat = U, rmat = s V^T;
  * backward: lmat = U s, rmat = V^T.  Replaces mpsxx::canonicalize(forward, wfnc,
  * lmat, rmat, M, noise) (src/canonicalize.hpp:88-106).  noise must be < 1e-8. */

@@ -28,6 +28,9 @@ SIGNATURES = {
     "mpsxx_context_tuning": (C.c_int, [vp, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_mpo_gradient": (C.c_int, [vp, vp, vp, vp, vp, vp, c_dbl_p, c_dbl_p]),
     "mpsxx_merge_rows": (C.c_int, [vp, vp, vpp]),
+    "mpsxx_diagonalize_projected": (C.c_int, [vp, vp, vp, vp, vp, C.c_double, C.c_int, vpp, vpp, c_dbl_p, c_dbl_p,
+                                              C.POINTER(C.c_int)]),
+    "mpsxx_tensor_accumulate": (C.c_int, [vp, C.c_double, vp, vp]),
     "mpsxx_optimize_twosite_merged_batch": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), vpp, vpp, vpp, vpp, vpp, vpp,
                                                       C.c_double, C.POINTER(C.c_int), c_dbl_p, vpp, vpp, vpp,
                                                       c_dbl_p]),

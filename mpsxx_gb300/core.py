@@ -284,6 +284,24 @@ def diagonalize(ctx: Context, lopr: Tensor, ropr: Tensor, diag: Tensor, wfnc: Te
     return e.value, {"n_sigma": st[0], "macro": st[1], "micro": st[2], "converged": st[3]}
 
 
+def diagonalize_projected(ctx: Context, lopr: Tensor, ropr: Tensor, diag: Tensor, wfnc: Tensor, tol: float,
+                          S: Sequence[Tensor], H: Sequence[Tensor], E: Sequence[float]):
+    """diagonalize with the lower roots (S_j, H_j, E_j) projected out."""
+    n = len(S)
+    e = C.c_double()
+    st = (C.c_int * 4)()
+    hs = lambda ts: (C.c_void_p * max(n, 1))(*[t.h.value if isinstance(t.h, C.c_void_p) else t.h for t in ts])  # noqa: E731
+    ev = (C.c_double * max(n, 1))(*E)
+    check(lib().mpsxx_diagonalize_projected(ctx.h, lopr.h, ropr.h, diag.h, wfnc.h, float(tol), n, hs(S), hs(H), ev,
+                                            C.byref(e), st))
+    return e.value, {"n_sigma": st[0], "macro": st[1], "micro": st[2], "converged": st[3]}
+
+
+def accumulate(ctx: Context, alpha: float, x: Tensor, y: Tensor):
+    """y += alpha x (x's blocks must be stored in y)."""
+    check(lib().mpsxx_tensor_accumulate(ctx.h, float(alpha), x.h, y.h))
+
+
 def canonicalize(ctx: Context, forward: bool, wfnc: Tensor, M: int = 0, noise: float = 0.0):
     lo, ro = _out(), _out()
     check(lib().mpsxx_canonicalize(ctx.h, int(bool(forward)), wfnc.h, int(M), float(noise), C.byref(lo), C.byref(ro)))

@@ -389,6 +389,72 @@ int mpsxx_diagonalize(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_
   });
 }
 
+int mpsxx_diagonalize_projected(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                                const mpsxx_tensor* diag, mpsxx_tensor* wfnc, double tol, int nproj,
+                                const mpsxx_tensor* const* S, const mpsxx_tensor* const* H, const double* E,
+                                double* energy, int* stats) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    need(nproj >= 0 && (nproj == 0 || (S && H && E)), "bad projection arguments");
+    const DTensor& w = ten_mut(wfnc);
+    Projection proj;
+    for (int j = 0; j < nproj; ++j) {
+      const DTensor& s = ten(S[j]);
+      const DTensor& h = ten(H[j]);
+      need(s.layout_id == w.layout_id && h.layout_id == w.layout_id,
+           "projected roots must have the wavefunction's block layout");
+      need_device(s);
+      need_device(h);
+      proj.S.push_back(s.d);
+      proj.H.push_back(h.d);
+      proj.E.push_back(E[j]);
+    }
+    c.projection = &proj;
+    DavidsonStats st;
+    double e = 0.0;
+    try {
+      e = diagonalize(c, ten(lopr), ten(ropr), ten(diag), ten_mut(wfnc), tol, &st);
+    } catch (...) {
+      c.projection = nullptr;
+      throw;
+    }
+    c.projection = nullptr;
+    if (energy) *energy = e;
+    if (stats) {
+      stats[0] = st.n_sigma;
+      stats[1] = st.macro;
+      stats[2] = st.micro;
+      stats[3] = st.converged;
+    }
+  });
+}
+
+int mpsxx_tensor_accumulate(mpsxx_context* ctx, double alpha, const mpsxx_tensor* x, mpsxx_tensor* y) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    const DTensor& X = ten(x);
+    DTensor& Y = ten_mut(y);
+    need(X.sh.rank == Y.sh.rank && X.sh.q == Y.sh.q, "accumulate: tensors of different shapes");
+    for (int i = 0; i < X.sh.rank; ++i)
+      need(X.sh.qshape[i] == Y.sh.qshape[i] && X.sh.dshape[i] == Y.sh.dshape[i],
+           "accumulate: tensors of different sectors");
+    need_device(X);
+    need_device(Y);
+    std::vector<DCopy> cp;
+    for (size_t b = 0; b < X.tags.size(); ++b) {
+      const int32_t s = Y.find(X.tags[b]);
+      need(s >= 0, "accumulate: a block of x is not stored in y");
+      const int64_t sz = X.block_size(static_cast<int32_t>(b));
+      if (sz > 0) cp.push_back(DCopy{Y.offsets[s], X.offsets[b], 1, static_cast<int>(sz), 0, 0, alpha});
+    }
+    DevArray<DCopy> dc;
+    dc.upload(cp, c.stream);
+    launch_copy(dc.get(), static_cast<int>(cp.size()), X.d, Y.d, 1, c.stream);
+    c.kernel_launches += 1;
+    c.sync();
+  });
+}
+
 int mpsxx_canonicalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* wfnc, int M, double noise,
                        mpsxx_tensor** lmat, mpsxx_tensor** rmat) {
   return guard([&] {

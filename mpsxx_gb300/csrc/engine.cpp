@@ -1788,10 +1788,28 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
   ctx.partial.ensure(size_t(nblk) * 100 * sizeof(double), ctx.stream);
   ctx.scalars.ensure(256 * sizeof(double), ctx.stream);
   double* part = ctx.partial.as<double>();
-  double* sc = ctx.scalars.as<double>();  // [0..99] dots, [100] norm, [101] dot, [128..227] rvec
+  double* sc = ctx.scalars.as<double>();  // [0..99] dots, [100] norm, [101] dot, [128..227] rvec, [230..] roots
   double* rvec_d = sc + 128;
 
   PhaseTimer trest(ctx, kPhDavidsonRest);
+  // Lower roots (multi-root, src/diagonalize.hpp:200-277): with s_j = <S_j|c> and
+  // h_j = <H_j|c>, H' c = H c - S_j h_j - H_j s_j + E_j S_j s_j for every projected
+  // root j, S_j / H_j being root j's wavefunction / H_eff times it in this basis.
+  const Projection* proj = ctx.projection;
+  if (proj && proj->S.size() > kMaxProjected) throw Error(kInvalidArgument, "diagonalize: too many lower roots");
+  std::vector<double> pdots;
+  auto project_dots = [&](const double* c) {
+    const size_t np = proj->S.size();
+    pdots.assign(2 * np, 0.0);
+    for (size_t j = 0; j < np; ++j) {
+      launch_multidot(proj->S[j], 1, c, 1, n, n, sc + 230 + 2 * j, part, nblk, st);
+      launch_multidot(proj->H[j], 1, c, 1, n, n, sc + 231 + 2 * j, part, nblk, st);
+      ctx.kernel_launches += 4;
+    }
+    cuda_check(cudaMemcpyAsync(pdots.data(), sc + 230, 2 * np * sizeof(double), cudaMemcpyDeviceToHost, st),
+               "projection d2h");
+    ctx.sync();
+  };
   auto sigma_of = [&](int k, int precision) {
     PhaseTimer tm(ctx, kPhSigma);
     cuda_check(cudaMemsetAsync(sigma + k * n, 0, n * sizeof(double), st), "sigma zero");
@@ -1800,6 +1818,22 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
     if (precision == kFP64) S.n_sigma_fp64 += 1;
     tm.stop();
     ctx.timers[kPhDavidsonRest] -= tm.dt;  // H_eff * psi is not part of the rest
+    if (proj && !proj->S.empty()) {
+      project_dots(trial + k * n);
+      for (size_t j = 0; j < proj->S.size(); ++j) {
+        const double s = pdots[2 * j], h = pdots[2 * j + 1];
+        launch_axpy(sigma + k * n, proj->S[j], n, -h + proj->E[j] * s, st);
+        launch_axpy(sigma + k * n, proj->H[j], n, -s, st);
+        ctx.kernel_launches += 2;
+      }
+    }
+  };
+  // c <- c - sum_j <S_j|c> S_j (before normalisation)
+  auto orthogonalize_roots = [&](double* c) {
+    if (!proj || proj->S.empty()) return;
+    project_dots(c);
+    for (size_t j = 0; j < proj->S.size(); ++j) launch_axpy(c, proj->S[j], n, -pdots[2 * j], st);
+    ctx.kernel_launches += static_cast<int64_t>(proj->S.size());
   };
   auto normalize = [&](double* x) {
     launch_multidot(x, 1, x, 1, n, n, sc + 100, part, nblk, st);
@@ -1808,6 +1842,7 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
   };
 
   launch_copy_vec(trial, wfnc.d, n, st);
+  orthogonalize_roots(trial);
   double eval = 0.0;
   int niter = 0, iconv = 0;
   std::vector<double> hdots(100), heff, rvec, rval;
@@ -1866,6 +1901,7 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
   S.macro += niter;
   S.converged = iconv;
   launch_copy_vec(wfnc.d, trial, n, st);
+  orthogonalize_roots(wfnc.d);  // multH.orthonormalize (src/diagonalize.hpp:446)
   normalize(wfnc.d);
   ctx.sync();
   return eval;

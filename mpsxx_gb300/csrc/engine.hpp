@@ -46,6 +46,14 @@ struct DevArray {
 
 struct Context;
 
+// Lower roots projected out of the Davidson operator (multi-root targeting): device
+// vectors in the wavefunction's layout and the roots' energies (at most 12).
+constexpr size_t kMaxProjected = 12;
+struct Projection {
+  std::vector<const double*> S, H;
+  std::vector<double> E;
+};
+
 // Device tensor: host layout descriptor + device storage (+ optional host data).
 struct DTensor : Tensor {
   Context* ctx = nullptr;
@@ -251,6 +259,7 @@ struct Context {
   std::vector<std::unique_ptr<SvdLane>> svd_lanes;
   cudaEvent_t svd_ready = nullptr;
   int precision = kFP64;
+  const Projection* projection = nullptr;  // set around a projected diagonalize
   // truncation: singular values within this relative window of the cutoff count as
   // equal to it and are kept together; < 0 selects the default (1e-10)
   double tie_rtol = -1.0;

@@ -427,3 +427,141 @@ def restart_state(ctx: Context, mpo: List[Tensor], st: DeviceState) -> DeviceSta
         renv[k - 1] = _right_env_step(ctx, new, renv[k], k)
     lenv[0] = _boundary(ctx)
     return new
+
+
+# ---------------------------------------------------------------------------
+# multiple roots: state-specific targeting with the lower roots projected out
+# ---------------------------------------------------------------------------
+def identity_mpo(ctx: Context, N: int) -> List[Tensor]:
+    """MPO of the identity (bond dimension 1): the overlap block operators of two
+    states are block operators of this MPO."""
+    from .mpogen import SiteMPO, _op_matrix
+
+    out = []
+    for _ in range(N):
+        W = SiteMPO([(0, 0)], [(0, 0)])
+        W.add(0, _op_matrix("I"), 0)
+        out.append(Tensor.from_dict(ctx, W.to_dict()))
+    return out
+
+
+@dataclass
+class LowerRoot:
+    """A converged lower root and its block operators against the state being
+    optimised (bra = current state, ket = this root): Hamiltonian (Lx, Rx) and
+    overlap (Lo, Ro).  Its own orthogonality centre follows the current bond."""
+    st: DeviceState
+    energy: float
+    Lx: List[Optional[Tensor]]
+    Rx: List[Optional[Tensor]]
+    Lo: List[Optional[Tensor]]
+    Ro: List[Optional[Tensor]]
+
+
+def _cross_sigma(ctx: Context, mL: Tensor, mR: Tensor, psi_k: Tensor, like: Tensor) -> Tensor:
+    """mL psi_k mR^T: a lower root's wavefunction carried into this bond's basis,
+    stored in `like`'s layout."""
+    scr = core.gemm(ctx, 0, 0, 1.0, mL, psi_k, 3)
+    out = core.gemm(ctx, 0, 1, 1.0, scr, mR, 2)
+    t = like.like()
+    core.accumulate(ctx, 1.0, out, t)
+    return t
+
+
+def _two_site(ctx: Context, a: Tensor, b: Tensor) -> Tensor:
+    return core.gemm(ctx, 0, 0, 1.0, core.merge_rows(ctx, a), core.merge_cols(ctx, b), 2)
+
+
+def make_lower_root(ctx: Context, st: DeviceState, root: DeviceState, energy: float,
+                    idm: List[Tensor]) -> LowerRoot:
+    """Cross block operators of a lower root against state `st`, both centred at site 0."""
+    N = len(st.mpo)
+    Lx, Rx, Lo, Ro = [None] * N, [None] * N, [None] * N, [None] * N
+    Lx[0], Lo[0], Rx[N - 1], Ro[N - 1] = _boundary(ctx), _boundary(ctx), _boundary(ctx), _boundary(ctx)
+    for i in range(N - 1, 0, -1):
+        vc = core.merge_cols(ctx, st.wave[i])
+        vk = core.merge_cols(ctx, root.wave[i])
+        Rx[i - 1] = core.renormalize(ctx, False, core.compute_merged_operator(ctx, False, st.mpo[i], Rx[i]), vc, vk)
+        Ro[i - 1] = core.renormalize(ctx, False, core.compute_merged_operator(ctx, False, idm[i], Ro[i]), vc, vk)
+    return LowerRoot(DeviceState(root.mpo, list(root.wave), [None] * N, [None] * N, root.M), energy, Lx, Rx, Lo, Ro)
+
+
+def optimize_twosite_projected(ctx: Context, forward: bool, st: DeviceState, i: int, tole: float,
+                               lowers: List[LowerRoot], idm: List[Tensor]) -> float:
+    """One two-site step at bond (i, i+1) (forward) or (i-1, i) (backward) with the lower
+    roots projected out (src/optimize.hpp:495-651 with the Functor<2> of
+    src/diagonalize.hpp:200-277); the lower roots' centres and cross operators move on."""
+    j = i if forward else i - 1  # left site of the bond
+    mL = core.compute_merged_operator(ctx, True, st.mpo[j], st.lenv[j])
+    mR = core.compute_merged_operator(ctx, False, st.mpo[j + 1], st.renv[j + 1])
+    psi = core.merge_wavefunction(ctx, st.mpo[j], st.mpo[j + 1], st.lenv[j], st.renv[j + 1], st.wave[j],
+                                  st.wave[j + 1])
+    diag = psi.like()
+    core.compute_diagonal_elements(ctx, mL, mR, diag)
+    S, H, E, cross = [], [], [], []
+    for lr in lowers:
+        psi_k = _two_site(ctx, lr.st.wave[j], lr.st.wave[j + 1])
+        mLx = core.compute_merged_operator(ctx, True, st.mpo[j], lr.Lx[j])
+        mRx = core.compute_merged_operator(ctx, False, st.mpo[j + 1], lr.Rx[j + 1])
+        mLo = core.compute_merged_operator(ctx, True, idm[j], lr.Lo[j])
+        mRo = core.compute_merged_operator(ctx, False, idm[j + 1], lr.Ro[j + 1])
+        S.append(_cross_sigma(ctx, mLo, mRo, psi_k, psi))
+        H.append(_cross_sigma(ctx, mLx, mRx, psi_k, psi))
+        E.append(lr.energy)
+        cross.append((psi_k, mLx, mRx, mLo, mRo))
+    e, _ = core.diagonalize_projected(ctx, mL, mR, diag, psi, tole, S, H, E)
+    if forward:
+        U, sV = core.canonicalize(ctx, True, psi, st.M)
+        st.wave[j], st.wave[j + 1] = core.expand_wavefunction(ctx, st.mpo[j], st.mpo[j + 1], st.lenv[j],
+                                                              st.renv[j + 1], U, sV)
+        st.lenv[j + 1] = core.renormalize(ctx, True, mL, U, U)
+        for lr, (psi_k, mLx, _, mLo, _) in zip(lowers, cross):
+            Uk, sVk = core.canonicalize(ctx, True, psi_k, lr.st.M)
+            lr.st.wave[j] = core.expand_rows(ctx, Uk, lr.st.wave[j])
+            lr.st.wave[j + 1] = core.expand_cols(ctx, sVk, lr.st.wave[j + 1])
+            lr.Lx[j + 1] = core.renormalize(ctx, True, mLx, U, Uk)
+            lr.Lo[j + 1] = core.renormalize(ctx, True, mLo, U, Uk)
+    else:
+        Us, V = core.canonicalize(ctx, False, psi, st.M)
+        st.wave[j], st.wave[j + 1] = core.expand_wavefunction(ctx, st.mpo[j], st.mpo[j + 1], st.lenv[j],
+                                                              st.renv[j + 1], Us, V)
+        st.renv[j] = core.renormalize(ctx, False, mR, V, V)
+        for lr, (psi_k, _, mRx, _, mRo) in zip(lowers, cross):
+            Usk, Vk = core.canonicalize(ctx, False, psi_k, lr.st.M)
+            lr.st.wave[j + 1] = core.expand_cols(ctx, Vk, lr.st.wave[j + 1])
+            lr.st.wave[j] = core.expand_rows(ctx, Usk, lr.st.wave[j])
+            lr.Rx[j] = core.renormalize(ctx, False, mRx, V, Vk)
+            lr.Ro[j] = core.renormalize(ctx, False, mRo, V, Vk)
+    return e
+
+
+def dmrg_roots(ctx: Context, mpo_dicts: List[dict], n_elec: int, two_sz: int, M: int, tole: float, max_sweeps: int,
+               nroots: int, seed: int = 0, verbose: bool = False):
+    """State-specific DMRG for the lowest nroots states (src/dmrg.cpp:37-79 over iroot):
+    each root is swept to |dE| < tole with every lower root projected out of H_eff.
+    Returns the roots' energies and states."""
+    mpo = [Tensor.from_dict(ctx, d) for d in mpo_dicts]
+    N = len(mpo)
+    idm = identity_mpo(ctx, N)
+    energies: List[float] = []
+    states: List[DeviceState] = []
+    for r in range(nroots):
+        if r == 0:
+            st = make_initial_state(ctx, mpo, n_elec, two_sz, M)
+        else:
+            st = make_random_state(ctx, mpo, n_elec, two_sz, M, seed=seed + r)
+        lowers = [make_lower_root(ctx, st, states[k], energies[k], idm) for k in range(r)]
+        e_prev = 0.0
+        e_sweep = 0.0
+        for it in range(max_sweeps):
+            es = [optimize_twosite_projected(ctx, True, st, i, 0.1 * tole, lowers, idm) for i in range(N - 1)]
+            es += [optimize_twosite_projected(ctx, False, st, i, 0.1 * tole, lowers, idm) for i in range(N - 1, 0, -1)]
+            e_sweep = min(es)
+            if verbose:
+                print(f"root {r} sweep {it}: E = {e_sweep:.14f}", flush=True)
+            if it > 0 and abs(e_sweep - e_prev) < tole:
+                break
+            e_prev = e_sweep
+        energies.append(e_sweep)
+        states.append(st)
+    return energies, states
