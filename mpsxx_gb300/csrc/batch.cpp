@@ -467,11 +467,15 @@ std::vector<BondOut> optimize_twosite_merged_batch(Context& ctx, const std::vect
   }
   std::vector<DavidsonStats> st;
   const std::vector<double> E = diagonalize_batch(ctx, Lp, Rp, Dp, Pp, tole, st);
+  // all bonds' SVDs in one solve
+  std::vector<CanonJob> jobs(N);
+  for (size_t c = 0; c < N; ++c) jobs[c] = CanonJob{args[c].forward, psi[c].get(), args[c].M};
+  std::vector<CanonResult> canon = canonicalize_many(ctx, jobs);
   for (size_t c = 0; c < N; ++c) {
     const BondArgs& a = args[c];
     out[c].stats.energy = E[c];
     out[c].stats.dav = st[c];
-    CanonResult cr = canonicalize(ctx, a.forward, *psi[c], a.M, 0.0);
+    CanonResult& cr = canon[c];
     if (a.forward)
       out[c].env = renormalize(ctx, true, *mL[c], *cr.lmat, *cr.lmat);
     else

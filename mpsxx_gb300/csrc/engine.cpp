@@ -1984,13 +1984,14 @@ constexpr int kEighMin = 96;
 // canonicalize phase 2.7x slower than the solver lanes, so only tiny blocks go there
 constexpr int kJacobiUseCols = 24;
 
-CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise) {
-  if (noise >= 1.0e-8) throw Error(kInvalidArgument, "canonicalize: noise injection is not supported");
-  if (wfnc.sh.rank != 2) throw Error(kInvalidArgument, "canonicalize: expects a merged (2-index) wavefunction");
+std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<CanonJob>& jobs) {
+  for (const CanonJob& jb : jobs)
+    if (jb.wfnc->sh.rank != 2) throw Error(kInvalidArgument, "canonicalize: expects a merged (2-index) wavefunction");
   cudaStream_t st = ctx.stream;
   PhaseTimer tsolve(ctx, kPhSvdSolve);
-  const int ncols = wfnc.sh.nsec(1);
   struct Blk {
+    int job;
+    const double* a;  // the block's data
     int32_t slot;
     int i, j, m, n, k;
     int64_t u_off, s_off, v_off;  // inside svd_mats
@@ -2001,16 +2002,20 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   std::vector<Blk> blks;
   int64_t nsv = 0;  // singular values first (one contiguous read-back), then U and V^T
   int64_t maxmn = 0;
-  for (size_t b = 0; b < wfnc.tags.size(); ++b) {
-    const int i = static_cast<int>(wfnc.tags[b] / ncols), j = static_cast<int>(wfnc.tags[b] % ncols);
-    const int m = wfnc.sh.dshape[0][i], n = wfnc.sh.dshape[1][j];
-    if (m == 0 || n == 0) continue;
-    const int k = std::min(m, n);
-    Blk x{static_cast<int32_t>(b), i, j, m, n, k, 0, 0, 0};
-    x.s_off = nsv;
-    nsv += k;
-    maxmn = std::max<int64_t>(maxmn, int64_t(m) * n);
-    blks.push_back(x);
+  for (size_t jb = 0; jb < jobs.size(); ++jb) {
+    const DTensor& wfnc = *jobs[jb].wfnc;
+    const int ncols = wfnc.sh.nsec(1);
+    for (size_t b = 0; b < wfnc.tags.size(); ++b) {
+      const int i = static_cast<int>(wfnc.tags[b] / ncols), j = static_cast<int>(wfnc.tags[b] % ncols);
+      const int m = wfnc.sh.dshape[0][i], n = wfnc.sh.dshape[1][j];
+      if (m == 0 || n == 0) continue;
+      const int k = std::min(m, n);
+      Blk x{static_cast<int>(jb), wfnc.d + wfnc.offsets[b], static_cast<int32_t>(b), i, j, m, n, k, 0, 0, 0};
+      x.s_off = nsv;
+      nsv += k;
+      maxmn = std::max<int64_t>(maxmn, int64_t(m) * n);
+      blks.push_back(x);
+    }
   }
   // Device layout (doubles): singular values | gesvd info per block (two ints per
   // double) | U and V^T per block.  The head (values and infos) is read back.
@@ -2040,7 +2045,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     Blk& x = blks[bi];
     if (x.k <= kJacobiUseCols && jacobi_svd_smem(x.m, x.n) <= kJacobiMaxSmem) {
       x.jacobi = true;
-      jac.push_back(DSvdBlock{wfnc.offsets[x.slot], x.u_off, x.s_off, x.v_off, x.m, x.n, static_cast<int>(bi), 0});
+      jac.push_back(DSvdBlock{x.a, x.u_off, x.s_off, x.v_off, x.m, x.n, static_cast<int>(bi), 0});
       jac_smem = std::max(jac_smem, jacobi_svd_smem(x.m, x.n));
     }
   }
@@ -2049,7 +2054,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     int lw = 0;
     x.eigh = x.k >= kEighMin;
     if (x.eigh) {
-      const int d = forward ? x.m : x.n;
+      const int d = jobs[x.job].forward ? x.m : x.n;
       solver_check(cusolverDnDsyevd_bufferSize(ctx.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, d,
                                                nullptr, d, nullptr, &lw),
                    "syevd bufferSize");
@@ -2087,7 +2092,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   DevArray<DSvdBlock> djac;
   if (!jac.empty()) {
     djac.upload(jac, st);
-    launch_jacobi_svd(djac.get(), static_cast<int>(jac.size()), jac_smem, wfnc.d, mats, infos, st);
+    launch_jacobi_svd(djac.get(), static_cast<int>(jac.size()), jac_smem, mats, infos, st);
     ctx.kernel_launches += 1;
   }
   std::atomic<int> next{0};
@@ -2107,7 +2112,8 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
       double* tV = tU + maxmn;                           // col-major VT when transposes are needed
       for (int i = next.fetch_add(1); i < static_cast<int>(by_cost.size()); i = next.fetch_add(1)) {
         const Blk& x = blks[by_cost[i]];
-        const double* a = wfnc.d + wfnc.offsets[x.slot];
+        const bool forward = jobs[x.job].forward;
+        const double* a = x.a;
         double* U = mats + x.u_off;
         double* S = mats + x.s_off;
         double* V = mats + x.v_off;
@@ -2182,6 +2188,11 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
         throw Error(kSolver, "canonicalize: block SVD did not converge (info " + std::to_string(hinfo[b]) + ")");
   }
   tsolve.stop();
+  std::vector<CanonResult> results(jobs.size());
+  for (size_t jb = 0; jb < jobs.size(); ++jb) {
+  const bool forward = jobs[jb].forward;
+  const DTensor& wfnc = *jobs[jb].wfnc;
+  const int M = jobs[jb].M;
   PhaseTimer tselect(ctx, kPhSvdSelect);
   // sector of each block's singular values: row sector (LeftArrow) or column sector (RightArrow)
   std::map<int, size_t> sec_of;
@@ -2189,6 +2200,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   std::vector<int> secs;
   std::vector<int> blk_sv(blks.size());
   for (size_t b = 0; b < blks.size(); ++b) {
+    if (blks[b].job != static_cast<int>(jb)) continue;
     const int sec = forward ? blks[b].i : blks[b].j;
     if (sec_of.count(sec)) throw Error(kInternal, "canonicalize: two blocks share one singular-value sector");
     sec_of[sec] = b;
@@ -2199,7 +2211,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
     svals.emplace_back(hmats.begin() + x.s_off, hmats.begin() + x.s_off + x.k);
     blk_sv[kv.second] = static_cast<int>(svals.size() - 1);
   }
-  CanonResult res;
+  CanonResult& res = results[jb];
   const double tie = ctx.tie_rtol >= 0.0 ? ctx.tie_rtol : kTieRtolDefault;
   std::vector<int> kept = select_kept(svals, M, tie, &res.discarded);
   // new bond sectors in ascending sector order
@@ -2234,6 +2246,7 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   };
   std::vector<Pl> pl;
   for (size_t b = 0; b < blks.size(); ++b) {
+    if (blks[b].job != static_cast<int>(jb)) continue;
     const int sec = forward ? blks[b].i : blks[b].j;
     auto it = newidx.find(sec);
     if (it == newidx.end()) continue;
@@ -2305,7 +2318,14 @@ CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M,
   ctx.kernel_launches += 3;
   res.lmat = std::move(U);
   res.rmat = std::move(V);
-  return res;
+  }
+  return results;
+}
+
+CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise) {
+  if (noise >= 1.0e-8) throw Error(kInvalidArgument, "canonicalize: noise injection is not supported");
+  std::vector<CanonResult> r = canonicalize_many(ctx, {CanonJob{forward, &wfnc, M}});
+  return std::move(r[0]);
 }
 
 // ---------------------------------------------------------------------------

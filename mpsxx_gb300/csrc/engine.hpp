@@ -348,6 +348,14 @@ struct CanonResult {
   double discarded = 0.0;
 };
 CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise);
+// Several independent canonicalisations sharing one solve (one Jacobi launch and one
+// set of solver lanes for all their blocks, one read-back of the singular values).
+struct CanonJob {
+  bool forward;
+  const DTensor* wfnc;
+  int M;
+};
+std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<CanonJob>& jobs);
 
 // global top-M selection with a relative tie window (QSTLAPACK.h:204-232)
 std::vector<int> select_kept(const std::vector<std::vector<double>>& svals, int M, double tie_rtol,

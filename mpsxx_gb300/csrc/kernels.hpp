@@ -29,10 +29,12 @@ struct DReduce {
   int task, tm, tn, slot0, nslot, pad;
 };
 
-// One block of a batched Jacobi SVD: row-major m x n at src_off; outputs U (row-major
-// m x k), s (k) and V^T (row-major k x n), k = min(m, n), descending s.
+// One block of a batched Jacobi SVD: row-major m x n at src; outputs (offsets into the
+// output buffer) U (row-major m x k), s (k) and V^T (row-major k x n), k = min(m, n),
+// descending s.
 struct DSvdBlock {
-  int64_t src_off, u_off, s_off, v_off;
+  const double* src;
+  int64_t u_off, s_off, v_off;
   int m, n, info_slot, pad;
 };
 constexpr int kJacobiMaxCols = 128;                  // min(m, n) limit of the Jacobi kernel
@@ -132,8 +134,8 @@ void launch_bproject(const DBatchProb* probs, int nprob, int64_t nmax, double* A
 // Batched one-sided Jacobi SVD (kernels_svd.cu); smem_bytes >= jacobi_svd_smem of
 // every block; info[info_slot] = 1 when a block did not converge.
 size_t jacobi_svd_smem(int m, int n);
-void launch_jacobi_svd(const DSvdBlock* blocks, int nblocks, size_t smem_bytes, const double* src, double* out,
-                       int* info, cudaStream_t st);
+void launch_jacobi_svd(const DSvdBlock* blocks, int nblocks, size_t smem_bytes, double* out, int* info,
+                       cudaStream_t st);
 // Eigenvectors G (d x d, column-major, eigenvalues w ascending) of a Gram matrix ->
 // the k leading ones in descending order: out (row-major d x k, or its transpose
 // k x d when transposed != 0), xcm (column-major d x k) and s_j = sqrt(w) with

@@ -47,8 +47,7 @@ __device__ inline void pair_of(int k, int r, int n2, int* p, int* q) {
 }
 
 __global__ void __launch_bounds__(kJt) jacobi_svd_kernel(const DSvdBlock* __restrict__ blocks,
-                                                         const double* __restrict__ src, double* __restrict__ out,
-                                                         int* __restrict__ info) {
+                                                         double* __restrict__ out, int* __restrict__ info) {
   extern __shared__ double sm[];
   __shared__ int rotated;
   __shared__ int perm[kJacobiMaxCols];
@@ -60,7 +59,7 @@ __global__ void __launch_bounds__(kJt) jacobi_svd_kernel(const DSvdBlock* __rest
   const int cols = tr ? b.m : b.n;    // columns of W (<= rows)
   double* W = sm;                     // column-major rows x cols
   double* V = sm + (int64_t)rows * cols;  // column-major cols x cols
-  const double* A = src + b.src_off;  // row-major m x n
+  const double* A = b.src;            // row-major m x n
   for (int e = threadIdx.x; e < rows * cols; e += kJt) {
     const int i = e % rows, j = e / rows;
     W[e] = tr ? A[(int64_t)j * b.n + i] : A[(int64_t)i * b.n + j];
@@ -181,15 +180,15 @@ size_t jacobi_svd_smem(int m, int n) {
   return (size_t(rows) * cols + size_t(cols) * cols) * sizeof(double);
 }
 
-void launch_jacobi_svd(const DSvdBlock* blocks, int nblocks, size_t smem_bytes, const double* src, double* out,
-                       int* info, cudaStream_t st) {
+void launch_jacobi_svd(const DSvdBlock* blocks, int nblocks, size_t smem_bytes, double* out, int* info,
+                       cudaStream_t st) {
   if (nblocks <= 0) return;
   static size_t configured = 0;
   if (smem_bytes > configured) {
     cudaFuncSetAttribute(jacobi_svd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_bytes));
     configured = smem_bytes;
   }
-  jacobi_svd_kernel<<<nblocks, kJt, smem_bytes, st>>>(blocks, src, out, info);
+  jacobi_svd_kernel<<<nblocks, kJt, smem_bytes, st>>>(blocks, out, info);
 }
 
 }  // namespace mpsxx
