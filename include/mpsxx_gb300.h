@@ -94,6 +94,11 @@ int mpsxx_context_profile(mpsxx_context* ctx, int enable, int reset, double* t, 
  * tuning's (budget bytes, target tiles, milliseconds) triples are written to out (up
  * to n values); *count receives their number. */
 int mpsxx_context_tuning(const mpsxx_context* ctx, double* out, int n, int* count);
+/* Fix the split-precision H_eff*psi schedule instead of autotuning it: the MPO index w
+ * processed in groups whose packed L*psi intermediate fits w_budget_bytes (0 = all of
+ * w at once), stage-2 split-K sized for target_tiles tensor-core tiles (0 = default).
+ * w_budget_bytes < 0 restores autotuning.  Cached plans are dropped. */
+int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes, int target_tiles);
 
 /* ---- tensors ------------------------------------------------------------- */
 /* Create a block-sparse tensor.  qn holds 2*sum(nsec) ints (p, 2Sz per sector,

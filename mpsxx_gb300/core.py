@@ -45,6 +45,10 @@ class Context:
         """Relative tie window at the truncation cutoff (< 0: the precision's default)."""
         check(lib().mpsxx_context_set_truncation(self.h, float(tie_rtol)))
 
+    def set_sigma_schedule(self, w_budget_bytes: int = -1, target_tiles: int = 0):
+        """Fix the split H_eff*psi schedule (w scratch budget, tile target); budget < 0: autotune."""
+        check(lib().mpsxx_context_set_sigma_schedule(self.h, int(w_budget_bytes), int(target_tiles)))
+
     def tuning(self):
         """Last sigma autotuning: [(w scratch budget bytes, target tiles, milliseconds), ...]."""
         buf = (C.c_double * 64)()

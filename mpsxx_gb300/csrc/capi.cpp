@@ -144,6 +144,17 @@ int mpsxx_context_profile(mpsxx_context* ctx, int enable, int reset, double* t, 
   });
 }
 
+int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes, int target_tiles) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    need(target_tiles >= 0, "negative tile target");
+    Context& c = *ctx->ctx;
+    c.sigma_w_budget = w_budget_bytes;
+    c.sigma_target_tiles = target_tiles;
+    c.sigma_plans.clear();  // plans are rebuilt (and scheduled) on next use
+  });
+}
+
 int mpsxx_context_tuning(const mpsxx_context* ctx, double* out, int n, int* count) {
   return guard([&] {
     need(ctx && ctx->ctx, "null context");

@@ -948,7 +948,27 @@ static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTe
   }
   launch_pack(p.pk_psi.packs.get(), static_cast<int>(p.pk_psi.h_packs.size()), psi, p.pk_psi.buf.as<uint8_t>(),
               ctx.stream);
-  if (p.group_budget < 0) tune_sigma_groups(ctx, p);
+  if (p.group_budget < 0) {
+    if (ctx.sigma_w_budget < 0) {
+      tune_sigma_groups(ctx, p);
+    } else if (ctx.sigma_w_budget > 0) {
+      build_sigma_groups(ctx, p, ctx.sigma_w_budget);
+      if (p.groups.size() < 2) {  // the budget does not split w: one pass
+        p.groups.clear();
+        p.group_budget = 0;
+      } else {
+        p.group_budget = ctx.sigma_w_budget;
+        p.pk_scr1.buf.release();
+      }
+    } else {
+      if (ctx.sigma_target_tiles > 0) {
+        tile_tc(p.s2, ctx.sigma_target_tiles);
+        p.s2.tiles_tc.upload(p.s2.h_tiles_tc, ctx.stream);
+        p.s2.reduce_tc.upload(p.s2.h_reduce_tc, ctx.stream);
+      }
+      p.group_budget = 0;
+    }
+  }
   if (p.group_budget > 0) {
     sigma_groups_graph(ctx, p, sigma);
     ctx.kernel_launches += 1;

@@ -263,6 +263,11 @@ struct Context {
   // truncation: singular values within this relative window of the cutoff count as
   // equal to it and are kept together; < 0 selects the default (1e-10)
   double tie_rtol = -1.0;
+  // split-precision sigma schedule chosen by the caller instead of the autotuner:
+  // w scratch budget in bytes (0 = all of w at once) and stage-2 tile target; a
+  // negative budget leaves the choice to the autotuner
+  int64_t sigma_w_budget = -1;
+  int sigma_target_tiles = 0;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<SigmaPlan>> sigma_plans;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<DiagPlan>> diag_plans;
   std::map<std::tuple<int, uint64_t, uint64_t, uint64_t>, std::unique_ptr<MergePlan>> merge_plans;

@@ -10,8 +10,13 @@
 // |w_p . w_q| > tol * |w_p| |w_q|.  Sweeps visit all pairs in a round-robin
 // tournament order (n/2 disjoint pairs per round, one warp per pair) until a sweep
 // rotates nothing or kJacobiSweeps sweeps have run.  Then s_j = |w_j|, u_j = w_j / s_j,
-// and the triplets are sorted by decreasing s.  The schedule and every reduction
-// are fixed, so results do not depend on timing.
+// and the triplets are sorted by decreasing s.  Columns that end at or below the
+// numerical-zero level (|w_j|^2 <= (rows eps)^2 |A|_F^2) took no part in the
+// rotations and are not orthogonal to the others: like LAPACK's gesvd, their u_j are
+// replaced by an orthonormal completion (unit vectors e_0, e_1, ... orthogonalised
+// twice against the columns before them, the first with a remaining norm above 1/2),
+// so both factors are orthonormal whatever the rank; s_j keeps its (tiny) value.  The
+// schedule and every reduction are fixed, so results do not depend on timing.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -142,6 +147,45 @@ __global__ void __launch_bounds__(kJt) jacobi_svd_kernel(const DSvdBlock* __rest
     perm[rank] = j;
   }
   __syncthreads();
+  // normalise the columns; then complete the numerically-zero ones (sorted last) in
+  // place, one at a time, against the columns before them in the sorted order
+  for (int e = threadIdx.x; e < rows * cols; e += kJt) {
+    const int c = e / rows;
+    const double s = norm[c];
+    if (s * s > tiny && s > 0.0) W[e] /= s;
+  }
+  __syncthreads();
+  if (warp == 0) {  // serial over the columns, reductions within the warp
+    for (int j = 0; j < cols; ++j) {
+      const int c = perm[j];
+      const double s = norm[c];
+      if (s * s > tiny && s > 0.0) continue;
+      double* wc = W + (int64_t)c * rows;
+      for (int cand = 0; cand < rows; ++cand) {
+        for (int i = lane; i < rows; i += 32) wc[i] = (i == cand) ? 1.0 : 0.0;
+        __syncwarp();
+        for (int pass = 0; pass < 2; ++pass) {
+          for (int l = 0; l < j; ++l) {
+            const double* wl = W + (int64_t)perm[l] * rows;
+            double d = 0.0;
+            for (int i = lane; i < rows; i += 32) d = fma(wl[i], wc[i], d);
+            d = warp_sum(d);
+            for (int i = lane; i < rows; i += 32) wc[i] = fma(-d, wl[i], wc[i]);
+            __syncwarp();
+          }
+        }
+        double nn = 0.0;
+        for (int i = lane; i < rows; i += 32) nn = fma(wc[i], wc[i], nn);
+        nn = sqrt(warp_sum(nn));
+        if (nn > 0.5) {
+          for (int i = lane; i < rows; i += 32) wc[i] /= nn;
+          __syncwarp();
+          break;
+        }
+      }
+    }
+  }
+  __syncthreads();
   // outputs: U row-major m x k, s (k), V^T row-major k x n, k = cols
   double* U = out + b.u_off;
   double* S = out + b.s_off;
@@ -149,26 +193,24 @@ __global__ void __launch_bounds__(kJt) jacobi_svd_kernel(const DSvdBlock* __rest
   const int k = cols;
   for (int j = threadIdx.x; j < k; j += kJt) S[j] = norm[perm[j]];
   if (!tr) {
-    // A = W-basis: U_j = w_perm(j) / s_j (m = rows), V^T[j][c] = V[c][perm(j)]
+    // A = W-basis: U_j = w_perm(j) (normalised, m = rows), V^T[j][c] = V[c][perm(j)]
     for (int e = threadIdx.x; e < b.m * k; e += kJt) {
-      const int i = e / k, j = e % k, c = perm[j];
-      const double s = norm[c];
-      U[e] = s > 0.0 ? W[(int64_t)c * rows + i] / s : 0.0;
+      const int i = e / k, j = e % k;
+      U[e] = W[(int64_t)perm[j] * rows + i];
     }
     for (int e = threadIdx.x; e < k * b.n; e += kJt) {
       const int j = e / b.n, c = e % b.n;
       Vt[e] = V[(int64_t)perm[j] * cols + c];
     }
   } else {
-    // A^T = W-basis: A = V S (W/s)^T, so U = V (m = cols rows), V^T_j = w_perm(j) / s_j
+    // A^T = W-basis: A = V S W^T, so U = V (m = cols rows), V^T_j = w_perm(j) (normalised)
     for (int e = threadIdx.x; e < b.m * k; e += kJt) {
       const int i = e / k, j = e % k;
       U[e] = V[(int64_t)perm[j] * cols + i];
     }
     for (int e = threadIdx.x; e < k * b.n; e += kJt) {
-      const int j = e / b.n, c = e % b.n, col = perm[j];
-      const double s = norm[col];
-      Vt[e] = s > 0.0 ? W[(int64_t)col * rows + c] / s : 0.0;
+      const int j = e / b.n, c = e % b.n;
+      Vt[e] = W[(int64_t)perm[j] * rows + c];
     }
   }
 }

@@ -174,3 +174,36 @@ def test_dmrg_hubbard12_energies_match_oracle(ctx):
     assert all(d < 1e-8 for d in diffs[:2]), diffs
     assert all(d < 1e-10 for d in diffs[2:]), diffs
     assert log.energy >= gold["exact"] - 1e-10
+
+
+@pytest.mark.parametrize("forward", [True, False])
+def test_canonicalize_rank_deficient_blocks_stay_orthonormal(ctx, forward):
+    """Blocks of rank 1 (and all-zero blocks): the singular vectors of the numerically
+    zero singular values that the truncation keeps are completed to an orthonormal set,
+    as LAPACK's gesvd does, so the isometric factor is orthonormal block by block and
+    U s V^T reproduces the wavefunction.  Tolerance 1e-12."""
+    from oracle import qsd as oq
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    rng = np.random.default_rng(7)
+    psi = case["psi"].empty_like()
+    for n, (t, b) in enumerate(sorted(case["psi"].blocks.items())):
+        m, k = b.shape
+        blk = 1.0e3 * np.outer(rng.standard_normal(m), rng.standard_normal(k))
+        psi.blocks[t] = np.zeros_like(b) if n % 5 == 4 else blk
+    lm, rm = core.canonicalize(ctx, forward, dev(ctx, psi), 0)
+    iso = lm if forward else rm
+    checked = 0
+    for blk in iso.to_blocks().values():
+        g = blk.T @ blk if forward else blk @ blk.T
+        assert np.max(np.abs(g - np.eye(g.shape[0]))) < 1e-12
+        checked += g.shape[0] > 1
+    assert checked > 0
+    gl = oq.QSDArray(lm.q, *lm.shape())
+    gl.blocks = lm.to_blocks()
+    gr = oq.QSDArray(rm.q, *rm.shape())
+    gr.blocks = rm.to_blocks()
+    c = oq.QSDArray()
+    oq.gemm("N", "N", 1.0, gl, gr, 1.0, c, nc=2)
+    assert max_block_diff(psi.blocks, c.blocks) < 1e-12

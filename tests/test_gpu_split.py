@@ -162,3 +162,31 @@ def test_split_renormalize_matches_fp64_qc_bond(ctx):
         err = rel_err(out[core.SPLIT_TF32_ALL], out[core.FP64])
         print("renormalize forward" if forward else "renormalize backward", "split rel err", err)
         assert err < 2e-6
+
+
+@pytest.mark.parametrize("schedule", [(0, 152 * 4), (256 * 1024, 0), (4 * 1024 * 1024, 152 * 2)])
+def test_split_sigma_schedules_agree(ctx, schedule):
+    """Every schedule of the split H_eff*psi (one pass over w with different split-K
+    targets, and w processed in groups out of an L2-sized scratch, through the CUDA
+    graph) gives the same result as FP64 within 2e-6."""
+    from mpsxx_gb300 import core, dmrg, mpogen
+
+    h, eri = mpogen.synthetic_qc_integrals(8, 16, 5)
+    mpo = [core.Tensor.from_dict(ctx, d) for d in mpogen.qc_mpo(h, eri)]
+    st = dmrg.make_random_state(ctx, mpo, 8, 0, 128, seed=4)
+    dmrg.advance_left(ctx, st, 3)
+    mL, mR, psi = dmrg.bond_operands(ctx, st, 3)
+    ctx.set_sigma_schedule(*schedule)
+    try:
+        s64, s32 = sigma_both(ctx, mL, mR, psi)
+        # a second application reuses the plan (and its graph)
+        core.set_precision(ctx, core.SPLIT_TF32)
+        again = psi.like()
+        core.compute_sigma_vector(ctx, mL, mR, psi, again)
+        core.set_precision(ctx, core.FP64)
+    finally:
+        ctx.set_sigma_schedule(-1)
+    err = rel_err(s32, s64)
+    print("schedule", schedule, "split-vs-fp64 rel err", err)
+    assert err < 2e-6
+    assert np.array_equal(again.download(), s32)
