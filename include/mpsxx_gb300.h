@@ -99,6 +99,14 @@ int mpsxx_context_tuning(const mpsxx_context* ctx, double* out, int n, int* coun
  * w at once), stage-2 split-K sized for target_tiles tensor-core tiles (0 = default).
  * w_budget_bytes < 0 restores autotuning.  Cached plans are dropped. */
 int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes, int target_tiles);
+/* Routing of canonicalize's per-block SVDs: blocks with min(m, n) <= jacobi_max_cols
+ * (at most 128) go to the batched one-sided Jacobi kernel; of the rest, blocks whose
+ * Gram matrix (rows for a forward step, columns backward) has dimension <=
+ * gram_max_dim go to the batched symmetric eigensolver (one grouped launch sequence
+ * for all of them); the remaining blocks take cuSOLVER gesvd (min(m, n) < 96) or
+ * syevd on the Gram matrix, on concurrent solver lanes.  A negative value selects the
+ * default (24 and 256); 0 switches a route off. */
+int mpsxx_context_set_svd_routes(mpsxx_context* ctx, int jacobi_max_cols, int gram_max_dim);
 
 /* ---- tensors ------------------------------------------------------------- */
 /* Create a block-sparse tensor.  qn holds 2*sum(nsec) ints (p, 2Sz per sector,

@@ -49,6 +49,11 @@ class Context:
         """Fix the split H_eff*psi schedule (w scratch budget, tile target); budget < 0: autotune."""
         check(lib().mpsxx_context_set_sigma_schedule(self.h, int(w_budget_bytes), int(target_tiles)))
 
+    def set_svd_routes(self, jacobi_max_cols: int = -1, gram_max_dim: int = -1):
+        """Routing of canonicalize's block SVDs (batched Jacobi / batched eigensolver /
+        solver lanes); negative: defaults, 0: route off."""
+        check(lib().mpsxx_context_set_svd_routes(self.h, int(jacobi_max_cols), int(gram_max_dim)))
+
     def tuning(self):
         """Last sigma autotuning: [(w scratch budget bytes, target tiles, milliseconds), ...]."""
         buf = (C.c_double * 64)()

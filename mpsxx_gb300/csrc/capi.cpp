@@ -155,6 +155,14 @@ int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes,
   });
 }
 
+int mpsxx_context_set_svd_routes(mpsxx_context* ctx, int jacobi_max_cols, int gram_max_dim) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    ctx->ctx->svd_jacobi_cols = jacobi_max_cols;
+    ctx->ctx->svd_gram_max = gram_max_dim;
+  });
+}
+
 int mpsxx_context_tuning(const mpsxx_context* ctx, double* out, int n, int* count) {
   return guard([&] {
     need(ctx && ctx->ctx, "null context");

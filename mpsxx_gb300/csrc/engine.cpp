@@ -224,7 +224,8 @@ Context::~Context() {
   diag_plans.clear();
   merge_plans.clear();
   renorm_plans.clear();
-  for (DevBuf* b : {&scr1, &scr2, &work, &partial, &scalars, &svd_work, &svd_mats, &gemm_part, &err_flag})
+  for (DevBuf* b : {&scr1, &scr2, &work, &partial, &scalars, &svd_work, &svd_mats, &gemm_part, &err_flag,
+                    &svd_gram, &svd_gram_work, &svd_ptrs})
     b->release();
   for (auto& l : svd_lanes) {
     cudaStreamSynchronize(l->stream);
@@ -238,6 +239,8 @@ Context::~Context() {
   if (svd_ready) cudaEventDestroy(svd_ready);
   block_cache().unregister_stream(stream);
   if (solver) cusolverDnDestroy(solver);
+  if (solver_params) cusolverDnDestroyParams(solver_params);
+  if (blas) cublasDestroy(blas);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -2003,6 +2006,9 @@ constexpr int kEighMin = 96;
 // ~8 GFLOP/s; measured on the 64-chain scan, limits of 64 and 128 columns made the
 // canonicalize phase 2.7x slower than the solver lanes, so only tiny blocks go there
 constexpr int kJacobiUseCols = 24;
+// largest Gram dimension (rows of the block for a forward step, columns backward) of
+// the batched eigensolver route; larger blocks take syevd on the lanes
+constexpr int kGramBatchMax = 256;
 
 std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<CanonJob>& jobs) {
   for (const CanonJob& jb : jobs)
@@ -2018,6 +2024,7 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
     bool eigh = false;            // density-matrix route: U (forward) or V (backward) from eigh,
                                   // the other factor stored already multiplied by s
     bool jacobi = false;          // batched one-sided Jacobi kernel (small blocks)
+    bool gram = false;            // batched eigensolver route (implies eigh)
   };
   std::vector<Blk> blks;
   int64_t nsv = 0;  // singular values first (one contiguous read-back), then U and V^T
@@ -2052,6 +2059,8 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
   ctx.svd_mats.ensure(size_t(tot) * sizeof(double), ctx.stream);
   double* mats = ctx.svd_mats.as<double>();
   int* infos = reinterpret_cast<int*>(mats + info_off);
+  // statuses of blocks that write none (batched eigensolver route) read as success
+  cuda_check(cudaMemsetAsync(infos, 0, size_t(head - info_off) * sizeof(double), ctx.stream), "svd info zero");
   // Blocks whose working copy fits in shared memory go to one launch of the batched
   // Jacobi SVD kernel.  Of the rest, blocks with min(m, n) >= kEighMin take the
   // reduced-density-matrix route: the eigenvectors of A A^T (forward) or A^T A
@@ -2061,16 +2070,23 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
   int64_t max_gram = 1;
   std::vector<DSvdBlock> jac;
   size_t jac_smem = 0;
+  const int jac_cols = ctx.svd_jacobi_cols >= 0 ? std::min(ctx.svd_jacobi_cols, kJacobiMaxCols) : kJacobiUseCols;
+  const int gram_max = ctx.svd_gram_max >= 0 ? ctx.svd_gram_max : kGramBatchMax;
+  std::vector<int> gram;  // blocks of the batched eigensolver route
   for (size_t bi = 0; bi < blks.size(); ++bi) {
     Blk& x = blks[bi];
-    if (x.k <= kJacobiUseCols && jacobi_svd_smem(x.m, x.n) <= kJacobiMaxSmem) {
+    if (x.k <= jac_cols && jacobi_svd_smem(x.m, x.n) <= kJacobiMaxSmem) {
       x.jacobi = true;
       jac.push_back(DSvdBlock{x.a, x.u_off, x.s_off, x.v_off, x.m, x.n, static_cast<int>(bi), 0});
       jac_smem = std::max(jac_smem, jacobi_svd_smem(x.m, x.n));
+    } else if ((jobs[x.job].forward ? x.m : x.n) <= gram_max) {
+      x.gram = true;
+      x.eigh = true;
+      gram.push_back(static_cast<int>(bi));
     }
   }
   for (auto& x : blks) {
-    if (x.jacobi) continue;
+    if (x.jacobi || x.gram) continue;
     int lw = 0;
     x.eigh = x.k >= kEighMin;
     if (x.eigh) {
@@ -2089,7 +2105,7 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
   const size_t lane_doubles = size_t(lwork) + 8 + 4 * size_t(std::max<int64_t>(maxmn, 1)) + 8 + size_t(max_gram);
   std::vector<int> by_cost;
   for (size_t bi = 0; bi < blks.size(); ++bi)
-    if (!blks[bi].jacobi) by_cost.push_back(static_cast<int>(bi));
+    if (!blks[bi].jacobi && !blks[bi].gram) by_cost.push_back(static_cast<int>(bi));
   std::stable_sort(by_cost.begin(), by_cost.end(), [&](int p, int q) {
     return double(blks[p].m) * blks[p].n * blks[p].k > double(blks[q].m) * blks[q].n * blks[q].k;
   });
@@ -2114,6 +2130,141 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
     djac.upload(jac, st);
     launch_jacobi_svd(djac.get(), static_cast<int>(jac.size()), jac_smem, mats, infos, st);
     ctx.kernel_launches += 1;
+  }
+  // The batched eigensolver route, also on the context's stream: the Gram matrices of
+  // all its blocks in one grouped GEMM, padded to multiples of 8 (-1 on the padded
+  // diagonal keeps the padding's eigenvectors apart, below every eigenvalue of a
+  // Gram matrix of a normalised wavefunction), one batched symmetric eigensolver call
+  // per padded size, the leading eigenvectors as the isometric factor, and the other
+  // factor (carrying s) from one grouped projection GEMM.  Replaces one latency-bound
+  // solver call per block.
+  std::vector<int> gram_info(gram.size(), 0);
+  DevArray<DEigBlock> deig;
+  int* gram_info_d = nullptr;
+  std::vector<char> gram_host_work;
+  if (!gram.empty()) {
+    if (!ctx.blas) {
+      if (cublasCreate(&ctx.blas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(ctx.blas, st) != CUBLAS_STATUS_SUCCESS)
+        throw Error(kCuda, "cublas handle for the batched eigensolver route");
+    }
+    if (!ctx.solver_params) solver_check(cusolverDnCreateParams(&ctx.solver_params), "cusolverDnCreateParams");
+    std::map<int, std::vector<int>> by_p;  // padded size -> blocks
+    for (int bi : gram) {
+      const Blk& x = blks[bi];
+      const int d = jobs[x.job].forward ? x.m : x.n;
+      by_p[(d + 7) & ~7].push_back(bi);
+    }
+    struct PGroup {
+      int P, cnt, first;
+      int64_t g0, w0;
+    };
+    std::vector<PGroup> pg;
+    std::vector<int> order;
+    int64_t gtot = 0;
+    for (auto& kv : by_p) {
+      const int P = kv.first, cnt = static_cast<int>(kv.second.size());
+      pg.push_back(PGroup{P, cnt, static_cast<int>(order.size()), gtot, gtot + int64_t(cnt) * P * P});
+      gtot += int64_t(cnt) * P * P + int64_t(cnt) * P;
+      order.insert(order.end(), kv.second.begin(), kv.second.end());
+    }
+    const int64_t ginfo_off = gtot;
+    gtot += (static_cast<int64_t>(order.size()) + 1) / 2 + 1;
+    ctx.svd_gram.ensure(size_t(gtot) * sizeof(double), st);
+    double* gb = ctx.svd_gram.as<double>();
+    gram_info_d = reinterpret_cast<int*>(gb + ginfo_off);
+    const int ng = static_cast<int>(order.size());
+    std::vector<DEigBlock> eb(ng);
+    std::vector<cublasOperation_t> ta1(ng), tb1(ng), ta2(ng), tb2(ng);
+    std::vector<int> m1(ng), n1(ng), k1(ng), lda1(ng), ldb1(ng), ldc1(ng);
+    std::vector<int> m2(ng), n2(ng), k2(ng), lda2(ng), ldb2(ng), ldc2(ng);
+    std::vector<double> one(ng, 1.0), zero(ng, 0.0);
+    std::vector<int> gsize(ng, 1);
+    std::vector<const double*> ptrs(6 * size_t(ng));  // A1 | B1 | C1 | A2 | B2 | C2
+    for (const PGroup& g : pg) {
+      for (int i = 0; i < g.cnt; ++i) {
+        const int pos = g.first + i;
+        const Blk& x = blks[order[pos]];
+        const bool fw = jobs[x.job].forward;
+        const int d = fw ? x.m : x.n;
+        const int64_t goff = g.g0 + int64_t(i) * g.P * g.P;
+        eb[pos] = DEigBlock{gb + g.w0 + int64_t(i) * g.P, fw ? mats + x.u_off : mats + x.v_off, mats + x.s_off, goff,
+                            g.P, d, x.k, fw ? 0 : 1};
+        // Gram matrix (column-major view of the row-major block: n x m, ld n)
+        ta1[pos] = fw ? CUBLAS_OP_T : CUBLAS_OP_N;
+        tb1[pos] = fw ? CUBLAS_OP_N : CUBLAS_OP_T;
+        m1[pos] = n1[pos] = d;
+        k1[pos] = fw ? x.n : x.m;
+        lda1[pos] = ldb1[pos] = x.n;
+        ldc1[pos] = g.P;
+        ptrs[pos] = x.a;
+        ptrs[ng + pos] = x.a;
+        ptrs[2 * size_t(ng) + pos] = gb + goff;
+        // projection: forward s V^T = U^T A (k x n row-major = A^T U column-major);
+        // backward U s = A V (m x k row-major = V^T A^T column-major)
+        if (fw) {
+          ta2[pos] = CUBLAS_OP_N;
+          tb2[pos] = CUBLAS_OP_T;
+          m2[pos] = x.n;
+          n2[pos] = x.k;
+          k2[pos] = x.m;
+          lda2[pos] = x.n;
+          ldb2[pos] = x.k;
+          ldc2[pos] = x.n;
+          ptrs[3 * size_t(ng) + pos] = x.a;
+          ptrs[4 * size_t(ng) + pos] = mats + x.u_off;
+          ptrs[5 * size_t(ng) + pos] = mats + x.v_off;
+        } else {
+          ta2[pos] = CUBLAS_OP_T;
+          tb2[pos] = CUBLAS_OP_N;
+          m2[pos] = x.k;
+          n2[pos] = x.m;
+          k2[pos] = x.n;
+          lda2[pos] = x.n;
+          ldb2[pos] = x.n;
+          ldc2[pos] = x.k;
+          ptrs[3 * size_t(ng) + pos] = mats + x.v_off;
+          ptrs[4 * size_t(ng) + pos] = x.a;
+          ptrs[5 * size_t(ng) + pos] = mats + x.u_off;
+        }
+      }
+    }
+    ctx.svd_ptrs.ensure(ptrs.size() * sizeof(double*), st);
+    cuda_check(cudaMemcpyAsync(ctx.svd_ptrs.p, ptrs.data(), ptrs.size() * sizeof(double*), cudaMemcpyHostToDevice, st),
+               "gram pointers");
+    const double* const* dp = reinterpret_cast<const double* const*>(ctx.svd_ptrs.p);
+    double* const* dc1 = reinterpret_cast<double* const*>(ctx.svd_ptrs.as<double*>() + 2 * size_t(ng));
+    double* const* dc2 = reinterpret_cast<double* const*>(ctx.svd_ptrs.as<double*>() + 5 * size_t(ng));
+    deig.upload(eb, st);
+    cuda_check(cudaMemsetAsync(gb, 0, size_t(ginfo_off) * sizeof(double), st), "gram zero");
+    launch_gram_pad(deig.get(), ng, gb, st);
+    if (cublasDgemmGroupedBatched(ctx.blas, ta1.data(), tb1.data(), m1.data(), n1.data(), k1.data(), one.data(), dp,
+                                  lda1.data(), dp + ng, ldb1.data(), zero.data(), dc1, ldc1.data(), ng,
+                                  gsize.data()) != CUBLAS_STATUS_SUCCESS)
+      throw Error(kCuda, "canonicalize: grouped Gram GEMM failed");
+    size_t dev_bytes = 0, host_bytes = 0;
+    for (const PGroup& g : pg) {
+      size_t db = 0, hb = 0;
+      solver_check(cusolverDnXsyevBatched_bufferSize(ctx.solver, ctx.solver_params, CUSOLVER_EIG_MODE_VECTOR,
+                                                     CUBLAS_FILL_MODE_LOWER, g.P, CUDA_R_64F, gb + g.g0, g.P,
+                                                     CUDA_R_64F, gb + g.w0, CUDA_R_64F, &db, &hb, g.cnt),
+                   "syevBatched bufferSize");
+      dev_bytes = std::max(dev_bytes, db);
+      host_bytes = std::max(host_bytes, hb);
+    }
+    ctx.svd_gram_work.ensure(std::max<size_t>(dev_bytes, 16), st);
+    gram_host_work.resize(std::max<size_t>(host_bytes, 16));
+    for (const PGroup& g : pg)
+      solver_check(cusolverDnXsyevBatched(ctx.solver, ctx.solver_params, CUSOLVER_EIG_MODE_VECTOR,
+                                          CUBLAS_FILL_MODE_LOWER, g.P, CUDA_R_64F, gb + g.g0, g.P, CUDA_R_64F,
+                                          gb + g.w0, CUDA_R_64F, ctx.svd_gram_work.p, dev_bytes,
+                                          gram_host_work.data(), host_bytes, gram_info_d + g.first, g.cnt),
+                   "syevBatched");
+    launch_eig_factors_batched(deig.get(), ng, gb, st);
+    if (cublasDgemmGroupedBatched(ctx.blas, ta2.data(), tb2.data(), m2.data(), n2.data(), k2.data(), one.data(),
+                                  dp + 3 * size_t(ng), lda2.data(), dp + 4 * size_t(ng), ldb2.data(), zero.data(), dc2,
+                                  ldc2.data(), ng, gsize.data()) != CUBLAS_STATUS_SUCCESS)
+      throw Error(kCuda, "canonicalize: grouped projection GEMM failed");
+    ctx.kernel_launches += 4 + static_cast<int64_t>(pg.size());
   }
   std::atomic<int> next{0};
   std::vector<std::exception_ptr> errs(nlanes);
@@ -2200,7 +2351,12 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
   // singular values and solver statuses to the host
   std::vector<double> hmats(head);
   cuda_check(cudaMemcpyAsync(hmats.data(), mats, head * sizeof(double), cudaMemcpyDeviceToHost, st), "s d2h");
+  if (!gram.empty())
+    cuda_check(cudaMemcpyAsync(gram_info.data(), gram_info_d, gram.size() * sizeof(int), cudaMemcpyDeviceToHost, st),
+               "gram info d2h");
   ctx.sync();
+  for (int v : gram_info)
+    if (v != 0) throw Error(kSolver, "canonicalize: batched eigensolver did not converge (info " + std::to_string(v) + ")");
   {
     const int* hinfo = reinterpret_cast<const int*>(hmats.data() + info_off);
     for (size_t b = 0; b < blks.size(); ++b)

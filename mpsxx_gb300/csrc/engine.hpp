@@ -238,6 +238,11 @@ struct Context {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cusolverDnHandle_t solver = nullptr;
+  cusolverDnParams_t solver_params = nullptr;  // 64-bit solver API (batched eigensolver)
+  cublasHandle_t blas = nullptr;               // on `stream` (grouped Gram/projection GEMMs)
+  DevBuf svd_gram;   // Gram matrices, eigenvalues and infos of the batched eigensolver route
+  DevBuf svd_gram_work;
+  DevBuf svd_ptrs;   // device pointer arrays of the grouped GEMMs
   DevBuf scr1;       // sigma stage-1 intermediates
   DevBuf scr2;       // renormalize intermediates
   DevBuf work;       // Davidson vectors
@@ -268,6 +273,11 @@ struct Context {
   // negative budget leaves the choice to the autotuner
   int64_t sigma_w_budget = -1;
   int sigma_target_tiles = 0;
+  // canonicalize routing: blocks with min(m, n) <= svd_jacobi_cols go to the batched
+  // Jacobi kernel, the rest with a Gram dimension <= svd_gram_max to the batched
+  // eigensolver; < 0 selects the defaults
+  int svd_jacobi_cols = -1;
+  int svd_gram_max = -1;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<SigmaPlan>> sigma_plans;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<DiagPlan>> diag_plans;
   std::map<std::tuple<int, uint64_t, uint64_t, uint64_t>, std::unique_ptr<MergePlan>> merge_plans;

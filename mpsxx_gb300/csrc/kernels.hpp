@@ -40,6 +40,19 @@ struct DSvdBlock {
 constexpr int kJacobiMaxCols = 128;                  // min(m, n) limit of the Jacobi kernel
 constexpr size_t kJacobiMaxSmem = 200 * 1024;        // its shared-memory limit per block
 
+// One Gram matrix of the batched eigensolver route: P x P (column-major, the block's
+// d x d Gram matrix in the leading corner, -1 on the rest of the diagonal) at G +
+// g_off, eigenvalues ascending at w.  The k leading eigenvectors go to out: row-major
+// d x k (transposed = 0) or k x d (transposed = 1); s_j = sqrt(lambda_j), zero for
+// eigenvalues under 64 eps lambda_max.
+struct DEigBlock {
+  const double* w;
+  double* out;
+  double* s;
+  int64_t g_off;
+  int P, d, k, transposed;
+};
+
 // Dense 2-D block copy: dst[r*dld + c] (+)= scale * src[r*sld + c].
 struct DCopy {
   int64_t dst_off, src_off;
@@ -134,6 +147,10 @@ void launch_bproject(const DBatchProb* probs, int nprob, int64_t nmax, double* A
 // Batched one-sided Jacobi SVD (kernels_svd.cu); smem_bytes >= jacobi_svd_smem of
 // every block; info[info_slot] = 1 when a block did not converge.
 size_t jacobi_svd_smem(int m, int n);
+// -1 on the padded diagonal (indices d..P-1) of every Gram matrix (G zeroed before)
+void launch_gram_pad(const DEigBlock* blocks, int nblocks, double* G, cudaStream_t st);
+// leading eigenvectors and singular values of every Gram matrix (DEigBlock)
+void launch_eig_factors_batched(const DEigBlock* blocks, int nblocks, const double* G, cudaStream_t st);
 void launch_jacobi_svd(const DSvdBlock* blocks, int nblocks, size_t smem_bytes, double* out, int* info,
                        cudaStream_t st);
 // Eigenvectors G (d x d, column-major, eigenvalues w ascending) of a Gram matrix ->

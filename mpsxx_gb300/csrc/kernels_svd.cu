@@ -215,7 +215,39 @@ __global__ void __launch_bounds__(kJt) jacobi_svd_kernel(const DSvdBlock* __rest
   }
 }
 
+__global__ void gram_pad_kernel(const DEigBlock* __restrict__ blocks, double* __restrict__ G) {
+  const DEigBlock b = blocks[blockIdx.x];
+  for (int i = b.d + threadIdx.x; i < b.P; i += blockDim.x) G[b.g_off + (int64_t)i * (b.P + 1)] = -1.0;
+}
+
+__global__ void eig_factors_batched_kernel(const DEigBlock* __restrict__ blocks, const double* __restrict__ G) {
+  const DEigBlock b = blocks[blockIdx.x];
+  const double top = b.w[b.P - 1];
+  for (int e = threadIdx.x; e < b.d * b.k; e += blockDim.x) {
+    const int r = e % b.d, j = e / b.d;
+    const double v = G[b.g_off + r + (int64_t)(b.P - 1 - j) * b.P];
+    if (b.transposed)
+      b.out[(int64_t)j * b.d + r] = v;
+    else
+      b.out[(int64_t)r * b.k + j] = v;
+  }
+  for (int j = threadIdx.x; j < b.k; j += blockDim.x) {
+    const double lam = b.w[b.P - 1 - j];
+    b.s[j] = lam > 64.0 * kEps * top ? sqrt(lam) : 0.0;
+  }
+}
+
 }  // namespace
+
+void launch_gram_pad(const DEigBlock* blocks, int nblocks, double* G, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  gram_pad_kernel<<<nblocks, 128, 0, st>>>(blocks, G);
+}
+
+void launch_eig_factors_batched(const DEigBlock* blocks, int nblocks, const double* G, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  eig_factors_batched_kernel<<<nblocks, 256, 0, st>>>(blocks, G);
+}
 
 size_t jacobi_svd_smem(int m, int n) {
   const int rows = m > n ? m : n, cols = m > n ? n : m;

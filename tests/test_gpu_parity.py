@@ -97,15 +97,24 @@ def test_merged_operator_matches_oracle(ctx, forward):
     assert max_block_diff(ref.blocks, got.to_blocks()) < 1e-13
 
 
+# canonicalize routes: (Jacobi column limit, batched-eigensolver Gram limit); -1 = default
+ROUTES = {"default": (-1, -1), "jacobi": (128, 0), "eigensolver": (0, 100000), "lanes": (0, 0)}
+
+
+@pytest.mark.parametrize("route", sorted(ROUTES))
 @pytest.mark.parametrize("forward", [True, False])
-def test_canonicalize_and_renormalize_match_oracle(ctx, forward):
+def test_canonicalize_and_renormalize_match_oracle(ctx, forward, route):
     from oracle import dmrg as od
     from mpsxx_gb300 import core
 
     case = hubbard_bond()
     M = case["M"]
     P = dev(ctx, case["psi"])
-    lm, rm = core.canonicalize(ctx, forward, P, M)
+    ctx.set_svd_routes(*ROUTES[route])
+    try:
+        lm, rm = core.canonicalize(ctx, forward, P, M)
+    finally:
+        ctx.set_svd_routes()
     U, V, kept = od.canonicalize_merged(forward, case["psi"], M)
     # same new bond (sectors and kept dims)
     assert lm.shape()[0][1] == U.qshape[1] and lm.shape()[1][1] == U.dshape[1]
@@ -176,12 +185,14 @@ def test_dmrg_hubbard12_energies_match_oracle(ctx):
     assert log.energy >= gold["exact"] - 1e-10
 
 
+@pytest.mark.parametrize("route", sorted(ROUTES))
 @pytest.mark.parametrize("forward", [True, False])
-def test_canonicalize_rank_deficient_blocks_stay_orthonormal(ctx, forward):
-    """Blocks of rank 1 (and all-zero blocks): the singular vectors of the numerically
-    zero singular values that the truncation keeps are completed to an orthonormal set,
-    as LAPACK's gesvd does, so the isometric factor is orthonormal block by block and
-    U s V^T reproduces the wavefunction.  Tolerance 1e-12."""
+def test_canonicalize_rank_deficient_blocks_stay_orthonormal(ctx, forward, route):
+    """Blocks of rank 2 (and all-zero blocks), on every route: the singular vectors of
+    the numerically zero singular values that the truncation keeps are completed to an
+    orthonormal set, as LAPACK's gesvd does (the eigensolver route drops them), so the
+    isometric factor is orthonormal block by block and U s V^T reproduces the
+    wavefunction.  Tolerance 1e-12."""
     from oracle import qsd as oq
     from mpsxx_gb300 import core
 
@@ -190,9 +201,13 @@ def test_canonicalize_rank_deficient_blocks_stay_orthonormal(ctx, forward):
     psi = case["psi"].empty_like()
     for n, (t, b) in enumerate(sorted(case["psi"].blocks.items())):
         m, k = b.shape
-        blk = 1.0e3 * np.outer(rng.standard_normal(m), rng.standard_normal(k))
+        blk = 1.0e3 * (rng.standard_normal((m, 2)) @ rng.standard_normal((2, k)))
         psi.blocks[t] = np.zeros_like(b) if n % 5 == 4 else blk
-    lm, rm = core.canonicalize(ctx, forward, dev(ctx, psi), 0)
+    ctx.set_svd_routes(*ROUTES[route])
+    try:
+        lm, rm = core.canonicalize(ctx, forward, dev(ctx, psi), 0)
+    finally:
+        ctx.set_svd_routes()
     iso = lm if forward else rm
     checked = 0
     for blk in iso.to_blocks().values():
