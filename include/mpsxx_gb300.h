@@ -105,7 +105,8 @@ int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes,
  * gram_max_dim go to the batched symmetric eigensolver (one grouped launch sequence
  * for all of them); the remaining blocks take cuSOLVER gesvd (min(m, n) < 96) or
  * syevd on the Gram matrix, on concurrent solver lanes.  A negative value selects the
- * default (24 and 256); 0 switches a route off. */
+ * default (24; 256, for padded sizes shared by at least 6 blocks); 0 switches a route
+ * off. */
 int mpsxx_context_set_svd_routes(mpsxx_context* ctx, int jacobi_max_cols, int gram_max_dim);
 
 /* ---- tensors ------------------------------------------------------------- */

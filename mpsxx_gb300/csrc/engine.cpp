@@ -2009,6 +2009,9 @@ constexpr int kJacobiUseCols = 24;
 // largest Gram dimension (rows of the block for a forward step, columns backward) of
 // the batched eigensolver route; larger blocks take syevd on the lanes
 constexpr int kGramBatchMax = 256;
+// fewest Gram matrices of one padded size that take the batched eigensolver; smaller
+// groups (a single bond's few blocks of each size) are faster on the solver lanes
+constexpr int kGramMinBatch = 6;
 
 std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<CanonJob>& jobs) {
   for (const CanonJob& jb : jobs)
@@ -2073,17 +2076,26 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
   const int jac_cols = ctx.svd_jacobi_cols >= 0 ? std::min(ctx.svd_jacobi_cols, kJacobiMaxCols) : kJacobiUseCols;
   const int gram_max = ctx.svd_gram_max >= 0 ? ctx.svd_gram_max : kGramBatchMax;
   std::vector<int> gram;  // blocks of the batched eigensolver route
+  std::map<int, int> per_p;  // candidates per padded Gram size
+  auto gram_dim = [&](const Blk& x) { return jobs[x.job].forward ? x.m : x.n; };
   for (size_t bi = 0; bi < blks.size(); ++bi) {
     Blk& x = blks[bi];
     if (x.k <= jac_cols && jacobi_svd_smem(x.m, x.n) <= kJacobiMaxSmem) {
       x.jacobi = true;
       jac.push_back(DSvdBlock{x.a, x.u_off, x.s_off, x.v_off, x.m, x.n, static_cast<int>(bi), 0});
       jac_smem = std::max(jac_smem, jacobi_svd_smem(x.m, x.n));
-    } else if ((jobs[x.job].forward ? x.m : x.n) <= gram_max) {
-      x.gram = true;
-      x.eigh = true;
-      gram.push_back(static_cast<int>(bi));
+    } else if (gram_dim(x) <= gram_max) {
+      ++per_p[(gram_dim(x) + 7) & ~7];
     }
+  }
+  // an explicit Gram limit (routing set by the caller) takes every candidate
+  const int min_batch = ctx.svd_gram_max >= 0 ? 1 : kGramMinBatch;
+  for (size_t bi = 0; bi < blks.size(); ++bi) {
+    Blk& x = blks[bi];
+    if (x.jacobi || gram_dim(x) > gram_max || per_p[(gram_dim(x) + 7) & ~7] < min_batch) continue;
+    x.gram = true;
+    x.eigh = true;
+    gram.push_back(static_cast<int>(bi));
   }
   for (auto& x : blks) {
     if (x.jacobi || x.gram) continue;
@@ -2149,11 +2161,7 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
     }
     if (!ctx.solver_params) solver_check(cusolverDnCreateParams(&ctx.solver_params), "cusolverDnCreateParams");
     std::map<int, std::vector<int>> by_p;  // padded size -> blocks
-    for (int bi : gram) {
-      const Blk& x = blks[bi];
-      const int d = jobs[x.job].forward ? x.m : x.n;
-      by_p[(d + 7) & ~7].push_back(bi);
-    }
+    for (int bi : gram) by_p[(gram_dim(blks[bi]) + 7) & ~7].push_back(bi);
     struct PGroup {
       int P, cnt, first;
       int64_t g0, w0;
