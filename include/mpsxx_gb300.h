@@ -84,7 +84,8 @@ int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* 
  * the order of MPSXX_PHASE_NAMES; *count receives the number of phases. */
 #define MPSXX_PHASE_NAMES                                                                                    \
   "merge_plan", "merge_alloc", "merge_run", "wave_merge", "sigma_plan", "sigma", "davidson_rest", "svd_solve", \
-      "svd_select", "svd_post", "renorm_plan", "renorm_run"
+      "svd_select", "svd_post", "renorm_plan", "renorm_run", "sigma_fp64", "batch_group", \
+      "batch_plan", "svd_jacobi", "svd_gram"
 int mpsxx_context_profile(mpsxx_context* ctx, int enable, int reset, double* t, int n, int* count);
 
 /* The split-precision H_eff*psi plan of a bond is autotuned on first use: candidate

@@ -405,7 +405,8 @@ def expand_wavefunction(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, 
 
 
 PHASE_NAMES = ("merge_plan", "merge_alloc", "merge_run", "wave_merge", "sigma_plan", "sigma", "davidson_rest",
-               "svd_solve", "svd_select", "svd_post", "renorm_plan", "renorm_run")
+               "svd_solve", "svd_select", "svd_post", "renorm_plan", "renorm_run", "sigma_fp64", "batch_group",
+               "batch_plan", "svd_jacobi", "svd_gram")
 
 BOND_STAT_KEYS = ("n_sigma", "sigma_flops", "t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "converged",
                   "rnorm", "energy_split", "rnorm_fp64", "n_sigma_fp64")

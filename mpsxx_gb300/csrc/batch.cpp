@@ -27,6 +27,19 @@ struct Item {
   SigmaPlan* sp;
   int64_t n = 0, off = 0;               // slice of the vector arena
   int64_t bL = 0, bR = 0, bPsi = 0, bScr = 0;  // byte bases in the packed arenas
+  int64_t bL64 = 0, bR64 = 0, bScr64 = 0;       // element bases in the FP64 arenas
+};
+
+// One grouped FP64 H_eff * psi (slot kSlotIn -> kSlotOut of every member): the members'
+// FP64 plans concatenated into one tile list per stage over the FP64 arenas.
+struct Grouped64 {
+  std::vector<int> members;
+  DevArray<DTile> t1, t2;
+  DevArray<DGemmTask> k1, k2;
+  DevArray<DGemmPair> p1, p2;
+  DevArray<DReduce> r1, r2;
+  int n1 = 0, n2 = 0, nr1 = 0, nr2 = 0, slots = 0;
+  Trans ta1 = kNoTrans, tb1 = kNoTrans, ta2 = kNoTrans, tb2 = kNoTrans;
 };
 
 // One grouped split-TF32 H_eff * psi: slot kSlotIn -> slot kSlotOut of every member.
@@ -97,6 +110,10 @@ class Batch {
   Context& ctx_;
   std::vector<Item>& it_;
   DevBuf vec_, arL_, arR_, arPsi_, arScr_, part_, sums_, small_;
+  DevBuf arL64_, arR64_, arScr64_;  // FP64 operators and stage-1 intermediates of all problems
+  int64_t scr64_elems_ = 0;
+  bool ar64_ready_ = false;
+  std::unique_ptr<Grouped64> g64_;
   DevArray<DBatchProb> all_probs_, act_probs_;
   std::unique_ptr<Grouped> grp_;
 
@@ -160,6 +177,133 @@ class Batch {
         ctx_.kernel_launches += 2;
       }
     }
+  }
+
+  // FP64 arenas: every problem's merged operators copied side by side (once per batch)
+  void setup_fp64() {
+    int64_t nL = 0, nR = 0, nS = 0;
+    for (Item& x : it_) {
+      x.bL64 = nL;
+      nL += (x.L->nnz + 31) / 32 * 32;
+      x.bR64 = nR;
+      nR += (x.R->nnz + 31) / 32 * 32;
+      x.bScr64 = nS;
+      nS += (x.sp->scr1.nnz + 31) / 32 * 32;
+    }
+    arL64_.ensure(size_t(std::max<int64_t>(nL, 1)) * sizeof(double), ctx_.stream);
+    arR64_.ensure(size_t(std::max<int64_t>(nR, 1)) * sizeof(double), ctx_.stream);
+    arScr64_.ensure(size_t(std::max<int64_t>(nS, 1)) * sizeof(double), ctx_.stream);
+    scr64_elems_ = nS;
+    for (Item& x : it_) {
+      if (x.L->nnz)
+        cuda_check(cudaMemcpyAsync(arL64_.as<double>() + x.bL64, x.L->d, x.L->nnz * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, ctx_.stream),
+                   "batch L64");
+      if (x.R->nnz)
+        cuda_check(cudaMemcpyAsync(arR64_.as<double>() + x.bR64, x.R->d, x.R->nnz * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, ctx_.stream),
+                   "batch R64");
+    }
+    ar64_ready_ = true;
+  }
+
+  void build_grouped64(const std::vector<int>& members) {
+    auto g = std::make_unique<Grouped64>();
+    g->members = members;
+    std::vector<DTile> t1, t2;
+    std::vector<DGemmTask> k1, k2;
+    std::vector<DGemmPair> p1, p2;
+    std::vector<DReduce> r1, r2;
+    int slots = 0;
+    // one problem's stage into the grouped lists: operand bases a0, b0 and result base
+    // c0 (elements), task, pair and split-K slot numbers shifted past the earlier ones
+    auto add = [&](const GemmPlan& s, int64_t a0, int64_t b0, int64_t c0, std::vector<DTile>& T,
+                   std::vector<DGemmTask>& K, std::vector<DGemmPair>& P, std::vector<DReduce>& R) {
+      const int tb = static_cast<int>(K.size()), pb = static_cast<int>(P.size());
+      for (DGemmTask t : s.h_tasks) {
+        t.c_off += c0;
+        t.p0 += pb;
+        t.p1 += pb;
+        K.push_back(t);
+      }
+      for (DGemmPair q : s.h_pairs) {
+        q.a_off += a0;
+        q.b_off += b0;
+        P.push_back(q);
+      }
+      for (DTile t : s.h_tiles) {
+        t.task += tb;
+        t.p0 += pb;
+        t.p1 += pb;
+        if (t.slot >= 0) t.slot += slots;
+        T.push_back(t);
+      }
+      for (DReduce r : s.h_reduce) {
+        r.task += tb;
+        r.slot0 += slots;
+        R.push_back(r);
+      }
+    };
+    int slots1 = 0;
+    for (int c : members) {
+      const Item& x = it_[c];
+      add(x.sp->s1, x.bL64, x.off + kSlotIn * x.n, x.bScr64, t1, k1, p1, r1);
+      slots += x.sp->s1.nslots;
+    }
+    slots1 = slots;
+    slots = 0;
+    for (int c : members) {
+      const Item& x = it_[c];
+      add(x.sp->s2, x.bScr64, x.bR64, x.off + kSlotOut * x.n, t2, k2, p2, r2);
+      slots += x.sp->s2.nslots;
+    }
+    g->slots = std::max(slots1, slots);
+    const GemmPlan& s0 = it_[members[0]].sp->s1;
+    const GemmPlan& q0 = it_[members[0]].sp->s2;
+    g->ta1 = s0.ta;
+    g->tb1 = s0.tb;
+    g->ta2 = q0.ta;
+    g->tb2 = q0.tb;
+    for (int c : members)
+      if (it_[c].sp->s1.ta != g->ta1 || it_[c].sp->s1.tb != g->tb1 || it_[c].sp->s2.ta != g->ta2 ||
+          it_[c].sp->s2.tb != g->tb2)
+        throw Error(kInternal, "batched FP64 sigma: stage transposes differ between problems");
+    g->n1 = static_cast<int>(t1.size());
+    g->n2 = static_cast<int>(t2.size());
+    g->nr1 = static_cast<int>(r1.size());
+    g->nr2 = static_cast<int>(r2.size());
+    g->t1.upload(t1, ctx_.stream);
+    g->t2.upload(t2, ctx_.stream);
+    g->k1.upload(k1, ctx_.stream);
+    g->k2.upload(k2, ctx_.stream);
+    g->p1.upload(p1, ctx_.stream);
+    g->p2.upload(p2, ctx_.stream);
+    g->r1.upload(r1, ctx_.stream);
+    g->r2.upload(r2, ctx_.stream);
+    g64_ = std::move(g);
+  }
+
+  // FP64 H_eff * psi of every member in one launch per stage (outputs zeroed by the caller)
+  void sigma64_grouped(const std::vector<int>& act) {
+    if (!ar64_ready_) setup_fp64();
+    if (!g64_ || g64_->members != act) {
+      PhaseTimer tg(ctx_, kPhBatchGroup);
+      build_grouped64(act);
+    }
+    const Grouped64& g = *g64_;
+    const cudaStream_t st = ctx_.stream;
+    if (scr64_elems_)
+      cuda_check(cudaMemsetAsync(arScr64_.p, 0, size_t(scr64_elems_) * sizeof(double), st), "batch scr64 zero");
+    ctx_.gemm_part.ensure(std::max<size_t>(size_t(g.slots) * kGemmTile * kGemmTile * sizeof(double), 16), st);
+    double* part = ctx_.gemm_part.as<double>();
+    double* V = vec_.as<double>();
+    launch_gemm_f64(g.ta1, g.tb1, 1.0, arL64_.as<double>(), V, arScr64_.as<double>(), g.t1.get(), g.n1, g.k1.get(),
+                    g.p1.get(), part, st);
+    if (g.nr1) launch_gemm_reduce(g.r1.get(), g.nr1, g.k1.get(), 1.0, part, arScr64_.as<double>(), st);
+    launch_gemm_f64(g.ta2, g.tb2, 1.0, arScr64_.as<double>(), arR64_.as<double>(), V, g.t2.get(), g.n2, g.k2.get(),
+                    g.p2.get(), part, st);
+    if (g.nr2) launch_gemm_reduce(g.r2.get(), g.nr2, g.k2.get(), 1.0, part, V, st);
+    ctx_.kernel_launches += 3 + (g.nr1 > 0) + (g.nr2 > 0);
   }
 
   // the grouped launch lists of a member set, and its graph
@@ -279,18 +423,14 @@ class Batch {
   // sigma of trial slot k for the active problems (prec: FP64 per problem, or one
   // grouped split launch whose members cover the active set)
   void sigma(const std::vector<int>& act, int k, int prec, std::vector<DavidsonStats>& S) {
-    PhaseTimer tm(ctx_, kPhSigma);
+    PhaseTimer tm(ctx_, prec == kFP64 && ctx_.precision != kFP64 ? kPhSigmaFP64 : kPhSigma);
     const int na = static_cast<int>(act.size());
     const int64_t nm = nmax(act);
     launch_bcopy(act_probs_.get(), na, nm, vec_.as<double>(), k, kSlotIn, ctx_.stream);
     if (prec == kFP64) {
       launch_bzero(act_probs_.get(), na, nm, vec_.as<double>(), kSlotOut, ctx_.stream);
-      for (int c : act) {
-        Item& x = it_[c];
-        double* base = vec_.as<double>() + x.off;
-        apply_sigma(ctx_, *x.sp, *x.L, *x.R, base + kSlotIn * x.n, base + kSlotOut * x.n, kFP64);
-        S[c].n_sigma_fp64 += 1;
-      }
+      sigma64_grouped(act);
+      for (int c : act) S[c].n_sigma_fp64 += 1;
     } else {
       // rebuild the grouped lists only when the active set has shrunk well below them
       bool ok = grp_ != nullptr;
@@ -305,7 +445,12 @@ class Batch {
         }
         if (ok && act.size() * 4 < grp_->members.size() * 3) ok = false;
       }
-      if (!ok) build_grouped(act);
+      if (!ok) {
+        PhaseTimer tg(ctx_, kPhBatchGroup);
+        build_grouped(act);
+        tg.stop();
+        ctx_.timers[tm.phase] -= tg.dt;
+      }
       cuda_check(cudaGraphLaunch(grp_->graph, ctx_.stream), "batch graph launch");
       ctx_.kernel_launches += 5;
     }
@@ -316,6 +461,8 @@ class Batch {
     }
     launch_bcopy(act_probs_.get(), na, nm, vec_.as<double>(), kSlotOut, kSlotSigma + k, ctx_.stream);
     ctx_.kernel_launches += 2;
+    tm.stop();
+    ctx_.timers[kPhDavidsonRest] -= tm.dt;  // H_eff * psi is not part of the rest
   }
 
   // Davidson over the problems in `set`, in lockstep; the loop of the single path
@@ -360,10 +507,8 @@ class Batch {
           std::copy(rvec.begin(), rvec.end(), rv.begin() + size_t(a) * kMaxDot * kMaxDot);
           S[act[a]].micro += 1;
         }
-        cuda_check(cudaMemcpyAsync(Rdev, rv.data(), rv.size() * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream),
-                   "batch rvec");
-        cuda_check(cudaMemcpyAsync(Edev, ev.data(), ev.size() * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream),
-                   "batch eval");
+        upload_staged(Rdev, rv.data(), rv.size() * sizeof(double), ctx_.stream);
+        upload_staged(Edev, ev.data(), ev.size() * sizeof(double), ctx_.stream);
         launch_brotate(act_probs_.get(), na, nmax(act), V, m, Rdev, ctx_.stream);
         launch_bresidual(act_probs_.get(), na, V, Edev, part_.as<double>(), sums_.as<double>(), ctx_.stream);
         ctx_.kernel_launches += 3;
@@ -390,9 +535,7 @@ class Batch {
           // the survivors' eigenvalues in their new order
           std::vector<double> ev2;
           for (int c : still) ev2.push_back(E[c]);
-          cuda_check(cudaMemcpyAsync(Edev, ev2.data(), ev2.size() * sizeof(double), cudaMemcpyHostToDevice,
-                                     ctx_.stream),
-                     "batch eval");
+          upload_staged(Edev, ev2.data(), ev2.size() * sizeof(double), ctx_.stream);
           act.swap(still);
           upload_probs(act, act_probs_);
         }
@@ -423,7 +566,14 @@ std::vector<double> diagonalize_batch(Context& ctx, const std::vector<const DTen
                                       const std::vector<DTensor*>& psi, double tol, std::vector<DavidsonStats>& stats) {
   const size_t N = psi.size();
   if (L.size() != N || R.size() != N || diag.size() != N) throw Error(kInvalidArgument, "batch: argument counts");
-  if (ctx.sigma_plans.size() + N > kMaxCachedPlans) ctx.sigma_plans.clear();  // keep the references below valid
+  {
+    // keep the references below valid: empty the cache only if this batch's plans do
+    // not fit beside it (they are usually built already, by the planning threads)
+    size_t missing = 0;
+    for (size_t c = 0; c < N; ++c)
+      missing += ctx.sigma_plans.count(std::make_tuple(L[c]->layout_id, R[c]->layout_id, psi[c]->layout_id)) == 0;
+    if (ctx.sigma_plans.size() + missing > kMaxCachedPlans) ctx.sigma_plans.clear();
+  }
   std::vector<Item> items(N);
   for (size_t c = 0; c < N; ++c) {
     if (diag[c]->nnz != psi[c]->nnz) throw Error(kInvalidArgument, "batch: diag and wavefunction layouts differ");
@@ -445,12 +595,32 @@ std::vector<BondOut> optimize_twosite_merged_batch(Context& ctx, const std::vect
   std::vector<std::unique_ptr<DTensor>> mL(N), mR(N), psi(N);
   std::vector<DTensor> diag(N);
   std::vector<WaveMerge> wm(N);
+  // Every bond's host plans first, on planning threads (they depend on layouts only):
+  // merged operators, wavefunction merge, H_eff * psi (with its packed-operand plan)
+  // and diagonal.  The device work then follows bond by bond on the stream.
+  std::vector<std::unique_ptr<WavePlan>> wp(N);
+  {
+    PhaseTimer tp(ctx, kPhBatchPlan);
+    reserve_plans(ctx, N);
+    parallel_plan(ctx, static_cast<int>(N), [&](int c) {
+      const BondArgs& a = args[c];
+      const Tensor& L = merge_plan(ctx, true, *a.lmpo, *a.lopr).layout;
+      const Tensor& R = merge_plan(ctx, false, *a.rmpo, *a.ropr).layout;
+      wm[c] = wave_merge_infos(*a.lmpo, *a.rmpo, *a.lopr, *a.ropr);
+      wp[c] = plan_merge_wave(ctx, wm[c], *a.lwfn, *a.rwfn);
+      SigmaPlan& sp = sigma_plan(ctx, L, R, wp[c]->psi);
+      diag_plan(ctx, L, R, wp[c]->psi);
+      if (ctx.precision != kFP64) ensure_sigma_pk(ctx, sp, L, R);
+    });
+  }
   for (size_t c = 0; c < N; ++c) {
     const BondArgs& a = args[c];
     mL[c] = compute_merged_operator(ctx, true, *a.lmpo, *a.lopr);
     mR[c] = compute_merged_operator(ctx, false, *a.rmpo, *a.ropr);
-    wm[c] = wave_merge_infos(*a.lmpo, *a.rmpo, *a.lopr, *a.ropr);
-    psi[c] = merge_wave(ctx, wm[c], *a.lwfn, *a.rwfn);
+    {
+      PhaseTimer tw(ctx, kPhWaveMerge);
+      psi[c] = run_merge_wave(ctx, *wp[c], *a.lwfn, *a.rwfn);
+    }
     static_cast<Tensor&>(diag[c]) = static_cast<const Tensor&>(*psi[c]);
     diag[c].d = nullptr;
     diag[c].ctx = &ctx;
@@ -471,6 +641,17 @@ std::vector<BondOut> optimize_twosite_merged_batch(Context& ctx, const std::vect
   std::vector<CanonJob> jobs(N);
   for (size_t c = 0; c < N; ++c) jobs[c] = CanonJob{args[c].forward, psi[c].get(), args[c].M};
   std::vector<CanonResult> canon = canonicalize_many(ctx, jobs);
+  {
+    PhaseTimer tp(ctx, kPhBatchPlan);
+    reserve_plans(ctx, N);
+    parallel_plan(ctx, static_cast<int>(N), [&](int c) {
+      const CanonResult& cr = canon[c];
+      if (args[c].forward)
+        renorm_plan(ctx, true, *mL[c], *cr.lmat, *cr.lmat);
+      else
+        renorm_plan(ctx, false, *mR[c], *cr.rmat, *cr.rmat);
+    });
+  }
   for (size_t c = 0; c < N; ++c) {
     const BondArgs& a = args[c];
     out[c].stats.energy = E[c];

@@ -29,11 +29,14 @@ static void solver_check(cusolverStatus_t s, const char* what) {
 // device block cache
 // ---------------------------------------------------------------------------
 namespace {
+// A released block remembers the stream of its last owner.  Taken again on the same
+// stream it needs no synchronisation (stream order); taken on another stream, that
+// stream waits for an event recorded on the old one at that moment (which covers the
+// old owner's work).  Released blocks thus cost no driver calls.
 struct CachedBlock {
   void* p;
   int device;
-  cudaStream_t st;    // stream of the last owner
-  cudaEvent_t ready;  // recorded on st at release: the last owner's work is queued before it
+  cudaStream_t st;  // stream of the last owner; nullptr: idle (its context drained it)
 };
 
 class BlockCache {
@@ -63,9 +66,14 @@ class BlockCache {
         *got = it->first;
         cached_ -= it->first;
         free_.erase(it);
-        if (b.ready) {
-          if (b.st != st) cuda_check(cudaStreamWaitEvent(st, b.ready, 0), "block cache wait");
-          cudaEventDestroy(b.ready);
+        if (b.st && b.st != st) {
+          // under the lock: the old stream cannot be unregistered and destroyed meanwhile
+          cudaEvent_t ev = nullptr;
+          cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "block cache event");
+          cuda_check(cudaEventRecord(ev, b.st), "block cache record");
+          const cudaError_t e = cudaStreamWaitEvent(st, ev, 0);
+          cudaEventDestroy(ev);
+          cuda_check(e, "block cache wait");
         }
         return b.p;
       }
@@ -89,24 +97,11 @@ class BlockCache {
   void put(void* p, size_t bytes, cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
-    bool live = false;
-    {
-      std::lock_guard<std::mutex> lk(mu_);
-      live = live_.count(st) > 0;
-    }
-    // A stream that is no longer registered belonged to a context that drained it
-    // before going away: the block is idle and needs no event.
-    cudaEvent_t ev = nullptr;
-    if (live && (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess ||
-                 cudaEventRecord(ev, st) != cudaSuccess)) {
-      // the context is failing: return the block for good
-      cudaGetLastError();
-      if (ev) cudaEventDestroy(ev);
-      cudaFree(p);
-      return;
-    }
     std::lock_guard<std::mutex> lk(mu_);
-    free_.emplace(bytes, CachedBlock{p, dev, live ? st : nullptr, ev});
+    // a stream that is no longer registered belonged to a context that drained it
+    // before going away: the block is idle
+    const bool live = live_.count(st) > 0;
+    free_.emplace(bytes, CachedBlock{p, dev, live ? st : nullptr});
     cached_ += bytes;
   }
 
@@ -114,13 +109,18 @@ class BlockCache {
     std::lock_guard<std::mutex> lk(mu_);
     live_[st] += 1;
   }
+  // the stream's owner has drained it: its cached blocks become idle
   void unregister_stream(cudaStream_t st) {
     std::lock_guard<std::mutex> lk(mu_);
     auto it = live_.find(st);
-    if (it != live_.end() && --it->second == 0) live_.erase(it);
+    if (it != live_.end() && --it->second == 0) {
+      live_.erase(it);
+      for (auto& kv : free_)
+        if (kv.second.st == st) kv.second.st = nullptr;
+    }
   }
 
-  // Free every cached block (waits for its last owner's work first).
+  // Free every cached block (cudaFree waits for the device's queued work first).
   void trim() {
     std::multimap<size_t, CachedBlock> blocks;
     {
@@ -128,13 +128,7 @@ class BlockCache {
       blocks.swap(free_);
       cached_ = 0;
     }
-    for (auto& kv : blocks) {
-      if (kv.second.ready) {
-        cudaEventSynchronize(kv.second.ready);
-        cudaEventDestroy(kv.second.ready);
-      }
-      cudaFree(kv.second.p);
-    }
+    for (auto& kv : blocks) cudaFree(kv.second.p);
   }
 
   size_t cached_bytes() {
@@ -175,11 +169,101 @@ void DevBuf::release() {
   cap = 0;
 }
 
+namespace {
+// Host-to-device uploads of small host arrays (plans, Ritz vectors) go through a
+// pinned staging area: the data is copied into it and the device copy is queued
+// asynchronously, so an upload costs a memcpy and a queued copy instead of the
+// driver's staging of pageable memory (which serialises concurrent planning threads).
+// Two halves alternate; a half is refilled only after the copies queued from it have
+// run (an event on every stream that read from it).  One stager per device.
+class Stager {
+ public:
+  static constexpr size_t kHalf = size_t(16) << 20;
+  static constexpr size_t kMaxStaged = size_t(1) << 20;  // larger uploads are copied directly
+
+  void upload(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    if (bytes == 0) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    if (!buf_[0] && !failed_) {
+      void* p = nullptr;
+      if (cudaHostAlloc(&p, 2 * kHalf, cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        failed_ = true;  // no pinned memory: plain copies
+      } else {
+        buf_[0] = static_cast<char*>(p);
+        buf_[1] = buf_[0] + kHalf;
+      }
+    }
+    if (failed_ || bytes > kMaxStaged) {
+      cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "upload");
+      return;
+    }
+    const size_t need = (bytes + 15) & ~size_t(15);
+    if (off_ + need > kHalf) switch_half();
+    char* p = buf_[cur_] + off_;
+    off_ += need;
+    std::memcpy(p, src, bytes);
+    cuda_check(cudaMemcpyAsync(dst, p, bytes, cudaMemcpyHostToDevice, st), "staged upload");
+    if (std::find(used_[cur_].begin(), used_[cur_].end(), st) == used_[cur_].end()) used_[cur_].push_back(st);
+  }
+
+  // a stream about to be destroyed (its work drained): no event is recorded on it
+  void forget(cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(mu_);
+    for (auto& u : used_) u.erase(std::remove(u.begin(), u.end(), st), u.end());
+  }
+
+ private:
+  void switch_half() {
+    for (cudaStream_t s : used_[cur_]) {
+      cudaEvent_t ev = nullptr;
+      cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "stager event");
+      cuda_check(cudaEventRecord(ev, s), "stager record");
+      done_[cur_].push_back(ev);
+    }
+    used_[cur_].clear();
+    cur_ ^= 1;
+    off_ = 0;
+    for (cudaEvent_t ev : done_[cur_]) {
+      cudaEventSynchronize(ev);
+      cudaEventDestroy(ev);
+    }
+    done_[cur_].clear();
+  }
+
+  std::mutex mu_;
+  char* buf_[2] = {nullptr, nullptr};
+  bool failed_ = false;
+  int cur_ = 0;
+  size_t off_ = 0;
+  std::vector<cudaStream_t> used_[2];
+  std::vector<cudaEvent_t> done_[2];
+};
+
+constexpr int kMaxDevices = 64;
+
+// Never destroyed (uploads may be queued during static destruction).
+Stager& stager() {
+  static Stager* s = new Stager[kMaxDevices];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return s[dev >= 0 && dev < kMaxDevices ? dev : 0];
+}
+}  // namespace
+
+void upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  stager().upload(dst, src, bytes, st);
+}
+
+void forget_stream_uploads(cudaStream_t st) {
+  stager().forget(st);
+}
+
 template <class T>
 void DevArray<T>::upload(const std::vector<T>& h, cudaStream_t st) {
   n = h.size();
   buf.ensure(std::max<size_t>(1, n) * sizeof(T), st);
-  if (n) cuda_check(cudaMemcpyAsync(buf.p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice, st), "plan upload");
+  if (n) upload_staged(buf.p, h.data(), n * sizeof(T), st);
 }
 template struct DevArray<DTile>;
 template struct DevArray<DPkPair>;
@@ -227,8 +311,10 @@ Context::~Context() {
   for (DevBuf* b : {&scr1, &scr2, &work, &partial, &scalars, &svd_work, &svd_mats, &gemm_part, &err_flag,
                     &svd_gram, &svd_gram_work, &svd_ptrs})
     b->release();
+  forget_stream_uploads(stream);
   for (auto& l : svd_lanes) {
     cudaStreamSynchronize(l->stream);
+    forget_stream_uploads(l->stream);
     l->work.release();
     block_cache().unregister_stream(l->stream);
     if (l->solver) cusolverDnDestroy(l->solver);
@@ -250,12 +336,23 @@ static double now() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-PhaseTimer::PhaseTimer(Context& c, int ph) : ctx(c), phase(ph), t0(c.profile ? now() : 0.0) {}
+// with profiling on, device work queued before the phase is drained first so that it
+// is not counted in this phase
+namespace {
+thread_local bool tl_planning = false;  // this thread builds plans for a batched step
+}
+
+PhaseTimer::PhaseTimer(Context& c, int ph) : ctx(c), phase(ph), on(c.profile && !tl_planning) {
+  if (on) {
+    cudaStreamSynchronize(c.stream);
+    t0 = now();
+  }
+}
 
 void PhaseTimer::stop() {
   if (!open) return;
   open = false;
-  if (!ctx.profile) return;
+  if (!on) return;
   cudaStreamSynchronize(ctx.stream);
   dt = now() - t0;
   ctx.timers[phase] += dt;
@@ -490,12 +587,70 @@ static bool same_qshape(const Shape& a, const Shape& b) {
 }
 
 // ---------------------------------------------------------------------------
+// plan caches (shared with planning threads)
+// ---------------------------------------------------------------------------
+template <class M, class K>
+static typename M::mapped_type::element_type* find_plan(Context& ctx, M& m, const K& key) {
+  std::lock_guard<std::mutex> lk(ctx.plan_mu);
+  auto it = m.find(key);
+  return it == m.end() ? nullptr : it->second.get();
+}
+
+// Inserts a freshly built plan, or returns the one another planning thread inserted
+// first.  A full cache is emptied first, except while planning threads hold
+// references into it.
+template <class M, class K, class P>
+static P& insert_plan(Context& ctx, M& m, const K& key, std::unique_ptr<P> p) {
+  std::lock_guard<std::mutex> lk(ctx.plan_mu);
+  auto it = m.find(key);
+  if (it != m.end()) return *it->second;
+  if (m.size() >= kMaxCachedPlans && !ctx.planning_threads) m.clear();
+  return *m.emplace(key, std::move(p)).first->second;
+}
+
+void reserve_plans(Context& ctx, size_t n) {
+  std::lock_guard<std::mutex> lk(ctx.plan_mu);
+  if (ctx.sigma_plans.size() + n > kMaxCachedPlans) ctx.sigma_plans.clear();
+  if (ctx.diag_plans.size() + n > kMaxCachedPlans) ctx.diag_plans.clear();
+  if (ctx.merge_plans.size() + 2 * n > kMaxCachedPlans) ctx.merge_plans.clear();
+  if (ctx.renorm_plans.size() + n > kMaxCachedPlans) ctx.renorm_plans.clear();
+}
+
+void parallel_plan(Context& ctx, int n, const std::function<void(int)>& f) {
+  const int hw = std::max(1, static_cast<int>(std::thread::hardware_concurrency()));
+  const int nt = std::min({n, hw, 16});
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  ctx.planning_threads = true;
+  std::atomic<int> next{0};
+  std::vector<std::exception_ptr> errs(nt);
+  auto work = [&](int t) {
+    tl_planning = true;
+    try {
+      cuda_check(cudaSetDevice(ctx.device), "cudaSetDevice");
+      for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) f(i);
+    } catch (...) {
+      errs[t] = std::current_exception();
+    }
+    tl_planning = false;
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+  ctx.planning_threads = false;
+  for (auto& e : errs)
+    if (e) std::rethrow_exception(e);
+}
+
+// ---------------------------------------------------------------------------
 // sigma vector
 // ---------------------------------------------------------------------------
-SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi) {
+SigmaPlan& sigma_plan(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& psi) {
   auto key = std::make_tuple(L.layout_id, R.layout_id, psi.layout_id);
-  auto it = ctx.sigma_plans.find(key);
-  if (it != ctx.sigma_plans.end()) return *it->second;
+  if (SigmaPlan* hit = find_plan(ctx, ctx.sigma_plans, key)) return *hit;
   PhaseTimer tm(ctx, kPhSigmaPlan);
   if (L.sh.rank != 3 || R.sh.rank != 3 || psi.sh.rank != 2)
     throw Error(kInvalidArgument, "compute_sigma_vector: expects 3-index operators and a 2-index wavefunction");
@@ -517,12 +672,9 @@ SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DT
   p->s2.upload(ctx.stream);
   p->flops = p->s1.flops + p->s2.flops;
   p->bytes_min = 8 * (L.nnz + R.nnz + 2 * psi.nnz);
-  p->psi_layout = static_cast<const Tensor&>(psi);
+  p->psi_layout = psi;
   p->psi_layout.d = nullptr;
-  auto& ref = *p;
-  if (ctx.sigma_plans.size() >= kMaxCachedPlans) ctx.sigma_plans.clear();
-  ctx.sigma_plans[key] = std::move(p);
-  return ref;
+  return insert_plan(ctx, ctx.sigma_plans, key, std::move(p));
 }
 
 // ---------------------------------------------------------------------------
@@ -1015,7 +1167,8 @@ static void sigma_run(Context& ctx, SigmaPlan& p, const DTensor& L, const DTenso
   ctx.sigma_calls += 1;
 }
 
-void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R) {
+void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R) {
+  std::lock_guard<std::mutex> lk(p.pk_mu);
   if (!p.pk_built) build_sigma_pk(ctx, p, L, R, p.psi_layout);
 }
 
@@ -1072,10 +1225,9 @@ double sigma_device_time(Context& ctx, const DTensor& L, const DTensor& R, const
 // ---------------------------------------------------------------------------
 // diagonal
 // ---------------------------------------------------------------------------
-DiagPlan& diag_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag) {
+DiagPlan& diag_plan(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& diag) {
   auto key = std::make_tuple(L.layout_id, R.layout_id, diag.layout_id);
-  auto it = ctx.diag_plans.find(key);
-  if (it != ctx.diag_plans.end()) return *it->second;
+  if (DiagPlan* hit = find_plan(ctx, ctx.diag_plans, key)) return *hit;
   PhaseTimer tm(ctx, kPhSigmaPlan);
   auto p = std::make_unique<DiagPlan>();
   // tied arrays: row sector -> [(w, block slot)] for blocks (i, w, i), ascending w
@@ -1125,10 +1277,7 @@ DiagPlan& diag_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTen
   }
   p->tasks.upload(p->h_tasks, ctx.stream);
   p->pairs.upload(p->h_pairs, ctx.stream);
-  auto& ref = *p;
-  if (ctx.diag_plans.size() >= kMaxCachedPlans) ctx.diag_plans.clear();
-  ctx.diag_plans[key] = std::move(p);
-  return ref;
+  return insert_plan(ctx, ctx.diag_plans, key, std::move(p));
 }
 
 void compute_diagonal_elements(Context& ctx, const DTensor& L, const DTensor& R, DTensor& diag) {
@@ -1168,16 +1317,16 @@ static std::unique_ptr<RenormPlan> build_renorm_plan(Context& ctx, bool forward,
   return rp;
 }
 
+RenormPlan& renorm_plan(Context& ctx, bool forward, const Tensor& opr0, const Tensor& bra, const Tensor& ket) {
+  const auto key = std::make_tuple(forward ? 1 : 0, opr0.layout_id, bra.layout_id, ket.layout_id);
+  if (RenormPlan* hit = find_plan(ctx, ctx.renorm_plans, key)) return *hit;
+  return insert_plan(ctx, ctx.renorm_plans, key, build_renorm_plan(ctx, forward, opr0, bra, ket));
+}
+
 std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& opr0, const DTensor& bra,
                                      const DTensor& ket) {
   PhaseTimer tplan(ctx, kPhRenormPlan);
-  const auto key = std::make_tuple(forward ? 1 : 0, opr0.layout_id, bra.layout_id, ket.layout_id);
-  auto it = ctx.renorm_plans.find(key);
-  if (it == ctx.renorm_plans.end()) {
-    if (ctx.renorm_plans.size() >= kMaxCachedPlans) ctx.renorm_plans.clear();
-    it = ctx.renorm_plans.emplace(key, build_renorm_plan(ctx, forward, opr0, bra, ket)).first;
-  }
-  RenormPlan& rp = *it->second;
+  RenormPlan& rp = renorm_plan(ctx, forward, opr0, bra, ket);
   const bool split = ctx.precision == kSplitTF32All;
   if (split && !rp.split_built) {
     build_split_gemm(ctx, rp.g1, rp.p1, conj_view(bra), opr0);
@@ -1212,7 +1361,7 @@ std::unique_ptr<DTensor> renormalize(Context& ctx, bool forward, const DTensor& 
 // merged super-block operators (scatter of scalar MPO blocks)
 // ---------------------------------------------------------------------------
 static std::unique_ptr<MergePlan> build_merge_plan(Context& ctx, bool forward, const DTensor& mpo,
-                                                   const DTensor& opr) {
+                                                   const Tensor& opr) {
   for (size_t b = 0; b < mpo.tags.size(); ++b)
     if ((b + 1 < mpo.tags.size() ? mpo.offsets[b + 1] : mpo.nnz) - mpo.offsets[b] != 1)
       throw Error(kInvalidArgument, "merged operator: MPO blocks must be scalars (1x1x1x1)");
@@ -1382,14 +1531,14 @@ static std::unique_ptr<MergePlan> build_merge_plan(Context& ctx, bool forward, c
   return plan;
 }
 
-static MergePlan& merge_plan(Context& ctx, bool forward, const DTensor& mpo, const DTensor& opr) {
+static MergePlan& merge_plan_mut(Context& ctx, bool forward, const DTensor& mpo, const Tensor& opr) {
   const auto key = std::make_tuple(forward ? 1 : 0, mpo.layout_id, mpo.data_version, opr.layout_id);
-  auto it = ctx.merge_plans.find(key);
-  if (it == ctx.merge_plans.end()) {
-    if (ctx.merge_plans.size() >= kMaxCachedPlans) ctx.merge_plans.clear();
-    it = ctx.merge_plans.emplace(key, build_merge_plan(ctx, forward, mpo, opr)).first;
-  }
-  return *it->second;
+  if (MergePlan* hit = find_plan(ctx, ctx.merge_plans, key)) return *hit;
+  return insert_plan(ctx, ctx.merge_plans, key, build_merge_plan(ctx, forward, mpo, opr));
+}
+
+const MergePlan& merge_plan(Context& ctx, bool forward, const DTensor& mpo, const Tensor& opr) {
+  return merge_plan_mut(ctx, forward, mpo, opr);
 }
 
 // dE/dW[e] = sum over the scatter records of MPO block e of <Y_sub, env_block>,
@@ -1397,7 +1546,7 @@ static MergePlan& merge_plan(Context& ctx, bool forward, const DTensor& mpo, con
 // merged operator's sector indices (the adjoint of compute_merged_operator).
 std::vector<double> mpo_gradient(Context& ctx, bool forward, const DTensor& mpo, const DTensor& opr,
                                  const DTensor& Y) {
-  MergePlan& plan = merge_plan(ctx, forward, mpo, opr);
+  MergePlan& plan = merge_plan_mut(ctx, forward, mpo, opr);
   if (Y.sh.rank != 3) throw Error(kInvalidArgument, "mpo gradient: adjoint operator must have 3 indices");
   for (int i = 0; i < 3; ++i)
     if (Y.sh.dshape[i] != plan.layout.sh.dshape[i])
@@ -1499,42 +1648,53 @@ WaveMerge wave_merge_infos(const DTensor& lmpo, const DTensor& rmpo, const DTens
   return wm;
 }
 
-std::unique_ptr<DTensor> merge_wave(Context& ctx, const WaveMerge& wm, const DTensor& lwfn, const DTensor& rwfn) {
-  PhaseTimer tm(ctx, kPhWaveMerge);
+std::unique_ptr<WavePlan> plan_merge_wave(Context& ctx, const WaveMerge& wm, const Tensor& lwfn, const Tensor& rwfn) {
+  auto wp = std::make_unique<WavePlan>();
   int K = 0;
   Shape t4 = gemm_result_shape(kNoTrans, kNoTrans, lwfn.sh, rwfn.sh, 4, &K);
   auto tasks = enumerate_gemm(kNoTrans, kNoTrans, lwfn, rwfn, t4, K);
-  auto psi = std::make_unique<DTensor>();
-  psi->sh.rank = 2;
-  psi->sh.q = t4.q;
-  psi->sh.qshape = {wm.ql.q_merged, wm.qr.q_merged};
-  psi->sh.dshape = {wm.ql.d_merged, wm.qr.d_merged};
-  psi->sh.finalize();
-  psi->allocate_allowed();
+  Tensor& psi = wp->psi;
+  psi.sh.rank = 2;
+  psi.sh.q = t4.q;
+  psi.sh.qshape = {wm.ql.q_merged, wm.qr.q_merged};
+  psi.sh.dshape = {wm.ql.d_merged, wm.qr.d_merged};
+  psi.sh.finalize();
+  psi.allocate_allowed();
   const int nn = t4.nsec(1), nr = t4.nsec(3);
-  GemmPlan plan;
-  build_plan_impl(plan, kNoTrans, kNoTrans, lwfn, rwfn, K, std::move(tasks), [&](int64_t ctag) {
+  build_plan_impl(wp->plan, kNoTrans, kNoTrans, lwfn, rwfn, K, std::move(tasks), [&](int64_t ctag) {
     int ti[kMaxRank];
     t4.index(ctag, ti);
     const int ipr = ti[0] * nn + ti[1], ipc = ti[2] * nr + ti[3];
     const int A = wm.ql.merged_of[ipr], B = wm.qr.merged_of[ipc];
     int pi[2] = {A, B};
-    const int32_t ps = psi->find(psi->sh.tag(pi));
+    const int32_t ps = psi.find(psi.sh.tag(pi));
     if (ps < 0) throw Error(kInternal, "merge_wave: psi block missing");
-    const int dB = psi->sh.dshape[1][B];
+    const int dB = psi.sh.dshape[1][B];
     CMap m;
-    m.off = psi->offsets[ps] + int64_t(wm.ql.offset_packed[ipr]) * dB + wm.qr.offset_packed[ipc];
+    m.off = psi.offsets[ps] + int64_t(wm.ql.offset_packed[ipr]) * dB + wm.qr.offset_packed[ipc];
     m.m = t4.dshape[0][ti[0]] * t4.dshape[1][ti[1]];
     m.n = t4.dshape[2][ti[2]] * t4.dshape[3][ti[3]];
     m.ldc = dB;
     return m;
   });
-  plan.upload(ctx.stream);
+  wp->plan.upload(ctx.stream);
+  return wp;
+}
+
+std::unique_ptr<DTensor> run_merge_wave(Context& ctx, WavePlan& wp, const DTensor& lwfn, const DTensor& rwfn) {
+  auto psi = std::make_unique<DTensor>();
+  static_cast<Tensor&>(*psi) = wp.psi;
   psi->ctx = &ctx;
   psi->alloc_device(ctx.stream, true);
-  plan.run(1.0, lwfn.d, rwfn.d, psi->d, gemm_scratch(ctx, plan), ctx.stream);
+  wp.plan.run(1.0, lwfn.d, rwfn.d, psi->d, gemm_scratch(ctx, wp.plan), ctx.stream);
   ctx.kernel_launches += 1;
   return psi;
+}
+
+std::unique_ptr<DTensor> merge_wave(Context& ctx, const WaveMerge& wm, const DTensor& lwfn, const DTensor& rwfn) {
+  PhaseTimer tm(ctx, kPhWaveMerge);
+  auto wp = plan_merge_wave(ctx, wm, lwfn, rwfn);
+  return run_merge_wave(ctx, *wp, lwfn, rwfn);
 }
 
 static std::vector<std::vector<Qn>> split_q(const MergeInfo& info) { return info.qshape; }
@@ -1834,7 +1994,7 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
     ctx.sync();
   };
   auto sigma_of = [&](int k, int precision) {
-    PhaseTimer tm(ctx, kPhSigma);
+    PhaseTimer tm(ctx, precision == kFP64 && ctx.precision != kFP64 ? kPhSigmaFP64 : kPhSigma);
     cuda_check(cudaMemsetAsync(sigma + k * n, 0, n * sizeof(double), st), "sigma zero");
     sigma_run(ctx, sp, L, R, trial + k * n, sigma + k * n, precision);
     S.n_sigma += 1;
@@ -1887,8 +2047,7 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
       jacobi_eigh(m, heff, rval, rvec);  // rvec[i*m + j]: component i of eigenvector j
       eval = rval[0];
       S.micro += 1;
-      cuda_check(cudaMemcpyAsync(rvec_d, rvec.data(), m * m * sizeof(double), cudaMemcpyHostToDevice, st),
-                 "rvec h2d");
+      upload_staged(rvec_d, rvec.data(), m * m * sizeof(double), st);
       launch_rotate(trial, m, n, n, rvec_d, m, nullptr, st);
       launch_rotate(sigma, m, n, n, rvec_d, m, nullptr, st);
       launch_copy_vec(errv, sigma, n, st);
@@ -2006,6 +2165,9 @@ constexpr int kEighMin = 96;
 // ~8 GFLOP/s; measured on the 64-chain scan, limits of 64 and 128 columns made the
 // canonicalize phase 2.7x slower than the solver lanes, so only tiny blocks go there
 constexpr int kJacobiUseCols = 24;
+// blocks up to this many columns take the Jacobi kernel even where the batched
+// eigensolver could take them (measured on the 64-chain scan: 12 beats 8, 16 and 24)
+constexpr int kJacobiFirstCols = 12;
 // largest Gram dimension (rows of the block for a forward step, columns backward) of
 // the batched eigensolver route; larger blocks take syevd on the lanes
 constexpr int kGramBatchMax = 256;
@@ -2078,24 +2240,40 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
   std::vector<int> gram;  // blocks of the batched eigensolver route
   std::map<int, int> per_p;  // candidates per padded Gram size
   auto gram_dim = [&](const Blk& x) { return jobs[x.job].forward ? x.m : x.n; };
+  auto jac_ok = [&](const Blk& x, int cols) {
+    return x.k <= cols && jacobi_svd_smem(x.m, x.n) <= kJacobiMaxSmem;
+  };
+  auto to_jacobi = [&](Blk& x, size_t bi) {
+    x.jacobi = true;
+    jac.push_back(DSvdBlock{x.a, x.u_off, x.s_off, x.v_off, x.m, x.n, static_cast<int>(bi), 0});
+    jac_smem = std::max(jac_smem, jacobi_svd_smem(x.m, x.n));
+  };
+  // Default routing: blocks up to kJacobiFirstCols columns always take the Jacobi
+  // kernel; larger ones take the batched eigensolver when their padded size is
+  // shared by enough blocks, else the Jacobi kernel up to kJacobiUseCols columns (its
+  // cost grows steeply with the columns), else the lanes.  Routing set by the caller
+  // applies its limits as given.
+  const bool by_default = ctx.svd_jacobi_cols < 0;
+  const int first_cols = by_default ? std::min(kJacobiFirstCols, jac_cols) : jac_cols;
   for (size_t bi = 0; bi < blks.size(); ++bi) {
     Blk& x = blks[bi];
-    if (x.k <= jac_cols && jacobi_svd_smem(x.m, x.n) <= kJacobiMaxSmem) {
-      x.jacobi = true;
-      jac.push_back(DSvdBlock{x.a, x.u_off, x.s_off, x.v_off, x.m, x.n, static_cast<int>(bi), 0});
-      jac_smem = std::max(jac_smem, jacobi_svd_smem(x.m, x.n));
-    } else if (gram_dim(x) <= gram_max) {
+    if (jac_ok(x, first_cols))
+      to_jacobi(x, bi);
+    else if (gram_dim(x) <= gram_max)
       ++per_p[(gram_dim(x) + 7) & ~7];
-    }
   }
   // an explicit Gram limit (routing set by the caller) takes every candidate
   const int min_batch = ctx.svd_gram_max >= 0 ? 1 : kGramMinBatch;
   for (size_t bi = 0; bi < blks.size(); ++bi) {
     Blk& x = blks[bi];
-    if (x.jacobi || gram_dim(x) > gram_max || per_p[(gram_dim(x) + 7) & ~7] < min_batch) continue;
-    x.gram = true;
-    x.eigh = true;
-    gram.push_back(static_cast<int>(bi));
+    if (x.jacobi) continue;
+    if (gram_dim(x) <= gram_max && per_p[(gram_dim(x) + 7) & ~7] >= min_batch) {
+      x.gram = true;
+      x.eigh = true;
+      gram.push_back(static_cast<int>(bi));
+    } else if (jac_ok(x, jac_cols)) {
+      to_jacobi(x, bi);
+    }
   }
   for (auto& x : blks) {
     if (x.jacobi || x.gram) continue;
@@ -2139,9 +2317,13 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
   // the small blocks on the context's stream, concurrently with the lanes
   DevArray<DSvdBlock> djac;
   if (!jac.empty()) {
+    // (with profiling on, each route is timed on its own: the sub-phases synchronise)
+    PhaseTimer tj(ctx, kPhSvdJacobi);
     djac.upload(jac, st);
     launch_jacobi_svd(djac.get(), static_cast<int>(jac.size()), jac_smem, mats, infos, st);
     ctx.kernel_launches += 1;
+    tj.stop();
+    ctx.timers[kPhSvdSolve] -= tj.dt;
   }
   // The batched eigensolver route, also on the context's stream: the Gram matrices of
   // all its blocks in one grouped GEMM, padded to multiples of 8 (-1 on the padded
@@ -2155,6 +2337,7 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
   int* gram_info_d = nullptr;
   std::vector<char> gram_host_work;
   if (!gram.empty()) {
+    PhaseTimer tg(ctx, kPhSvdGram);
     if (!ctx.blas) {
       if (cublasCreate(&ctx.blas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(ctx.blas, st) != CUBLAS_STATUS_SUCCESS)
         throw Error(kCuda, "cublas handle for the batched eigensolver route");
@@ -2237,8 +2420,7 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
       }
     }
     ctx.svd_ptrs.ensure(ptrs.size() * sizeof(double*), st);
-    cuda_check(cudaMemcpyAsync(ctx.svd_ptrs.p, ptrs.data(), ptrs.size() * sizeof(double*), cudaMemcpyHostToDevice, st),
-               "gram pointers");
+    upload_staged(ctx.svd_ptrs.p, ptrs.data(), ptrs.size() * sizeof(double*), st);
     const double* const* dp = reinterpret_cast<const double* const*>(ctx.svd_ptrs.p);
     double* const* dc1 = reinterpret_cast<double* const*>(ctx.svd_ptrs.as<double*>() + 2 * size_t(ng));
     double* const* dc2 = reinterpret_cast<double* const*>(ctx.svd_ptrs.as<double*>() + 5 * size_t(ng));
@@ -2273,6 +2455,8 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
                                   ldc2.data(), ng, gsize.data()) != CUBLAS_STATUS_SUCCESS)
       throw Error(kCuda, "canonicalize: grouped projection GEMM failed");
     ctx.kernel_launches += 4 + static_cast<int64_t>(pg.size());
+    tg.stop();
+    ctx.timers[kPhSvdSolve] -= tg.dt;
   }
   std::atomic<int> next{0};
   std::vector<std::exception_ptr> errs(nlanes);

@@ -5,6 +5,7 @@
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
+#include <functional>
 #include <map>
 #include <mutex>
 #include <memory>
@@ -45,6 +46,12 @@ struct DevArray {
 };
 
 struct Context;
+
+// Queued host-to-device copy of a small host array through pinned staging memory (the
+// source may be reused as soon as the call returns).
+void upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t st);
+// Drops a stream (drained, about to be destroyed) from the staging bookkeeping.
+void forget_stream_uploads(cudaStream_t st);
 
 // Lower roots projected out of the Davidson operator (multi-root targeting): device
 // vectors in the wavefunction's layout and the roots' energies (at most 12).
@@ -129,6 +136,7 @@ struct SplitGemm {
 };
 
 struct SigmaPlan {
+  std::mutex pk_mu;  // guards the packed-operand plan (built once, possibly by a planning thread)
   uint64_t l_id = 0, r_id = 0, psi_id = 0;
   Tensor scr1;  // layout of L*psi
   GemmPlan s1, s2;
@@ -205,6 +213,12 @@ struct DiagPlan {
   std::vector<std::pair<int64_t, std::vector<std::pair<int64_t, int64_t>>>> ref;  // (psi tag, [(L tag, R tag)])
 };
 
+// A two-site wavefunction merge: the merged layout and the grouped GEMM producing it.
+struct WavePlan {
+  Tensor psi;
+  GemmPlan plan;
+};
+
 struct DavidsonStats {
   int n_sigma = 0;
   int macro = 0;
@@ -230,6 +244,11 @@ enum Phase {
   kPhSvdPost,         // U / sV^T copies and scaling
   kPhRenormPlan,      // renormalisation plans (host)
   kPhRenormRun,       // renormalisation contractions
+  kPhSigmaFP64,       // FP64 H_eff * psi of the split path (refinement anchors)
+  kPhBatchGroup,      // batched steps: grouped sigma lists and their graph capture
+  kPhBatchPlan,       // batched steps: every bond's host plans (planning threads)
+  kPhSvdJacobi,       // canonicalize: batched Jacobi kernel (part of svd_solve)
+  kPhSvdGram,         // canonicalize: batched eigensolver route (part of svd_solve)
   kNumPhases
 };
 
@@ -278,6 +297,10 @@ struct Context {
   // eigensolver; < 0 selects the defaults
   int svd_jacobi_cols = -1;
   int svd_gram_max = -1;
+  // plan caches are shared with the planning threads of a batched step: lookups and
+  // insertions under plan_mu; while planning_threads is set no cache is emptied
+  std::mutex plan_mu;
+  bool planning_threads = false;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<SigmaPlan>> sigma_plans;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<DiagPlan>> diag_plans;
   std::map<std::tuple<int, uint64_t, uint64_t, uint64_t>, std::unique_ptr<MergePlan>> merge_plans;
@@ -303,9 +326,10 @@ struct Context {
 struct PhaseTimer {
   Context& ctx;
   int phase;
-  double t0;
+  double t0 = 0.0;
   double dt = 0.0;  // measured duration (0 when profiling is off)
   bool open = true;
+  bool on = false;  // profiling on and not on a planning thread
   PhaseTimer(Context& c, int ph);
   void stop();
   ~PhaseTimer() { stop(); }
@@ -313,7 +337,7 @@ struct PhaseTimer {
 
 // Packed-operand layouts of a sigma plan (built once), and one H_eff*psi of the plan
 // in the given precision (sigma += H psi) — the building blocks of batched steps.
-void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R);
+void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R);
 void apply_sigma(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi, double* sigma,
                  int precision);
 
@@ -330,7 +354,7 @@ void release_bond_buffers(Context& ctx);
 // --- hot-path operations (reference names) ---------------------------------
 
 // src/compute_sigma_vector.hpp:85-96: sigma += L psi R^T over (w, B').
-SigmaPlan& sigma_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi);
+SigmaPlan& sigma_plan(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& psi);
 void compute_sigma_vector(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& psi, DTensor& sigma);
 
 int* device_err_flag(Context& ctx);
@@ -341,7 +365,16 @@ double sigma_device_time(Context& ctx, const DTensor& L, const DTensor& R, const
                          int reps);
 
 // src/compute_diagonal_elements.hpp:65-80
-DiagPlan& diag_plan(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag);
+DiagPlan& diag_plan(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& diag);
+// Plans by layout (no device data read): cached, safe on planning threads.
+const MergePlan& merge_plan(Context& ctx, bool forward, const DTensor& mpo, const Tensor& opr);
+RenormPlan& renorm_plan(Context& ctx, bool forward, const Tensor& opr0, const Tensor& bra, const Tensor& ket);
+// f(0..n-1) on up to 16 host threads with ctx.planning_threads set (plan building
+// only: no launches); the first exception is rethrown after all threads joined
+void parallel_plan(Context& ctx, int n, const std::function<void(int)>& f);
+// empties the plan caches that could not take n more plans (call with no plan
+// references held, before planning threads start)
+void reserve_plans(Context& ctx, size_t n);
 void compute_diagonal_elements(Context& ctx, const DTensor& L, const DTensor& R, DTensor& diag);
 
 // src/renormalize.hpp:57-95 (merged operator); result allocated by the callee
@@ -382,6 +415,9 @@ struct WaveMerge {
 };
 WaveMerge wave_merge_infos(const DTensor& lmpo, const DTensor& rmpo, const DTensor& lopr, const DTensor& ropr);
 std::unique_ptr<DTensor> merge_wave(Context& ctx, const WaveMerge& wm, const DTensor& lwfn, const DTensor& rwfn);
+// merge_wave in two halves: the plan by layouts (safe on planning threads), the run
+std::unique_ptr<WavePlan> plan_merge_wave(Context& ctx, const WaveMerge& wm, const Tensor& lwfn, const Tensor& rwfn);
+std::unique_ptr<DTensor> run_merge_wave(Context& ctx, WavePlan& wp, const DTensor& lwfn, const DTensor& rwfn);
 std::unique_ptr<DTensor> expand_rows(Context& ctx, const MergeInfo& info, const DTensor& b);
 std::unique_ptr<DTensor> expand_cols(Context& ctx, const DTensor& b, const MergeInfo& info);
 // QSTmerge column merge of the trailing indices (include/btas/QSPARSE/QSTmerge.h:85-140)
