@@ -550,6 +550,7 @@ def main():
     for _ in range(args.warmup):
         core.compute_sigma_vector(ctx, mL, mR, psi, sig)
     tuning = ctx.tuning()
+    plan_stats = core.sigma_plan_stats(ctx, mL, mR, psi)
     barrier(ws)
     torch.cuda.synchronize()
     launches0 = ctx.counters()["launches"]
@@ -631,7 +632,9 @@ def main():
                           "peak": fp64_peak, "frac": fl_per_step / fp64_s / 1e12 / fp64_peak,
                           "speedup_of_headline": fp64_s / kt["sigma_kernels_s"]},
             "accuracy": {"max_rel_err_vs_fp64": rel},
-            "sigma_tuning": [{"w_scratch_mb": b / 2**20, "target_tiles": tt, "ms": ms} for b, tt, ms in tuning],
+            "sigma_tuning": [{"w_scratch_mb": b / 2**20, "target_tiles": tt, "fp32_intermediate": f, "ms": ms}
+                             for b, tt, f, ms in tuning],
+            "sigma_plan": plan_stats,
             "bond_step": bond,
             "sweeps": sweep,
             "gradient": grad,

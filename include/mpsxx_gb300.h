@@ -89,17 +89,20 @@ int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* 
 int mpsxx_context_profile(mpsxx_context* ctx, int enable, int reset, double* t, int n, int* count);
 
 /* The split-precision H_eff*psi plan of a bond is autotuned on first use: candidate
- * schedules (stage-2 split-K sized for a target number of tensor-core tiles, and for
- * very large L*psi intermediates the MPO index w processed in groups that fit a
- * scratch budget) are timed and the fastest is kept with the plan.  The last
- * tuning's (budget bytes, target tiles, milliseconds) triples are written to out (up
- * to n values); *count receives their number. */
+ * schedules (stage-2 split-K sized for a target number of tensor-core tiles; the L*psi
+ * intermediate stored as hi|lo TF32 tiles or as FP32 tiles split on chip; for very
+ * large intermediates the MPO index w processed in groups that fit a scratch budget)
+ * are timed and the fastest is kept with the plan.  The last tuning's (budget bytes,
+ * target tiles, FP32 intermediate (0/1), milliseconds) quadruples are written to out
+ * (up to n values); *count receives the number of values. */
 int mpsxx_context_tuning(const mpsxx_context* ctx, double* out, int n, int* count);
 /* Fix the split-precision H_eff*psi schedule instead of autotuning it: the MPO index w
  * processed in groups whose packed L*psi intermediate fits w_budget_bytes (0 = all of
- * w at once), stage-2 split-K sized for target_tiles tensor-core tiles (0 = default).
- * w_budget_bytes < 0 restores autotuning.  Cached plans are dropped. */
-int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes, int target_tiles);
+ * w at once), stage-2 split-K sized for target_tiles tensor-core tiles (0 = default),
+ * the intermediate as FP32 tiles split on chip (fp32_intermediate = 1) or as hi|lo
+ * tiles (0).  w_budget_bytes < 0 restores autotuning.  Cached plans are dropped. */
+int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes, int target_tiles,
+                                     int fp32_intermediate);
 /* Routing of canonicalize's per-block SVDs: blocks with min(m, n) <= jacobi_max_cols
  * (at most 128) go to the batched one-sided Jacobi kernel; of the rest, blocks whose
  * Gram matrix (rows for a forward step, columns backward) has dimension <=
@@ -147,6 +150,16 @@ int mpsxx_gemm_tasks(int transa, int transb, const mpsxx_tensor* a, const mpsxx_
  * (src/compute_sigma_vector.hpp:85-96).  sgv must have wfn's block layout. */
 int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                                const mpsxx_tensor* wfn, mpsxx_tensor* sgv);
+
+/* Work of the split-precision H_eff*psi plan for these operands (the plan is built if
+ * needed; no device data is read): out[0..12] = useful FLOPs of stage 1 and 2, tile
+ * FLOPs of stage 1 and 2 (128 x 64 tensor-core tiles, K slices of 32, padding
+ * included), K slices of stage 1 and 2, tiles of stage 1 and 2, packed bytes of lopr,
+ * ropr, the L*psi intermediate and wfn, and the intermediate's element count;
+ * out[13..18] = FLOPs of stage 1 and then stage 2 with only the rows (to 128), only
+ * the columns (to 64) or only K (to 32) padded. */
+int mpsxx_sigma_plan_stats(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                           const mpsxx_tensor* wfn, double* out, int n, int* count);
 
 /* diag[A,B] += sum_w lopr[A,w,A] ropr[B,w,B] on diag's blocks.
  * Replaces mpsxx::compute_diagonal_elements(lopr, ropr, diag)

@@ -26,8 +26,9 @@ SIGNATURES = {
     "mpsxx_context_counters": (C.c_int, [vp, c_i64_p, c_dbl_p, c_i64_p]),
     "mpsxx_context_set_truncation": (C.c_int, [vp, C.c_double]),
     "mpsxx_context_tuning": (C.c_int, [vp, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
-    "mpsxx_context_set_sigma_schedule": (C.c_int, [vp, C.c_int64, C.c_int]),
+    "mpsxx_context_set_sigma_schedule": (C.c_int, [vp, C.c_int64, C.c_int, C.c_int]),
     "mpsxx_context_set_svd_routes": (C.c_int, [vp, C.c_int, C.c_int]),
+    "mpsxx_sigma_plan_stats": (C.c_int, [vp, vp, vp, vp, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_mpo_gradient": (C.c_int, [vp, vp, vp, vp, vp, vp, c_dbl_p, c_dbl_p]),
     "mpsxx_merge_rows": (C.c_int, [vp, vp, vpp]),
     "mpsxx_diagonalize_projected": (C.c_int, [vp, vp, vp, vp, vp, C.c_double, C.c_int, vpp, vpp, c_dbl_p, c_dbl_p,

@@ -45,9 +45,11 @@ class Context:
         """Relative tie window at the truncation cutoff (< 0: the precision's default)."""
         check(lib().mpsxx_context_set_truncation(self.h, float(tie_rtol)))
 
-    def set_sigma_schedule(self, w_budget_bytes: int = -1, target_tiles: int = 0):
-        """Fix the split H_eff*psi schedule (w scratch budget, tile target); budget < 0: autotune."""
-        check(lib().mpsxx_context_set_sigma_schedule(self.h, int(w_budget_bytes), int(target_tiles)))
+    def set_sigma_schedule(self, w_budget_bytes: int = -1, target_tiles: int = 0, fp32_intermediate: bool = False):
+        """Fix the split H_eff*psi schedule (w scratch budget, tile target, FP32 L*psi
+        intermediate split on chip); budget < 0: autotune."""
+        check(lib().mpsxx_context_set_sigma_schedule(self.h, int(w_budget_bytes), int(target_tiles),
+                                                     int(bool(fp32_intermediate))))
 
     def set_svd_routes(self, jacobi_max_cols: int = -1, gram_max_dim: int = -1):
         """Routing of canonicalize's block SVDs (batched Jacobi / batched eigensolver /
@@ -55,12 +57,13 @@ class Context:
         check(lib().mpsxx_context_set_svd_routes(self.h, int(jacobi_max_cols), int(gram_max_dim)))
 
     def tuning(self):
-        """Last sigma autotuning: [(w scratch budget bytes, target tiles, milliseconds), ...]."""
+        """Last sigma autotuning: [(w scratch budget bytes, target tiles, FP32 intermediate,
+        milliseconds), ...]."""
         buf = (C.c_double * 64)()
         cnt = C.c_int()
         check(lib().mpsxx_context_tuning(self.h, buf, 64, C.byref(cnt)))
-        v = list(buf)[: cnt.value]
-        return [(int(v[i]), int(v[i + 1]), v[i + 2]) for i in range(0, len(v), 3)]
+        v = list(buf)[: min(cnt.value, 64)]
+        return [(int(v[i]), int(v[i + 1]), bool(v[i + 2]), v[i + 3]) for i in range(0, len(v) - 3, 4)]
 
     def profile(self, enable=-1, reset=False):
         """Phase timers in seconds (PHASE_NAMES); enable=1/0 switches timing on/off."""
@@ -268,6 +271,21 @@ def gemm_tasks(transa: int, transb: int, a: Tensor, b: Tensor, c_rank: int):
 
 def compute_sigma_vector(ctx: Context, lopr: Tensor, ropr: Tensor, wfn: Tensor, sgv: Tensor):
     check(lib().mpsxx_compute_sigma_vector(ctx.h, lopr.h, ropr.h, wfn.h, sgv.h))
+
+
+SIGMA_PLAN_KEYS = ("flops_stage1", "flops_stage2", "tile_flops_stage1", "tile_flops_stage2", "slices_stage1",
+                   "slices_stage2", "tiles_stage1", "tiles_stage2", "packed_bytes_L", "packed_bytes_R",
+                   "packed_bytes_intermediate", "packed_bytes_psi", "intermediate_elements",
+                   "flops_rows_padded_stage1", "flops_cols_padded_stage1", "flops_k_padded_stage1",
+                   "flops_rows_padded_stage2", "flops_cols_padded_stage2", "flops_k_padded_stage2")
+
+
+def sigma_plan_stats(ctx: Context, lopr: Tensor, ropr: Tensor, wfn: Tensor) -> dict:
+    """Useful vs tensor-core tile work and packed bytes of the split H_eff*psi plan."""
+    out = (C.c_double * len(SIGMA_PLAN_KEYS))()
+    cnt = C.c_int()
+    check(lib().mpsxx_sigma_plan_stats(ctx.h, lopr.h, ropr.h, wfn.h, out, len(SIGMA_PLAN_KEYS), C.byref(cnt)))
+    return dict(zip(SIGMA_PLAN_KEYS, list(out)))
 
 
 def compute_diagonal_elements(ctx: Context, lopr: Tensor, ropr: Tensor, diag: Tensor):

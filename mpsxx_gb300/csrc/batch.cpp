@@ -139,7 +139,9 @@ class Batch {
       x.off = off;
       off += kSlots * std::max<int64_t>(x.n, 1);
       if (ctx_.precision != kFP64) {
-        ensure_sigma_pk(ctx_, *x.sp, *x.L, *x.R);
+        // one launch serves all members: their intermediates share the hi|lo format
+        // (a plan tuned by a single-bond run may hold the FP32 one)
+        set_scr1_format(ctx_, *x.sp, *x.L, *x.R, false);
         x.bL = bL;
         bL += (x.sp->pk_L.bytes + 255) / 256 * 256;
         x.bR = bR;
@@ -401,6 +403,10 @@ class Batch {
     upload_probs(members, g->probs);
     ctx_.gemm_part.ensure(std::max<size_t>(size_t(nslots) * kTcTileM * kTcTileN * sizeof(double), 16), ctx_.stream);
     int* err = device_err_flag(ctx_);
+    // the members' intermediates share one format (set in setup)
+    const bool single = it_[members[0]].sp->scr1_single;
+    for (int c : members)
+      if (it_[c].sp->scr1_single != single) throw Error(kInternal, "batched sigma: intermediate formats differ");
     // capture: zero the outputs, pack the inputs, both stages, the split-K sums
     cudaGraph_t graph = nullptr;
     cuda_check(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal), "batch capture");
@@ -408,9 +414,9 @@ class Batch {
     launch_bzero(g->probs.get(), nm, g->nmax, vec_.as<double>(), kSlotOut, ctx_.stream);
     launch_pack(g->packs.get(), g->npacks, vec_.as<double>(), arPsi_.as<uint8_t>(), ctx_.stream);
     launch_gemm_pk(arL_.as<uint8_t>(), arPsi_.as<uint8_t>(), 1.0, nullptr, arScr_.as<uint8_t>(), g->t1.get(), g->n1,
-                   g->k1.get(), g->p1.get(), nullptr, 1, err, ctx_.stream);
+                   g->k1.get(), g->p1.get(), nullptr, single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx_.stream);
     launch_gemm_pk(arScr_.as<uint8_t>(), arR_.as<uint8_t>(), 1.0, vec_.as<double>(), nullptr, g->t2.get(), g->n2,
-                   g->k2.get(), g->p2.get(), ctx_.gemm_part.as<double>(), 0, err, ctx_.stream);
+                   g->k2.get(), g->p2.get(), ctx_.gemm_part.as<double>(), kOutFP64, single ? 1 : 0, err, ctx_.stream);
     launch_gemm_pk_reduce(g->red.get(), g->nred, g->k2.get(), 1.0, ctx_.gemm_part.as<double>(), vec_.as<double>(),
                           ctx_.stream);
     cuda_check(cudaStreamEndCapture(ctx_.stream, &graph), "batch capture end");

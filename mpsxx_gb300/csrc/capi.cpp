@@ -144,13 +144,15 @@ int mpsxx_context_profile(mpsxx_context* ctx, int enable, int reset, double* t, 
   });
 }
 
-int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes, int target_tiles) {
+int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes, int target_tiles,
+                                     int fp32_intermediate) {
   return guard([&] {
     need(ctx && ctx->ctx, "null context");
     need(target_tiles >= 0, "negative tile target");
     Context& c = *ctx->ctx;
     c.sigma_w_budget = w_budget_bytes;
     c.sigma_target_tiles = target_tiles;
+    c.sigma_fp32_intermediate = fp32_intermediate != 0;
     c.sigma_plans.clear();  // plans are rebuilt (and scheduled) on next use
   });
 }
@@ -353,6 +355,17 @@ int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, con
     compute_sigma_vector(c, L, R, P, S);
     c.sync();
     if (c.precision != kFP64) check_device_error(c);
+  });
+}
+
+int mpsxx_sigma_plan_stats(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                           const mpsxx_tensor* wfn, double* out, int n, int* count) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    need(out != nullptr || n == 0, "null output");
+    const std::vector<double> v = sigma_plan_stats(c, ten(lopr), ten(ropr), ten(wfn));
+    for (int i = 0; i < n && i < static_cast<int>(v.size()); ++i) out[i] = v[i];
+    if (count) *count = static_cast<int>(v.size());
   });
 }
 

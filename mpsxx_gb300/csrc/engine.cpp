@@ -723,7 +723,8 @@ static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Te
     return Orient{d[1], d[0], d[1], 1};
   });
   // stage-1 output = stage-2 A operand: scr1 block (dA x dB')
-  packed_layout(p.pk_scr1, p.scr1, kTcTileM, kPkTileABytes, [&](int32_t b) {
+  // written by stage 1 and read once by stage 2: hi|lo tiles, or FP32 tiles split on chip
+  packed_layout(p.pk_scr1, p.scr1, kTcTileM, p.scr1_single ? kPkTileA1Bytes : kPkTileABytes, [&](int32_t b) {
     int d[kMaxRank];
     dims3(p.scr1, b, d);
     return Orient{d[0] * d[1], d[2], d[2], 0};
@@ -806,7 +807,8 @@ static void run_split_gemm(Context& ctx, SplitGemm& sg, const GemmPlan& g, doubl
   double* part = ctx.gemm_part.as<double>();
   int* err = device_err_flag(ctx);
   launch_gemm_pk(sg.pa.buf.as<uint8_t>(), sg.pb.buf.as<uint8_t>(), alpha, C, nullptr, g.tiles_tc.get(),
-                 static_cast<int>(g.h_tiles_tc.size()), g.dtasks.get(), sg.pk.get(), part, 0, err, ctx.stream);
+                 static_cast<int>(g.h_tiles_tc.size()), g.dtasks.get(), sg.pk.get(), part, kOutFP64, 0, err,
+                 ctx.stream);
   if (g.nslots_tc > 0)
     launch_gemm_pk_reduce(g.reduce_tc.get(), static_cast<int>(g.h_reduce_tc.size()), g.dtasks.get(), alpha, part, C,
                           ctx.stream);
@@ -830,7 +832,7 @@ static void build_sigma_groups(Context& ctx, SigmaPlan& p, int64_t budget) {
     blk_w[b] = idx[1];
     if (p.pk_scr1.base[b] < 0) continue;
     const int64_t ntr = (int64_t(d[0]) * d[1] + kTcTileM - 1) / kTcTileM;
-    blk_bytes[b] = ntr * p.pk_scr1.nks[b] * kPkTileABytes;
+    blk_bytes[b] = ntr * p.pk_scr1.nks[b] * (p.scr1_single ? kPkTileA1Bytes : kPkTileABytes);
     w_bytes[idx[1]] += blk_bytes[b];
   }
   std::vector<int> group_of_w(nw, 0);
@@ -1005,12 +1007,12 @@ static void sigma_groups_run(Context& ctx, SigmaPlan& p, double* sigma) {
   for (const SigmaPlan::Group& G : p.groups) {
     if (G.t1_count)
       launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.group_scr.as<uint8_t>(),
-                     p.gt1.get() + G.t1_begin, G.t1_count, p.gtasks1.get(), p.pk1.get(), nullptr, 1, err,
-                     ctx.stream);
+                     p.gt1.get() + G.t1_begin, G.t1_count, p.gtasks1.get(), p.pk1.get(), nullptr,
+                     p.scr1_single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx.stream);
     if (G.t2_count)
       launch_gemm_pk(p.group_scr.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
-                     p.gt2.get() + G.t2_begin, G.t2_count, p.s2.dtasks.get(), p.gpk2.get(), part, 0, err,
-                     ctx.stream);
+                     p.gt2.get() + G.t2_begin, G.t2_count, p.s2.dtasks.get(), p.gpk2.get(), part, kOutFP64,
+                     p.scr1_single ? 1 : 0, err, ctx.stream);
     if (G.r_count)
       launch_gemm_pk_reduce(p.gred.get() + G.r_begin, G.r_count, p.s2.dtasks.get(), 1.0, part, sigma, ctx.stream);
     ctx.kernel_launches += (G.t1_count > 0) + (G.t2_count > 0) + (G.r_count > 0);
@@ -1021,7 +1023,19 @@ static void sigma_groups_run(Context& ctx, SigmaPlan& p, double* sigma) {
 // a scratch result for a few stage-2 split-K granularities (and, for very large
 // intermediates, w blocking) and keeps the fastest.  Runs once per plan; plans are
 // kept across bonds and sweeps.
-static void tune_sigma_groups(Context& ctx, SigmaPlan& p) {
+// Switches a plan's L*psi intermediate between hi|lo and FP32 tiles (packed layouts of
+// L, R and psi are unchanged, so their packed data stays valid; the intermediate's
+// buffer is sized by the caller that runs the plan).
+void set_scr1_format(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R, bool single) {
+  std::lock_guard<std::mutex> lk(p.pk_mu);
+  if (p.scr1_single == single && p.pk_built) return;
+  p.scr1_single = single;
+  p.pk_built = false;
+  build_sigma_pk(ctx, p, L, R, p.psi_layout);
+  p.drop_graph();
+}
+
+static void tune_sigma_groups(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R) {
   const int64_t n = std::max<int64_t>(p.psi_layout.nnz, 1);
   DevBuf out;
   out.ensure(size_t(n) * sizeof(double), ctx.stream);
@@ -1029,23 +1043,34 @@ static void tune_sigma_groups(Context& ctx, SigmaPlan& p) {
   cuda_check(cudaEventCreate(&e0), "tune event");
   cuda_check(cudaEventCreate(&e1), "tune event");
   const int64_t mb = int64_t(1) << 20;
-  // candidates: (w budget, stage-2 CTA target); budget 0 = all of w at once.  w
-  // blocking pays per-group pipeline fill and tail costs (measured 2x slower than one
-  // pass when the intermediate fits), so it is tried only when the whole-w
-  // intermediate is large enough to matter for memory.
-  std::vector<std::pair<int64_t, int>> cands = {{0, 152 * 4}, {0, 152 * 8}, {0, 152 * 16}};
-  if (p.pk_scr1.bytes > (int64_t(8) << 30)) cands.push_back({128 * mb, 152 * 8});
-  std::pair<int64_t, int> best = cands[0];
+  // candidates: (w budget, stage-2 CTA target, intermediate format); budget 0 = all of
+  // w at once.  w blocking pays per-group pipeline fill and tail costs (measured 2x
+  // slower than one pass when the intermediate fits), so it is tried only when the
+  // whole-w intermediate is large enough to matter for memory.  The FP32 intermediate
+  // halves its HBM bytes but adds shared-memory traffic (the on-chip split), which
+  // bounds the kernel on the measured workloads; both are timed.
+  struct Cand {
+    int64_t budget;
+    int target;
+    bool single;
+  };
+  std::vector<Cand> cands;
+  for (bool single : {false, true})
+    for (int target : {152 * 4, 152 * 8, 152 * 16}) cands.push_back({0, target, single});
+  if (p.pk_scr1.bytes > (int64_t(8) << 30)) cands.push_back({128 * mb, 152 * 8, false});
+  Cand best = cands[0];
   float best_ms = 0.0f;
   ctx.last_tuning.clear();
-  for (const auto& cand : cands) {
-    const int64_t b = cand.first;
+  for (const Cand& cand : cands) {
+    const int64_t b = cand.budget;
+    set_scr1_format(ctx, p, L, R, cand.single);
+    p.pk_scr1.buf.ensure(std::max<int64_t>(p.pk_scr1.bytes, 16), ctx.stream);
     if (b > 0) {
       build_sigma_groups(ctx, p, b);
       p.drop_graph();
       if (p.groups.size() < 2) continue;  // no blocking at this budget
     } else {
-      tile_tc(p.s2, cand.second);
+      tile_tc(p.s2, cand.target);
       p.s2.tiles_tc.upload(p.s2.h_tiles_tc, ctx.stream);
       p.s2.reduce_tc.upload(p.s2.h_reduce_tc, ctx.stream);
     }
@@ -1062,7 +1087,8 @@ static void tune_sigma_groups(Context& ctx, SigmaPlan& p) {
       cuda_check(cudaEventElapsedTime(&ms, e0, e1), "tune time");
     }
     ctx.last_tuning.push_back(double(b));
-    ctx.last_tuning.push_back(double(cand.second));
+    ctx.last_tuning.push_back(double(cand.target));
+    ctx.last_tuning.push_back(cand.single ? 1.0 : 0.0);
     ctx.last_tuning.push_back(ms);
     if (best_ms == 0.0f || ms < best_ms) {
       best = cand;
@@ -1071,17 +1097,19 @@ static void tune_sigma_groups(Context& ctx, SigmaPlan& p) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  set_scr1_format(ctx, p, L, R, best.single);
+  p.pk_scr1.buf.ensure(std::max<int64_t>(p.pk_scr1.bytes, 16), ctx.stream);
   p.drop_graph();
-  if (best.first > 0) {
-    build_sigma_groups(ctx, p, best.first);
+  if (best.budget > 0) {
+    build_sigma_groups(ctx, p, best.budget);
     p.pk_scr1.buf.release();
   } else {
     p.groups.clear();
-    tile_tc(p.s2, best.second);
+    tile_tc(p.s2, best.target);
     p.s2.tiles_tc.upload(p.s2.h_tiles_tc, ctx.stream);
     p.s2.reduce_tc.upload(p.s2.h_reduce_tc, ctx.stream);
   }
-  p.group_budget = best.first;
+  p.group_budget = best.budget;
   p.tuned_ms = best_ms;
 }
 
@@ -1105,8 +1133,9 @@ static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTe
               ctx.stream);
   if (p.group_budget < 0) {
     if (ctx.sigma_w_budget < 0) {
-      tune_sigma_groups(ctx, p);
+      tune_sigma_groups(ctx, p, L, R);
     } else if (ctx.sigma_w_budget > 0) {
+      set_scr1_format(ctx, p, L, R, ctx.sigma_fp32_intermediate);
       build_sigma_groups(ctx, p, ctx.sigma_w_budget);
       if (p.groups.size() < 2) {  // the budget does not split w: one pass
         p.groups.clear();
@@ -1116,6 +1145,8 @@ static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTe
         p.pk_scr1.buf.release();
       }
     } else {
+      set_scr1_format(ctx, p, L, R, ctx.sigma_fp32_intermediate);
+      p.pk_scr1.buf.ensure(std::max<int64_t>(p.pk_scr1.bytes, 16), ctx.stream);
       if (ctx.sigma_target_tiles > 0) {
         tile_tc(p.s2, ctx.sigma_target_tiles);
         p.s2.tiles_tc.upload(p.s2.h_tiles_tc, ctx.stream);
@@ -1137,12 +1168,12 @@ static void sigma_run_pk_whole(Context& ctx, SigmaPlan& p, double* sigma) {
   int* err = device_err_flag(ctx);
   launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.pk_scr1.buf.as<uint8_t>(),
                  p.s1.tiles_tc.get(), static_cast<int>(p.s1.h_tiles_tc.size()), p.pk_tasks1.get(), p.pk1.get(),
-                 nullptr, 1, err, ctx.stream);
+                 nullptr, p.scr1_single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx.stream);
   ctx.gemm_part.ensure(std::max<size_t>(p.s2.partial_bytes_tc(), 16), ctx.stream);
   double* part = ctx.gemm_part.as<double>();
   launch_gemm_pk(p.pk_scr1.buf.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
                  p.s2.tiles_tc.get(), static_cast<int>(p.s2.h_tiles_tc.size()), p.s2.dtasks.get(), p.pk2.get(), part,
-                 0, err, ctx.stream);
+                 kOutFP64, p.scr1_single ? 1 : 0, err, ctx.stream);
   if (p.s2.nslots_tc > 0)
     launch_gemm_pk_reduce(p.s2.reduce_tc.get(), static_cast<int>(p.s2.h_reduce_tc.size()), p.s2.dtasks.get(), 1.0,
                           part, sigma, ctx.stream);
@@ -1165,6 +1196,55 @@ static void sigma_run(Context& ctx, SigmaPlan& p, const DTensor& L, const DTenso
   }
   ctx.sigma_flops += p.flops;
   ctx.sigma_calls += 1;
+}
+
+std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& psi) {
+  SigmaPlan& p = sigma_plan(ctx, L, R, psi);
+  ensure_sigma_pk(ctx, p, L, R);
+  const double tile_flops = 2.0 * kTcTileM * kTcTileN * kPkTileK;  // one K slice of one tile
+  auto work = [&](const std::vector<DTile>& tiles, const std::vector<DPkPair>& pairs, double* slices) {
+    double s = 0.0;
+    for (const DTile& t : tiles)
+      for (int q = t.p0; q < t.p1; ++q) s += pairs[q].nks;
+    *slices = s;
+    return s * tile_flops;
+  };
+  double sl1 = 0.0, sl2 = 0.0;
+  const double w1 = work(p.s1.h_tiles_tc, p.h_pk1, &sl1);
+  const double w2 = work(p.s2.h_tiles_tc, p.h_pk2, &sl2);
+  // FLOPs with one dimension padded at a time (rows to 128, columns to 64, K to 32)
+  auto padded = [](const GemmPlan& g, double* pm, double* pn, double* pk) {
+    auto up = [](int x, int q) { return double((x + q - 1) / q * q); };
+    for (const DGemmTask& t : g.h_tasks)
+      for (int q = t.p0; q < t.p1; ++q) {
+        const double m = t.m, n = t.n, k = g.h_pairs[q].k;
+        *pm += 2.0 * up(t.m, kTcTileM) * n * k;
+        *pn += 2.0 * m * up(t.n, kTcTileN) * k;
+        *pk += 2.0 * m * n * up(g.h_pairs[q].k, kPkTileK);
+      }
+  };
+  double pm1 = 0, pn1 = 0, pk1 = 0, pm2 = 0, pn2 = 0, pk2 = 0;
+  padded(p.s1, &pm1, &pn1, &pk1);
+  padded(p.s2, &pm2, &pn2, &pk2);
+  return {p.s1.flops,
+          p.s2.flops,
+          w1,
+          w2,
+          sl1,
+          sl2,
+          double(p.s1.h_tiles_tc.size()),
+          double(p.s2.h_tiles_tc.size()),
+          double(p.pk_L.bytes),
+          double(p.pk_R.bytes),
+          double(p.pk_scr1.bytes),
+          double(p.pk_psi.bytes),
+          double(p.scr1.nnz),
+          pm1,
+          pn1,
+          pk1,
+          pm2,
+          pn2,
+          pk2};
 }
 
 void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R) {

@@ -145,6 +145,9 @@ struct SigmaPlan {
   // split-TF32 path over packed operands
   Tensor psi_layout;  // the wavefunction layout the plan was built for
   bool pk_built = false;
+  // L*psi intermediate stored as FP32 tiles split on chip (true) or as hi|lo tiles:
+  // half the HBM bytes against more shared-memory traffic; chosen by the autotuner
+  bool scr1_single = false;
   Packed pk_L, pk_R, pk_psi, pk_scr1;
   std::vector<DPkPair> h_pk1, h_pk2;
   std::vector<DGemmTask> h_pk_tasks1;
@@ -292,6 +295,7 @@ struct Context {
   // negative budget leaves the choice to the autotuner
   int64_t sigma_w_budget = -1;
   int sigma_target_tiles = 0;
+  bool sigma_fp32_intermediate = false;  // with a forced schedule: FP32 L*psi tiles
   // canonicalize routing: blocks with min(m, n) <= svd_jacobi_cols go to the batched
   // Jacobi kernel, the rest with a Gram dimension <= svd_gram_max to the batched
   // eigensolver; < 0 selects the defaults
@@ -338,6 +342,8 @@ struct PhaseTimer {
 // Packed-operand layouts of a sigma plan (built once), and one H_eff*psi of the plan
 // in the given precision (sigma += H psi) — the building blocks of batched steps.
 void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R);
+// the plan's L*psi intermediate as FP32 tiles split on chip (single) or hi|lo tiles
+void set_scr1_format(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R, bool single);
 void apply_sigma(Context& ctx, SigmaPlan& p, const DTensor& L, const DTensor& R, const double* psi, double* sigma,
                  int precision);
 
@@ -366,6 +372,10 @@ double sigma_device_time(Context& ctx, const DTensor& L, const DTensor& R, const
 
 // src/compute_diagonal_elements.hpp:65-80
 DiagPlan& diag_plan(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& diag);
+// Work and bytes of a split-precision H_eff * psi plan: useful FLOPs of both stages,
+// tensor-core tile FLOPs (tiles padded to 128 x 64, K slices of 32), K slices, tiles,
+// packed bytes of L, R, the L*psi intermediate and psi, and the intermediate's size.
+std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& psi);
 // Plans by layout (no device data read): cached, safe on planning threads.
 const MergePlan& merge_plan(Context& ctx, bool forward, const DTensor& mpo, const Tensor& opr);
 RenormPlan& renorm_plan(Context& ctx, bool forward, const Tensor& opr0, const Tensor& bra, const Tensor& ket);

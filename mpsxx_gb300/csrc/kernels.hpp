@@ -95,6 +95,10 @@ constexpr int kTcTileN = 64;
 // ---- pre-packed split-TF32 operands -----------------------------------------
 constexpr int kPkTileK = 32;                          // K elements per packed slice
 constexpr uint32_t kPkTileABytes = 128 * 32 * 4 * 2;  // A tile: hi|lo TF32, 128 rows
+constexpr uint32_t kPkTileA1Bytes = 128 * 32 * 4;     // A tile as FP32 values, split on chip
+// launch_gemm_pk outputs: FP64 C (or split-K partials), packed hi|lo A tiles, packed
+// FP32 A tiles (the next GEMM splits them in shared memory)
+constexpr int kOutFP64 = 0, kOutPackedSplit = 1, kOutPackedSingle = 2;
 constexpr uint32_t kPkTileBBytes = 64 * 32 * 4 * 2;   // B tile: hi|lo TF32, 64 rows
 
 // One (A, B) pair over packed operands: byte offsets of the blocks' tile grids.
@@ -109,11 +113,13 @@ struct DPack {
   int rows, k, ld, trans, tile_rows, tr, tk, pad;
 };
 
-// out_packed: C is written as packed A tiles of the next GEMM (c_off = byte offset of
-// the block's grid, ldc = its K slices per row tile) instead of FP64 C / partials.
+// out_packed (kOut*): C is written as packed A tiles of the next GEMM (c_off = byte
+// offset of the block's grid, ldc = its K slices per row tile) instead of FP64 C /
+// partials.  a_single: the A tiles are FP32 (kPkTileA1Bytes each), split into hi|lo
+// in shared memory before the MMAs; otherwise packed hi|lo (kPkTileABytes).
 void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
-                    int out_packed, int* err, cudaStream_t st);
+                    int out_packed, int a_single, int* err, cudaStream_t st);
 void launch_gemm_pk_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
                            double* C, cudaStream_t st);
 void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst, cudaStream_t st);

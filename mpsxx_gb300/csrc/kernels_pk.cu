@@ -7,14 +7,22 @@
 // no-swizzle core-matrix layout the MMA descriptors address (8 rows x 16 bytes per
 // core matrix).  hi = tf32(x), lo = tf32(x - hi); a product is hi*hi + hi*lo + lo*hi.
 //
+// An intermediate that one GEMM writes and the next reads once (stage 1 -> stage 2 of
+// H_eff * psi) is stored as FP32 values instead (16 KB A tiles, half the bytes) and
+// split on chip: hi and lo from an FP32 value carry no more than the value itself.
+//
 // GEMM CTA (256 threads, warp-specialised):
 //   warp 0 lane 0 : producer — per K slice, one bulk copy (TMA engine) of the A tile
 //                   and one of the B tile into a 4-stage shared-memory ring,
 //                   completion counted in bytes on the stage's "full" mbarrier;
-//   warp 1 lane 0 : MMA issuer — 4 K-steps x 3 products of tcgen05.mma kind::tf32
-//                   per slice into one of two TMEM accumulators (one per block pair,
-//                   alternating), commits release the stage ("empty") and, at the end
-//                   of a pair, hand the accumulator to the epilogue ("acc_full");
+//   warps 2-3     : (FP32 A tiles only) converter — split the landed A tile in place
+//                   into hi | lo, fence it for the tensor core (async proxy) and mark
+//                   the stage "converted";
+//   warp 1 lane 0 : MMA issuer — per K-step of 8, A_hi x [B_hi; B_lo] (N = 128) and
+//                   A_lo x B_hi (N = 64), tcgen05.mma kind::tf32, into one of two TMEM
+//                   accumulators (alternating per group of block pairs); commits
+//                   release the stage ("empty") and, at the end of a group, hand the
+//                   accumulator to the epilogue ("acc_full");
 //   warps 4-7     : epilogue — per pair, tcgen05.ld of the FP32 accumulator into FP64
 //                   registers (FP32 rounding spans one block pair), then release it
 //                   ("acc_empty"); at the end write FP64 C (+=), an FP64 split-K
@@ -37,10 +45,18 @@ constexpr int BK = kPkTileK;  // 32
 constexpr int NTHREADS = 256;
 constexpr int STAGES = 4;
 constexpr uint32_t A_BYTES = kPkTileABytes;  // 32 KB
+constexpr uint32_t A1_BYTES = kPkTileA1Bytes;  // 16 KB (FP32 A tile)
+constexpr int CONV_THREADS = 64;               // warps 2-3
 constexpr uint32_t B_BYTES = kPkTileBBytes;  // 16 KB
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
-constexpr uint32_t TMEM_COLS = 128;  // two 64-column FP32 accumulators
+// Each K step is two MMAs: A_hi x [B_hi; B_lo] as one N = 128 operand (the packed B
+// tile is exactly that: hi rows then lo rows) into accumulator columns [0, 128), and
+// A_lo x B_hi (N = 64) into columns [0, 64).  The product is then columns
+// [0, 64) + [64, 128).  Fewer, wider MMAs read fewer operand bytes from shared memory,
+// whose bandwidth (with the bulk copies and the on-chip split) bounds the kernel.
+constexpr uint32_t ACC_COLS = 2 * BN;             // one accumulator: 128 columns
+constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;       // two accumulators
 // Consecutive block pairs of a tile accumulate in the FP32 tensor-memory tile until
 // their summed contraction length reaches FLUSH_K; then the group is flushed into
 // the FP64 accumulators.  This bounds the FP32 accumulation length (rounding ~
@@ -79,8 +95,8 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
-__host__ __device__ constexpr uint32_t tf32_idesc() {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+__host__ __device__ constexpr uint32_t tf32_idesc(int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
@@ -158,11 +174,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     gemm_pk_kernel(const uint8_t* __restrict__ Apk, const uint8_t* __restrict__ Bpk, double alpha,
                    double* __restrict__ C, uint8_t* __restrict__ Cpk, const DTile* __restrict__ tiles, int ntiles,
                    const DGemmTask* __restrict__ tasks, const DPkPair* __restrict__ pairs,
-                   double* __restrict__ partial, int out_packed, int* __restrict__ err, uint64_t timeout_ns) {
+                   double* __restrict__ partial, int out_packed, int a_single, int* __restrict__ err,
+                   uint64_t timeout_ns) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t conv_bar[STAGES];
   __shared__ __align__(8) uint64_t accf_bar[2];
   __shared__ __align__(8) uint64_t acce_bar[2];
   __shared__ uint32_t tmem_slot;
@@ -179,6 +197,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(smem_u32(&full_bar[s]), 1);
       mbar_init(smem_u32(&empty_bar[s]), 1);
+      mbar_init(smem_u32(&conv_bar[s]), CONV_THREADS);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(smem_u32(&accf_bar[b]), 1);
@@ -192,6 +211,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_slot;
   const uint64_t deadline = global_ns() + timeout_ns;
+  const uint32_t a_bytes = a_single ? A1_BYTES : A_BYTES;  // A tile in global memory
 
   // Persistent: the CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...; every
   // role walks the same sequence, so slice and pair counters continue across tiles.
@@ -199,18 +219,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // ---------------- producer ----------------
     if (lane == 0) {
       int slice = 0;
+      // descriptors are loaded one pair (and one tile) ahead, so that their latency
+      // hides behind the current pair's copies
+      DTile t_next = blockIdx.x < ntiles ? tiles[blockIdx.x] : DTile{};
       for (int ti = blockIdx.x; ti < ntiles && !abort_flag; ti += gridDim.x) {
-        const DTile t = tiles[ti];
+        const DTile t = t_next;
+        if (ti + (int)gridDim.x < ntiles) t_next = tiles[ti + gridDim.x];
+        DPkPair pr_next = t.p0 < t.p1 ? pairs[t.p0] : DPkPair{};
         for (int p = t.p0; p < t.p1 && !abort_flag; ++p) {
-          const DPkPair pr = pairs[p];
+          const DPkPair pr = pr_next;
+          if (p + 1 < t.p1) pr_next = pairs[p + 1];
           for (int ks = 0; ks < pr.nks; ++ks, ++slice) {
             const int s = slice % STAGES;
             const uint32_t round = slice / STAGES;
             if (!mbar_wait(smem_u32(&empty_bar[s]), (round & 1u) ^ 1u, deadline, &abort_flag)) break;
             const uint32_t fb = smem_u32(&full_bar[s]);
-            mbar_expect_tx(fb, STAGE_BYTES);
+            mbar_expect_tx(fb, a_bytes + B_BYTES);
             const uint32_t dst = smem_u32(ring + s * STAGE_BYTES);
-            bulk_g2s(dst, Apk + pr.a_pk + ((int64_t)t.tm * pr.nks + ks) * A_BYTES, A_BYTES, fb);
+            bulk_g2s(dst, Apk + pr.a_pk + ((int64_t)t.tm * pr.nks + ks) * a_bytes, a_bytes, fb);
             bulk_g2s(dst + A_BYTES, Bpk + pr.b_pk + ((int64_t)t.tn * pr.nks + ks) * B_BYTES, B_BYTES, fb);
           }
         }
@@ -219,15 +245,28 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc = tf32_idesc();
+      const uint32_t idesc_w = tf32_idesc(2 * BN), idesc = tf32_idesc(BN);
       const uint32_t lbo = 128, sbo = (BK / 4) * 128;
+      // Descriptors of the stages' A and B tiles, built once: the start address sits in
+      // the low 14 bits (address >> 4), so the K steps and the lo halves are immediate
+      // additions (every shared address stays below 2^18: no carry out of the field).
+      uint64_t dA[STAGES], dB[STAGES];
+#pragma unroll
+      for (int s = 0; s < STAGES; ++s) {
+        dA[s] = smem_desc(smem_u32(ring + s * STAGE_BYTES), lbo, sbo);
+        dB[s] = smem_desc(smem_u32(ring + s * STAGE_BYTES + A_BYTES), lbo, sbo);
+      }
       int slice = 0, gc = 0;
       bool ok = true;
+      DTile t_next = blockIdx.x < ntiles ? tiles[blockIdx.x] : DTile{};
       for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
-        const DTile t = tiles[ti];
+        const DTile t = t_next;
+        if (ti + (int)gridDim.x < ntiles) t_next = tiles[ti + gridDim.x];
         int kacc = 0;
+        int nks_next = t.p0 < t.p1 ? pairs[t.p0].nks : 0;
         for (int p = t.p0; p < t.p1 && ok; ++p) {
-          const DPkPair pr = pairs[p];
+          const int nks = nks_next;
+          if (p + 1 < t.p1) nks_next = pairs[p + 1].nks;
           const int b = gc & 1;
           const bool group_start = (kacc == 0);
           if (group_start) {
@@ -238,36 +277,87 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
           }
-          const uint32_t d = tmem + b * BN;
-          for (int ks = 0; ks < pr.nks; ++ks, ++slice) {
+          const uint32_t d = tmem + b * ACC_COLS;
+          for (int ks = 0; ks < nks; ++ks, ++slice) {
+            const int s = slice % STAGES;
+            const uint32_t round = slice / STAGES;
+            if (!mbar_wait(smem_u32(a_single ? &conv_bar[s] : &full_bar[s]), round & 1u, deadline, &abort_flag)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            uint64_t a0d = dA[0], b0d = dB[0];
+#pragma unroll
+            for (int q = 1; q < STAGES; ++q)
+              if (s == q) {
+                a0d = dA[q];
+                b0d = dB[q];
+              }
+#pragma unroll
+            for (int kk = 0; kk < BK / 8; ++kk) {
+              const uint64_t koff = (uint64_t)(kk * 256) >> 4;
+              const uint64_t ah = a0d + koff;
+              const uint64_t al = a0d + ((A_BYTES / 2) >> 4) + koff;
+              const uint64_t bh = b0d + koff;
+              const uint64_t bl = b0d + ((B_BYTES / 2) >> 4) + koff;
+              mma_tf32(d, ah, bh, idesc_w, (group_start && ks == 0 && kk == 0) ? 0u : 1u);
+              mma_tf32(d, al, bh, idesc, 1u);
+              (void)bl;
+            }
+            mma_commit(smem_u32(&empty_bar[s]));  // stage free once these MMAs completed
+          }
+          if (!ok) break;
+          kacc += nks * BK;
+          if (group_ends(kacc, p, t.p1 - 1)) {
+            mma_commit(smem_u32(&accf_bar[b]));  // group accumulated
+            ++gc;
+            kacc = 0;
+          }
+        }
+      }
+    }
+  } else if (warp == 2 || warp == 3) {
+    // ---------------- converter (FP32 A tiles) ----------------
+    if (a_single) {
+      const int ct = threadIdx.x - 64;
+      int slice = 0;
+      bool ok = true;
+      DTile t_next = blockIdx.x < ntiles ? tiles[blockIdx.x] : DTile{};
+      for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+        const DTile t = t_next;
+        if (ti + (int)gridDim.x < ntiles) t_next = tiles[ti + gridDim.x];
+        int nks_next = t.p0 < t.p1 ? pairs[t.p0].nks : 0;
+        for (int p = t.p0; p < t.p1 && ok; ++p) {
+          const int nks = nks_next;
+          if (p + 1 < t.p1) nks_next = pairs[p + 1].nks;
+          for (int ks = 0; ks < nks; ++ks, ++slice) {
             const int s = slice % STAGES;
             const uint32_t round = slice / STAGES;
             if (!mbar_wait(smem_u32(&full_bar[s]), round & 1u, deadline, &abort_flag)) {
               ok = false;
               break;
             }
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t a0 = smem_u32(ring + s * STAGE_BYTES);
-            const uint32_t b0 = a0 + A_BYTES;
-#pragma unroll
-            for (int kk = 0; kk < BK / 8; ++kk) {
-              const uint32_t koff = kk * 256;
-              const uint64_t ah = smem_desc(a0 + koff, lbo, sbo);
-              const uint64_t al = smem_desc(a0 + A_BYTES / 2 + koff, lbo, sbo);
-              const uint64_t bh = smem_desc(b0 + koff, lbo, sbo);
-              const uint64_t bl = smem_desc(b0 + B_BYTES / 2 + koff, lbo, sbo);
-              mma_tf32(d, ah, bh, idesc, (group_start && ks == 0 && kk == 0) ? 0u : 1u);
-              mma_tf32(d, ah, bl, idesc, 1u);
-              mma_tf32(d, al, bh, idesc, 1u);
+            // element-wise, so the core-matrix layout carries over: hi in place, lo
+            // at the same offset in the second half of the A region
+            uint4* hi = reinterpret_cast<uint4*>(ring + s * STAGE_BYTES);
+            uint4* lo = reinterpret_cast<uint4*>(ring + s * STAGE_BYTES + A_BYTES / 2);
+#pragma unroll 4
+            for (int i = ct; i < static_cast<int>(A1_BYTES / 16); i += CONV_THREADS) {
+              const uint4 x = hi[i];
+              uint4 h, l;
+              h.x = tf32_rna(__uint_as_float(x.x));
+              h.y = tf32_rna(__uint_as_float(x.y));
+              h.z = tf32_rna(__uint_as_float(x.z));
+              h.w = tf32_rna(__uint_as_float(x.w));
+              l.x = tf32_rna(__uint_as_float(x.x) - __uint_as_float(h.x));
+              l.y = tf32_rna(__uint_as_float(x.y) - __uint_as_float(h.y));
+              l.z = tf32_rna(__uint_as_float(x.z) - __uint_as_float(h.z));
+              l.w = tf32_rna(__uint_as_float(x.w) - __uint_as_float(h.w));
+              hi[i] = h;
+              lo[i] = l;
             }
-            mma_commit(smem_u32(&empty_bar[s]));  // stage free once these MMAs completed
-          }
-          if (!ok) break;
-          kacc += pr.nks * BK;
-          if (group_ends(kacc, p, t.p1 - 1)) {
-            mma_commit(smem_u32(&accf_bar[b]));  // group accumulated
-            ++gc;
-            kacc = 0;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(smem_u32(&conv_bar[s]));
           }
         }
       }
@@ -297,24 +387,45 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * BN;
-          uint8_t* tile0 = Cpk + task.c_off + ((int64_t)t.tm * task.ldc + 2 * t.tn) * A_BYTES;
+          const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * ACC_COLS;
+          const bool single = out_packed == kOutPackedSingle;
+          const uint32_t ot_bytes = single ? A1_BYTES : A_BYTES;  // output tile
+          uint8_t* tile0 = Cpk + task.c_off + ((int64_t)t.tm * task.ldc + 2 * t.tn) * ot_bytes;
           const float fa = static_cast<float>(alpha);
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
-            float v[BK];
+            float v[BK], w[BK];
             tmem_ld16(taddr + h * BK, v);
             tmem_ld16(taddr + h * BK + 16, v + 16);
+            tmem_ld16(taddr + BN + h * BK, w);
+            tmem_ld16(taddr + BN + h * BK + 16, w + 16);
             asm volatile("tcgen05.wait::ld.sync.aligned;");
-            if (2 * t.tn + h >= task.ldc) continue;
-            uint8_t* tile = tile0 + h * A_BYTES;
 #pragma unroll
-            for (int kk = 0; kk < BK; ++kk) {
-              const float x = fa * v[kk];
-              const uint32_t hi = tf32_rna(x);
-              const uint32_t lo = tf32_rna(x - __uint_as_float(hi));
-              *reinterpret_cast<uint32_t*>(tile + core_off(row, kk)) = hi;
-              *reinterpret_cast<uint32_t*>(tile + A_BYTES / 2 + core_off(row, kk)) = lo;
+            for (int kk = 0; kk < BK; ++kk) v[kk] += w[kk];
+            if (2 * t.tn + h >= task.ldc) continue;
+            uint8_t* tile = tile0 + h * ot_bytes;
+            // 16-byte stores: k .. k+3 of a row are contiguous in the core-matrix
+            // layout, and a warp's 32 rows fill four whole 128-byte lines
+            if (single) {
+#pragma unroll
+              for (int kk = 0; kk < BK; kk += 4)
+                *reinterpret_cast<float4*>(tile + core_off(row, kk)) =
+                    make_float4(fa * v[kk], fa * v[kk + 1], fa * v[kk + 2], fa * v[kk + 3]);
+            } else {
+#pragma unroll
+              for (int kk = 0; kk < BK; kk += 4) {
+                uint4 hi, lo;
+                uint32_t* h = &hi.x;
+                uint32_t* l = &lo.x;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                  const float x = fa * v[kk + e];
+                  h[e] = tf32_rna(x);
+                  l[e] = tf32_rna(x - __uint_as_float(h[e]));
+                }
+                *reinterpret_cast<uint4*>(tile + core_off(row, kk)) = hi;
+                *reinterpret_cast<uint4*>(tile + A_BYTES / 2 + core_off(row, kk)) = lo;
+              }
             }
           }
           asm volatile("tcgen05.fence::before_thread_sync;");
@@ -337,14 +448,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * BN;
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * ACC_COLS;
 #pragma unroll
         for (int c0 = 0; c0 < BN; c0 += 16) {
-          float v[16];
+          float v[16], w[16];
           tmem_ld16(taddr + c0, v);
+          tmem_ld16(taddr + BN + c0, w);
           asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-          for (int i = 0; i < 16; ++i) acc[c0 + i] += static_cast<double>(v[i]);
+          for (int i = 0; i < 16; ++i) acc[c0 + i] += static_cast<double>(v[i] + w[i]);
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
         mbar_arrive(smem_u32(&acce_bar[b]));
@@ -426,7 +538,7 @@ int pk_smem_bytes() { return SMEM_BYTES; }
 
 void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
-                    int out_packed, int* err, cudaStream_t st) {
+                    int out_packed, int a_single, int* err, cudaStream_t st) {
   if (ntiles <= 0) return;
   static int nsm = 0;
   if (nsm == 0) {
@@ -440,7 +552,7 @@ void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double
   const uint64_t timeout_ns = 20000000000ull;  // 20 s
   const int grid = ntiles < nsm ? ntiles : nsm;
   gemm_pk_kernel<<<grid, NTHREADS, SMEM_BYTES, st>>>(Apk, Bpk, alpha, C, Cpk, tiles, ntiles, tasks, pairs, partial,
-                                                     out_packed, err, timeout_ns);
+                                                     out_packed, a_single, err, timeout_ns);
 }
 
 void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst, cudaStream_t st) {

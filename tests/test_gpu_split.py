@@ -164,11 +164,13 @@ def test_split_renormalize_matches_fp64_qc_bond(ctx):
         assert err < 2e-6
 
 
-@pytest.mark.parametrize("schedule", [(0, 152 * 4), (256 * 1024, 0), (4 * 1024 * 1024, 152 * 2)])
+@pytest.mark.parametrize("schedule", [(0, 152 * 4, False), (256 * 1024, 0, False), (4 * 1024 * 1024, 152 * 2, False),
+                                      (0, 152 * 8, True), (256 * 1024, 0, True)])
 def test_split_sigma_schedules_agree(ctx, schedule):
     """Every schedule of the split H_eff*psi (one pass over w with different split-K
     targets, and w processed in groups out of an L2-sized scratch, through the CUDA
-    graph) gives the same result as FP64 within 2e-6."""
+    graph; the L*psi intermediate as hi|lo tiles or as FP32 tiles split on chip) gives
+    the same result as FP64 within 2e-6."""
     from mpsxx_gb300 import core, dmrg, mpogen
 
     h, eri = mpogen.synthetic_qc_integrals(8, 16, 5)
