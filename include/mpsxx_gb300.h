@@ -157,7 +157,8 @@ int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, con
  * included), K slices of stage 1 and 2, tiles of stage 1 and 2, packed bytes of lopr,
  * ropr, the L*psi intermediate and wfn, and the intermediate's element count;
  * out[13..18] = FLOPs of stage 1 and then stage 2 with only the rows (to 128), only
- * the columns (to 64) or only K (to 32) padded. */
+ * the columns (to 64) or only K (to 32) padded; out[19..20] = tile FLOPs of stage 1
+ * and 2 were a block's last row tile 64 rows high where its remainder fits. */
 int mpsxx_sigma_plan_stats(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                            const mpsxx_tensor* wfn, double* out, int n, int* count);
 

@@ -277,7 +277,8 @@ SIGMA_PLAN_KEYS = ("flops_stage1", "flops_stage2", "tile_flops_stage1", "tile_fl
                    "slices_stage2", "tiles_stage1", "tiles_stage2", "packed_bytes_L", "packed_bytes_R",
                    "packed_bytes_intermediate", "packed_bytes_psi", "intermediate_elements",
                    "flops_rows_padded_stage1", "flops_cols_padded_stage1", "flops_k_padded_stage1",
-                   "flops_rows_padded_stage2", "flops_cols_padded_stage2", "flops_k_padded_stage2")
+                   "flops_rows_padded_stage2", "flops_cols_padded_stage2", "flops_k_padded_stage2",
+                   "tile_flops_64row_tail_stage1", "tile_flops_64row_tail_stage2")
 
 
 def sigma_plan_stats(ctx: Context, lopr: Tensor, ropr: Tensor, wfn: Tensor) -> dict:

@@ -499,6 +499,7 @@ static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a,
 // c + #SM, ...), so this is a longest-processing-time-first balance.
 static void tile_tc(GemmPlan& plan, int target_ctas) {
   make_tiles(plan, kTcTileM, kTcTileN, plan.h_tiles_tc, plan.h_reduce_tc, plan.nslots_tc, target_ctas);
+  for (DTile& t : plan.h_tiles_tc) t.h64 = tail64(plan.h_tasks[t.task].m, t.tm) ? 1 : 0;
   std::vector<std::pair<int64_t, int>> work(plan.h_tiles_tc.size());
   for (size_t i = 0; i < plan.h_tiles_tc.size(); ++i) {
     int64_t w = 0;
@@ -687,11 +688,17 @@ struct Orient {
   int rows, k, ld, trans;
 };
 
+// Packed tile grid of an operand: per block, row tiles x K slices, row tile tr slice tk
+// at base + (tr * nks + tk) * tile_bytes.  A operands (128-row tiles) end in a compact
+// 64-row tile where tail64 says so: its slices at base + tr * nks * tile_bytes +
+// tk * tile_bytes / 2 (the pack kernel gets tile_rows 64 and row tile 2 tr, which
+// starts at the same row).
 template <class F>
 static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t tile_bytes, F orient) {
   P.base.assign(t.tags.size(), -1);
   P.nks.assign(t.tags.size(), 0);
   P.h_packs.clear();
+  const bool a_operand = tile_rows == kTcTileM;
   int64_t off = 0;
   for (size_t b = 0; b < t.tags.size(); ++b) {
     const Orient o = orient(static_cast<int32_t>(b));
@@ -700,11 +707,19 @@ static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t ti
     const int nks = (o.k + kPkTileK - 1) / kPkTileK;
     P.base[b] = off;
     P.nks[b] = nks;
-    for (int tr = 0; tr < ntr; ++tr)
-      for (int tk = 0; tk < nks; ++tk)
-        P.h_packs.push_back(DPack{t.offsets[b], off + (int64_t(tr) * nks + tk) * tile_bytes, o.rows, o.k, o.ld,
-                                  o.trans, tile_rows, tr, tk, 0});
-    off += int64_t(ntr) * nks * tile_bytes;
+    for (int tr = 0; tr < ntr; ++tr) {
+      const bool t64 = a_operand && tail64(o.rows, tr);
+      for (int tk = 0; tk < nks; ++tk) {
+        if (t64)
+          P.h_packs.push_back(DPack{t.offsets[b], off + int64_t(tr) * nks * tile_bytes + int64_t(tk) * (tile_bytes / 2),
+                                    o.rows, o.k, o.ld, o.trans, 64, 2 * tr, tk, 0});
+        else
+          P.h_packs.push_back(DPack{t.offsets[b], off + (int64_t(tr) * nks + tk) * tile_bytes, o.rows, o.k, o.ld,
+                                    o.trans, tile_rows, tr, tk, 0});
+      }
+    }
+    const bool last64 = a_operand && tail64(o.rows, ntr - 1);
+    off += int64_t(ntr - (last64 ? 1 : 0)) * nks * tile_bytes + (last64 ? int64_t(nks) * (tile_bytes / 2) : 0);
   }
   P.bytes = off;
 }
@@ -831,8 +846,12 @@ static void build_sigma_groups(Context& ctx, SigmaPlan& p, int64_t budget) {
     s.sh.index(s.tags[b], idx);
     blk_w[b] = idx[1];
     if (p.pk_scr1.base[b] < 0) continue;
-    const int64_t ntr = (int64_t(d[0]) * d[1] + kTcTileM - 1) / kTcTileM;
-    blk_bytes[b] = ntr * p.pk_scr1.nks[b] * (p.scr1_single ? kPkTileA1Bytes : kPkTileABytes);
+    const int rows = d[0] * d[1];
+    const int64_t ntr = (rows + kTcTileM - 1) / kTcTileM;
+    const int64_t tb = p.scr1_single ? kPkTileA1Bytes : kPkTileABytes;
+    // as packed_layout: a compact 64-row tail tile takes half a tile's bytes
+    blk_bytes[b] = (ntr - (tail64(rows, ntr - 1) ? 1 : 0)) * p.pk_scr1.nks[b] * tb +
+                   (tail64(rows, ntr - 1) ? p.pk_scr1.nks[b] * (tb / 2) : 0);
     w_bytes[idx[1]] += blk_bytes[b];
   }
   std::vector<int> group_of_w(nw, 0);
@@ -921,10 +940,11 @@ static void build_sigma_groups(Context& ctx, SigmaPlan& p, int64_t budget) {
       for (int tm = 0; tm * kTcTileM < dt.m; ++tm)
         for (int tn = 0; tn * kTcTileN < dt.n; ++tn) {
           if (nc == 1) {
-            t2[g].push_back(DTile{r.task, tm, tn, bnd[0], bnd[1], -1});
+            t2[g].push_back(DTile{r.task, tm, tn, bnd[0], bnd[1], -1, tail64(dt.m, tm) ? 1 : 0});
             continue;
           }
-          for (int ch = 0; ch < nc; ++ch) t2[g].push_back(DTile{r.task, tm, tn, bnd[ch], bnd[ch + 1], slots[g] + ch});
+          for (int ch = 0; ch < nc; ++ch)
+            t2[g].push_back(DTile{r.task, tm, tn, bnd[ch], bnd[ch + 1], slots[g] + ch, tail64(dt.m, tm) ? 1 : 0});
           red[g].push_back(DReduce{r.task, tm, tn, slots[g], nc, 0});
           slots[g] += nc;
         }
@@ -1226,6 +1246,17 @@ std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor
   double pm1 = 0, pn1 = 0, pk1 = 0, pm2 = 0, pn2 = 0, pk2 = 0;
   padded(p.s1, &pm1, &pn1, &pk1);
   padded(p.s2, &pm2, &pn2, &pk2);
+  // tile FLOPs if a block's last row tile were 64 rows high where its remainder fits
+  auto tile64 = [](const GemmPlan& g) {
+    double s = 0.0;
+    for (const DGemmTask& t : g.h_tasks) {
+      const int full = t.m / kTcTileM, rem = t.m % kTcTileM;
+      const double rows = double(full) * kTcTileM + (rem == 0 ? 0 : rem <= 64 ? 64 : kTcTileM);
+      const double cols = double((t.n + kTcTileN - 1) / kTcTileN * kTcTileN);
+      for (int q = t.p0; q < t.p1; ++q) s += 2.0 * rows * cols * ((g.h_pairs[q].k + kPkTileK - 1) / kPkTileK * kPkTileK);
+    }
+    return s;
+  };
   return {p.s1.flops,
           p.s2.flops,
           w1,
@@ -1244,7 +1275,9 @@ std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor
           pk1,
           pm2,
           pn2,
-          pk2};
+          pk2,
+          tile64(p.s1),
+          tile64(p.s2)};
 }
 
 void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R) {

@@ -23,6 +23,7 @@ struct DGemmPair {
 // reduction adds into C (split-K for tasks with long pair lists).
 struct DTile {
   int task, tm, tn, p0, p1, slot;
+  int h64;  // tensor-core tiles: the A rows are a block's 64-row tail tile (see tail64)
 };
 // Reduction of the split partials of one output tile.
 struct DReduce {
@@ -93,6 +94,12 @@ constexpr int kTcTileM = 128;
 constexpr int kTcTileN = 64;
 
 // ---- pre-packed split-TF32 operands -----------------------------------------
+// A block of `rows` rows used as a tensor-core A operand is cut into 128-row tiles; a
+// last tile whose rows fit in 64 is a 64-row tile instead (packed compact, half the
+// bytes, M = 64 MMAs): row tile tm of the block is such a tile when this holds.
+__host__ __device__ constexpr bool tail64(int rows, int tm) {
+  return rows % 128 != 0 && rows % 128 <= 64 && tm == rows / 128;
+}
 constexpr int kPkTileK = 32;                          // K elements per packed slice
 constexpr uint32_t kPkTileABytes = 128 * 32 * 4 * 2;  // A tile: hi|lo TF32, 128 rows
 constexpr uint32_t kPkTileA1Bytes = 128 * 32 * 4;     // A tile as FP32 values, split on chip

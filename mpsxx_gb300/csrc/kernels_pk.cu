@@ -95,8 +95,8 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
-__host__ __device__ constexpr uint32_t tf32_idesc(int n) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+__host__ __device__ constexpr uint32_t tf32_idesc(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
@@ -234,9 +234,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t round = slice / STAGES;
             if (!mbar_wait(smem_u32(&empty_bar[s]), (round & 1u) ^ 1u, deadline, &abort_flag)) break;
             const uint32_t fb = smem_u32(&full_bar[s]);
-            mbar_expect_tx(fb, a_bytes + B_BYTES);
+            // a 64-row tail tile is packed compact: half the bytes; its hi and lo
+            // halves (split format) land where the MMA expects a 128-row tile's
+            const uint32_t at = t.h64 ? a_bytes / 2 : a_bytes;
+            mbar_expect_tx(fb, at + B_BYTES);
             const uint32_t dst = smem_u32(ring + s * STAGE_BYTES);
-            bulk_g2s(dst, Apk + pr.a_pk + ((int64_t)t.tm * pr.nks + ks) * a_bytes, a_bytes, fb);
+            const uint8_t* asrc = Apk + pr.a_pk + (int64_t)t.tm * pr.nks * a_bytes + (int64_t)ks * at;
+            if (t.h64 && !a_single) {
+              bulk_g2s(dst, asrc, at / 2, fb);
+              bulk_g2s(dst + A_BYTES / 2, asrc + at / 2, at / 2, fb);
+            } else {
+              bulk_g2s(dst, asrc, at, fb);
+            }
             bulk_g2s(dst + A_BYTES, Bpk + pr.b_pk + ((int64_t)t.tn * pr.nks + ks) * B_BYTES, B_BYTES, fb);
           }
         }
@@ -245,7 +254,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc_w = tf32_idesc(2 * BN), idesc = tf32_idesc(BN);
+      const uint32_t idesc_w128 = tf32_idesc(BM, 2 * BN), idesc_128 = tf32_idesc(BM, BN);
+      const uint32_t idesc_w64 = tf32_idesc(64, 2 * BN), idesc_64 = tf32_idesc(64, BN);
       const uint32_t lbo = 128, sbo = (BK / 4) * 128;
       // Descriptors of the stages' A and B tiles, built once: the start address sits in
       // the low 14 bits (address >> 4), so the K steps and the lo halves are immediate
@@ -262,6 +272,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
         const DTile t = t_next;
         if (ti + (int)gridDim.x < ntiles) t_next = tiles[ti + gridDim.x];
+        const uint32_t idesc_w = t.h64 ? idesc_w64 : idesc_w128, idesc = t.h64 ? idesc_64 : idesc_128;
         int kacc = 0;
         int nks_next = t.p0 < t.p1 ? pairs[t.p0].nks : 0;
         for (int p = t.p0; p < t.p1 && ok; ++p) {
@@ -341,8 +352,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // at the same offset in the second half of the A region
             uint4* hi = reinterpret_cast<uint4*>(ring + s * STAGE_BYTES);
             uint4* lo = reinterpret_cast<uint4*>(ring + s * STAGE_BYTES + A_BYTES / 2);
+            const int n16 = static_cast<int>(A1_BYTES / 16) >> (t.h64 ? 1 : 0);  // rows 0-63 only
 #pragma unroll 4
-            for (int i = ct; i < static_cast<int>(A1_BYTES / 16); i += CONV_THREADS) {
+            for (int i = ct; i < n16; i += CONV_THREADS) {
               const uint4 x = hi[i];
               uint4 h, l;
               h.x = tf32_rna(__uint_as_float(x.x));
@@ -365,12 +377,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp >= 4) {
     // ---------------- epilogue ----------------
     const int q = warp - 4;  // TMEM lane quarter
-    const int row = q * 32 + lane;
     int gc = 0;
     bool ok = true;
     for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
       const DTile t = tiles[ti];
       const DGemmTask task = tasks[t.task];
+      // the tile row this thread's TMEM lane holds: 128-row tiles, lane 32 q + i holds
+      // row 32 q + i; M = 64 tiles, lane 32 q + i holds row 16 q + i for i < 16 (and
+      // nothing for i >= 16); -1: no row
+      const int row = t.h64 ? (lane < 16 ? q * 16 + lane : -1) : q * 32 + lane;
       const int r = t.tm * BM + row;
       if (out_packed) {
         // stage-1 output (one group): FP32 straight from tensor memory, re-split into
@@ -389,8 +404,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * ACC_COLS;
           const bool single = out_packed == kOutPackedSingle;
-          const uint32_t ot_bytes = single ? A1_BYTES : A_BYTES;  // output tile
-          uint8_t* tile0 = Cpk + task.c_off + ((int64_t)t.tm * task.ldc + 2 * t.tn) * ot_bytes;
+          const uint32_t ot_bytes = single ? A1_BYTES : A_BYTES;  // output tile (128 rows)
+          // the next GEMM's A tile grid for this row tile: a 64-row tail tile is
+          // compact (half the bytes, its lo half a quarter tile in)
+          const uint32_t ts = t.h64 ? ot_bytes / 2 : ot_bytes;
+          const uint32_t lo_off = ts / 2;
+          uint8_t* tile0 = Cpk + task.c_off + (int64_t)t.tm * task.ldc * ot_bytes + (int64_t)(2 * t.tn) * ts;
           const float fa = static_cast<float>(alpha);
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
@@ -402,8 +421,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
             for (int kk = 0; kk < BK; ++kk) v[kk] += w[kk];
-            if (2 * t.tn + h >= task.ldc) continue;
-            uint8_t* tile = tile0 + h * ot_bytes;
+            if (2 * t.tn + h >= task.ldc || row < 0) continue;
+            uint8_t* tile = tile0 + h * ts;
             // 16-byte stores: k .. k+3 of a row are contiguous in the core-matrix
             // layout, and a warp's 32 rows fill four whole 128-byte lines
             if (single) {
@@ -424,7 +443,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                   l[e] = tf32_rna(x - __uint_as_float(h[e]));
                 }
                 *reinterpret_cast<uint4*>(tile + core_off(row, kk)) = hi;
-                *reinterpret_cast<uint4*>(tile + A_BYTES / 2 + core_off(row, kk)) = lo;
+                *reinterpret_cast<uint4*>(tile + lo_off + core_off(row, kk)) = lo;
               }
             }
           }
@@ -463,6 +482,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         ++gc;
       }
       if (!ok) break;
+      if (row < 0) continue;  // lanes without a row in an M = 64 tile
       if (t.slot >= 0) {
         double* part = partial + (int64_t)t.slot * (BM * BN) + (int64_t)row * BN;
 #pragma unroll
