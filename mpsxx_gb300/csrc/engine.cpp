@@ -499,7 +499,10 @@ static void build_plan_impl(GemmPlan& plan, Trans ta, Trans tb, const Tensor& a,
 // c + #SM, ...), so this is a longest-processing-time-first balance.
 static void tile_tc(GemmPlan& plan, int target_ctas) {
   make_tiles(plan, kTcTileM, kTcTileN, plan.h_tiles_tc, plan.h_reduce_tc, plan.nslots_tc, target_ctas);
-  for (DTile& t : plan.h_tiles_tc) t.h64 = tail64(plan.h_tasks[t.task].m, t.tm) ? 1 : 0;
+  for (DTile& t : plan.h_tiles_tc) {
+    t.h64 = tail64(plan.h_tasks[t.task].m, t.tm) ? 1 : 0;
+    t.n64 = tail64(plan.h_tasks[t.task].n, t.tn) ? 1 : 0;
+  }
   std::vector<std::pair<int64_t, int>> work(plan.h_tiles_tc.size());
   for (size_t i = 0; i < plan.h_tiles_tc.size(); ++i) {
     int64_t w = 0;
@@ -689,16 +692,16 @@ struct Orient {
 };
 
 // Packed tile grid of an operand: per block, row tiles x K slices, row tile tr slice tk
-// at base + (tr * nks + tk) * tile_bytes.  A operands (128-row tiles) end in a compact
-// 64-row tile where tail64 says so: its slices at base + tr * nks * tile_bytes +
-// tk * tile_bytes / 2 (the pack kernel gets tile_rows 64 and row tile 2 tr, which
-// starts at the same row).
+// at base + (tr * nks + tk) * tile_bytes.  Tensor-core operands (128-row tiles) end in
+// a compact 64-row tile where tail64 says so: its slices at base + tr * nks *
+// tile_bytes + tk * tile_bytes / 2 (the pack kernel gets tile_rows 64 and row tile
+// 2 tr, which starts at the same row).
 template <class F>
 static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t tile_bytes, F orient) {
   P.base.assign(t.tags.size(), -1);
   P.nks.assign(t.tags.size(), 0);
   P.h_packs.clear();
-  const bool a_operand = tile_rows == kTcTileM;
+  const bool tailed = tile_rows == 128;
   int64_t off = 0;
   for (size_t b = 0; b < t.tags.size(); ++b) {
     const Orient o = orient(static_cast<int32_t>(b));
@@ -708,7 +711,7 @@ static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t ti
     P.base[b] = off;
     P.nks[b] = nks;
     for (int tr = 0; tr < ntr; ++tr) {
-      const bool t64 = a_operand && tail64(o.rows, tr);
+      const bool t64 = tailed && tail64(o.rows, tr);
       for (int tk = 0; tk < nks; ++tk) {
         if (t64)
           P.h_packs.push_back(DPack{t.offsets[b], off + int64_t(tr) * nks * tile_bytes + int64_t(tk) * (tile_bytes / 2),
@@ -718,7 +721,7 @@ static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t ti
                                     o.trans, tile_rows, tr, tk, 0});
       }
     }
-    const bool last64 = a_operand && tail64(o.rows, ntr - 1);
+    const bool last64 = tailed && tail64(o.rows, ntr - 1);
     off += int64_t(ntr - (last64 ? 1 : 0)) * nks * tile_bytes + (last64 ? int64_t(nks) * (tile_bytes / 2) : 0);
   }
   P.bytes = off;
@@ -940,11 +943,13 @@ static void build_sigma_groups(Context& ctx, SigmaPlan& p, int64_t budget) {
       for (int tm = 0; tm * kTcTileM < dt.m; ++tm)
         for (int tn = 0; tn * kTcTileN < dt.n; ++tn) {
           if (nc == 1) {
-            t2[g].push_back(DTile{r.task, tm, tn, bnd[0], bnd[1], -1, tail64(dt.m, tm) ? 1 : 0});
+            t2[g].push_back(DTile{r.task, tm, tn, bnd[0], bnd[1], -1, tail64(dt.m, tm) ? 1 : 0,
+                                  tail64(dt.n, tn) ? 1 : 0});
             continue;
           }
           for (int ch = 0; ch < nc; ++ch)
-            t2[g].push_back(DTile{r.task, tm, tn, bnd[ch], bnd[ch + 1], slots[g] + ch, tail64(dt.m, tm) ? 1 : 0});
+            t2[g].push_back(DTile{r.task, tm, tn, bnd[ch], bnd[ch + 1], slots[g] + ch, tail64(dt.m, tm) ? 1 : 0,
+                                  tail64(dt.n, tn) ? 1 : 0});
           red[g].push_back(DReduce{r.task, tm, tn, slots[g], nc, 0});
           slots[g] += nc;
         }
@@ -1221,13 +1226,18 @@ static void sigma_run(Context& ctx, SigmaPlan& p, const DTensor& L, const DTenso
 std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& psi) {
   SigmaPlan& p = sigma_plan(ctx, L, R, psi);
   ensure_sigma_pk(ctx, p, L, R);
-  const double tile_flops = 2.0 * kTcTileM * kTcTileN * kPkTileK;  // one K slice of one tile
   auto work = [&](const std::vector<DTile>& tiles, const std::vector<DPkPair>& pairs, double* slices) {
-    double s = 0.0;
-    for (const DTile& t : tiles)
-      for (int q = t.p0; q < t.p1; ++q) s += pairs[q].nks;
+    double s = 0.0, w = 0.0;
+    for (const DTile& t : tiles) {
+      // one K slice of the tile (64-row tails counted at their size)
+      const double tf = 2.0 * (t.h64 ? 64 : kTcTileM) * (t.n64 ? 64 : kTcTileN) * kPkTileK;
+      for (int q = t.p0; q < t.p1; ++q) {
+        s += pairs[q].nks;
+        w += pairs[q].nks * tf;
+      }
+    }
     *slices = s;
-    return s * tile_flops;
+    return w;
   };
   double sl1 = 0.0, sl2 = 0.0;
   const double w1 = work(p.s1.h_tiles_tc, p.h_pk1, &sl1);

@@ -24,6 +24,7 @@ struct DGemmPair {
 struct DTile {
   int task, tm, tn, p0, p1, slot;
   int h64;  // tensor-core tiles: the A rows are a block's 64-row tail tile (see tail64)
+  int n64;  // tensor-core tiles: the B rows (output columns) are a 64-row tail tile
 };
 // Reduction of the split partials of one output tile.
 struct DReduce {
@@ -89,14 +90,15 @@ struct DBatchProb {
 constexpr int kBatchBlocks = 16;  // blocks per problem in the batched reductions
 
 constexpr int kGemmTile = 64;
-// tensor-core (split TF32) tile: 128 rows x 64 columns
+// tensor-core (split TF32) tile: 128 rows x 128 columns (64 on a block's tail)
 constexpr int kTcTileM = 128;
-constexpr int kTcTileN = 64;
+constexpr int kTcTileN = 128;
 
 // ---- pre-packed split-TF32 operands -----------------------------------------
-// A block of `rows` rows used as a tensor-core A operand is cut into 128-row tiles; a
-// last tile whose rows fit in 64 is a 64-row tile instead (packed compact, half the
-// bytes, M = 64 MMAs): row tile tm of the block is such a tile when this holds.
+// A block of `rows` rows used as a tensor-core operand (A: rows of the result, B: its
+// columns) is cut into 128-row tiles; a last tile whose rows fit in 64 is a 64-row tile
+// instead (packed compact, half the bytes; M = 64 or N = 64 MMAs): row tile tm of the
+// block is such a tile when this holds.
 __host__ __device__ constexpr bool tail64(int rows, int tm) {
   return rows % 128 != 0 && rows % 128 <= 64 && tm == rows / 128;
 }
@@ -106,7 +108,7 @@ constexpr uint32_t kPkTileA1Bytes = 128 * 32 * 4;     // A tile as FP32 values, 
 // launch_gemm_pk outputs: FP64 C (or split-K partials), packed hi|lo A tiles, packed
 // FP32 A tiles (the next GEMM splits them in shared memory)
 constexpr int kOutFP64 = 0, kOutPackedSplit = 1, kOutPackedSingle = 2;
-constexpr uint32_t kPkTileBBytes = 64 * 32 * 4 * 2;   // B tile: hi|lo TF32, 64 rows
+constexpr uint32_t kPkTileBBytes = 128 * 32 * 4 * 2;  // B tile: hi|lo TF32, 128 rows
 
 // One (A, B) pair over packed operands: byte offsets of the blocks' tile grids.
 struct DPkPair {

@@ -1,32 +1,33 @@
 // Split-precision grouped block GEMM over pre-packed operands (sm_103a).
 //
 // Operands are packed once into the tensor-core tile format: a block used as the
-// A operand (rows x K) becomes ceil(rows/128) x ceil(K/32) tiles of 32 KB
-// [hi TF32 128x32 | lo TF32 128x32], a block used as B (rows = output columns)
-// becomes ceil(rows/64) x ceil(K/32) tiles of 16 KB, each half in the K-major
-// no-swizzle core-matrix layout the MMA descriptors address (8 rows x 16 bytes per
-// core matrix).  hi = tf32(x), lo = tf32(x - hi); a product is hi*hi + hi*lo + lo*hi.
+// A operand (rows x K) or as B (rows = output columns) becomes ceil(rows/128) x
+// ceil(K/32) tiles of 32 KB [hi TF32 128x32 | lo TF32 128x32] (a last tile of at most
+// 64 rows is packed compact: 16 KB), each half in the K-major no-swizzle core-matrix
+// layout the MMA descriptors address (8 rows x 16 bytes per core matrix).
+// hi = tf32(x), lo = tf32(x - hi); a product is hi*hi + hi*lo + lo*hi.
 //
 // An intermediate that one GEMM writes and the next reads once (stage 1 -> stage 2 of
 // H_eff * psi) is stored as FP32 values instead (16 KB A tiles, half the bytes) and
 // split on chip: hi and lo from an FP32 value carry no more than the value itself.
 //
-// GEMM CTA (256 threads, warp-specialised):
+// GEMM CTA (384 threads, warp-specialised), one output tile of 128 x 128:
 //   warp 0 lane 0 : producer — per K slice, one bulk copy (TMA engine) of the A tile
-//                   and one of the B tile into a 4-stage shared-memory ring,
+//                   and one of the B tile into a 3-stage shared-memory ring,
 //                   completion counted in bytes on the stage's "full" mbarrier;
 //   warps 2-3     : (FP32 A tiles only) converter — split the landed A tile in place
 //                   into hi | lo, fence it for the tensor core (async proxy) and mark
 //                   the stage "converted";
-//   warp 1 lane 0 : MMA issuer — per K-step of 8, A_hi x [B_hi; B_lo] (N = 128) and
-//                   A_lo x B_hi (N = 64), tcgen05.mma kind::tf32, into one of two TMEM
-//                   accumulators (alternating per group of block pairs); commits
-//                   release the stage ("empty") and, at the end of a group, hand the
-//                   accumulator to the epilogue ("acc_full");
-//   warps 4-7     : epilogue — per pair, tcgen05.ld of the FP32 accumulator into FP64
-//                   registers (FP32 rounding spans one block pair), then release it
-//                   ("acc_empty"); at the end write FP64 C (+=), an FP64 split-K
-//                   partial, or the packed A tiles of the next GEMM (stage-1 output).
+//   warp 1 lane 0 : MMA issuer — per K-step of 8, A_hi x [B_hi; B_lo] (N = 256) and
+//                   A_lo x B_hi (N = 128), tcgen05.mma kind::tf32 (M = 64 / N halved
+//                   on tail tiles), into one of two TMEM accumulators (alternating per
+//                   group of block pairs); commits release the stage ("empty") and, at
+//                   the end of a group, hand the accumulator to the epilogue ("acc_full");
+//   warps 4-11    : epilogue — warp 4 + 4 c + q reads TMEM lane quarter q, output
+//                   columns [64 c, 64 c + 64): per group, tcgen05.ld of the FP32
+//                   accumulator into FP64 registers, then release it ("acc_empty"); at
+//                   the end write FP64 C (+=), an FP64 split-K partial, or the packed A
+//                   tiles of the next GEMM (stage-1 output).
 // Every wait is bounded by a global-timer deadline; a timeout sets a shared abort
 // flag that ends all roles and the device error flag the host checks.
 #include <cuda_runtime.h>
@@ -40,23 +41,25 @@ namespace mpsxx {
 namespace {
 
 constexpr int BM = kTcTileM;  // 128
-constexpr int BN = kTcTileN;  // 64
+constexpr int BN = kTcTileN;  // 128
 constexpr int BK = kPkTileK;  // 32
-constexpr int NTHREADS = 256;
-constexpr int STAGES = 4;
+constexpr int NTHREADS = 384;
+constexpr int EPI_THREADS = 256;  // warps 4-11
+constexpr int STAGES = 3;
 constexpr uint32_t A_BYTES = kPkTileABytes;  // 32 KB
 constexpr uint32_t A1_BYTES = kPkTileA1Bytes;  // 16 KB (FP32 A tile)
 constexpr int CONV_THREADS = 64;               // warps 2-3
-constexpr uint32_t B_BYTES = kPkTileBBytes;  // 16 KB
+constexpr uint32_t B_BYTES = kPkTileBBytes;  // 32 KB
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
-// Each K step is two MMAs: A_hi x [B_hi; B_lo] as one N = 128 operand (the packed B
-// tile is exactly that: hi rows then lo rows) into accumulator columns [0, 128), and
-// A_lo x B_hi (N = 64) into columns [0, 64).  The product is then columns
-// [0, 64) + [64, 128).  Fewer, wider MMAs read fewer operand bytes from shared memory,
-// whose bandwidth (with the bulk copies and the on-chip split) bounds the kernel.
-constexpr uint32_t ACC_COLS = 2 * BN;             // one accumulator: 128 columns
-constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;       // two accumulators
+// Each K step is two MMAs: A_hi x [B_hi; B_lo] as one N = 2 Nt operand (the packed B
+// tile is exactly that: hi rows then lo rows; Nt = 128, or 64 on a tail tile) into
+// accumulator columns [0, 2 Nt), and A_lo x B_hi (N = Nt) into columns [0, Nt).  The
+// product is then columns [0, Nt) + [Nt, 2 Nt).  Fewer, wider MMAs read fewer operand
+// bytes from shared memory, whose bandwidth (with the bulk copies and the on-chip
+// split) bounds the kernel.
+constexpr uint32_t ACC_COLS = 2 * BN;             // one accumulator: 256 columns
+constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;       // two accumulators: all 512 columns
 // Consecutive block pairs of a tile accumulate in the FP32 tensor-memory tile until
 // their summed contraction length reaches FLUSH_K; then the group is flushed into
 // the FP64 accumulators.  This bounds the FP32 accumulation length (rounding ~
@@ -170,6 +173,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __global__ void __launch_bounds__(NTHREADS, 1)
     gemm_pk_kernel(const uint8_t* __restrict__ Apk, const uint8_t* __restrict__ Bpk, double alpha,
                    double* __restrict__ C, uint8_t* __restrict__ Cpk, const DTile* __restrict__ tiles, int ntiles,
@@ -201,7 +213,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(smem_u32(&accf_bar[b]), 1);
-      mbar_init(smem_u32(&acce_bar[b]), 128);
+      mbar_init(smem_u32(&acce_bar[b]), EPI_THREADS);
     }
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
@@ -237,7 +249,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // a 64-row tail tile is packed compact: half the bytes; its hi and lo
             // halves (split format) land where the MMA expects a 128-row tile's
             const uint32_t at = t.h64 ? a_bytes / 2 : a_bytes;
-            mbar_expect_tx(fb, at + B_BYTES);
+            mbar_expect_tx(fb, at + (t.n64 ? B_BYTES / 2 : B_BYTES));
             const uint32_t dst = smem_u32(ring + s * STAGE_BYTES);
             const uint8_t* asrc = Apk + pr.a_pk + (int64_t)t.tm * pr.nks * a_bytes + (int64_t)ks * at;
             if (t.h64 && !a_single) {
@@ -246,7 +258,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             } else {
               bulk_g2s(dst, asrc, at, fb);
             }
-            bulk_g2s(dst + A_BYTES, Bpk + pr.b_pk + ((int64_t)t.tn * pr.nks + ks) * B_BYTES, B_BYTES, fb);
+            const uint32_t bt = t.n64 ? B_BYTES / 2 : B_BYTES;  // compact [hi 64 | lo 64] on a tail
+            bulk_g2s(dst + A_BYTES, Bpk + pr.b_pk + (int64_t)t.tn * pr.nks * B_BYTES + (int64_t)ks * bt, bt, fb);
           }
         }
       }
@@ -254,8 +267,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc_w128 = tf32_idesc(BM, 2 * BN), idesc_128 = tf32_idesc(BM, BN);
-      const uint32_t idesc_w64 = tf32_idesc(64, 2 * BN), idesc_64 = tf32_idesc(64, BN);
+
       const uint32_t lbo = 128, sbo = (BK / 4) * 128;
       // Descriptors of the stages' A and B tiles, built once: the start address sits in
       // the low 14 bits (address >> 4), so the K steps and the lo halves are immediate
@@ -272,7 +284,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
         const DTile t = t_next;
         if (ti + (int)gridDim.x < ntiles) t_next = tiles[ti + gridDim.x];
-        const uint32_t idesc_w = t.h64 ? idesc_w64 : idesc_w128, idesc = t.h64 ? idesc_64 : idesc_128;
+        const int mt = t.h64 ? 64 : BM, nt = t.n64 ? 64 : BN;
+        const uint32_t idesc_w = tf32_idesc(mt, 2 * nt), idesc = tf32_idesc(mt, nt);
         int kacc = 0;
         int nks_next = t.p0 < t.p1 ? pairs[t.p0].nks : 0;
         for (int p = t.p0; p < t.p1 && ok; ++p) {
@@ -309,11 +322,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const uint64_t koff = (uint64_t)(kk * 256) >> 4;
               const uint64_t ah = a0d + koff;
               const uint64_t al = a0d + ((A_BYTES / 2) >> 4) + koff;
-              const uint64_t bh = b0d + koff;
-              const uint64_t bl = b0d + ((B_BYTES / 2) >> 4) + koff;
+              const uint64_t bh = b0d + koff;  // [B_hi; B_lo] for the wide MMA, B_hi for the other
               mma_tf32(d, ah, bh, idesc_w, (group_start && ks == 0 && kk == 0) ? 0u : 1u);
               mma_tf32(d, al, bh, idesc, 1u);
-              (void)bl;
             }
             mma_commit(smem_u32(&empty_bar[s]));  // stage free once these MMAs completed
           }
@@ -376,7 +387,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
   } else if (warp >= 4) {
     // ---------------- epilogue ----------------
-    const int q = warp - 4;  // TMEM lane quarter
+    const int q = (warp - 4) & 3;   // TMEM lane quarter (warp id mod 4)
+    const int ch = (warp - 4) >> 2;  // column half: output columns [64 ch, 64 ch + 64)
     int gc = 0;
     bool ok = true;
     for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
@@ -387,10 +399,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       // nothing for i >= 16); -1: no row
       const int row = t.h64 ? (lane < 16 ? q * 16 + lane : -1) : q * 32 + lane;
       const int r = t.tm * BM + row;
+      const int nt = t.n64 ? 64 : BN;     // output columns of the tile
+      const bool cols = 64 * ch < nt;     // this warp has columns (not on a 64-column tail)
+      const uint32_t c1 = 64 * ch, c2 = nt + 64 * ch;  // its columns in both accumulator parts
       if (out_packed) {
         // stage-1 output (one group): FP32 straight from tensor memory, re-split into
-        // the packed A tiles of the next GEMM; columns [64 tn, 64 tn + 64) are its K
-        // slices 2 tn and 2 tn + 1, ldc carries that GEMM's slices per row tile
+        // the packed A tiles of the next GEMM; output columns [128 tn + 64 ch, +64) are
+        // its K slices 4 tn + 2 ch and 4 tn + 2 ch + 1, ldc carries that GEMM's slices
+        // per row tile
         int kacc = 0;
         for (int p = t.p0; p < t.p1 && ok; ++p) {
           kacc += pairs[p].nks * BK;
@@ -409,41 +425,42 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           // compact (half the bytes, its lo half a quarter tile in)
           const uint32_t ts = t.h64 ? ot_bytes / 2 : ot_bytes;
           const uint32_t lo_off = ts / 2;
-          uint8_t* tile0 = Cpk + task.c_off + (int64_t)t.tm * task.ldc * ot_bytes + (int64_t)(2 * t.tn) * ts;
+          uint8_t* tile0 = Cpk + task.c_off + (int64_t)t.tm * task.ldc * ot_bytes;
           const float fa = static_cast<float>(alpha);
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            float v[BK], w[BK];
-            tmem_ld16(taddr + h * BK, v);
-            tmem_ld16(taddr + h * BK + 16, v + 16);
-            tmem_ld16(taddr + BN + h * BK, w);
-            tmem_ld16(taddr + BN + h * BK + 16, w + 16);
+          // 16 columns at a time: half a K slice of the next GEMM
+#pragma unroll 1
+          for (int hq = 0; hq < 4 && cols; ++hq) {
+            const int h = hq >> 1, k0 = (hq & 1) * 16;
+            float v[16], w[16];
+            tmem_ld16(taddr + c1 + h * BK + k0, v);
+            tmem_ld16(taddr + c2 + h * BK + k0, w);
             asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-            for (int kk = 0; kk < BK; ++kk) v[kk] += w[kk];
-            if (2 * t.tn + h >= task.ldc || row < 0) continue;
-            uint8_t* tile = tile0 + h * ts;
+            for (int kk = 0; kk < 16; ++kk) v[kk] += w[kk];
+            const int slice = 4 * t.tn + 2 * ch + h;
+            if (slice >= task.ldc || row < 0) continue;
+            uint8_t* tile = tile0 + (int64_t)slice * ts;
             // 16-byte stores: k .. k+3 of a row are contiguous in the core-matrix
             // layout, and a warp's 32 rows fill four whole 128-byte lines
             if (single) {
 #pragma unroll
-              for (int kk = 0; kk < BK; kk += 4)
-                *reinterpret_cast<float4*>(tile + core_off(row, kk)) =
+              for (int kk = 0; kk < 16; kk += 4)
+                *reinterpret_cast<float4*>(tile + core_off(row, k0 + kk)) =
                     make_float4(fa * v[kk], fa * v[kk + 1], fa * v[kk + 2], fa * v[kk + 3]);
             } else {
 #pragma unroll
-              for (int kk = 0; kk < BK; kk += 4) {
+              for (int kk = 0; kk < 16; kk += 4) {
                 uint4 hi, lo;
-                uint32_t* h = &hi.x;
-                uint32_t* l = &lo.x;
+                uint32_t* hp = &hi.x;
+                uint32_t* lp = &lo.x;
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                   const float x = fa * v[kk + e];
-                  h[e] = tf32_rna(x);
-                  l[e] = tf32_rna(x - __uint_as_float(h[e]));
+                  hp[e] = tf32_rna(x);
+                  lp[e] = tf32_rna(x - __uint_as_float(hp[e]));
                 }
-                *reinterpret_cast<uint4*>(tile + core_off(row, kk)) = hi;
-                *reinterpret_cast<uint4*>(tile + lo_off + core_off(row, kk)) = lo;
+                *reinterpret_cast<uint4*>(tile + core_off(row, k0 + kk)) = hi;
+                *reinterpret_cast<uint4*>(tile + lo_off + core_off(row, k0 + kk)) = lo;
               }
             }
           }
@@ -453,9 +470,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         continue;
       }
-      double acc[BN];
+      double acc[64];
 #pragma unroll
-      for (int j = 0; j < BN; ++j) acc[j] = 0.0;
+      for (int j = 0; j < 64; ++j) acc[j] = 0.0;
       int kacc = 0;
       for (int p = t.p0; p < t.p1; ++p) {
         kacc += pairs[p].nks * BK;
@@ -468,35 +485,36 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * ACC_COLS;
+        if (cols) {
 #pragma unroll
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-          float v[16], w[16];
-          tmem_ld16(taddr + c0, v);
-          tmem_ld16(taddr + BN + c0, w);
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
+          for (int c0 = 0; c0 < 64; c0 += 8) {
+            float v[8], w[8];
+            tmem_ld8(taddr + c1 + c0, v);
+            tmem_ld8(taddr + c2 + c0, w);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-          for (int i = 0; i < 16; ++i) acc[c0 + i] += static_cast<double>(v[i] + w[i]);
+            for (int i = 0; i < 8; ++i) acc[c0 + i] += static_cast<double>(v[i] + w[i]);
+          }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
         mbar_arrive(smem_u32(&acce_bar[b]));
         ++gc;
       }
       if (!ok) break;
-      if (row < 0) continue;  // lanes without a row in an M = 64 tile
+      if (row < 0 || !cols) continue;  // lanes without a row (M = 64), warps without columns
       if (t.slot >= 0) {
-        double* part = partial + (int64_t)t.slot * (BM * BN) + (int64_t)row * BN;
+        double* part = partial + (int64_t)t.slot * (BM * BN) + (int64_t)row * BN + c1;
 #pragma unroll
-        for (int j = 0; j < BN; ++j) part[j] = acc[j];
+        for (int j = 0; j < 64; ++j) part[j] = acc[j];
       } else if (r < task.m) {
-        const int n0 = t.tn * BN;
+        const int n0 = t.tn * BN + c1;
         double* dst = C + task.c_off + (int64_t)r * task.ldc + n0;
 #pragma unroll
-        for (int j = 0; j < BN; ++j)
+        for (int j = 0; j < 64; ++j)
           if (n0 + j < task.n) dst[j] += alpha * acc[j];
       }
     }
   }
-
   __syncthreads();
   if (threadIdx.x == 0 && abort_flag) atomicExch(err, 1);
   asm volatile("tcgen05.fence::before_thread_sync;");
