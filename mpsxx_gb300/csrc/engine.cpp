@@ -404,17 +404,22 @@ static void make_tiles(const GemmPlan& plan, int tile_m, int tile_n, std::vector
     }
     bnd.push_back(dt.p1);
     const int nc = static_cast<int>(bnd.size()) - 1;
-    for (int tm = 0; tm * tile_m < dt.m; ++tm)
-      for (int tn = 0; tn * tile_n < dt.n; ++tn) {
-        if (nc == 1) {
-          tiles.push_back(DTile{ti, tm, tn, bnd[0], bnd[1], -1});
-          continue;
-        }
-        const int slot0 = nslots;
-        for (int ch = 0; ch < nc; ++ch) tiles.push_back(DTile{ti, tm, tn, bnd[ch], bnd[ch + 1], slot0 + ch});
-        nslots += nc;
-        reduce.push_back(DReduce{ti, tm, tn, slot0, nc, 0});
-      }
+    const int ntm = (dt.m + tile_m - 1) / tile_m, ntn = (dt.n + tile_n - 1) / tile_n;
+    if (nc == 1) {
+      for (int tm = 0; tm < ntm; ++tm)
+        for (int tn = 0; tn < ntn; ++tn) tiles.push_back(DTile{ti, tm, tn, bnd[0], bnd[1], -1});
+      continue;
+    }
+    // chunk-major: tiles over the same K range follow each other, so the CTAs that run
+    // together share their A row panels and B column panels in L2
+    const int slot0 = nslots;
+    for (int tm = 0; tm < ntm; ++tm)
+      for (int tn = 0; tn < ntn; ++tn) reduce.push_back(DReduce{ti, tm, tn, slot0 + (tm * ntn + tn) * nc, nc, 0});
+    for (int ch = 0; ch < nc; ++ch)
+      for (int tm = 0; tm < ntm; ++tm)
+        for (int tn = 0; tn < ntn; ++tn)
+          tiles.push_back(DTile{ti, tm, tn, bnd[ch], bnd[ch + 1], slot0 + (tm * ntn + tn) * nc + ch});
+    nslots += ntm * ntn * nc;
   }
 }
 
