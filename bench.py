@@ -31,7 +31,7 @@ L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per H_eff*psi of the default
 # workload (QC n=20, K=40, seed 1, M=512, bond (9,10)), summed over the launches of one
 # step, from one ncu capture of the launch list (one pass); None for other workloads.
-MEASURED_TRAFFIC = {("split", 20, 40, 1, 512): 7.59e9, }
+MEASURED_TRAFFIC = {("split", 20, 40, 1, 512): 6.75e9, }
 
 
 def parse():
