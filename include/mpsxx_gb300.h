@@ -112,6 +112,11 @@ int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes,
  * default (24; 256, for padded sizes shared by at least 6 blocks); 0 switches a route
  * off. */
 int mpsxx_context_set_svd_routes(mpsxx_context* ctx, int jacobi_max_cols, int gram_max_dim);
+/* Plans (H_eff*psi, diagonal, merged-operator, renormalisation) kept per kind before
+ * the context empties a cache (default 512).  Plans are keyed by structural layouts,
+ * so a converged sweep reuses the previous sweep's plans when they are still cached;
+ * a batched scan of many chains needs room for all of one sweep's bonds. */
+int mpsxx_context_set_plan_cache(mpsxx_context* ctx, int64_t max_plans);
 
 /* ---- tensors ------------------------------------------------------------- */
 /* Create a block-sparse tensor.  qn holds 2*sum(nsec) ints (p, 2Sz per sector,

@@ -51,6 +51,10 @@ class Context:
         check(lib().mpsxx_context_set_sigma_schedule(self.h, int(w_budget_bytes), int(target_tiles),
                                                      int(bool(fp32_intermediate))))
 
+    def set_plan_cache(self, max_plans: int = 512):
+        """Plans kept per kind before a cache is emptied."""
+        check(lib().mpsxx_context_set_plan_cache(self.h, int(max_plans)))
+
     def set_svd_routes(self, jacobi_max_cols: int = -1, gram_max_dim: int = -1):
         """Routing of canonicalize's block SVDs (batched Jacobi / batched eigensolver /
         solver lanes); negative: defaults, 0: route off."""

@@ -578,7 +578,7 @@ std::vector<double> diagonalize_batch(Context& ctx, const std::vector<const DTen
     size_t missing = 0;
     for (size_t c = 0; c < N; ++c)
       missing += ctx.sigma_plans.count(std::make_tuple(L[c]->layout_id, R[c]->layout_id, psi[c]->layout_id)) == 0;
-    if (ctx.sigma_plans.size() + missing > kMaxCachedPlans) ctx.sigma_plans.clear();
+    if (ctx.sigma_plans.size() + missing > ctx.max_plans) ctx.sigma_plans.clear();
   }
   std::vector<Item> items(N);
   for (size_t c = 0; c < N; ++c) {

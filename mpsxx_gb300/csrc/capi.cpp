@@ -157,6 +157,14 @@ int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes,
   });
 }
 
+int mpsxx_context_set_plan_cache(mpsxx_context* ctx, int64_t max_plans) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    need(max_plans > 0, "plan cache size must be positive");
+    ctx->ctx->max_plans = static_cast<size_t>(max_plans);
+  });
+}
+
 int mpsxx_context_set_svd_routes(mpsxx_context* ctx, int jacobi_max_cols, int gram_max_dim) {
   return guard([&] {
     need(ctx && ctx->ctx, "null context");

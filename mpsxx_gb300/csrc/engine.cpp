@@ -613,16 +613,16 @@ static P& insert_plan(Context& ctx, M& m, const K& key, std::unique_ptr<P> p) {
   std::lock_guard<std::mutex> lk(ctx.plan_mu);
   auto it = m.find(key);
   if (it != m.end()) return *it->second;
-  if (m.size() >= kMaxCachedPlans && !ctx.planning_threads) m.clear();
+  if (m.size() >= ctx.max_plans && !ctx.planning_threads) m.clear();
   return *m.emplace(key, std::move(p)).first->second;
 }
 
 void reserve_plans(Context& ctx, size_t n) {
   std::lock_guard<std::mutex> lk(ctx.plan_mu);
-  if (ctx.sigma_plans.size() + n > kMaxCachedPlans) ctx.sigma_plans.clear();
-  if (ctx.diag_plans.size() + n > kMaxCachedPlans) ctx.diag_plans.clear();
-  if (ctx.merge_plans.size() + 2 * n > kMaxCachedPlans) ctx.merge_plans.clear();
-  if (ctx.renorm_plans.size() + n > kMaxCachedPlans) ctx.renorm_plans.clear();
+  if (ctx.sigma_plans.size() + n > ctx.max_plans) ctx.sigma_plans.clear();
+  if (ctx.diag_plans.size() + n > ctx.max_plans) ctx.diag_plans.clear();
+  if (ctx.merge_plans.size() + 2 * n > ctx.max_plans) ctx.merge_plans.clear();
+  if (ctx.renorm_plans.size() + n > ctx.max_plans) ctx.renorm_plans.clear();
 }
 
 void parallel_plan(Context& ctx, int n, const std::function<void(int)>& f) {
@@ -2842,10 +2842,10 @@ void release_bond_buffers(Context& ctx) {
     kv.second->staged.release();
     kv.second->drop_graph();
   }
-  if (ctx.sigma_plans.size() > kMaxCachedPlans) ctx.sigma_plans.clear();
-  if (ctx.diag_plans.size() > kMaxCachedPlans) ctx.diag_plans.clear();
-  if (ctx.merge_plans.size() > kMaxCachedPlans) ctx.merge_plans.clear();
-  if (ctx.renorm_plans.size() > kMaxCachedPlans) ctx.renorm_plans.clear();
+  if (ctx.sigma_plans.size() > ctx.max_plans) ctx.sigma_plans.clear();
+  if (ctx.diag_plans.size() > ctx.max_plans) ctx.diag_plans.clear();
+  if (ctx.merge_plans.size() > ctx.max_plans) ctx.merge_plans.clear();
+  if (ctx.renorm_plans.size() > ctx.max_plans) ctx.renorm_plans.clear();
 }
 
 BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo, const DTensor& rmpo,

@@ -108,7 +108,7 @@ enum Precision : int { kFP64 = 0, kSplitTF32 = 1, kSplitTF32All = 2 };
 constexpr int kTargetCtas = 152 * 8;
 
 // plans kept per kind in a context before the cache is emptied
-constexpr size_t kMaxCachedPlans = 512;
+constexpr size_t kMaxCachedPlans = 512;  // default of Context::max_plans
 
 // GEMM plan into a C whose layout is `c` (block offsets).  C blocks may be
 // sub-blocks of a larger block when `cmap` is provided (fused merges).
@@ -305,6 +305,9 @@ struct Context {
   // insertions under plan_mu; while planning_threads is set no cache is emptied
   std::mutex plan_mu;
   bool planning_threads = false;
+  // plans kept per kind before a cache is emptied (a batched scan of many chains
+  // raises it so that converged sweeps find the previous sweep's plans)
+  size_t max_plans = kMaxCachedPlans;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<SigmaPlan>> sigma_plans;
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, std::unique_ptr<DiagPlan>> diag_plans;
   std::map<std::tuple<int, uint64_t, uint64_t, uint64_t>, std::unique_ptr<MergePlan>> merge_plans;

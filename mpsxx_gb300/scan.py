@@ -36,6 +36,10 @@ def make_chains(ctx: Context, specs: Sequence[tuple], M0: int) -> List[Chain]:
     for L, U, t in specs:
         mpo = [core.Tensor.from_dict(ctx, d) for d in hubbard_mpo(L, t, U)]
         chains.append(Chain(L, U, t, dmrg.make_initial_state(ctx, mpo, L, L % 2, M0)))
+    # room for a whole sweep's plans of every chain (two merged operators per bond step),
+    # so that converged sweeps reuse them
+    steps = sum(2 * (L - 1) for L, _, _ in specs)
+    ctx.set_plan_cache(max(512, 4 * steps))
     return chains
 
 
