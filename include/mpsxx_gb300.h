@@ -158,12 +158,12 @@ int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, con
 
 /* Work of the split-precision H_eff*psi plan for these operands (the plan is built if
  * needed; no device data is read): out[0..12] = useful FLOPs of stage 1 and 2, tile
- * FLOPs of stage 1 and 2 (128 x 64 tensor-core tiles, K slices of 32, padding
+ * FLOPs of stage 1 and 2 (128 x 128 tensor-core tiles, 64 on tails, K slices of 32, padding
  * included), K slices of stage 1 and 2, tiles of stage 1 and 2, packed bytes of lopr,
  * ropr, the L*psi intermediate and wfn, and the intermediate's element count;
  * out[13..18] = FLOPs of stage 1 and then stage 2 with only the rows (to 128), only
- * the columns (to 64) or only K (to 32) padded; out[19..20] = tile FLOPs of stage 1
- * and 2 were a block's last row tile 64 rows high where its remainder fits. */
+ * the columns (to 128) or only K (to 32) padded; out[19..20] = tile FLOPs of stage 1
+ * and 2 with 64-row tails on the rows only (columns padded to 128). */
 int mpsxx_sigma_plan_stats(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                            const mpsxx_tensor* wfn, double* out, int n, int* count);
 

@@ -85,7 +85,8 @@ struct GemmPlan {
   DevArray<DGemmPair> pairs;
   DevArray<DReduce> reduce;
   int nslots = 0;  // split-K partial tiles
-  // tensor-core (split TF32) tiling of the same tasks: 128 x 64 tiles
+  // tensor-core (split TF32) tiling of the same tasks: 128 x 128 tiles (64-row and
+  // 64-column tails flagged per tile)
   std::vector<DTile> h_tiles_tc;
   std::vector<DReduce> h_reduce_tc;
   DevArray<DTile> tiles_tc;
@@ -376,7 +377,7 @@ double sigma_device_time(Context& ctx, const DTensor& L, const DTensor& R, const
 // src/compute_diagonal_elements.hpp:65-80
 DiagPlan& diag_plan(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& diag);
 // Work and bytes of a split-precision H_eff * psi plan: useful FLOPs of both stages,
-// tensor-core tile FLOPs (tiles padded to 128 x 64, K slices of 32), K slices, tiles,
+// tensor-core tile FLOPs (tiles padded to 128 x 128 or their 64 tails, K slices of 32), K slices, tiles,
 // packed bytes of L, R, the L*psi intermediate and psi, and the intermediate's size.
 std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor& R, const Tensor& psi);
 // Plans by layout (no device data read): cached, safe on planning threads.
