@@ -8,8 +8,10 @@
 // hi = tf32(x), lo = tf32(x - hi); a product is hi*hi + hi*lo + lo*hi.
 //
 // An intermediate that one GEMM writes and the next reads once (stage 1 -> stage 2 of
-// H_eff * psi) is stored as FP32 values instead (16 KB A tiles, half the bytes) and
-// split on chip: hi and lo from an FP32 value carry no more than the value itself.
+// H_eff * psi) is written either in that packed hi|lo format or as FP32 values (16 KB
+// A tiles, half the bytes) that the next GEMM splits on chip — hi and lo from an FP32
+// value carry no more than the value itself; the split costs shared-memory traffic, so
+// the plan's autotuner picks the format.
 //
 // GEMM CTA (384 threads, warp-specialised), one output tile of 128 x 128:
 //   warp 0 lane 0 : producer — per K slice, one bulk copy (TMA engine) of the A tile
