@@ -769,6 +769,16 @@ static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Te
   };
   pairs_of(p.s1, p.pk_L, p.pk_psi, p.h_pk1);
   pairs_of(p.s2, p.pk_scr1, p.pk_R, p.h_pk2);
+  // Stage 1 writes each tile's result straight into the intermediate's packed tiles,
+  // which is right only for a tile summed in one piece: not split along K, one
+  // accumulation group (psi has one block per column sector, so each L*psi block has
+  // a single contributing pair)
+  for (const DTile& t : p.s1.h_tiles_tc) {
+    int64_t kpad = 0;
+    for (int q = t.p0; q + 1 < t.p1; ++q) kpad += int64_t(p.h_pk1[q].nks) * kPkTileK;
+    if (t.slot >= 0 || kpad >= kFlushK)
+      throw Error(kInternal, "packed sigma plan: a stage-1 tile is not summed in one piece");
+  }
   // stage-1 tasks write packed scr1: c_off = byte base of the block, ldc = its K slices
   p.h_pk_tasks1 = p.s1.h_tasks;
   for (size_t ti = 0; ti < p.h_pk_tasks1.size(); ++ti) {

@@ -103,6 +103,9 @@ __host__ __device__ constexpr bool tail64(int rows, int tm) {
   return rows % 128 != 0 && rows % 128 <= 64 && tm == rows / 128;
 }
 constexpr int kPkTileK = 32;                          // K elements per packed slice
+// a tile's block pairs accumulate in FP32 (tensor memory) until their padded K reaches
+// this, then the group is added into FP64
+constexpr int kFlushK = 1024;
 constexpr uint32_t kPkTileABytes = 128 * 32 * 4 * 2;  // A tile: hi|lo TF32, 128 rows
 constexpr uint32_t kPkTileA1Bytes = 128 * 32 * 4;     // A tile as FP32 values, split on chip
 // launch_gemm_pk outputs: FP64 C (or split-K partials), packed hi|lo A tiles, packed

@@ -67,7 +67,7 @@ constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;       // two accumulators: all 512 
 // the FP64 accumulators.  This bounds the FP32 accumulation length (rounding ~
 // sqrt(FLUSH_K) * 2^-24, below the TF32 split error) while keeping FP64 work —
 // GB300's narrowest pipe — off the per-pair path.
-constexpr int FLUSH_K = 1024;
+constexpr int FLUSH_K = kFlushK;
 
 // group boundary: after pair p (with running contraction length kacc) of a tile
 __device__ __forceinline__ bool group_ends(int kacc, int p, int p_last) { return kacc >= FLUSH_K || p == p_last; }
