@@ -1072,6 +1072,8 @@ void set_scr1_format(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& 
   p.scr1_single = single;
   p.pk_built = false;
   build_sigma_pk(ctx, p, L, R, p.psi_layout);
+  // w groups place the intermediate's blocks by their packed size: rebuild them
+  if (!p.groups.empty()) build_sigma_groups(ctx, p, p.group_budget);
   p.drop_graph();
 }
 
