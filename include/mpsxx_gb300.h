@@ -163,7 +163,8 @@ int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, con
  * ropr, the L*psi intermediate and wfn, and the intermediate's element count;
  * out[13..18] = FLOPs of stage 1 and then stage 2 with only the rows (to 128), only
  * the columns (to 128) or only K (to 32) padded; out[19..20] = tile FLOPs of stage 1
- * and 2 with 64-row tails on the rows only (columns padded to 128). */
+ * and 2 with 64-row tails on the rows only (columns padded to 128); out[21..22] =
+ * tiles of both stages on a 64-row and on a 64-column tail. */
 int mpsxx_sigma_plan_stats(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                            const mpsxx_tensor* wfn, double* out, int n, int* count);
 

@@ -282,7 +282,8 @@ SIGMA_PLAN_KEYS = ("flops_stage1", "flops_stage2", "tile_flops_stage1", "tile_fl
                    "packed_bytes_intermediate", "packed_bytes_psi", "intermediate_elements",
                    "flops_rows_padded_stage1", "flops_cols_padded_stage1", "flops_k_padded_stage1",
                    "flops_rows_padded_stage2", "flops_cols_padded_stage2", "flops_k_padded_stage2",
-                   "tile_flops_64row_tail_stage1", "tile_flops_64row_tail_stage2")
+                   "tile_flops_64row_tail_stage1", "tile_flops_64row_tail_stage2", "tiles_64row_tail",
+                   "tiles_64col_tail")
 
 
 def sigma_plan_stats(ctx: Context, lopr: Tensor, ropr: Tensor, wfn: Tensor) -> dict:

@@ -1273,6 +1273,11 @@ std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor
   double pm1 = 0, pn1 = 0, pk1 = 0, pm2 = 0, pn2 = 0, pk2 = 0;
   padded(p.s1, &pm1, &pn1, &pk1);
   padded(p.s2, &pm2, &pn2, &pk2);
+  auto tails = [](const std::vector<DTile>& tiles, bool rows) {
+    double c = 0.0;
+    for (const DTile& t : tiles) c += rows ? t.h64 : t.n64;
+    return c;
+  };
   // tile FLOPs if a block's last row tile were 64 rows high where its remainder fits
   auto tile64 = [](const GemmPlan& g) {
     double s = 0.0;
@@ -1304,7 +1309,9 @@ std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor
           pn2,
           pk2,
           tile64(p.s1),
-          tile64(p.s2)};
+          tile64(p.s2),
+          tails(p.s1.h_tiles_tc, true) + tails(p.s2.h_tiles_tc, true),
+          tails(p.s1.h_tiles_tc, false) + tails(p.s2.h_tiles_tc, false)};
 }
 
 void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R) {

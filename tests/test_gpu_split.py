@@ -75,6 +75,28 @@ def test_split_sigma_matches_fp64_qc_bond(ctx):
     assert err < 2e-6
 
 
+def test_split_sigma_tail_tiles_are_exercised(ctx):
+    """A QC n=12, M=256 bond: its plan has full 128x128 tiles and 64-row and 64-column
+    tail tiles (M=64 / N=64 MMAs, compact packing), and its split H_eff*psi matches
+    FP64 within 2e-6 (the plan statistics count the tiles; no device data is read for
+    that).  The smaller test bonds have tail tiles only."""
+    from mpsxx_gb300 import core, dmrg, mpogen
+
+    h, eri = mpogen.synthetic_qc_integrals(12, 24, 5)
+    mpo = [core.Tensor.from_dict(ctx, d) for d in mpogen.qc_mpo(h, eri)]
+    st = dmrg.make_random_state(ctx, mpo, 12, 0, 256, seed=4)
+    dmrg.advance_left(ctx, st, 5)
+    mL, mR, psi = dmrg.bond_operands(ctx, st, 5)
+    stats = core.sigma_plan_stats(ctx, mL, mR, psi)
+    print({k: stats[k] for k in ("tiles_stage1", "tiles_stage2", "tiles_64row_tail", "tiles_64col_tail")})
+    assert stats["tiles_64row_tail"] > 0 and stats["tiles_64col_tail"] > 0
+    # and full 128-row / 128-column tiles as well
+    assert stats["tiles_64row_tail"] < stats["tiles_stage1"] + stats["tiles_stage2"]
+    assert stats["tiles_64col_tail"] < stats["tiles_stage1"] + stats["tiles_stage2"]
+    s64, s32 = sigma_both(ctx, mL, mR, psi)
+    assert rel_err(s32, s64) < 2e-6
+
+
 def test_split_davidson_refined_energy_matches_fp64(ctx):
     from mpsxx_gb300 import core
 
