@@ -95,6 +95,15 @@ def test_split_sigma_tail_tiles_are_exercised(ctx):
     assert stats["tiles_64col_tail"] < stats["tiles_stage1"] + stats["tiles_stage2"]
     s64, s32 = sigma_both(ctx, mL, mR, psi)
     assert rel_err(s32, s64) < 2e-6
+    # every schedule on these tiles: FP32 intermediate in one pass, w groups in both formats
+    for schedule in ((0, 152 * 8, True), (1 << 20, 0, True), (1 << 20, 0, False)):
+        ctx.set_sigma_schedule(*schedule)
+        try:
+            _, s = sigma_both(ctx, mL, mR, psi)
+        finally:
+            ctx.set_sigma_schedule(-1)
+        print("schedule", schedule, rel_err(s, s64))
+        assert rel_err(s, s64) < 2e-6
 
 
 def test_split_davidson_refined_energy_matches_fp64(ctx):
