@@ -43,3 +43,38 @@ def test_batched_sweeps_match_sequential(ctx, precision):
     # L=6 with M=64 is exact
     exact = ed.hubbard_ground_energy(6, -1.0, 4.0, 3, 3)[0]
     assert abs(batched[0].energies[-1] - exact) < 1e-9
+
+
+def test_batched_bond_steps_on_full_tiles_match_single_steps(ctx):
+    """Two QC bonds (n=12, M=256, different integrals; states converged by four sweeps)
+    advanced in one batched step — grouped split H_eff*psi over full 128x128
+    tensor-core tiles and tails — give the energies of the same bond steps taken one at
+    a time from identical inputs to 1e-9 Eh (split precision with the FP64 anchor)."""
+    from mpsxx_gb300 import core, dmrg, mpogen
+
+    bonds = []
+    core.set_precision(ctx, core.SPLIT_TF32)
+    try:
+        for seed in (5, 6):
+            h, eri = mpogen.synthetic_qc_integrals(12, 24, seed)
+            mpo = [core.Tensor.from_dict(ctx, d) for d in mpogen.qc_mpo(h, eri)]
+            st = dmrg.make_initial_state(ctx, mpo, 12, 0, 256)
+            for _ in range(4):
+                dmrg.make_sweep(ctx, st, 1e-9)
+            dmrg.advance_left(ctx, st, 5)
+            bonds.append(st)
+    finally:
+        core.set_precision(ctx, core.FP64)
+    tole = 1e-9
+    core.set_precision(ctx, core.SPLIT_TF32)
+    try:
+        args = [(st.mpo[5], st.mpo[6], st.lenv[5], st.renv[6], st.wave[5], st.wave[6]) for st in bonds]
+        single = [core.optimize_twosite_merged(ctx, True, *a, 0.1 * tole, 256) for a in args]
+        e, env, nl, nr, stats = core.optimize_twosite_merged_batch(ctx, [True, True], *[list(x) for x in zip(*args)],
+                                                                   0.1 * tole, 256)
+    finally:
+        core.set_precision(ctx, core.FP64)
+    for b, (es, _, _, _, ss) in enumerate(single):
+        print("bond", b, "batched", e[b], stats[b]["converged"], "single", es, ss["converged"])
+        assert stats[b]["converged"] and ss["converged"]
+        assert abs(e[b] - es) < 1e-9
