@@ -117,6 +117,10 @@ int mpsxx_context_set_svd_routes(mpsxx_context* ctx, int jacobi_max_cols, int gr
  * so a converged sweep reuses the previous sweep's plans when they are still cached;
  * a batched scan of many chains needs room for all of one sweep's bonds. */
 int mpsxx_context_set_plan_cache(mpsxx_context* ctx, int64_t max_plans);
+/* Wait limit of the tensor-core kernels (one launch; <= 0: the default 20 s).  A kernel
+ * that runs out drains its own bulk copies and MMAs, frees its tensor memory and
+ * returns; the call reports MPSXX_DEVICE_TIMEOUT and the context stays usable. */
+int mpsxx_context_set_device_timeout(mpsxx_context* ctx, int64_t timeout_ns);
 
 /* ---- tensors ------------------------------------------------------------- */
 /* Create a block-sparse tensor.  qn holds 2*sum(nsec) ints (p, 2Sz per sector,

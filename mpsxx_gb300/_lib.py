@@ -29,6 +29,7 @@ SIGNATURES = {
     "mpsxx_context_set_sigma_schedule": (C.c_int, [vp, C.c_int64, C.c_int, C.c_int]),
     "mpsxx_context_set_svd_routes": (C.c_int, [vp, C.c_int, C.c_int]),
     "mpsxx_context_set_plan_cache": (C.c_int, [vp, C.c_int64]),
+    "mpsxx_context_set_device_timeout": (C.c_int, [vp, C.c_int64]),
     "mpsxx_sigma_plan_stats": (C.c_int, [vp, vp, vp, vp, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_mpo_gradient": (C.c_int, [vp, vp, vp, vp, vp, vp, c_dbl_p, c_dbl_p]),
     "mpsxx_merge_rows": (C.c_int, [vp, vp, vpp]),

@@ -51,6 +51,10 @@ class Context:
         check(lib().mpsxx_context_set_sigma_schedule(self.h, int(w_budget_bytes), int(target_tiles),
                                                      int(bool(fp32_intermediate))))
 
+    def set_device_timeout(self, timeout_ns: int = 0):
+        """Wait limit of the tensor-core kernels in ns (<= 0: the default 20 s)."""
+        check(lib().mpsxx_context_set_device_timeout(self.h, int(timeout_ns)))
+
     def set_plan_cache(self, max_plans: int = 512):
         """Plans kept per kind before a cache is emptied."""
         check(lib().mpsxx_context_set_plan_cache(self.h, int(max_plans)))

@@ -414,9 +414,9 @@ class Batch {
     launch_bzero(g->probs.get(), nm, g->nmax, vec_.as<double>(), kSlotOut, ctx_.stream);
     launch_pack(g->packs.get(), g->npacks, vec_.as<double>(), arPsi_.as<uint8_t>(), ctx_.stream);
     launch_gemm_pk(arL_.as<uint8_t>(), arPsi_.as<uint8_t>(), 1.0, nullptr, arScr_.as<uint8_t>(), g->t1.get(), g->n1,
-                   g->k1.get(), g->p1.get(), nullptr, single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx_.stream);
+                   g->k1.get(), g->p1.get(), nullptr, single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx_.stream, ctx_.device_timeout_ns);
     launch_gemm_pk(arScr_.as<uint8_t>(), arR_.as<uint8_t>(), 1.0, vec_.as<double>(), nullptr, g->t2.get(), g->n2,
-                   g->k2.get(), g->p2.get(), ctx_.gemm_part.as<double>(), kOutFP64, single ? 1 : 0, err, ctx_.stream);
+                   g->k2.get(), g->p2.get(), ctx_.gemm_part.as<double>(), kOutFP64, single ? 1 : 0, err, ctx_.stream, ctx_.device_timeout_ns);
     launch_gemm_pk_reduce(g->red.get(), g->nred, g->k2.get(), 1.0, ctx_.gemm_part.as<double>(), vec_.as<double>(),
                           ctx_.stream);
     cuda_check(cudaStreamEndCapture(ctx_.stream, &graph), "batch capture end");

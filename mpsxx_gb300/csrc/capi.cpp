@@ -157,6 +157,13 @@ int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes,
   });
 }
 
+int mpsxx_context_set_device_timeout(mpsxx_context* ctx, int64_t timeout_ns) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    ctx->ctx->device_timeout_ns = timeout_ns > 0 ? static_cast<uint64_t>(timeout_ns) : kPkTimeoutNs;
+  });
+}
+
 int mpsxx_context_set_plan_cache(mpsxx_context* ctx, int64_t max_plans) {
   return guard([&] {
     need(ctx && ctx->ctx, "null context");

@@ -841,7 +841,7 @@ static void run_split_gemm(Context& ctx, SplitGemm& sg, const GemmPlan& g, doubl
   int* err = device_err_flag(ctx);
   launch_gemm_pk(sg.pa.buf.as<uint8_t>(), sg.pb.buf.as<uint8_t>(), alpha, C, nullptr, g.tiles_tc.get(),
                  static_cast<int>(g.h_tiles_tc.size()), g.dtasks.get(), sg.pk.get(), part, kOutFP64, 0, err,
-                 ctx.stream);
+                 ctx.stream, ctx.device_timeout_ns);
   if (g.nslots_tc > 0)
     launch_gemm_pk_reduce(g.reduce_tc.get(), static_cast<int>(g.h_reduce_tc.size()), g.dtasks.get(), alpha, part, C,
                           ctx.stream);
@@ -1048,11 +1048,11 @@ static void sigma_groups_run(Context& ctx, SigmaPlan& p, double* sigma) {
     if (G.t1_count)
       launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.group_scr.as<uint8_t>(),
                      p.gt1.get() + G.t1_begin, G.t1_count, p.gtasks1.get(), p.pk1.get(), nullptr,
-                     p.scr1_single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx.stream);
+                     p.scr1_single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx.stream, ctx.device_timeout_ns);
     if (G.t2_count)
       launch_gemm_pk(p.group_scr.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
                      p.gt2.get() + G.t2_begin, G.t2_count, p.s2.dtasks.get(), p.gpk2.get(), part, kOutFP64,
-                     p.scr1_single ? 1 : 0, err, ctx.stream);
+                     p.scr1_single ? 1 : 0, err, ctx.stream, ctx.device_timeout_ns);
     if (G.r_count)
       launch_gemm_pk_reduce(p.gred.get() + G.r_begin, G.r_count, p.s2.dtasks.get(), 1.0, part, sigma, ctx.stream);
     ctx.kernel_launches += (G.t1_count > 0) + (G.t2_count > 0) + (G.r_count > 0);
@@ -1210,12 +1210,12 @@ static void sigma_run_pk_whole(Context& ctx, SigmaPlan& p, double* sigma) {
   int* err = device_err_flag(ctx);
   launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.pk_scr1.buf.as<uint8_t>(),
                  p.s1.tiles_tc.get(), static_cast<int>(p.s1.h_tiles_tc.size()), p.pk_tasks1.get(), p.pk1.get(),
-                 nullptr, p.scr1_single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx.stream);
+                 nullptr, p.scr1_single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx.stream, ctx.device_timeout_ns);
   ctx.gemm_part.ensure(std::max<size_t>(p.s2.partial_bytes_tc(), 16), ctx.stream);
   double* part = ctx.gemm_part.as<double>();
   launch_gemm_pk(p.pk_scr1.buf.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
                  p.s2.tiles_tc.get(), static_cast<int>(p.s2.h_tiles_tc.size()), p.s2.dtasks.get(), p.pk2.get(), part,
-                 kOutFP64, p.scr1_single ? 1 : 0, err, ctx.stream);
+                 kOutFP64, p.scr1_single ? 1 : 0, err, ctx.stream, ctx.device_timeout_ns);
   if (p.s2.nslots_tc > 0)
     launch_gemm_pk_reduce(p.s2.reduce_tc.get(), static_cast<int>(p.s2.h_reduce_tc.size()), p.s2.dtasks.get(), 1.0,
                           part, sigma, ctx.stream);

@@ -297,6 +297,7 @@ struct Context {
   int64_t sigma_w_budget = -1;
   int sigma_target_tiles = 0;
   bool sigma_fp32_intermediate = false;  // with a forced schedule: FP32 L*psi tiles
+  uint64_t device_timeout_ns = kPkTimeoutNs;  // wait limit of the tensor-core kernels
   // canonicalize routing: blocks with min(m, n) <= svd_jacobi_cols go to the batched
   // Jacobi kernel, the rest with a Gram dimension <= svd_gram_max to the batched
   // eigensolver; < 0 selects the defaults

@@ -129,9 +129,12 @@ struct DPack {
 // offset of the block's grid, ldc = its K slices per row tile) instead of FP64 C /
 // partials.  a_single: the A tiles are FP32 (kPkTileA1Bytes each), split into hi|lo
 // in shared memory before the MMAs; otherwise packed hi|lo (kPkTileABytes).
+// Every wait of the kernel gives up after timeout_ns (the whole launch): the kernel then
+// drains its own bulk copies and MMAs, frees its tensor memory, sets *err and returns.
+constexpr uint64_t kPkTimeoutNs = 20000000000ull;  // 20 s
 void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
-                    int out_packed, int a_single, int* err, cudaStream_t st);
+                    int out_packed, int a_single, int* err, cudaStream_t st, uint64_t timeout_ns = kPkTimeoutNs);
 void launch_gemm_pk_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
                            double* C, cudaStream_t st);
 void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst, cudaStream_t st);

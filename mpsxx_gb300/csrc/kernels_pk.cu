@@ -132,9 +132,14 @@ __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
   return done != 0;
 }
 
-// bounded wait; false on timeout or when another role aborted
+// bounded wait; false on timeout (the deadline is checked on entry too, so a limit
+// already past always ends the kernel) or when another role aborted
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint64_t deadline,
                                           volatile int* abort_flag) {
+  if (global_ns() > deadline) {
+    *abort_flag = 1;
+    return false;
+  }
   while (!mbar_try(mbar, parity)) {
     if (*abort_flag) return false;
     if (global_ns() > deadline) {
@@ -144,6 +149,14 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint64
   }
   return true;
 }
+
+// bounded wait that ignores the abort flag: draining the kernel's own asynchronous
+// work (bulk copies, MMAs) before it frees tensor memory and exits
+__device__ __forceinline__ void mbar_drain(uint32_t mbar, uint32_t parity, uint64_t deadline) {
+  while (!mbar_try(mbar, parity) && global_ns() <= deadline) {
+  }
+}
+constexpr uint64_t DRAIN_NS = 1000000000ull;  // 1 s
 
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
@@ -195,6 +208,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
   __shared__ __align__(8) uint64_t conv_bar[STAGES];
+  __shared__ __align__(8) uint64_t drain_bar;
   __shared__ __align__(8) uint64_t accf_bar[2];
   __shared__ __align__(8) uint64_t acce_bar[2];
   __shared__ uint32_t tmem_slot;
@@ -217,6 +231,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       mbar_init(smem_u32(&accf_bar[b]), 1);
       mbar_init(smem_u32(&acce_bar[b]), EPI_THREADS);
     }
+    mbar_init(smem_u32(&drain_bar), 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
@@ -265,6 +280,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
         }
       }
+      // every bulk copy issued lands before the kernel exits (after an abort the
+      // consumers no longer wait for them): the last STAGES slices' phases
+      const uint64_t dl = global_ns() + DRAIN_NS;
+      for (int k = slice - STAGES < 0 ? 0 : slice - STAGES; k < slice; ++k)
+        mbar_drain(smem_u32(&full_bar[k % STAGES]), (uint32_t)(k / STAGES) & 1u, dl);
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
@@ -339,6 +359,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
         }
       }
+      // every MMA issued has completed before tensor memory is freed
+      mma_commit(smem_u32(&drain_bar));
+      mbar_drain(smem_u32(&drain_bar), 0u, global_ns() + DRAIN_NS);
     }
   } else if (warp == 2 || warp == 3) {
     // ---------------- converter (FP32 A tiles) ----------------
@@ -578,7 +601,7 @@ int pk_smem_bytes() { return SMEM_BYTES; }
 
 void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
-                    int out_packed, int a_single, int* err, cudaStream_t st) {
+                    int out_packed, int a_single, int* err, cudaStream_t st, uint64_t timeout_ns) {
   if (ntiles <= 0) return;
   static int nsm = 0;
   if (nsm == 0) {
@@ -589,7 +612,6 @@ void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double
     if (nsm <= 0) nsm = 152;
   }
   // one persistent CTA per SM; the bound covers the whole launch, not one tile
-  const uint64_t timeout_ns = 20000000000ull;  // 20 s
   const int grid = ntiles < nsm ? ntiles : nsm;
   gemm_pk_kernel<<<grid, NTHREADS, SMEM_BYTES, st>>>(Apk, Bpk, alpha, C, Cpk, tiles, ntiles, tasks, pairs, partial,
                                                      out_packed, a_single, err, timeout_ns);

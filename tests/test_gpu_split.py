@@ -223,3 +223,28 @@ def test_split_sigma_schedules_agree(ctx, schedule):
     print("schedule", schedule, "split-vs-fp64 rel err", err)
     assert err < 2e-6
     assert np.array_equal(again.download(), s32)
+
+
+def test_split_sigma_wait_limit_reports_timeout_and_context_stays_usable(ctx):
+    """Failure detection without a GPU fault: with a 1 ns wait limit the tensor-core
+    kernel's first wait gives up (the limit is checked on entry), it drains its own
+    copies and MMAs, frees its tensor memory and returns; the call reports
+    DEVICE_TIMEOUT, and with the default limit back the same context computes the split
+    H_eff*psi within 2e-6 of FP64."""
+    from mpsxx_gb300 import core
+    from mpsxx_gb300._lib import MpsxxError
+
+    case = hubbard_bond()
+    L, R, P = dev(ctx, case["mL"]), dev(ctx, case["mR"]), dev(ctx, case["full"])
+    core.set_precision(ctx, core.SPLIT_TF32)
+    ctx.set_device_timeout(1)
+    try:
+        S = P.like()
+        with pytest.raises(MpsxxError) as err:
+            core.compute_sigma_vector(ctx, L, R, P, S)
+        assert "DEVICE_TIMEOUT" in str(err.value) or getattr(err.value, "code", None) == 4
+    finally:
+        ctx.set_device_timeout(0)
+        core.set_precision(ctx, core.FP64)
+    s64, s32 = sigma_both(ctx, L, R, P)
+    assert rel_err(s32, s64) < 2e-6
