@@ -598,7 +598,9 @@ def main():
     peaks, src = roofline_peaks()
     fp64_peak = measure_fp64_peak(torch)
     bond = bond_compare(ctx, wl, args.M, args.tole) if args.bond_step else None
-    sweep = sweep_compare(args, local) if not args.no_sweep else None
+    # the sweep comparison and the CPU baseline belong to the one-GPU line; replicas
+    # (N > 1) time H_eff*psi only
+    sweep = sweep_compare(args, local) if not args.no_sweep and ws == 1 else None
     grad = gradient_bench(args, local) if args.gradient else None
     scan_res = scan_bench(args, local) if args.scan else None
     out = None
@@ -649,7 +651,7 @@ def main():
             "scan": scan_res,
             "clocks": clk.summary(),
         }
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and ws == 1:
             out["cpu_baseline"] = cpu_sigma_sample(wl, args.cpu_seconds)
         print(json.dumps(out), flush=True)
     barrier(ws)
