@@ -18,6 +18,10 @@
 namespace mpsxx {
 
 void cuda_check(cudaError_t e, const char* what);
+void solver_check(cusolverStatus_t s, const char* what);
+// the block cache serves a new stream (its blocks then wait on events when taken by
+// another stream)
+void register_cache_stream(cudaStream_t st);
 
 // Grow-only device buffer.  Storage comes from the process-wide block cache:
 // released blocks are kept for reuse instead of being returned with cudaFree, which
