@@ -213,9 +213,22 @@ int mpsxx_tensor_accumulate(mpsxx_context* ctx, double alpha, const mpsxx_tensor
 
 /* Truncated SVD of a merged wavefunction; forward: lmat = U, rmat = s V^T;
  * backward: lmat = U s, rmat = V^T.  Replaces mpsxx::canonicalize(forward, wfnc,
- * lmat, rmat, M, noise) (src/canonicalize.hpp:88-106).  noise must be < 1e-8. */
+ * lmat, rmat, M, noise) (src/canonicalize.hpp:88-106).  With noise >= 1e-8 the SVD
+ * runs on make_noise(wfnc, noise); wfnc itself is left unchanged (the reference
+ * noises it in place and its callers do not read it afterwards). */
 int mpsxx_canonicalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* wfnc, int M, double noise,
                        mpsxx_tensor** lmat, mpsxx_tensor** rmat);
+
+/* wfnc += noise * (array of the reference's noise sequence), in place; nothing when
+ * noise < 1e-8.  Replaces mpsxx::make_noise(wfnc, noise) (src/canonicalize.hpp:11-24):
+ * the array holds every allowed block whose sectors have a block in wfnc (blocks
+ * wfnc lacks are added), and each of its blocks holds, row-major, the leading values
+ * of the sequence of mpsxx_noise_sequence. */
+int mpsxx_make_noise(mpsxx_context* ctx, mpsxx_tensor* wfnc, double noise);
+
+/* Host only: the first n values make_noise draws (a default-seeded std::mt19937 through
+ * std::uniform_real_distribution<double>(-1, 1), src/canonicalize.hpp:16-21). */
+int mpsxx_noise_sequence(int64_t n, double* out);
 
 /* One bond of the two-site sweep (src/optimize.hpp:495-651), single root and one
  * operator group: returns the Ritz value, the renormalised operator of the grown
@@ -226,7 +239,7 @@ int mpsxx_canonicalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* wfnc
 int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_tensor* lmpo,
                                   const mpsxx_tensor* rmpo, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                                   const mpsxx_tensor* lwfn, const mpsxx_tensor* rwfn, double tole, int M,
-                                  double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
+                                  double noise, double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
                                   mpsxx_tensor** new_rwfn, double* stats);
 
 /* optimize_twosite_merged for n independent bonds at once (e.g. the chains of a
@@ -234,15 +247,16 @@ int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_t
  * run in lockstep: in split precision every H_eff*psi of the unconverged bonds is
  * one grouped tensor-core launch per stage (captured with its packing as a CUDA
  * graph) and the vector algebra is one batched launch per operation; the results
- * equal n separate mpsxx_optimize_twosite_merged calls up to rounding.  stats:
- * 6 doubles per bond (n_sigma, n_sigma_fp64, micro iterations, converged,
- * |r|^2, energy before refinement). */
+ * equal n separate mpsxx_optimize_twosite_merged calls up to rounding.  noise (may be
+ * NULL: no noise) holds each bond's make_noise amplitude.  stats: 6 doubles per bond
+ * (n_sigma, n_sigma_fp64, micro iterations, converged, |r|^2, energy before
+ * refinement). */
 int mpsxx_optimize_twosite_merged_batch(mpsxx_context* ctx, int n, const int* forward,
                                         const mpsxx_tensor* const* lmpo, const mpsxx_tensor* const* rmpo,
                                         const mpsxx_tensor* const* lopr, const mpsxx_tensor* const* ropr,
                                         const mpsxx_tensor* const* lwfn, const mpsxx_tensor* const* rwfn, double tole,
-                                        const int* M, double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
-                                        mpsxx_tensor** new_rwfn, double* stats);
+                                        const int* M, const double* noise, double* energy, mpsxx_tensor** env,
+                                        mpsxx_tensor** new_lwfn, mpsxx_tensor** new_rwfn, double* stats);
 
 /* Adjoint of the bond energy with respect to the MPO: for the normalised merged
  * two-site wavefunction psi[A,B] of the bond between lmpo and rmpo,
@@ -258,13 +272,14 @@ int mpsxx_mpo_gradient(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx
                        const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* psi, double* grad_l,
                        double* grad_r);
 
-/* a[i, j, k] -> out[(i, j), k] and its inverse (QSTmerge / QSTexpand over the
- * leading two indices, include/btas/QSPARSE/QSTmerge.h:31-120,218-295) for the
- * one-site algorithm; `like` supplies the unmerged sectors. */
+/* a[i, j, k, ...] -> out[(i, j), k, ...] and its inverse (QSTmerge / QSTexpand over
+ * the leading two indices, include/btas/QSPARSE/QSTmerge.h:31-120,218-295) for the
+ * one-site algorithm; a has 3 or more indices; `like` (3 indices) supplies the
+ * unmerged sectors. */
 int mpsxx_merge_rows(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** out);
 int mpsxx_expand_rows(mpsxx_context* ctx, const mpsxx_tensor* b, const mpsxx_tensor* like, mpsxx_tensor** out);
 
-/* Merge the last two indices of a 3-index site tensor in place of the
+/* Merge the last two indices of a tensor of 3 or more indices in place of the
  * reference's QSTmerge(a, cols_info, b) (include/btas/QSPARSE/QSTmerge.h:85-140). */
 int mpsxx_merge_cols(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** out);
 

@@ -146,6 +146,11 @@ inline double diagonalize(Context& ctx, const QSDArray& lopr, const QSDArray& ro
 }
 }  // namespace Davidson
 
+// wfnc += noise * noise array, in place; nothing when noise < 1e-8 (src/canonicalize.hpp:11-24).
+inline void make_noise(Context& ctx, QSDArray& wfnc, double noise) {
+  check(mpsxx_make_noise(ctx.get(), wfnc.get(), noise));
+}
+
 // Truncated SVD: forward -> lmat = U, rmat = s V^T; backward -> lmat = U s, rmat = V^T.
 inline void canonicalize(Context& ctx, bool forward, const QSDArray& wfnc, QSDArray& lmat, QSDArray& rmat,
                          int M = 0, double noise = 0.0) {

@@ -37,8 +37,8 @@ SIGNATURES = {
                                               C.POINTER(C.c_int)]),
     "mpsxx_tensor_accumulate": (C.c_int, [vp, C.c_double, vp, vp]),
     "mpsxx_optimize_twosite_merged_batch": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), vpp, vpp, vpp, vpp, vpp, vpp,
-                                                      C.c_double, C.POINTER(C.c_int), c_dbl_p, vpp, vpp, vpp,
-                                                      c_dbl_p]),
+                                                      C.c_double, C.POINTER(C.c_int), c_dbl_p, c_dbl_p, vpp, vpp,
+                                                      vpp, c_dbl_p]),
     "mpsxx_expand_rows": (C.c_int, [vp, vp, vp, vpp]),
     "mpsxx_context_profile": (C.c_int, [vp, C.c_int, C.c_int, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_context_set_precision": (C.c_int, [vp, C.c_int]),
@@ -60,8 +60,10 @@ SIGNATURES = {
     "mpsxx_compute_merged_operator": (C.c_int, [vp, C.c_int, vp, vp, vpp]),
     "mpsxx_diagonalize": (C.c_int, [vp, vp, vp, vp, vp, C.c_double, c_dbl_p, c_int_p]),
     "mpsxx_canonicalize": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_double, vpp, vpp]),
-    "mpsxx_optimize_twosite_merged": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, C.c_int, c_dbl_p,
-                                                vpp, vpp, vpp, c_dbl_p]),
+    "mpsxx_optimize_twosite_merged": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, C.c_int,
+                                                C.c_double, c_dbl_p, vpp, vpp, vpp, c_dbl_p]),
+    "mpsxx_make_noise": (C.c_int, [vp, vp, C.c_double]),
+    "mpsxx_noise_sequence": (C.c_int, [C.c_int64, c_dbl_p]),
     "mpsxx_merge_cols": (C.c_int, [vp, vp, vpp]),
     "mpsxx_gemm": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, vp, vp, C.c_int, vpp]),
     "mpsxx_expand_cols": (C.c_int, [vp, vp, vp, vpp]),

@@ -340,9 +340,24 @@ def accumulate(ctx: Context, alpha: float, x: Tensor, y: Tensor):
 
 
 def canonicalize(ctx: Context, forward: bool, wfnc: Tensor, M: int = 0, noise: float = 0.0):
+    """Truncated SVD (src/canonicalize.hpp:88-106); with noise >= 1e-8 of
+    make_noise(wfnc, noise), wfnc itself unchanged."""
     lo, ro = _out(), _out()
     check(lib().mpsxx_canonicalize(ctx.h, int(bool(forward)), wfnc.h, int(M), float(noise), C.byref(lo), C.byref(ro)))
     return Tensor(lo, ctx), Tensor(ro, ctx)
+
+
+def make_noise(ctx: Context, wfnc: Tensor, noise: float):
+    """wfnc += noise * noise array, in place (src/canonicalize.hpp:11-24); nothing
+    when noise < 1e-8.  Blocks the noise array has and wfnc lacks are added."""
+    check(lib().mpsxx_make_noise(ctx.h, wfnc.h, float(noise)))
+
+
+def noise_sequence(n: int) -> np.ndarray:
+    """The first n values make_noise draws (host only)."""
+    out = np.zeros(max(int(n), 0))
+    check(lib().mpsxx_noise_sequence(int(n), out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
 
 
 def gemm(ctx: Context, transa: int, transb: int, alpha: float, a: Tensor, b: Tensor, c_rank: int) -> Tensor:
@@ -354,12 +369,14 @@ def gemm(ctx: Context, transa: int, transb: int, alpha: float, a: Tensor, b: Ten
 BATCH_STAT_KEYS = ("n_sigma", "n_sigma_fp64", "micro", "converged", "rnorm", "energy_split")
 
 
-def optimize_twosite_merged_batch(ctx: Context, forward, lmpo, rmpo, lopr, ropr, lwfn, rwfn, tole: float, M):
+def optimize_twosite_merged_batch(ctx: Context, forward, lmpo, rmpo, lopr, ropr, lwfn, rwfn, tole: float, M,
+                                  noise=0.0):
     """optimize_twosite_merged for n independent bonds at once (lists of n entries;
-    forward and M may be scalars).  Returns (energies, envs, new_lwfns, new_rwfns, stats)."""
+    forward, M and noise may be scalars).  Returns (energies, envs, new_lwfns, new_rwfns, stats)."""
     n = len(lmpo)
     fw = [int(bool(forward))] * n if isinstance(forward, (bool, int)) else [int(bool(f)) for f in forward]
     Ms = [int(M)] * n if isinstance(M, int) else [int(m) for m in M]
+    nz = np.full(max(n, 1), float(noise)) if np.isscalar(noise) else np.asarray(noise, dtype=np.float64)
 
     def handles(ts):
         return (C.c_void_p * n)(*[t.h.value if isinstance(t.h, C.c_void_p) else t.h for t in ts])
@@ -370,7 +387,8 @@ def optimize_twosite_merged_batch(ctx: Context, forward, lmpo, rmpo, lopr, ropr,
     dp = C.POINTER(C.c_double)
     check(lib().mpsxx_optimize_twosite_merged_batch(
         ctx.h, n, (C.c_int * n)(*fw), handles(lmpo), handles(rmpo), handles(lopr), handles(ropr), handles(lwfn),
-        handles(rwfn), float(tole), (C.c_int * n)(*Ms), e.ctypes.data_as(dp), env, nl, nr, st.ctypes.data_as(dp)))
+        handles(rwfn), float(tole), (C.c_int * n)(*Ms), nz.ctypes.data_as(dp), e.ctypes.data_as(dp), env, nl, nr,
+        st.ctypes.data_as(dp)))
     wrap = lambda arr: [Tensor(C.c_void_p(arr[i]), ctx) for i in range(n)]  # noqa: E731
     stats = [dict(zip(BATCH_STAT_KEYS, st[6 * i:6 * i + 6])) for i in range(n)]
     return e, wrap(env), wrap(nl), wrap(nr), stats
@@ -456,12 +474,12 @@ def get_precision(ctx: Context) -> int:
 
 
 def optimize_twosite_merged(ctx: Context, forward: bool, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor,
-                            lwfn: Tensor, rwfn: Tensor, tole: float, M: int):
+                            lwfn: Tensor, rwfn: Tensor, tole: float, M: int, noise: float = 0.0):
     e = C.c_double()
     env, nl, nr = _out(), _out(), _out()
     st = (C.c_double * 12)()
     check(lib().mpsxx_optimize_twosite_merged(ctx.h, int(bool(forward)), lmpo.h, rmpo.h, lopr.h, ropr.h, lwfn.h,
-                                              rwfn.h, float(tole), int(M), C.byref(e), C.byref(env), C.byref(nl),
-                                              C.byref(nr), st))
+                                              rwfn.h, float(tole), int(M), float(noise), C.byref(e), C.byref(env),
+                                              C.byref(nl), C.byref(nr), st))
     stats = dict(zip(BOND_STAT_KEYS, list(st)))
     return e.value, Tensor(env, ctx), Tensor(nl, ctx), Tensor(nr, ctx), stats

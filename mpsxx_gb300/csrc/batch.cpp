@@ -645,7 +645,11 @@ std::vector<BondOut> optimize_twosite_merged_batch(Context& ctx, const std::vect
   const std::vector<double> E = diagonalize_batch(ctx, Lp, Rp, Dp, Pp, tole, st);
   // all bonds' SVDs in one solve
   std::vector<CanonJob> jobs(N);
-  for (size_t c = 0; c < N; ++c) jobs[c] = CanonJob{args[c].forward, psi[c].get(), args[c].M};
+  std::vector<std::unique_ptr<DTensor>> noised(N);
+  for (size_t c = 0; c < N; ++c) {
+    noised[c] = make_noise(ctx, *psi[c], args[c].noise);
+    jobs[c] = CanonJob{args[c].forward, noised[c] ? noised[c].get() : psi[c].get(), args[c].M};
+  }
   std::vector<CanonResult> canon = canonicalize_many(ctx, jobs);
   {
     PhaseTimer tp(ctx, kPhBatchPlan);

@@ -9,7 +9,9 @@
 #include <atomic>
 #include <cmath>
 #include <exception>
+#include <iterator>
 #include <map>
+#include <random>
 #include <thread>
 
 #include "engine.hpp"
@@ -576,9 +578,93 @@ std::vector<CanonResult> canonicalize_many(Context& ctx, const std::vector<Canon
   return results;
 }
 
+// ---------------------------------------------------------------------------
+// make_noise (src/canonicalize.hpp:11-24)
+// ---------------------------------------------------------------------------
+// The reference builds the noise array as QSTArray(q, qshape, net dshape,
+// bind(dist, rgen)).  STArray::generate and TArray::generate take the generator by
+// value (include/btas/SPARSE/STArray.h:259-262, include/btas/DENSE/TArray.h:780-782),
+// so every block is filled by its own copy of the freshly seeded engine: element j of
+// any block (row-major) is the j-th value of one sequence, drawn here through the same
+// standard-library engine and distribution.
+std::vector<double> noise_sequence(int64_t n) {
+  std::vector<double> seq(static_cast<size_t>(std::max<int64_t>(n, 0)));
+  std::mt19937 rgen;
+  std::uniform_real_distribution<double> dist(-1.0, 1.0);
+  for (auto& v : seq) v = dist(rgen);
+  return seq;
+}
+
+std::unique_ptr<DTensor> make_noise(Context& ctx, const DTensor& wfnc, double noise) {
+  if (noise < 1.0e-8) return nullptr;
+  const Shape& sh = wfnc.sh;
+  // check_net_dshape (include/btas/SPARSE/STArray.h:386-401): the sector dimensions
+  // seen in the stored blocks, 0 for sectors without one
+  std::vector<std::vector<int>> net(sh.rank);
+  for (int i = 0; i < sh.rank; ++i) net[i].assign(sh.nsec(i), 0);
+  int idx[kMaxRank];
+  for (int64_t t : wfnc.tags) {
+    sh.index(t, idx);
+    for (int i = 0; i < sh.rank; ++i) net[i][idx[i]] = sh.dshape[i][idx[i]];
+  }
+  // allocate() of the noise array (STArray.h:219-237): allowed blocks of non-zero
+  // net size, ascending
+  std::vector<int64_t> ntags;
+  for (int64_t t = 0; t < sh.nsparse; ++t) {
+    sh.index(t, idx);
+    if (!sh.allowed(idx)) continue;
+    int64_t n = 1;
+    for (int i = 0; i < sh.rank; ++i) n *= net[i][idx[i]];
+    if (n > 0) ntags.push_back(t);
+  }
+  // Axpy reserves the noise blocks wfnc lacks (include/btas/SPARSE/STBLAS.h:133-145)
+  std::vector<int64_t> utags;
+  std::set_union(wfnc.tags.begin(), wfnc.tags.end(), ntags.begin(), ntags.end(), std::back_inserter(utags));
+  cudaStream_t st = ctx.stream;
+  auto out = std::make_unique<DTensor>();
+  static_cast<Tensor&>(*out) = static_cast<const Tensor&>(wfnc);
+  out->d = nullptr;
+  out->own = false;
+  out->ctx = &ctx;
+  if (utags.size() != wfnc.tags.size()) out->set_blocks(utags);
+  out->alloc_device(st, utags.size() != wfnc.tags.size());
+  if (utags.size() == wfnc.tags.size()) {
+    if (wfnc.nnz)
+      cuda_check(cudaMemcpyAsync(out->d, wfnc.d, wfnc.nnz * sizeof(double), cudaMemcpyDeviceToDevice, st),
+                 "make_noise copy");
+  } else {
+    std::vector<DCopy> cp;
+    for (size_t b = 0; b < wfnc.tags.size(); ++b) {
+      const int64_t n = wfnc.block_size(static_cast<int32_t>(b));
+      if (n > 0x7fffffff) throw Error(kInvalidArgument, "make_noise: block too large");
+      cp.push_back(DCopy{out->offsets[out->find(wfnc.tags[b])], wfnc.offsets[b], 1, static_cast<int>(n),
+                         static_cast<int>(n), static_cast<int>(n), 1.0});
+    }
+    DevArray<DCopy> dcp;
+    dcp.upload(cp, st);
+    launch_copy(dcp.get(), static_cast<int>(cp.size()), wfnc.d, out->d, 0, st);
+    ctx.kernel_launches += 1;
+  }
+  std::vector<DNoise> nb;
+  int64_t nmax = 0;
+  for (int64_t t : ntags) {
+    const int32_t b = out->find(t);
+    const int64_t n = out->block_size(b);
+    nb.push_back(DNoise{out->offsets[b], n});
+    nmax = std::max(nmax, n);
+  }
+  if (static_cast<int64_t>(ctx.noise_seq.n) < nmax) ctx.noise_seq.upload(noise_sequence(nmax), st);
+  DevArray<DNoise> dnb;
+  dnb.upload(nb, st);
+  launch_noise_axpy(dnb.get(), static_cast<int>(nb.size()), ctx.noise_seq.get(), noise, out->d, st);
+  ctx.kernel_launches += 1;
+  return out;
+}
+
 CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise) {
-  if (noise >= 1.0e-8) throw Error(kInvalidArgument, "canonicalize: noise injection is not supported");
-  std::vector<CanonResult> r = canonicalize_many(ctx, {CanonJob{forward, &wfnc, M}});
+  std::unique_ptr<DTensor> noised = make_noise(ctx, wfnc, noise);
+  std::vector<CanonResult> r = canonicalize_many(ctx, {CanonJob{forward, noised ? noised.get() : &wfnc, M}});
+  if (noised) ctx.sync();  // the noised copy is freed on return
   return std::move(r[0]);
 }
 

@@ -514,16 +514,36 @@ int mpsxx_canonicalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* wfnc
   });
 }
 
+int mpsxx_make_noise(mpsxx_context* ctx, mpsxx_tensor* wfnc, double noise) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    DTensor& x = ten_mut(wfnc);
+    need_device(x);
+    std::unique_ptr<DTensor> n = make_noise(c, x, noise);
+    if (!n) return;
+    c.sync();
+    wfnc->t = std::move(n);
+  });
+}
+
+int mpsxx_noise_sequence(int64_t n, double* out) {
+  return guard([&] {
+    need(n >= 0 && (n == 0 || out), "invalid noise sequence request");
+    const std::vector<double> seq = noise_sequence(n);
+    if (n) std::memcpy(out, seq.data(), static_cast<size_t>(n) * sizeof(double));
+  });
+}
+
 int mpsxx_optimize_twosite_merged(mpsxx_context* ctx, int forward, const mpsxx_tensor* lmpo,
                                   const mpsxx_tensor* rmpo, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                                   const mpsxx_tensor* lwfn, const mpsxx_tensor* rwfn, double tole, int M,
-                                  double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
+                                  double noise, double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
                                   mpsxx_tensor** new_rwfn, double* stats) {
   return guard([&] {
     need(env && new_lwfn && new_rwfn, "null output");
     Context& c = ctx_of(ctx);
     BondOut b = optimize_twosite_merged(c, forward != 0, ten(lmpo), ten(rmpo), ten(lopr), ten(ropr), ten(lwfn),
-                                        ten(rwfn), tole, M);
+                                        ten(rwfn), tole, M, noise);
     c.sync();
     if (energy) *energy = b.stats.energy;
     if (stats) {
@@ -550,8 +570,8 @@ int mpsxx_optimize_twosite_merged_batch(mpsxx_context* ctx, int n, const int* fo
                                         const mpsxx_tensor* const* lmpo, const mpsxx_tensor* const* rmpo,
                                         const mpsxx_tensor* const* lopr, const mpsxx_tensor* const* ropr,
                                         const mpsxx_tensor* const* lwfn, const mpsxx_tensor* const* rwfn, double tole,
-                                        const int* M, double* energy, mpsxx_tensor** env, mpsxx_tensor** new_lwfn,
-                                        mpsxx_tensor** new_rwfn, double* stats) {
+                                        const int* M, const double* noise, double* energy, mpsxx_tensor** env,
+                                        mpsxx_tensor** new_lwfn, mpsxx_tensor** new_rwfn, double* stats) {
   return guard([&] {
     need(n >= 0, "negative batch size");
     need(n == 0 || (forward && lmpo && rmpo && lopr && ropr && lwfn && rwfn && M && energy && env && new_lwfn &&
@@ -568,6 +588,7 @@ int mpsxx_optimize_twosite_merged_batch(mpsxx_context* ctx, int n, const int* fo
       args[i].lwfn = &ten(lwfn[i]);
       args[i].rwfn = &ten(rwfn[i]);
       args[i].M = M[i];
+      args[i].noise = noise ? noise[i] : 0.0;
     }
     std::vector<BondOut> out = optimize_twosite_merged_batch(c, args, tole);
     for (int i = 0; i < n; ++i) {
@@ -607,8 +628,9 @@ int mpsxx_merge_cols(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** o
     need(out != nullptr, "null output");
     Context& c = ctx_of(ctx);
     const DTensor& A = ten(a);
-    need(A.sh.rank == 3, "merge_cols: expects a 3-index tensor");
-    MergeInfo info({A.sh.qshape[1], A.sh.qshape[2]}, {A.sh.dshape[1], A.sh.dshape[2]});
+    need(A.sh.rank >= 3, "merge_cols: expects a tensor of 3 or more indices");
+    const int r = A.sh.rank;
+    MergeInfo info({A.sh.qshape[r - 2], A.sh.qshape[r - 1]}, {A.sh.dshape[r - 2], A.sh.dshape[r - 1]});
     *out = wrap(merge_cols(c, A, info), ctx);
     c.sync();
   });
@@ -619,7 +641,7 @@ int mpsxx_merge_rows(mpsxx_context* ctx, const mpsxx_tensor* a, mpsxx_tensor** o
     need(out != nullptr, "null output");
     Context& c = ctx_of(ctx);
     const DTensor& A = ten(a);
-    need(A.sh.rank == 3, "merge_rows: expects a 3-index tensor");
+    need(A.sh.rank >= 3, "merge_rows: expects a tensor of 3 or more indices");
     MergeInfo info({A.sh.qshape[0], A.sh.qshape[1]}, {A.sh.dshape[0], A.sh.dshape[1]});
     *out = wrap(merge_rows(c, info, A), ctx);
     c.sync();

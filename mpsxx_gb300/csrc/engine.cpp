@@ -280,6 +280,7 @@ template struct DevArray<DDiagPair>;
 template struct DevArray<DCopy>;
 template struct DevArray<DScatterDst>;
 template struct DevArray<DScatterSrc>;
+template struct DevArray<DNoise>;
 template struct DevArray<double>;
 template struct DevArray<int64_t>;
 template struct DevArray<int>;
@@ -2307,7 +2308,7 @@ void release_bond_buffers(Context& ctx) {
 
 BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo, const DTensor& rmpo,
                                 const DTensor& lopr, const DTensor& ropr, const DTensor& lwfn, const DTensor& rwfn,
-                                double tole, int M) {
+                                double tole, int M, double noise) {
   BondOut out;
   double t0 = now();
   auto mL = compute_merged_operator(ctx, true, lmpo, lopr);
@@ -2330,7 +2331,7 @@ BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo,
   out.stats.sigma_flops = ctx.sigma_flops - f0;
   double t3 = now();
   out.stats.t_davidson = t3 - t2;
-  CanonResult cr = canonicalize(ctx, forward, *psi, M, 0.0);
+  CanonResult cr = canonicalize(ctx, forward, *psi, M, noise);
   double t4 = now();
   out.stats.t_svd = t4 - t3;
   if (forward)

@@ -307,6 +307,8 @@ struct Context {
   // eigensolver; < 0 selects the defaults
   int svd_jacobi_cols = -1;
   int svd_gram_max = -1;
+  // make_noise: the leading values of the noise sequence on the device (grown on demand)
+  DevArray<double> noise_seq;
   // plan caches are shared with the planning threads of a batched step: lookups and
   // insertions under plan_mu; while planning_threads is set no cache is emptied
   std::mutex plan_mu;
@@ -415,6 +417,14 @@ struct CanonResult {
   double discarded = 0.0;
 };
 CanonResult canonicalize(Context& ctx, bool forward, const DTensor& wfnc, int M, double noise);
+// src/canonicalize.hpp:11-24: the first n values of the sequence make_noise draws
+// (a default-seeded std::mt19937 through std::uniform_real_distribution<double>(-1, 1)).
+std::vector<double> noise_sequence(int64_t n);
+// make_noise: a copy of wfnc plus noise times the noise array (null when noise < 1e-8,
+// which leaves wfnc unchanged).  The noise array holds every allowed block whose
+// sectors have a block in wfnc; each of its blocks holds the leading values of
+// noise_sequence in row-major order, and blocks that wfnc lacks are added.
+std::unique_ptr<DTensor> make_noise(Context& ctx, const DTensor& wfnc, double noise);
 // Several independent canonicalisations sharing one solve (one Jacobi launch and one
 // set of solver lanes for all their blocks, one read-back of the singular values).
 struct CanonJob {
@@ -462,7 +472,8 @@ struct BondOut {
 };
 BondOut optimize_twosite_merged(Context& ctx, bool forward, const DTensor& lmpo, const DTensor& rmpo,
                                 const DTensor& lopr, const DTensor& ropr, const DTensor& lwfn,
-                                const DTensor& rwfn, double tole, int M);
+                                const DTensor& rwfn, double tole, int M,
+                                double noise = 0.0);
 
 // --- batched steps over independent problems (batch.cpp) --------------------
 // Lowest eigenpairs of independent effective Hamiltonians, Davidson in lockstep with
@@ -475,6 +486,7 @@ struct BondArgs {
   const DTensor *lmpo = nullptr, *rmpo = nullptr, *lopr = nullptr, *ropr = nullptr, *lwfn = nullptr,
                 *rwfn = nullptr;
   int M = 0;
+  double noise = 0.0;  // make_noise before the truncation (src/canonicalize.hpp:95)
 };
 // optimize_twosite_merged for every bond of `args` (independent problems), their
 // Davidson iterations batched.

@@ -79,6 +79,10 @@ struct DDiagTask {
 struct DDiagPair {
   int64_t l_off, r_off;
 };
+// Noise block of make_noise: y[off + j] += noise * seq[j] for j < n.
+struct DNoise {
+  int64_t off, n;
+};
 
 // Davidson subspace size: multi-dot and rotation kernels handle up to 10 vectors
 constexpr int kMaxDot = 10;
@@ -196,6 +200,10 @@ void launch_scal_dev(double* x, int64_t n, const double* s, int mode, cudaStream
 void launch_axpy_dev(double* y, const double* x, int64_t n, const double* s, double sign, cudaStream_t st);
 void launch_axpy(double* y, const double* x, int64_t n, double a, cudaStream_t st);
 void launch_copy_vec(double* y, const double* x, int64_t n, cudaStream_t st);
+// y[b.off + j] = y[b.off + j] + noise * seq[j] for every block b (product and sum
+// rounded separately, as y + noise*x in double arithmetic without contraction)
+void launch_noise_axpy(const DNoise* blocks, int nblocks, const double* seq, double noise, double* y,
+                       cudaStream_t st);
 // out[i*m + j] = dot(X_i, Y_j) for i < nx, j < ny (vectors strided by `stride`)
 void launch_multidot(const double* X, int nx, const double* Y, int ny, int64_t n, int64_t stride, double* out,
                      double* partial, int nblocks, cudaStream_t st);

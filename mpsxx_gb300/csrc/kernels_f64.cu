@@ -251,6 +251,13 @@ __global__ void axpy_kernel(double* y, const double* x, int64_t n, double a) {
     y[i] = fma(a, x[i], y[i]);
 }
 
+__global__ void noise_axpy_kernel(const DNoise* __restrict__ blocks, const double* __restrict__ seq, double noise,
+                                  double* __restrict__ y) {
+  const DNoise b = blocks[blockIdx.x];
+  for (int64_t j = threadIdx.x; j < b.n; j += blockDim.x)
+    y[b.off + j] = __dadd_rn(y[b.off + j], __dmul_rn(noise, seq[j]));
+}
+
 __global__ void copy_vec_kernel(double* y, const double* x, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = x[i];
@@ -424,6 +431,12 @@ void launch_axpy_dev(double* y, const double* x, int64_t n, const double* s, dou
 void launch_axpy(double* y, const double* x, int64_t n, double a, cudaStream_t st) {
   if (n <= 0) return;
   axpy_kernel<<<grid_for(n), 256, 0, st>>>(y, x, n, a);
+}
+
+void launch_noise_axpy(const DNoise* blocks, int nblocks, const double* seq, double noise, double* y,
+                       cudaStream_t st) {
+  if (nblocks <= 0) return;
+  noise_axpy_kernel<<<nblocks, 256, 0, st>>>(blocks, seq, noise, y);
 }
 
 void launch_copy_vec(double* y, const double* x, int64_t n, cudaStream_t st) {

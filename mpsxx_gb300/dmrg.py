@@ -207,9 +207,10 @@ class SweepLog:
     kind: str = "twosite"
 
 
-def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None) -> SweepLog:
+def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None, noise: float = 0.0) -> SweepLog:
     """Forward then backward sweep; Davidson tolerance 0.1*tole; sweep energy =
-    minimum over bonds (src/make_sweep.cpp:12-253)."""
+    minimum over bonds (src/make_sweep.cpp:12-253); ``noise`` is added to every bond's
+    wavefunction before its truncation (make_noise, src/canonicalize.hpp:11-24)."""
     N = len(st.mpo)
     t0 = time.perf_counter()
     es: List[float] = []
@@ -227,7 +228,7 @@ def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None) -> Sw
     for i in range(N - 1):
         e, env, nl, nr, stats = core.optimize_twosite_merged(ctx, True, st.mpo[i], st.mpo[i + 1], st.lenv[i],
                                                              st.renv[i + 1], st.wave[i], st.wave[i + 1],
-                                                             0.1 * tole, st.M)
+                                                             0.1 * tole, st.M, noise)
         st.lenv[i + 1] = env
         st.wave[i], st.wave[i + 1] = nl, nr
         es.append(e)
@@ -237,7 +238,7 @@ def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None) -> Sw
     for i in range(N - 1, 0, -1):
         e, env, nl, nr, stats = core.optimize_twosite_merged(ctx, False, st.mpo[i - 1], st.mpo[i], st.lenv[i - 1],
                                                              st.renv[i], st.wave[i - 1], st.wave[i], 0.1 * tole,
-                                                             st.M)
+                                                             st.M, noise)
         st.renv[i - 1] = env
         st.wave[i - 1], st.wave[i] = nl, nr
         es.append(e)
@@ -247,7 +248,27 @@ def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None) -> Sw
     return SweepLog(min(es), es, nsig, flops, time.perf_counter() - t0, times)
 
 
-def optimize_onesite(ctx: Context, forward: bool, st: DeviceState, i: int, tole: float):
+def split_onesite_noise(ctx: Context, forward: bool, wf: Tensor, nb: Tensor, M: int, noise: float):
+    """One-site canonicalize with noise (src/canonicalize.hpp:48-66): the optimised site
+    tensor wf is joined with its neighbour nb (forward: wf[l,n,a] nb[a,n',r]; backward:
+    nb[l,n',a] wf[a,n,r]) into a two-site tensor, which is noised (make_noise) and split
+    again with truncation M (Gesvd<4,3>, src/canonicalize.hpp:27-45).  Returns (left,
+    right, merged factor): forward (U[l,n,a], sV[a,n',r], U merged over (l,n)); backward
+    (Us[l,n',a], V[a,n,r], V merged over (n,r))."""
+    if forward:
+        t4 = core.gemm(ctx, 0, 0, 1.0, wf, nb, 4)
+    else:
+        t4 = core.gemm(ctx, 0, 0, 1.0, nb, wf, 4)
+    core.make_noise(ctx, t4, noise)
+    m = core.merge_cols(ctx, core.merge_rows(ctx, t4))
+    a, b = core.canonicalize(ctx, forward, m, M)
+    lk, rk = (wf, nb) if forward else (nb, wf)
+    left = core.expand_rows(ctx, a, lk)
+    right = core.expand_cols(ctx, b, rk)
+    return left, right, (a if forward else b)
+
+
+def optimize_onesite(ctx: Context, forward: bool, st: DeviceState, i: int, tole: float, noise: float = 0.0):
     """One-site step at site i (src/optimize.hpp:37-145) through the merged hot path:
     forward, psi[(l,n), r] with mL = merge(L_i, W_i) and the unmerged R_i; backward,
     psi[l, (n,r)] with the unmerged L_i and mR = merge(R_i, W_i).  Davidson, truncated
@@ -265,6 +286,17 @@ def optimize_onesite(ctx: Context, forward: bool, st: DeviceState, i: int, tole:
     diag = psi.like()
     core.compute_diagonal_elements(ctx, L, R, diag)
     e, stats = core.diagonalize(ctx, L, R, diag, psi, tole)
+    if noise >= 1.0e-8:
+        wf_opt = core.expand_rows(ctx, psi, wf) if forward else core.expand_cols(ctx, psi, wf)
+        j = i + 1 if forward else i - 1
+        left, right, f = split_onesite_noise(ctx, forward, wf_opt, st.wave[j], st.M, noise)
+        if forward:
+            st.wave[i], st.wave[i + 1] = left, right
+            st.lenv[i + 1] = core.renormalize(ctx, True, op, f, f)
+        else:
+            st.wave[i - 1], st.wave[i] = left, right
+            st.renv[i - 1] = core.renormalize(ctx, False, op, f, f)
+        return e, stats
     if forward:
         U, sV = core.canonicalize(ctx, True, psi, st.M)
         st.wave[i] = core.expand_rows(ctx, U, wf)
@@ -280,7 +312,7 @@ def optimize_onesite(ctx: Context, forward: bool, st: DeviceState, i: int, tole:
     return e, stats
 
 
-def make_sweep_onesite(ctx: Context, st: DeviceState, tole: float) -> SweepLog:
+def make_sweep_onesite(ctx: Context, st: DeviceState, tole: float, noise: float = 0.0) -> SweepLog:
     """One-site forward then backward sweep (sites 0..N-2, then N-1..1); Davidson
     tolerance 0.1*tole; sweep energy = minimum over sites."""
     N = len(st.mpo)
@@ -288,21 +320,22 @@ def make_sweep_onesite(ctx: Context, st: DeviceState, tole: float) -> SweepLog:
     es: List[float] = []
     nsig = 0
     for i in range(N - 1):
-        e, s = optimize_onesite(ctx, True, st, i, 0.1 * tole)
+        e, s = optimize_onesite(ctx, True, st, i, 0.1 * tole, noise)
         es.append(e)
         nsig += s["n_sigma"]
     for i in range(N - 1, 0, -1):
-        e, s = optimize_onesite(ctx, False, st, i, 0.1 * tole)
+        e, s = optimize_onesite(ctx, False, st, i, 0.1 * tole, noise)
         es.append(e)
         nsig += s["n_sigma"]
     return SweepLog(min(es), es, nsig, 0.0, time.perf_counter() - t0, kind="onesite")
 
 
 def dmrg(ctx: Context, mpo_dicts: List[dict], n_elec: int, two_sz: int, M: int, tole: float, max_sweeps: int,
-         min_sweeps: int = 0, verbose: bool = False, onesite: bool = False):
+         min_sweeps: int = 0, verbose: bool = False, onesite: bool = False, noise: float = 0.0):
     """Sweeps until |dE| < tole after at least one iteration (src/dmrg.cpp:37-79); with
     ``onesite``, the reference's second stage follows: one-site sweeps from the
-    converged two-site state until |dE| < tole again (src/dmrg.cpp:80-115)."""
+    converged two-site state until |dE| < tole again (src/dmrg.cpp:80-115).  ``noise``
+    is the dmrg.conf keyword of that name, passed to every truncation."""
     mpo = [Tensor.from_dict(ctx, d) for d in mpo_dicts]
     st = make_initial_state(ctx, mpo, n_elec, two_sz, M)
     e_prev = 0.0
@@ -310,7 +343,7 @@ def dmrg(ctx: Context, mpo_dicts: List[dict], n_elec: int, two_sz: int, M: int, 
     stages = [make_sweep] + ([make_sweep_onesite] if onesite else [])
     for stage in stages:
         for it in range(max_sweeps):
-            log = stage(ctx, st, tole)
+            log = stage(ctx, st, tole, noise=noise)
             logs.append(log)
             de = log.energy - e_prev
             e_prev = log.energy

@@ -266,10 +266,101 @@ def gesvd_merged(a: QSDArray, M: int, left_arrow: bool, tie_rtol: float = SVD_TI
     return s_out, U, V, kept, dnorm
 
 
+# ----------------------------------------------------------------------------
+# a8: make_noise (src/canonicalize.hpp:11-24)
+# ----------------------------------------------------------------------------
+
+MT_N, MT_M = 624, 397
+MT_MATRIX_A = 0x9908B0DF
+MT_UPPER, MT_LOWER = 0x80000000, 0x7FFFFFFF
+MT_DEFAULT_SEED = 5489  # seed of a default-constructed std::mt19937
+
+
+def _mt_twist(mt: np.ndarray) -> None:
+    """One regeneration of the 624-word state, in place, in the three stretches
+    whose far word (i + 397 mod 624) is already regenerated or not."""
+    def step(cur, nxt, far):
+        y = (cur & MT_UPPER) | (nxt & MT_LOWER)
+        return far ^ (y >> np.uint64(1)) ^ np.where((y & np.uint64(1)) != 0, np.uint64(MT_MATRIX_A), np.uint64(0))
+
+    a = MT_N - MT_M  # 227
+    mt[0:a] = step(mt[0:a], mt[1:a + 1], mt[MT_M:MT_N])
+    mt[a:2 * a] = step(mt[a:2 * a], mt[a + 1:2 * a + 1], mt[0:a])
+    mt[2 * a:MT_N - 1] = step(mt[2 * a:MT_N - 1], mt[2 * a + 1:MT_N], mt[a:MT_N - 1 - a])
+    mt[MT_N - 1:] = step(mt[MT_N - 1:], mt[0:1], mt[MT_M - 1:MT_M])
+
+
+def mt19937_words(count: int, seed: int = MT_DEFAULT_SEED) -> np.ndarray:
+    """The first ``count`` 32-bit outputs of MT19937 (Matsumoto and Nishimura, ACM
+    TOMACS 8(1), 1998: initialisation by x[i] = 1812433253 (x[i-1] ^ (x[i-1] >> 30)) + i,
+    the twist and the tempering of that paper; the C++ standard defines std::mt19937
+    with the same parameters).  The reference draws from a default-constructed engine
+    (``src/canonicalize.hpp:16``)."""
+    mask = 0xFFFFFFFF
+    mt = np.zeros(MT_N, dtype=np.uint64)
+    mt[0] = seed & mask
+    for i in range(1, MT_N):
+        p = int(mt[i - 1])
+        mt[i] = (1812433253 * (p ^ (p >> 30)) + i) & mask
+    out = np.empty(count, dtype=np.uint64)
+    pos = 0
+    while pos < count:
+        _mt_twist(mt)
+        y = mt.copy()
+        y ^= y >> np.uint64(11)
+        y ^= (y << np.uint64(7)) & np.uint64(0x9D2C5680)
+        y ^= (y << np.uint64(15)) & np.uint64(0xEFC60000)
+        y ^= y >> np.uint64(18)
+        take = min(MT_N, count - pos)
+        out[pos:pos + take] = y[:take] & np.uint64(mask)
+        pos += take
+    return out
+
+
+def noise_sequence(n: int) -> np.ndarray:
+    """The first n values of ``uniform_real_distribution<double>(-1, 1)`` over a
+    default-seeded mt19937 (``src/canonicalize.hpp:16-17``): generate_canonical<double,
+    53> takes two 32-bit words per value, r = (w0 + w1 2^32) / 2^64 with the sum rounded
+    to double (C++ standard [rand.util.canonical]; libstdc++ returns the largest double
+    below 1 when r rounds to 1), and the distribution returns r (b - a) + a."""
+    w = mt19937_words(2 * int(n)).astype(np.float64)
+    s = w[0::2] + w[1::2] * 4294967296.0
+    r = s / 18446744073709551616.0
+    r = np.where(r >= 1.0, np.nextafter(1.0, 0.0), r)
+    return r * 2.0 + (-1.0)
+
+
+def make_noise(wfnc: QSDArray, noise: float) -> None:
+    """``make_noise`` (``src/canonicalize.hpp:11-24``), in place: wfnc += noise * wfpt.
+    wfpt holds every allowed block of non-zero size under the net dense shape of wfnc
+    (``check_net_dshape``, ``include/btas/SPARSE/STArray.h:386-401``; ``allocate``,
+    ``:219-237``).  STArray::generate passes the generator to each block by value
+    (``STArray.h:259-262``), so every block is filled, row-major, with the leading values
+    of the same sequence; Axpy adds the blocks wfnc lacks (``SPARSE/STBLAS.h:133-145``)."""
+    if noise < 1.0e-8:
+        return
+    net = [[0] * len(x) for x in wfnc.qshape]
+    for t, b in wfnc.blocks.items():
+        for k, i in enumerate(wfnc.index(t)):
+            net[k][i] = b.shape[k]
+    wfpt = QSDArray(wfnc.q, wfnc.qshape, net)
+    tags = []
+    for t in range(wfpt.nsparse):
+        idx = wfpt.index(t)
+        dims = wfpt.block_dims(idx)
+        if wfpt.allowed(idx) and int(np.prod(dims)) > 0:
+            tags.append((t, dims))
+    nmax = max((int(np.prod(d)) for _, d in tags), default=0)
+    seq = noise_sequence(nmax)
+    for t, dims in tags:
+        wfpt.blocks[t] = seq[:int(np.prod(dims))].reshape(dims).copy()
+    axpy(noise, wfpt, wfnc)
+
+
 def canonicalize_merged(forward: bool, wfnc: QSDArray, M: int, noise: float = 0.0):
-    """``canonicalize`` for merged MPS (``src/canonicalize.hpp:88-106``); noise < 1e-8 only."""
-    if noise >= 1.0e-8:
-        raise NotImplementedError("noise injection is not part of the oracle")
+    """``canonicalize`` for merged MPS (``src/canonicalize.hpp:88-106``); wfnc is
+    noised in place first, as in the reference."""
+    make_noise(wfnc, noise)
     if forward:
         s, U, V, kept, dn = gesvd_merged(wfnc, M, True)
         dimm_rows(s, V)
@@ -277,6 +368,35 @@ def canonicalize_merged(forward: bool, wfnc: QSDArray, M: int, noise: float = 0.
         s, U, V, kept, dn = gesvd_merged(wfnc, M, False)
         dimm_cols(U, s)
     return U, V, kept
+
+
+def canonicalize_twosite(forward: bool, wfnc: QSDArray, M: int, noise: float = 0.0):
+    """``canonicalize`` of a two-site wavefunction wfnc[l,n,n',r]
+    (``src/canonicalize.hpp:27-45``): make_noise, then Gesvd<4,3> over the row
+    merge (l,n) and the column merge (n',r); forward returns (U, s V), backward (U s, V),
+    both as three-index site tensors."""
+    make_noise(wfnc, noise)
+    rinfo = MergeInfo(wfnc.qshape[:2], wfnc.dshape[:2])
+    cinfo = MergeInfo(wfnc.qshape[2:], wfnc.dshape[2:])
+    a2 = merge_rows(rinfo, merge_cols(wfnc, cinfo))
+    s, U, V, kept, dn = gesvd_merged(a2, M, forward)
+    if forward:
+        dimm_rows(s, V)
+    else:
+        dimm_cols(U, s)
+    return expand_rows(rinfo, U), expand_cols(V, cinfo)
+
+
+def canonicalize_onesite_noise(forward: bool, wfnc: QSDArray, nb: QSDArray, M: int, noise: float):
+    """One-site ``canonicalize`` with noise >= 1e-8 (``src/canonicalize.hpp:56-66``):
+    wfnc is joined with the neighbouring site nb (forward wfnc*nb, backward nb*wfnc) and
+    the two-site tensor is canonicalised with noise; returns (lmps, rmps)."""
+    t = QSDArray()
+    if forward:
+        gemm(NoTrans, NoTrans, 1.0, wfnc, nb, 1.0, t, nc=4)
+    else:
+        gemm(NoTrans, NoTrans, 1.0, nb, wfnc, 1.0, t, nc=4)
+    return canonicalize_twosite(forward, t, M, noise)
 
 
 def canonicalize_onesite_backward(wfnc: QSDArray, lmps: QSDArray, M: int):
@@ -339,7 +459,8 @@ class BondResult:
 
 
 def optimize_twosite_merged(forward: bool, lmpo: QSDArray, rmpo: QSDArray, lopr: QSDArray,
-                            ropr: QSDArray, lwfn: QSDArray, rwfn: QSDArray, tole: float, M: int):
+                            ropr: QSDArray, lwfn: QSDArray, rwfn: QSDArray, tole: float, M: int,
+                            noise: float = 0.0):
     """Returns (BondResult, new_env, new_lwfn, new_rwfn); new_env is the renormalised
     left (forward) or right (backward) operator."""
     times = {}
@@ -364,7 +485,7 @@ def optimize_twosite_merged(forward: bool, lmpo: QSDArray, rmpo: QSDArray, lopr:
     energy = davidson(multH, diag, psi, tole, st)
     t3 = time.perf_counter()
     times["davidson"] = t3 - t2
-    U, V, kept = canonicalize_merged(forward, psi, M)
+    U, V, kept = canonicalize_merged(forward, psi, M, noise)
     t4 = time.perf_counter()
     times["svd"] = t4 - t3
     if forward:

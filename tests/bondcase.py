@@ -34,5 +34,20 @@ def hubbard_bond(L: int = 10, M: int = 32, bond: int = 4, U: float = 4.0):
     return dict(mpo=mpo, st=st, i=i, mL=mL, mR=mR, psi=psi, full=full, M=M)
 
 
+def repeated_sector_psi() -> oq.QSDArray:
+    """A wavefunction whose sectors repeat quantum numbers, so four blocks are allowed
+    among rows 0-1 and columns 0-1; two are stored, and they show the dimension of
+    each of those sectors (row 2 / column 2 allow one more block but appear in none)."""
+    import numpy as np
+
+    qrow = [(0, 0), (0, 0), (1, 1)]
+    qcol = [(2, 0), (2, 0), (1, -1)]
+    psi = oq.QSDArray((2, 0), [qrow, qcol], [[2, 3, 4], [5, 3, 2]])
+    rng = np.random.default_rng(3)
+    psi.blocks[psi.tag((0, 0))] = rng.standard_normal((2, 5))
+    psi.blocks[psi.tag((1, 1))] = rng.standard_normal((3, 3))
+    return psi
+
+
 def to_dict(a: oq.QSDArray) -> dict:
     return {"q": a.q, "qshape": a.qshape, "dshape": a.dshape, "blocks": a.blocks}

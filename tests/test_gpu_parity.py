@@ -222,3 +222,117 @@ def test_canonicalize_rank_deficient_blocks_stay_orthonormal(ctx, forward, route
     c = oq.QSDArray()
     oq.gemm("N", "N", 1.0, gl, gr, 1.0, c, nc=2)
     assert max_block_diff(psi.blocks, c.blocks) < 1e-12
+
+
+# ---------------------------------------------------------------------------
+# make_noise (src/canonicalize.hpp:11-24) and the truncations that use it.  The
+# noise itself is bit-exact (same sequence, product and sum rounded separately);
+# the noised SVDs are compared through their sign-free products.
+# ---------------------------------------------------------------------------
+
+NOISE = 1e-3
+
+
+def oracle_of(t):
+    from oracle import qsd as oq
+
+    a = oq.QSDArray(t.q, *t.shape())
+    a.blocks = t.to_blocks()
+    return a
+
+
+def product(a, b, nc):
+    from oracle import qsd as oq
+
+    c = oq.QSDArray()
+    oq.gemm("N", "N", 1.0, a, b, 1.0, c, nc=nc)
+    return c.blocks
+
+
+def two_site(case):
+    from oracle import qsd as oq
+
+    st, i = case["st"], case["i"]
+    t = oq.QSDArray()
+    oq.gemm("N", "N", 1.0, st.wave[i], st.wave[i + 1], 1.0, t, nc=4)
+    return t
+
+
+def test_make_noise_bit_exact(ctx):
+    from oracle import dmrg as od
+    from tests.bondcase import repeated_sector_psi
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    # merged two-site wavefunction, a wavefunction whose noise array adds blocks, and
+    # a four-index two-site tensor (the one-site stage's noise path)
+    for a in (case["psi"], repeated_sector_psi(), two_site(case)):
+        d = dev(ctx, a)
+        core.make_noise(ctx, d, 1e-9)  # below the threshold: nothing happens
+        assert max_block_diff(a.blocks, d.to_blocks()) == 0.0
+        core.make_noise(ctx, d, NOISE)
+        ref = a.copy()
+        od.make_noise(ref, NOISE)
+        got = d.to_blocks()
+        assert sorted(got) == sorted(ref.blocks)
+        for t, b in ref.blocks.items():
+            assert np.array_equal(got[t], b), t
+
+
+@pytest.mark.parametrize("forward", [True, False])
+def test_canonicalize_with_noise_matches_oracle(ctx, forward):
+    from oracle import dmrg as od
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    M = case["M"]
+    P = dev(ctx, case["psi"])
+    lm, rm = core.canonicalize(ctx, forward, P, M, NOISE)
+    assert max_block_diff(case["psi"].blocks, P.to_blocks()) == 0.0  # wfnc is left as it was
+    U, V, kept = od.canonicalize_merged(forward, case["psi"].copy(), M, NOISE)
+    U0, V0, kept0 = od.canonicalize_merged(forward, case["psi"].copy(), M, 0.0)
+    assert kept != kept0  # the noise reaches the truncation
+    assert lm.shape()[0][1] == U.qshape[1] and lm.shape()[1][1] == U.dshape[1]
+    assert max_block_diff(product(U, V, 2), product(oracle_of(lm), oracle_of(rm), 2)) < 1e-12
+
+
+@pytest.mark.parametrize("forward", [True, False])
+def test_onesite_noise_split_matches_oracle(ctx, forward):
+    from oracle import dmrg as od
+    from mpsxx_gb300 import dmrg as gd
+
+    case = hubbard_bond()
+    st, i, M = case["st"], case["i"], case["M"]
+    wf = st.wave[i]
+    nb = st.wave[i + 1] if forward else st.wave[i - 1]
+    left, right, f = gd.split_onesite_noise(ctx, forward, dev(ctx, wf), dev(ctx, nb), M, NOISE)
+    lo, ro = od.canonicalize_onesite_noise(forward, wf.copy(), nb.copy(), M, NOISE)
+    gl, gr = oracle_of(left), oracle_of(right)
+    assert gl.qshape == lo.qshape and gl.dshape == lo.dshape
+    assert gr.qshape == ro.qshape and gr.dshape == ro.dshape
+    assert max_block_diff(product(lo, ro, 4), product(gl, gr, 4)) < 1e-12
+
+
+def test_bond_step_with_noise(ctx):
+    from oracle import dmrg as od
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    st, i, M, mpo = case["st"], case["i"], case["M"], case["mpo"]
+    args = [dev(ctx, x) for x in (mpo[i], mpo[i + 1], st.lenv[i], st.renv[i + 1], st.wave[i], st.wave[i + 1])]
+    e0, _, nl0, _, _ = core.optimize_twosite_merged(ctx, True, *args, 1e-11, M, 0.0)
+    e1, _, nl1, nr1, _ = core.optimize_twosite_merged(ctx, True, *args, 1e-11, M, NOISE)
+    res, _, _, _ = od.optimize_twosite_merged(True, mpo[i], mpo[i + 1], st.lenv[i], st.renv[i + 1], st.wave[i],
+                                              st.wave[i + 1], 1e-11, M, NOISE)
+    # the noise follows the eigensolver: energies unchanged
+    assert abs(e1 - e0) < 1e-12 and abs(e1 - res.energy) < 1e-10
+    assert nl1.shape()[1][2] != nl0.shape()[1][2]  # a different truncation
+    # the new left site is still left-normalised over (l, n)
+    u = oracle_of(nl1)
+    gram = {}
+    for t, b in u.blocks.items():
+        a = u.index(t)[2]
+        m = b.reshape(-1, b.shape[2])
+        gram[a] = gram.get(a, 0.0) + m.T @ m
+    for a, g in gram.items():
+        assert np.abs(g - np.eye(g.shape[0])).max() < 1e-12, a
