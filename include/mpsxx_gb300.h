@@ -160,6 +160,26 @@ int mpsxx_gemm_tasks(int transa, int transb, const mpsxx_tensor* a, const mpsxx_
 int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                                const mpsxx_tensor* wfn, mpsxx_tensor* sgv);
 
+/* The other rank overloads of mpsxx::compute_sigma_vector, with the reference's
+ * allocate-or-accumulate output: *sgv == NULL -> the result is allocated; otherwise it
+ * is added to *sgv, whose missing blocks are added (the handle then refers to the
+ * grown tensor).  The H forms run as the merged product above on every allowed merged
+ * block of wfn's sectors.
+ * one-site, sgv[l,n,r] += sum lopr[l,w,l'] mpo[w,n,n',w'] wfn[l',n',r'] ropr[r,w',r']
+ *   (src/compute_sigma_vector.hpp:9-22; used by the one-site Functor<3>); */
+int mpsxx_compute_sigma_vector_onesite(mpsxx_context* ctx, const mpsxx_tensor* mpo, const mpsxx_tensor* lopr,
+                                       const mpsxx_tensor* ropr, const mpsxx_tensor* wfn, mpsxx_tensor** sgv);
+/* two-site four-index, sgv[l,n,n',r] += H_eff wfn with both site MPOs
+ *   (src/compute_sigma_vector.hpp:53-70); */
+int mpsxx_compute_sigma_vector_twosite(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                                       const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* wfn,
+                                       mpsxx_tensor** sgv);
+/* overlap, sgv += lopr wfn ropr^T for two-index (S) block operators and wfn of 2, 3 or 4
+ *   indices: Gemm(N, N, lopr, wfn) then Gemm(N, T, ., ropr)
+ *   (src/compute_sigma_vector.hpp:24-35, 72-83, 98-109). */
+int mpsxx_compute_sigma_vector_overlap(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                                       const mpsxx_tensor* wfn, mpsxx_tensor** sgv);
+
 /* Work of the split-precision H_eff*psi plan for these operands (the plan is built if
  * needed; no device data is read): out[0..12] = useful FLOPs of stage 1 and 2, tile
  * FLOPs of stage 1 and 2 (128 x 128 tensor-core tiles, 64 on tails, K slices of 32, padding

@@ -103,6 +103,11 @@ class QSDArray {
     check(mpsxx_tensor_info(h_, nullptr, nullptr, &n, nullptr));
     return n;
   }
+  int rank() const {
+    int r = 0;
+    check(mpsxx_tensor_info(h_, &r, nullptr, nullptr, nullptr));
+    return r;
+  }
   void upload(const double* host) { check(mpsxx_tensor_upload(h_, host)); }
   void download(double* host) const { check(mpsxx_tensor_download(h_, host)); }
 
@@ -112,15 +117,51 @@ class QSDArray {
 
 // --- the reference's call surface ------------------------------------------
 
-// sgv0 += H_eff * wfn0; an empty sgv0 is created with wfn0's layout first.
+namespace detail {
+// the allocate-or-accumulate output of the rank overloads: an empty sgv0 receives the
+// result, a non-empty one is added to (and grows by any missing blocks)
+template <class F>
+inline void into(QSDArray& sgv0, F call) {
+  mpsxx_tensor* h = sgv0.get();
+  check(call(&h));
+  if (sgv0.empty()) sgv0 = QSDArray::adopt(h);
+}
+}  // namespace detail
+
+// sgv0 += H_eff * wfn0 for merged operators; an empty sgv0 is created with wfn0's
+// layout first.  With two-index (overlap) operators: sgv0 += lopr wfn0 ropr^T
+// (src/compute_sigma_vector.hpp:24-35, 72-83, 98-109), for wfn0 of 2, 3 or 4 indices.
 inline void compute_sigma_vector(Context& ctx, const QSDArray& lopr, const QSDArray& ropr, const QSDArray& wfn0,
                                  QSDArray& sgv0) {
+  if (lopr.rank() == 2) {
+    detail::into(sgv0, [&](mpsxx_tensor** o) {
+      return mpsxx_compute_sigma_vector_overlap(ctx.get(), lopr.get(), ropr.get(), wfn0.get(), o);
+    });
+    return;
+  }
   if (sgv0.empty()) {
     mpsxx_tensor* h = nullptr;
     check(mpsxx_tensor_create_like(ctx.get(), wfn0.get(), &h));
     sgv0 = QSDArray::adopt(h);
   }
   check(mpsxx_compute_sigma_vector(ctx.get(), lopr.get(), ropr.get(), wfn0.get(), sgv0.get()));
+}
+
+// One-site: sgv0 (+)= H wfn0 with the site MPO (src/compute_sigma_vector.hpp:9-22).
+inline void compute_sigma_vector(Context& ctx, const QSDArray& mpo0, const QSDArray& lopr, const QSDArray& ropr,
+                                 const QSDArray& wfn0, QSDArray& sgv0) {
+  detail::into(sgv0, [&](mpsxx_tensor** o) {
+    return mpsxx_compute_sigma_vector_onesite(ctx.get(), mpo0.get(), lopr.get(), ropr.get(), wfn0.get(), o);
+  });
+}
+
+// Two-site, four-index wavefunction (src/compute_sigma_vector.hpp:53-70).
+inline void compute_sigma_vector(Context& ctx, const QSDArray& lmpo, const QSDArray& rmpo, const QSDArray& lopr,
+                                 const QSDArray& ropr, const QSDArray& wfn0, QSDArray& sgv0) {
+  detail::into(sgv0, [&](mpsxx_tensor** o) {
+    return mpsxx_compute_sigma_vector_twosite(ctx.get(), lmpo.get(), rmpo.get(), lopr.get(), ropr.get(),
+                                              wfn0.get(), o);
+  });
 }
 
 // diag += sum_w lopr[A,w,A] ropr[B,w,B] on diag's blocks.

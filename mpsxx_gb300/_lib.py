@@ -63,6 +63,9 @@ SIGNATURES = {
     "mpsxx_optimize_twosite_merged": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, C.c_int,
                                                 C.c_double, c_dbl_p, vpp, vpp, vpp, c_dbl_p]),
     "mpsxx_make_noise": (C.c_int, [vp, vp, C.c_double]),
+    "mpsxx_compute_sigma_vector_onesite": (C.c_int, [vp, vp, vp, vp, vp, vpp]),
+    "mpsxx_compute_sigma_vector_twosite": (C.c_int, [vp, vp, vp, vp, vp, vp, vpp]),
+    "mpsxx_compute_sigma_vector_overlap": (C.c_int, [vp, vp, vp, vp, vpp]),
     "mpsxx_noise_sequence": (C.c_int, [C.c_int64, c_dbl_p]),
     "mpsxx_merge_cols": (C.c_int, [vp, vp, vpp]),
     "mpsxx_gemm": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, vp, vp, C.c_int, vpp]),

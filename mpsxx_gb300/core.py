@@ -281,6 +281,34 @@ def compute_sigma_vector(ctx: Context, lopr: Tensor, ropr: Tensor, wfn: Tensor, 
     check(lib().mpsxx_compute_sigma_vector(ctx.h, lopr.h, ropr.h, wfn.h, sgv.h))
 
 
+def _in_out(ctx: Context, sgv: Optional[Tensor], call) -> Tensor:
+    h = C.c_void_p(sgv.h.value if isinstance(sgv.h, C.c_void_p) else sgv.h) if sgv is not None else C.c_void_p()
+    check(call(C.byref(h)))
+    return sgv if sgv is not None else Tensor(h, ctx)
+
+
+def compute_sigma_vector_onesite(ctx: Context, mpo: Tensor, lopr: Tensor, ropr: Tensor, wfn: Tensor,
+                                 sgv: Optional[Tensor] = None) -> Tensor:
+    """One-site H wfn with the site MPO (src/compute_sigma_vector.hpp:9-22); allocated
+    when sgv is None, otherwise added to sgv (which grows by any missing blocks)."""
+    return _in_out(ctx, sgv, lambda o: lib().mpsxx_compute_sigma_vector_onesite(ctx.h, mpo.h, lopr.h, ropr.h,
+                                                                                  wfn.h, o))
+
+
+def compute_sigma_vector_twosite(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor, wfn: Tensor,
+                                 sgv: Optional[Tensor] = None) -> Tensor:
+    """Four-index two-site H wfn (src/compute_sigma_vector.hpp:53-70)."""
+    return _in_out(ctx, sgv, lambda o: lib().mpsxx_compute_sigma_vector_twosite(ctx.h, lmpo.h, rmpo.h, lopr.h,
+                                                                                  ropr.h, wfn.h, o))
+
+
+def compute_sigma_vector_overlap(ctx: Context, lopr: Tensor, ropr: Tensor, wfn: Tensor,
+                                 sgv: Optional[Tensor] = None) -> Tensor:
+    """lopr wfn ropr^T for two-index overlap operators (src/compute_sigma_vector.hpp:24-35,
+    72-83, 98-109)."""
+    return _in_out(ctx, sgv, lambda o: lib().mpsxx_compute_sigma_vector_overlap(ctx.h, lopr.h, ropr.h, wfn.h, o))
+
+
 SIGMA_PLAN_KEYS = ("flops_stage1", "flops_stage2", "tile_flops_stage1", "tile_flops_stage2", "slices_stage1",
                    "slices_stage2", "tiles_stage1", "tiles_stage2", "packed_bytes_L", "packed_bytes_R",
                    "packed_bytes_intermediate", "packed_bytes_psi", "intermediate_elements",

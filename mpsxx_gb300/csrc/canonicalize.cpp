@@ -621,30 +621,7 @@ std::unique_ptr<DTensor> make_noise(Context& ctx, const DTensor& wfnc, double no
   std::vector<int64_t> utags;
   std::set_union(wfnc.tags.begin(), wfnc.tags.end(), ntags.begin(), ntags.end(), std::back_inserter(utags));
   cudaStream_t st = ctx.stream;
-  auto out = std::make_unique<DTensor>();
-  static_cast<Tensor&>(*out) = static_cast<const Tensor&>(wfnc);
-  out->d = nullptr;
-  out->own = false;
-  out->ctx = &ctx;
-  if (utags.size() != wfnc.tags.size()) out->set_blocks(utags);
-  out->alloc_device(st, utags.size() != wfnc.tags.size());
-  if (utags.size() == wfnc.tags.size()) {
-    if (wfnc.nnz)
-      cuda_check(cudaMemcpyAsync(out->d, wfnc.d, wfnc.nnz * sizeof(double), cudaMemcpyDeviceToDevice, st),
-                 "make_noise copy");
-  } else {
-    std::vector<DCopy> cp;
-    for (size_t b = 0; b < wfnc.tags.size(); ++b) {
-      const int64_t n = wfnc.block_size(static_cast<int32_t>(b));
-      if (n > 0x7fffffff) throw Error(kInvalidArgument, "make_noise: block too large");
-      cp.push_back(DCopy{out->offsets[out->find(wfnc.tags[b])], wfnc.offsets[b], 1, static_cast<int>(n),
-                         static_cast<int>(n), static_cast<int>(n), 1.0});
-    }
-    DevArray<DCopy> dcp;
-    dcp.upload(cp, st);
-    launch_copy(dcp.get(), static_cast<int>(cp.size()), wfnc.d, out->d, 0, st);
-    ctx.kernel_launches += 1;
-  }
+  std::unique_ptr<DTensor> out = relayout(ctx, wfnc, utags);
   std::vector<DNoise> nb;
   int64_t nmax = 0;
   for (int64_t t : ntags) {

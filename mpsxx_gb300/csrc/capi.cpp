@@ -373,6 +373,61 @@ int mpsxx_compute_sigma_vector(mpsxx_context* ctx, const mpsxx_tensor* lopr, con
   });
 }
 
+namespace {
+// the reference's allocate-or-accumulate contract for sgv0 (include/btas/QSPARSE/QSTBLAS.h:201-211)
+void deliver(mpsxx_context* ctx, std::unique_ptr<DTensor> r, mpsxx_tensor** sgv) {
+  Context& c = ctx_of(ctx);
+  if (!*sgv) {
+    c.sync();
+    *sgv = wrap(std::move(r), ctx);
+    return;
+  }
+  DTensor& S = ten_mut(*sgv);
+  need_device(S);
+  accumulate_into(c, 1.0, *r, (*sgv)->t);
+  c.sync();
+}
+}  // namespace
+
+int mpsxx_compute_sigma_vector_onesite(mpsxx_context* ctx, const mpsxx_tensor* mpo, const mpsxx_tensor* lopr,
+                                       const mpsxx_tensor* ropr, const mpsxx_tensor* wfn, mpsxx_tensor** sgv) {
+  return guard([&] {
+    need(sgv != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    need_device(ten(lopr));
+    need_device(ten(ropr));
+    need_device(ten(wfn));
+    deliver(ctx, sigma_onesite(c, ten(mpo), ten(lopr), ten(ropr), ten(wfn)), sgv);
+    if (c.precision != kFP64) check_device_error(c);
+  });
+}
+
+int mpsxx_compute_sigma_vector_twosite(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                                       const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, const mpsxx_tensor* wfn,
+                                       mpsxx_tensor** sgv) {
+  return guard([&] {
+    need(sgv != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    need_device(ten(lopr));
+    need_device(ten(ropr));
+    need_device(ten(wfn));
+    deliver(ctx, sigma_twosite(c, ten(lmpo), ten(rmpo), ten(lopr), ten(ropr), ten(wfn)), sgv);
+    if (c.precision != kFP64) check_device_error(c);
+  });
+}
+
+int mpsxx_compute_sigma_vector_overlap(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
+                                       const mpsxx_tensor* wfn, mpsxx_tensor** sgv) {
+  return guard([&] {
+    need(sgv != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    need_device(ten(lopr));
+    need_device(ten(ropr));
+    need_device(ten(wfn));
+    deliver(ctx, sigma_overlap(c, ten(lopr), ten(ropr), ten(wfn)), sgv);
+  });
+}
+
 int mpsxx_sigma_plan_stats(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                            const mpsxx_tensor* wfn, double* out, int n, int* count) {
   return guard([&] {

@@ -459,6 +459,22 @@ std::unique_ptr<DTensor> gemm_new(Context& ctx, Trans ta, Trans tb, double alpha
 // btas::Normalize; returns the norm before scaling
 double normalize_tensor(Context& ctx, DTensor& x);
 
+// A copy of x in the block layout `tags` (ascending, a superset of x's blocks; the
+// added blocks are zero).
+std::unique_ptr<DTensor> relayout(Context& ctx, const DTensor& x, const std::vector<int64_t>& tags);
+// y += alpha x (btas::Axpy, include/btas/SPARSE/STBLAS.h:133-145): same sectors; the
+// blocks of x that y lacks are added to y (y is replaced by a grown copy then).
+void accumulate_into(Context& ctx, double alpha, const DTensor& x, std::unique_ptr<DTensor>& y);
+// The other compute_sigma_vector overloads (src/compute_sigma_vector.hpp), results
+// allocated by the callee: one-site with the site MPO (:9-22), two-site four-index
+// (:53-70), and lopr wfn ropr^T with two-index overlap operators for wfn of 2, 3 or 4
+// indices (:24-35, :72-83, :98-109).
+std::unique_ptr<DTensor> sigma_onesite(Context& ctx, const DTensor& mpo, const DTensor& lopr, const DTensor& ropr,
+                                       const DTensor& wfn);
+std::unique_ptr<DTensor> sigma_twosite(Context& ctx, const DTensor& lmpo, const DTensor& rmpo, const DTensor& lopr,
+                                       const DTensor& ropr, const DTensor& wfn);
+std::unique_ptr<DTensor> sigma_overlap(Context& ctx, const DTensor& lopr, const DTensor& ropr, const DTensor& wfn);
+
 // One bond (src/optimize.hpp:495-651)
 struct BondStats {
   double energy = 0.0;

@@ -1,0 +1,141 @@
+// The other rank overloads of the reference's compute_sigma_vector
+// (src/compute_sigma_vector.hpp) on the device path, and the block-layout helpers
+// they share with make_noise:
+//   one-site   sgv[l,n,r]    += H wfn with the site MPO            (:9-22)
+//   two-site   sgv[l,n,n',r] += H wfn with both site MPOs          (:53-70)
+//   overlap    sgv           += lS wfn rS^T for two-index S blocks  (:24-35, :72-83, :98-109)
+// The H forms run as the merged product: the left (and right) block operator is merged
+// with its site MPO (compute_merged_operator), wfn is merged over the same index
+// pairs, sigma = L psi R^T runs on every allowed merged block, and the result is
+// expanded back.  The merged sectors follow first appearance in packed order, so
+// merging wfn's ket sectors and the operator's (negated) ket sectors gives the same
+// sector order.  The overlap forms are the reference's two Gemms.
+#include <algorithm>
+#include <iterator>
+
+#include "engine.hpp"
+
+namespace mpsxx {
+
+std::unique_ptr<DTensor> relayout(Context& ctx, const DTensor& x, const std::vector<int64_t>& tags) {
+  cudaStream_t st = ctx.stream;
+  auto out = std::make_unique<DTensor>();
+  static_cast<Tensor&>(*out) = static_cast<const Tensor&>(x);
+  out->d = nullptr;
+  out->own = false;
+  out->ctx = &ctx;
+  const bool same = tags == x.tags;
+  if (!same) out->set_blocks(tags);
+  out->alloc_device(st, !same);
+  if (same) {
+    if (x.nnz)
+      cuda_check(cudaMemcpyAsync(out->d, x.d, x.nnz * sizeof(double), cudaMemcpyDeviceToDevice, st), "relayout copy");
+    return out;
+  }
+  std::vector<DCopy> cp;
+  for (size_t b = 0; b < x.tags.size(); ++b) {
+    const int32_t s = out->find(x.tags[b]);
+    if (s < 0) throw Error(kInternal, "relayout: a block of the source is not in the new layout");
+    const int64_t n = x.block_size(static_cast<int32_t>(b));
+    if (n > 0x7fffffff) throw Error(kInvalidArgument, "relayout: block too large");
+    if (n > 0)
+      cp.push_back(DCopy{out->offsets[s], x.offsets[b], 1, static_cast<int>(n), static_cast<int>(n),
+                         static_cast<int>(n), 1.0});
+  }
+  if (!cp.empty()) {
+    DevArray<DCopy> dcp;
+    dcp.upload(cp, st);
+    launch_copy(dcp.get(), static_cast<int>(cp.size()), x.d, out->d, 0, st);
+    ctx.kernel_launches += 1;
+  }
+  return out;
+}
+
+void accumulate_into(Context& ctx, double alpha, const DTensor& x, std::unique_ptr<DTensor>& y) {
+  if (x.sh.rank != y->sh.rank || !(x.sh.q == y->sh.q))
+    throw Error(kQShapeMismatch, "Axpy(QSPARSE): x and y must have the same quantum number.");
+  for (int i = 0; i < x.sh.rank; ++i)
+    if (x.sh.qshape[i] != y->sh.qshape[i] || x.sh.dshape[i] != y->sh.dshape[i])
+      throw Error(kQShapeMismatch, "Axpy(QSPARSE): x and y must have the same quantum shape.");
+  std::vector<int64_t> u;
+  std::set_union(y->tags.begin(), y->tags.end(), x.tags.begin(), x.tags.end(), std::back_inserter(u));
+  if (u.size() != y->tags.size()) y = relayout(ctx, *y, u);
+  std::vector<DCopy> cp;
+  for (size_t b = 0; b < x.tags.size(); ++b) {
+    const int32_t s = y->find(x.tags[b]);
+    const int64_t n = x.block_size(static_cast<int32_t>(b));
+    if (n > 0x7fffffff) throw Error(kInvalidArgument, "accumulate: block too large");
+    if (n > 0) cp.push_back(DCopy{y->offsets[s], x.offsets[b], 1, static_cast<int>(n), 0, 0, alpha});
+  }
+  if (cp.empty()) return;
+  DevArray<DCopy> dcp;
+  dcp.upload(cp, ctx.stream);
+  launch_copy(dcp.get(), static_cast<int>(cp.size()), x.d, y->d, 1, ctx.stream);
+  ctx.kernel_launches += 1;
+}
+
+namespace {
+// psi with every allowed block of its merged shape (zero where wfn had no data), so
+// that the merged product reaches every block H * wfn can have
+std::unique_ptr<DTensor> all_allowed(Context& ctx, const DTensor& psi) {
+  Tensor full;
+  full.sh = psi.sh;
+  full.allocate_allowed();
+  return relayout(ctx, psi, full.tags);
+}
+
+std::unique_ptr<DTensor> zeros_like(Context& ctx, const DTensor& x) {
+  auto z = std::make_unique<DTensor>();
+  static_cast<Tensor&>(*z) = static_cast<const Tensor&>(x);
+  z->d = nullptr;
+  z->own = false;
+  z->ctx = &ctx;
+  z->alloc_device(ctx.stream, true);
+  return z;
+}
+
+void need_rank(const DTensor& t, int r, const char* what) {
+  if (t.sh.rank != r) throw Error(kInvalidArgument, std::string("compute_sigma_vector: ") + what);
+}
+}  // namespace
+
+std::unique_ptr<DTensor> sigma_onesite(Context& ctx, const DTensor& mpo, const DTensor& lopr, const DTensor& ropr,
+                                       const DTensor& wfn) {
+  need_rank(mpo, 4, "the site MPO must have 4 indices");
+  need_rank(lopr, 3, "the block operators must have 3 indices");
+  need_rank(ropr, 3, "the block operators must have 3 indices");
+  need_rank(wfn, 3, "the one-site wavefunction must have 3 indices");
+  auto mL = compute_merged_operator(ctx, true, mpo, lopr);
+  const MergeInfo rows({wfn.sh.qshape[0], wfn.sh.qshape[1]}, {wfn.sh.dshape[0], wfn.sh.dshape[1]});
+  auto psi = all_allowed(ctx, *merge_rows(ctx, rows, wfn));
+  auto sig = zeros_like(ctx, *psi);
+  compute_sigma_vector(ctx, *mL, ropr, *psi, *sig);
+  return expand_rows(ctx, rows, *sig);
+}
+
+std::unique_ptr<DTensor> sigma_twosite(Context& ctx, const DTensor& lmpo, const DTensor& rmpo, const DTensor& lopr,
+                                       const DTensor& ropr, const DTensor& wfn) {
+  need_rank(lmpo, 4, "the site MPOs must have 4 indices");
+  need_rank(rmpo, 4, "the site MPOs must have 4 indices");
+  need_rank(lopr, 3, "the block operators must have 3 indices");
+  need_rank(ropr, 3, "the block operators must have 3 indices");
+  need_rank(wfn, 4, "the two-site wavefunction must have 4 indices");
+  auto mL = compute_merged_operator(ctx, true, lmpo, lopr);
+  auto mR = compute_merged_operator(ctx, false, rmpo, ropr);
+  const MergeInfo rows({wfn.sh.qshape[0], wfn.sh.qshape[1]}, {wfn.sh.dshape[0], wfn.sh.dshape[1]});
+  const MergeInfo cols({wfn.sh.qshape[2], wfn.sh.qshape[3]}, {wfn.sh.dshape[2], wfn.sh.dshape[3]});
+  auto psi = all_allowed(ctx, *merge_rows(ctx, rows, *merge_cols(ctx, wfn, cols)));
+  auto sig = zeros_like(ctx, *psi);
+  compute_sigma_vector(ctx, *mL, *mR, *psi, *sig);
+  return expand_cols(ctx, *expand_rows(ctx, rows, *sig), cols);
+}
+
+std::unique_ptr<DTensor> sigma_overlap(Context& ctx, const DTensor& lopr, const DTensor& ropr, const DTensor& wfn) {
+  need_rank(lopr, 2, "overlap block operators must have 2 indices");
+  need_rank(ropr, 2, "overlap block operators must have 2 indices");
+  if (wfn.sh.rank < 2 || wfn.sh.rank > 4) throw Error(kInvalidArgument, "compute_sigma_vector: wfn of 2 to 4 indices");
+  auto scr1 = gemm_new(ctx, kNoTrans, kNoTrans, 1.0, lopr, wfn, wfn.sh.rank);
+  return gemm_new(ctx, kNoTrans, kTrans, 1.0, *scr1, ropr, wfn.sh.rank);
+}
+
+}  // namespace mpsxx

@@ -39,6 +39,36 @@ def compute_sigma_vector(lopr: QSDArray, ropr: QSDArray, wfn0: QSDArray, sgv0: Q
     return scr1
 
 
+def compute_sigma_vector_onesite(mpo0: QSDArray, lopr: QSDArray, ropr: QSDArray, wfn0: QSDArray,
+                                 sgv0: QSDArray) -> QSDArray:
+    """One-site sigma with the site MPO (``src/compute_sigma_vector.hpp:9-22``):
+    scr1 = Gemm(lopr, wfn0); scr2 = Contract(scr1 (1,2), mpo0 (0,2));
+    sgv0 += Contract(scr2 (3,1), ropr (1,2))."""
+    scr1 = QSDArray()
+    gemm(NoTrans, NoTrans, 1.0, lopr, wfn0, 1.0, scr1, nc=4)
+    scr2 = contract(scr1, "awnr", mpo0, "wmnv", "armv")
+    return contract(scr2, "armv", ropr, "svr", "ams", c=sgv0)
+
+
+def compute_sigma_vector_twosite(lmpo: QSDArray, rmpo: QSDArray, lopr: QSDArray, ropr: QSDArray, wfn0: QSDArray,
+                                 sgv0: QSDArray) -> QSDArray:
+    """Four-index two-site sigma (``src/compute_sigma_vector.hpp:53-70``): four
+    Contracts, lopr (2)-wfn0 (0), lmpo (0,2), rmpo (0,2), ropr (1,2)."""
+    scr1 = contract(lopr, "awk", wfn0, "knpr", "awnpr")
+    scr2 = contract(scr1, "awnpr", lmpo, "wmnv", "aprmv")
+    scr3 = contract(scr2, "aprmv", rmpo, "vqpx", "armqx")
+    return contract(scr3, "armqx", ropr, "sxr", "amqs", c=sgv0)
+
+
+def compute_sigma_vector_overlap(lopr: QSDArray, ropr: QSDArray, wfn0: QSDArray, sgv0: QSDArray) -> QSDArray:
+    """sgv0 += lopr wfn0 ropr^T with two-index (S) operators, wfn0 of 2 to 4 indices
+    (``src/compute_sigma_vector.hpp:24-35, 72-83, 98-109``): two Gemms."""
+    scr1 = QSDArray()
+    gemm(NoTrans, NoTrans, 1.0, lopr, wfn0, 1.0, scr1, nc=wfn0.rank)
+    gemm(NoTrans, Trans, 1.0, scr1, ropr, 1.0, sgv0, nc=wfn0.rank)
+    return sgv0
+
+
 # ----------------------------------------------------------------------------
 # a9: renormalize merged operator / overlap (src/renormalize.hpp:57-95)
 # ----------------------------------------------------------------------------

@@ -336,3 +336,60 @@ def test_bond_step_with_noise(ctx):
         gram[a] = gram.get(a, 0.0) + m.T @ m
     for a, g in gram.items():
         assert np.abs(g - np.eye(g.shape[0])).max() < 1e-12, a
+
+
+# ---------------------------------------------------------------------------
+# The other compute_sigma_vector overloads (src/compute_sigma_vector.hpp:9-35,
+# 53-83, 98-109) against the oracle's literal restatement of the reference's
+# Gemm/Contract sequences, allocated and accumulated.
+# ---------------------------------------------------------------------------
+
+def overlap_operators(w, seed=1):
+    from oracle import qsd as oq
+
+    rng = np.random.default_rng(seed)
+
+    def S(qs, ds):
+        a = oq.QSDArray((0, 0), [qs, [oq.qneg(q) for q in qs]], [ds, ds])
+        for x in range(len(qs)):
+            for y in range(len(qs)):
+                if a.allowed((x, y)) and ds[x] and ds[y]:
+                    a.blocks[a.tag((x, y))] = rng.standard_normal((ds[x], ds[y]))
+        return a
+
+    return S(w.qshape[0], w.dshape[0]), S(w.qshape[-1], w.dshape[-1])
+
+
+@pytest.mark.parametrize("kind", ["onesite", "twosite", "overlap2", "overlap3", "overlap4"])
+def test_sigma_overloads_match_oracle(ctx, kind):
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    st, i, mpo = case["st"], case["i"], case["mpo"]
+    if kind == "onesite":
+        w = st.wave[i]
+        ref = od.compute_sigma_vector_onesite(mpo[i], st.lenv[i], st.renv[i], w, oq.QSDArray())
+        ops = [dev(ctx, x) for x in (mpo[i], st.lenv[i], st.renv[i])]
+        fn = core.compute_sigma_vector_onesite
+    elif kind == "twosite":
+        w = two_site(case)
+        ref = od.compute_sigma_vector_twosite(mpo[i], mpo[i + 1], st.lenv[i], st.renv[i + 1], w, oq.QSDArray())
+        ops = [dev(ctx, x) for x in (mpo[i], mpo[i + 1], st.lenv[i], st.renv[i + 1])]
+        fn = core.compute_sigma_vector_twosite
+    else:
+        w = {"overlap2": case["psi"], "overlap3": st.wave[i], "overlap4": two_site(case)}[kind]
+        lS, rS = overlap_operators(w)
+        ref = od.compute_sigma_vector_overlap(lS, rS, w, oq.QSDArray())
+        ops = [dev(ctx, lS), dev(ctx, rS)]
+        fn = core.compute_sigma_vector_overlap
+    W = dev(ctx, w)
+    got = fn(ctx, *ops, W)
+    assert max_block_diff(ref.blocks, got.to_blocks()) < 1e-12
+    # accumulate into an existing tensor (wfn itself): missing blocks are added
+    acc = dev(ctx, w)
+    fn(ctx, *ops, W, acc)
+    expect = w.copy()
+    oq.axpy(1.0, ref, expect)
+    assert max_block_diff(expect.blocks, acc.to_blocks()) < 1e-12

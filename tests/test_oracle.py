@@ -123,3 +123,46 @@ def test_fcidump_round_trip_and_energy(tmp_path):
     assert np.array_equal(d["eri"], eri)
     e = ed.qc_ground_energy(d["h1"], d["eri"], 2, 2, ecore=d["ecore"])[0]
     assert abs(e - (ed.qc_ground_energy(h1, eri, 2, 2)[0] + 0.75)) < 1e-12
+
+
+def _merged_sigma(mL, mR, psi):
+    from oracle import dmrg as od
+
+    full = psi.empty_like()
+    full.allocate(0.0)
+    for k, b in psi.blocks.items():
+        full.blocks[k] = b
+    sg = full.empty_like()
+    od.compute_sigma_vector(mL, mR, full, sg)
+    return sg
+
+
+def _max_diff(a, b):
+    keys = set(a.blocks) | set(b.blocks)
+    return max(float(np.abs(a.blocks.get(k, 0.0) - b.blocks.get(k, 0.0)).max()) for k in keys)
+
+
+def test_rank_overloads_equal_the_merged_product():
+    """The one-site and four-index two-site compute_sigma_vector overloads, restated
+    literally (the reference's Gemm/Contract sequences), equal the merged product on
+    every allowed merged block expanded back: the route the library takes for them."""
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+    from tests.bondcase import hubbard_bond
+
+    case = hubbard_bond()
+    st, i, mpo = case["st"], case["i"], case["mpo"]
+    w = st.wave[i]
+    lit = od.compute_sigma_vector_onesite(mpo[i], st.lenv[i], st.renv[i], w, oq.QSDArray())
+    rows = oq.MergeInfo(w.qshape[:2], w.dshape[:2])
+    mL = od.compute_merged_operator(True, mpo[i], st.lenv[i])
+    merged = oq.expand_rows(rows, _merged_sigma(mL, st.renv[i], oq.merge_rows(rows, w)))
+    assert _max_diff(lit, merged) < 1e-13
+    t = oq.QSDArray()
+    oq.gemm("N", "N", 1.0, st.wave[i], st.wave[i + 1], 1.0, t, nc=4)
+    lit = od.compute_sigma_vector_twosite(mpo[i], mpo[i + 1], st.lenv[i], st.renv[i + 1], t, oq.QSDArray())
+    rows = oq.MergeInfo(t.qshape[:2], t.dshape[:2])
+    cols = oq.MergeInfo(t.qshape[2:], t.dshape[2:])
+    mR = od.compute_merged_operator(False, mpo[i + 1], st.renv[i + 1])
+    sg = _merged_sigma(mL, mR, oq.merge_rows(rows, oq.merge_cols(t, cols)))
+    assert _max_diff(lit, oq.expand_cols(oq.expand_rows(rows, sg), cols)) < 1e-13
