@@ -198,11 +198,33 @@ int mpsxx_sigma_plan_stats(mpsxx_context* ctx, const mpsxx_tensor* lopr, const m
 int mpsxx_compute_diagonal_elements(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                                     mpsxx_tensor* diag);
 
+/* diag += the diagonal of H for one-site (src/compute_diagonal_elements.hpp:10-32,
+ * diag[l,n,r] = sum lopr[l,w,l] mpo[w,n,n,w'] ropr[r,w',r]) and four-index two-site
+ * wavefunctions (:35-62).  diag supplies the sectors and q; every allowed block is
+ * computed and blocks diag lacks are added (the handle then refers to the grown
+ * tensor), as the reference's group sum does with Axpy (:84-100). */
+int mpsxx_compute_diagonal_elements_onesite(mpsxx_context* ctx, const mpsxx_tensor* mpo, const mpsxx_tensor* lopr,
+                                            const mpsxx_tensor* ropr, mpsxx_tensor* diag);
+int mpsxx_compute_diagonal_elements_twosite(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                                            const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, mpsxx_tensor* diag);
+
 /* opr1 = bra^T opr0 ket (forward) or bra opr0 ket^T (backward), allocated by the callee.
  * Replaces mpsxx::renormalize(forward, opr0, bra0, ket0, opr1) for merged operators
  * (src/renormalize.hpp:57-95). */
 int mpsxx_renormalize(mpsxx_context* ctx, int forward, const mpsxx_tensor* opr0, const mpsxx_tensor* bra,
                       const mpsxx_tensor* ket, mpsxx_tensor** opr1);
+
+/* renormalize with the site MPO, opr1 (+)= the new block operator (src/renormalize.hpp:10-32;
+ * the one-site step and the initial state use it): forward,
+ * opr1[a,w',a'] = sum bra*[l,n,a] opr0[l,w,l'] mpo[w,n,n',w'] ket[l',n',a'];
+ * backward, opr1[a,w,a'] = sum bra*[a,n,r] opr0[r,w',r'] mpo[w,n,n',w'] ket[a',n',r'].
+ * Allocate-or-accumulate output as for the compute_sigma_vector overloads. */
+int mpsxx_renormalize_mpo(mpsxx_context* ctx, int forward, const mpsxx_tensor* mpo, const mpsxx_tensor* opr0,
+                          const mpsxx_tensor* bra, const mpsxx_tensor* ket, mpsxx_tensor** opr1);
+/* renormalize an overlap matrix (src/renormalize.hpp:35-54): forward
+ * sov1 = (sov0^T bra*)^T ket over (l, n), backward sov1 = (bra* sov0) ket^T over (n, r). */
+int mpsxx_renormalize_overlap(mpsxx_context* ctx, int forward, const mpsxx_tensor* sov0, const mpsxx_tensor* bra,
+                              const mpsxx_tensor* ket, mpsxx_tensor** sov1);
 
 /* Merged super-block operator of one MPO site and one block operator.
  * Replaces the per-group body of mpsxx::compute_merged_operator

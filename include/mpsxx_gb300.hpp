@@ -169,12 +169,41 @@ inline void compute_diagonal_elements(Context& ctx, const QSDArray& lopr, const 
   check(mpsxx_compute_diagonal_elements(ctx.get(), lopr.get(), ropr.get(), diag.get()));
 }
 
+// One-site and four-index two-site diagonals (src/compute_diagonal_elements.hpp:10-62):
+// diag += the diagonal on every allowed block of diag's sectors (diag grows by the
+// blocks it lacks).
+inline void compute_diagonal_elements(Context& ctx, const QSDArray& mpo0, const QSDArray& lopr, const QSDArray& ropr,
+                                      QSDArray& diag) {
+  check(mpsxx_compute_diagonal_elements_onesite(ctx.get(), mpo0.get(), lopr.get(), ropr.get(), diag.get()));
+}
+inline void compute_diagonal_elements(Context& ctx, const QSDArray& lmpo, const QSDArray& rmpo, const QSDArray& lopr,
+                                      const QSDArray& ropr, QSDArray& diag) {
+  check(mpsxx_compute_diagonal_elements_twosite(ctx.get(), lmpo.get(), rmpo.get(), lopr.get(), ropr.get(),
+                                                diag.get()));
+}
+
 // opr1 = renormalised merged operator (allocated here, as a Gemm into an empty array).
+// With a two-index opr0 it renormalises an overlap matrix (src/renormalize.hpp:35-54),
+// allocate-or-accumulate.
 inline void renormalize(Context& ctx, bool forward, const QSDArray& opr0, const QSDArray& bra0, const QSDArray& ket0,
                         QSDArray& opr1) {
+  if (opr0.rank() == 2) {
+    detail::into(opr1, [&](mpsxx_tensor** o) {
+      return mpsxx_renormalize_overlap(ctx.get(), forward ? 1 : 0, opr0.get(), bra0.get(), ket0.get(), o);
+    });
+    return;
+  }
   mpsxx_tensor* h = nullptr;
   check(mpsxx_renormalize(ctx.get(), forward ? 1 : 0, opr0.get(), bra0.get(), ket0.get(), &h));
   opr1 = QSDArray::adopt(h);
+}
+
+// renormalize with the site MPO (src/renormalize.hpp:10-32), allocate-or-accumulate.
+inline void renormalize(Context& ctx, bool forward, const QSDArray& mpo0, const QSDArray& opr0, const QSDArray& bra0,
+                        const QSDArray& ket0, QSDArray& opr1) {
+  detail::into(opr1, [&](mpsxx_tensor** o) {
+    return mpsxx_renormalize_mpo(ctx.get(), forward ? 1 : 0, mpo0.get(), opr0.get(), bra0.get(), ket0.get(), o);
+  });
 }
 
 namespace Davidson {

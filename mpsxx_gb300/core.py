@@ -302,6 +302,32 @@ def compute_sigma_vector_twosite(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr:
                                                                                   ropr.h, wfn.h, o))
 
 
+def renormalize_mpo(ctx: Context, forward: bool, mpo: Tensor, opr0: Tensor, bra: Tensor, ket: Tensor,
+                    opr1: Optional[Tensor] = None) -> Tensor:
+    """renormalize with the site MPO (src/renormalize.hpp:10-32)."""
+    return _in_out(ctx, opr1, lambda o: lib().mpsxx_renormalize_mpo(ctx.h, int(bool(forward)), mpo.h, opr0.h, bra.h,
+                                                                     ket.h, o))
+
+
+def renormalize_overlap(ctx: Context, forward: bool, sov0: Tensor, bra: Tensor, ket: Tensor,
+                        sov1: Optional[Tensor] = None) -> Tensor:
+    """renormalize an overlap matrix (src/renormalize.hpp:35-54)."""
+    return _in_out(ctx, sov1, lambda o: lib().mpsxx_renormalize_overlap(ctx.h, int(bool(forward)), sov0.h, bra.h,
+                                                                         ket.h, o))
+
+
+def compute_diagonal_elements_onesite(ctx: Context, mpo: Tensor, lopr: Tensor, ropr: Tensor, diag: Tensor):
+    """diag += one-site diagonal (src/compute_diagonal_elements.hpp:10-32); diag grows
+    by any allowed blocks it lacks."""
+    check(lib().mpsxx_compute_diagonal_elements_onesite(ctx.h, mpo.h, lopr.h, ropr.h, diag.h))
+
+
+def compute_diagonal_elements_twosite(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor,
+                                      diag: Tensor):
+    """diag += four-index two-site diagonal (src/compute_diagonal_elements.hpp:35-62)."""
+    check(lib().mpsxx_compute_diagonal_elements_twosite(ctx.h, lmpo.h, rmpo.h, lopr.h, ropr.h, diag.h))
+
+
 def compute_sigma_vector_overlap(ctx: Context, lopr: Tensor, ropr: Tensor, wfn: Tensor,
                                  sgv: Optional[Tensor] = None) -> Tensor:
     """lopr wfn ropr^T for two-index overlap operators (src/compute_sigma_vector.hpp:24-35,

@@ -428,6 +428,56 @@ int mpsxx_compute_sigma_vector_overlap(mpsxx_context* ctx, const mpsxx_tensor* l
   });
 }
 
+int mpsxx_renormalize_mpo(mpsxx_context* ctx, int forward, const mpsxx_tensor* mpo, const mpsxx_tensor* opr0,
+                          const mpsxx_tensor* bra, const mpsxx_tensor* ket, mpsxx_tensor** opr1) {
+  return guard([&] {
+    need(opr1 != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    need_device(ten(opr0));
+    need_device(ten(bra));
+    need_device(ten(ket));
+    deliver(ctx, renormalize_mpo(c, forward != 0, ten(mpo), ten(opr0), ten(bra), ten(ket)), opr1);
+  });
+}
+
+int mpsxx_renormalize_overlap(mpsxx_context* ctx, int forward, const mpsxx_tensor* sov0, const mpsxx_tensor* bra,
+                              const mpsxx_tensor* ket, mpsxx_tensor** sov1) {
+  return guard([&] {
+    need(sov1 != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    need_device(ten(sov0));
+    need_device(ten(bra));
+    need_device(ten(ket));
+    deliver(ctx, renormalize_overlap(c, forward != 0, ten(sov0), ten(bra), ten(ket)), sov1);
+  });
+}
+
+int mpsxx_compute_diagonal_elements_onesite(mpsxx_context* ctx, const mpsxx_tensor* mpo, const mpsxx_tensor* lopr,
+                                            const mpsxx_tensor* ropr, mpsxx_tensor* diag) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    need_device(ten(lopr));
+    need_device(ten(ropr));
+    need_device(ten(diag));
+    auto d = diagonal_onesite(c, ten(mpo), ten(lopr), ten(ropr), ten(diag));
+    accumulate_into(c, 1.0, *d, diag->t);
+    c.sync();
+  });
+}
+
+int mpsxx_compute_diagonal_elements_twosite(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,
+                                            const mpsxx_tensor* lopr, const mpsxx_tensor* ropr, mpsxx_tensor* diag) {
+  return guard([&] {
+    Context& c = ctx_of(ctx);
+    need_device(ten(lopr));
+    need_device(ten(ropr));
+    need_device(ten(diag));
+    auto d = diagonal_twosite(c, ten(lmpo), ten(rmpo), ten(lopr), ten(ropr), ten(diag));
+    accumulate_into(c, 1.0, *d, diag->t);
+    c.sync();
+  });
+}
+
 int mpsxx_sigma_plan_stats(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                            const mpsxx_tensor* wfn, double* out, int n, int* count) {
   return guard([&] {

@@ -474,6 +474,18 @@ std::unique_ptr<DTensor> sigma_onesite(Context& ctx, const DTensor& mpo, const D
 std::unique_ptr<DTensor> sigma_twosite(Context& ctx, const DTensor& lmpo, const DTensor& rmpo, const DTensor& lopr,
                                        const DTensor& ropr, const DTensor& wfn);
 std::unique_ptr<DTensor> sigma_overlap(Context& ctx, const DTensor& lopr, const DTensor& ropr, const DTensor& wfn);
+// renormalize with the site MPO (src/renormalize.hpp:10-32) and of an overlap matrix
+// (:35-54), results allocated by the callee
+std::unique_ptr<DTensor> renormalize_mpo(Context& ctx, bool forward, const DTensor& mpo, const DTensor& opr0,
+                                         const DTensor& bra, const DTensor& ket);
+std::unique_ptr<DTensor> renormalize_overlap(Context& ctx, bool forward, const DTensor& sov0, const DTensor& bra,
+                                             const DTensor& ket);
+// compute_diagonal_elements, one-site (src/compute_diagonal_elements.hpp:10-32) and
+// four-index two-site (:35-62): the diagonal on every allowed block of like's sectors
+std::unique_ptr<DTensor> diagonal_onesite(Context& ctx, const DTensor& mpo, const DTensor& lopr, const DTensor& ropr,
+                                          const DTensor& like);
+std::unique_ptr<DTensor> diagonal_twosite(Context& ctx, const DTensor& lmpo, const DTensor& rmpo, const DTensor& lopr,
+                                          const DTensor& ropr, const DTensor& like);
 
 // One bond (src/optimize.hpp:495-651)
 struct BondStats {

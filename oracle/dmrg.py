@@ -73,6 +73,30 @@ def compute_sigma_vector_overlap(lopr: QSDArray, ropr: QSDArray, wfn0: QSDArray,
 # a9: renormalize merged operator / overlap (src/renormalize.hpp:57-95)
 # ----------------------------------------------------------------------------
 
+def renormalize_mpo(forward: bool, mpo0: QSDArray, opr0: QSDArray, bra0: QSDArray, ket0: QSDArray) -> QSDArray:
+    """renormalize with the site MPO (``src/renormalize.hpp:10-32``): three Contracts."""
+    b = bra0.conjugate()
+    if forward:
+        scr1 = contract(opr0, "lwk", b, "lna", "wkna")
+        scr2 = contract(scr1, "wkna", mpo0, "wnmv", "kamv")
+        return contract(scr2, "kamv", ket0, "kmb", "avb")
+    scr1 = contract(b, "anr", opr0, "rvs", "anvs")
+    scr2 = contract(scr1, "anvs", mpo0, "wnmv", "aswm")
+    return contract(scr2, "aswm", ket0, "bms", "awb")
+
+
+def renormalize_overlap(forward: bool, sov0: QSDArray, bra0: QSDArray, ket0: QSDArray) -> QSDArray:
+    """renormalize an overlap matrix (``src/renormalize.hpp:35-54``): two Gemms."""
+    scr1, sov1 = QSDArray(), QSDArray()
+    if forward:
+        gemm(Trans, NoTrans, 1.0, sov0, bra0.conjugate(), 1.0, scr1, nc=3)
+        gemm(Trans, NoTrans, 1.0, scr1, ket0, 1.0, sov1, nc=2)
+    else:
+        gemm(NoTrans, NoTrans, 1.0, bra0.conjugate(), sov0, 1.0, scr1, nc=3)
+        gemm(NoTrans, Trans, 1.0, scr1, ket0, 1.0, sov1, nc=2)
+    return sov1
+
+
 def renormalize_merged(forward: bool, opr0: QSDArray, bra0: QSDArray, ket0: QSDArray,
                        tasks: Optional[list] = None) -> QSDArray:
     opr1 = QSDArray()
@@ -135,6 +159,65 @@ def compute_diagonal_elements(lopr: QSDArray, ropr: QSDArray, diag: QSDArray):
                 diag.blocks[t] = diag.blocks[t] + blk
             else:
                 diag.blocks[t] = blk.copy()
+
+
+def _tie_mpo(mpo: QSDArray) -> Dict[tuple, np.ndarray]:
+    """``Tie(mpo, shape(1,2))``: y[w,n,w'] = mpo[w,n,n,w'] as an un-quantised block map."""
+    out = {}
+    for t in sorted(mpo.blocks):
+        w, n, m, v = mpo.index(t)
+        if n == m:
+            out[(w, n, v)] = np.einsum("wnnv->wnv", mpo.blocks[t])
+    return out
+
+
+def _copy_allowed(scr: Dict[tuple, np.ndarray], diag: QSDArray):
+    """``Copy(scr, diag, 1)`` followed by the group Axpy: add the blocks diag's quantum
+    numbers allow (``src/compute_diagonal_elements.hpp:30,94-95``)."""
+    for idx, blk in scr.items():
+        if diag.allowed(idx):
+            t = diag.tag(idx)
+            diag.blocks[t] = diag.blocks[t] + blk if t in diag.blocks else blk.copy()
+
+
+def compute_diagonal_elements_onesite(mpo0: QSDArray, lopr: QSDArray, ropr: QSDArray, diag: QSDArray):
+    """One-site diagonal (``src/compute_diagonal_elements.hpp:10-32``): Tie the MPO over
+    (1,2) and the operators over (0,2), then diag[l,n,r] = sum Ld[l,w] Wd[w,n,w'] Rd[r,w']."""
+    ld, rd, wd = tie_02(lopr), tie_02(ropr), _tie_mpo(mpo0)
+    scr: Dict[tuple, np.ndarray] = {}
+    for (l, w), a in sorted(ld.items()):
+        for (w2, n, v), b in sorted(wd.items()):
+            if w2 != w:
+                continue
+            for (r, v2), c in sorted(rd.items()):
+                if v2 != v:
+                    continue
+                val = np.einsum("lw,wnv,rv->lnr", a, b, c)
+                k = (l, n, r)
+                scr[k] = scr[k] + val if k in scr else val
+    _copy_allowed(scr, diag)
+
+
+def compute_diagonal_elements_twosite(lmpo: QSDArray, rmpo: QSDArray, lopr: QSDArray, ropr: QSDArray,
+                                      diag: QSDArray):
+    """Four-index two-site diagonal (``src/compute_diagonal_elements.hpp:35-62``):
+    diag[l,n,m,r] = sum Ld[l,w] Wl[w,n,v] Wr[v,m,x] Rd[r,x]."""
+    ld, rd, wl, wr = tie_02(lopr), tie_02(ropr), _tie_mpo(lmpo), _tie_mpo(rmpo)
+    scr: Dict[tuple, np.ndarray] = {}
+    for (l, w), a in sorted(ld.items()):
+        for (w2, n, v), b in sorted(wl.items()):
+            if w2 != w:
+                continue
+            for (v2, m, x), c in sorted(wr.items()):
+                if v2 != v:
+                    continue
+                for (r, x2), d in sorted(rd.items()):
+                    if x2 != x:
+                        continue
+                    val = np.einsum("lw,wnv,vmx,rx->lnmr", a, b, c, d)
+                    k = (l, n, m, r)
+                    scr[k] = scr[k] + val if k in scr else val
+    _copy_allowed(scr, diag)
 
 
 # ----------------------------------------------------------------------------

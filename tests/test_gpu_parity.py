@@ -393,3 +393,58 @@ def test_sigma_overloads_match_oracle(ctx, kind):
     expect = w.copy()
     oq.axpy(1.0, ref, expect)
     assert max_block_diff(expect.blocks, acc.to_blocks()) < 1e-12
+
+
+@pytest.mark.parametrize("forward", [True, False])
+def test_renormalize_overloads_match_oracle(ctx, forward):
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    st, i, mpo = case["st"], case["i"], case["mpo"]
+    if forward:
+        k, opr, w = i, st.lenv[i], st.wave[i]
+    else:
+        k, opr, w = i + 1, st.renv[i + 1], st.wave[i + 1]
+    ref = od.renormalize_mpo(forward, mpo[k], opr, w, w)
+    W = dev(ctx, w)
+    got = core.renormalize_mpo(ctx, forward, dev(ctx, mpo[k]), dev(ctx, opr), W, W)
+    assert max_block_diff(ref.blocks, got.to_blocks()) < 1e-12
+    again = core.renormalize_mpo(ctx, forward, dev(ctx, mpo[k]), dev(ctx, opr), W, W, got)  # accumulates
+    assert again is got
+    assert max_block_diff({t: 2 * b for t, b in ref.blocks.items()}, got.to_blocks()) < 1e-12
+    # overlap matrix, with a random S on the contracted sectors
+    rng = np.random.default_rng(5)
+    qs, ds = (w.qshape[0], w.dshape[0]) if forward else (w.qshape[2], w.dshape[2])
+    S = oq.QSDArray((0, 0), [qs, [oq.qneg(q) for q in qs]], [ds, ds])
+    for x in range(len(qs)):
+        for y in range(len(qs)):
+            if S.allowed((x, y)) and ds[x] and ds[y]:
+                S.blocks[S.tag((x, y))] = rng.standard_normal((ds[x], ds[y]))
+    ref = od.renormalize_overlap(forward, S, w, w)
+    got = core.renormalize_overlap(ctx, forward, dev(ctx, S), W, W)
+    assert max_block_diff(ref.blocks, got.to_blocks()) < 1e-12
+
+
+@pytest.mark.parametrize("kind", ["onesite", "twosite"])
+def test_diagonal_overloads_match_oracle(ctx, kind):
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+    from mpsxx_gb300 import core
+
+    case = hubbard_bond()
+    st, i, mpo = case["st"], case["i"], case["mpo"]
+    w = st.wave[i] if kind == "onesite" else two_site(case)
+    ref = oq.QSDArray(w.q, w.qshape, w.dshape)
+    D = dev(ctx, w)  # starts from w's data: the diagonal is added to it
+    if kind == "onesite":
+        od.compute_diagonal_elements_onesite(mpo[i], st.lenv[i], st.renv[i], ref)
+        core.compute_diagonal_elements_onesite(ctx, *[dev(ctx, x) for x in (mpo[i], st.lenv[i], st.renv[i])], D)
+    else:
+        od.compute_diagonal_elements_twosite(mpo[i], mpo[i + 1], st.lenv[i], st.renv[i + 1], ref)
+        core.compute_diagonal_elements_twosite(
+            ctx, *[dev(ctx, x) for x in (mpo[i], mpo[i + 1], st.lenv[i], st.renv[i + 1])], D)
+    expect = w.copy()
+    oq.axpy(1.0, ref, expect)
+    assert max_block_diff(expect.blocks, D.to_blocks()) < 1e-12

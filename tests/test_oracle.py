@@ -166,3 +166,30 @@ def test_rank_overloads_equal_the_merged_product():
     mR = od.compute_merged_operator(False, mpo[i + 1], st.renv[i + 1])
     sg = _merged_sigma(mL, mR, oq.merge_rows(rows, oq.merge_cols(t, cols)))
     assert _max_diff(lit, oq.expand_cols(oq.expand_rows(rows, sg), cols)) < 1e-13
+
+
+def test_renormalize_and_diagonal_overloads_equal_the_merged_forms():
+    """renormalize with the site MPO (forward and backward) and the one-site / four-index
+    diagonals, restated literally, equal the merged forms the library runs them as."""
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+    from tests.bondcase import hubbard_bond
+
+    case = hubbard_bond()
+    st, i, mpo = case["st"], case["i"], case["mpo"]
+    w, w2 = st.wave[i], st.wave[i + 1]
+    mL = od.compute_merged_operator(True, mpo[i], st.lenv[i])
+    mR = od.compute_merged_operator(False, mpo[i + 1], st.renv[i + 1])
+    rows = oq.MergeInfo(w.qshape[:2], w.dshape[:2])
+    U = oq.merge_rows(rows, w)
+    assert _max_diff(od.renormalize_mpo(True, mpo[i], st.lenv[i], w, w), od.renormalize_merged(True, mL, U, U)) < 1e-13
+    cols = oq.MergeInfo(w2.qshape[1:], w2.dshape[1:])
+    V = oq.merge_cols(w2, cols)
+    assert _max_diff(od.renormalize_mpo(False, mpo[i + 1], st.renv[i + 1], w2, w2),
+                     od.renormalize_merged(False, mR, V, V)) < 1e-13
+    d = oq.QSDArray(w.q, w.qshape, w.dshape)
+    od.compute_diagonal_elements_onesite(mpo[i], st.lenv[i], st.renv[i], d)
+    dm = U.empty_like()
+    dm.allocate(0.0)
+    od.compute_diagonal_elements(mL, st.renv[i], dm)
+    assert _max_diff(d, oq.expand_rows(rows, dm)) < 1e-13
