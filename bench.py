@@ -500,8 +500,8 @@ def run_reference(args, ws, rank):
     ctx = core.Context(0)
     wl = build_workload(args, ctx)
     samples = []
-    for _ in range(args.warmup):
-        pass
+    for _ in range(args.warmup):  # untimed: one psi-block chunk each (BLAS threads, page-in)
+        cpu_sigma_sample(wl, 1e-9)
     for _ in range(max(1, args.steps)):
         s = cpu_sigma_sample(wl, args.cpu_seconds / max(1, args.steps))
         samples.append(s["value"])

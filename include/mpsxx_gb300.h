@@ -360,9 +360,9 @@ int mpsxx_normalize(mpsxx_context* ctx, mpsxx_tensor* x, double* norm);
 /* Allocation-free multi-dot; this entry point has no counterpart in the reference.
  * out[i*ny + j] = dot(X + i*stride, Y + j*stride) over n doubles (all device
  * pointers), 1 <= nx, ny <= 10: the Rayleigh-Ritz products of the Davidson solver.
- * It is for callers that must not allocate device memory while they run — code
- * being recorded into a CUDA graph, a host framework that owns the device memory
- * through its own pool, or a loop that cannot afford the synchronisation an
+ * It is for callers that cannot call cudaMalloc while they run — a host application
+ * that has claimed the device memory for its own pool and hands plugins only its own
+ * buffers, or a loop that cannot afford the device-wide synchronisation an
  * allocation may cause.  It needs no context and calls no allocator: its reduction
  * scratch is a fixed array of 304 x 100 doubles (243 KB) built into the library,
  * which every device that loads the library holds until the process exits.  The

@@ -1,19 +1,22 @@
 // Allocation-free variant of the Davidson multi-dot reduction.
 //
-// Who needs it: host code that must never allocate device memory while it runs —
-// a caller recording work into a CUDA graph (cudaMalloc is not allowed inside a
-// stream capture), a host framework that owns the whole device-memory budget
-// through its own pool, or a latency-sensitive loop that cannot afford the
-// device-wide synchronisation cudaMalloc/cudaFree may cause.  The regular path
-// keeps its reduction partials in a context-owned buffer that grows with
-// cudaMalloc; this entry point takes them from a fixed array compiled into the
-// library instead.
+// Who needs it: host code that cannot call cudaMalloc while it runs — a solver
+// embedded in a host application that has claimed the device memory for its own
+// pool allocator and hands its plugins only buffers it allocated itself, or a
+// latency-sensitive loop that cannot afford the device-wide synchronisation that
+// cudaMalloc/cudaFree may cause (or an allocation that fails half-way through a
+// step once the environments have filled the device).  The regular path keeps its
+// reduction partials in a context-owned buffer that grows with cudaMalloc; this
+// entry point takes them from a fixed array compiled into the library instead.
 //
 // The array is a file-scope __device__ variable: every GPU that loads the library
 // holds it (kNoAllocPartials doubles) until the process exits, and all calls on a
 // device share it.  Each call overwrites the partials it uses before reading them,
 // so nothing has to start at zero, but two calls whose kernels overlap on the GPU
-// (different streams, or concurrent host threads) race on the array.
+// (different streams, or concurrent host threads) race on the array.  The first
+// call on a device looks up the array's device address for that device (with it
+// current); a caller that captures streams makes that first call before any
+// capture.
 #include <cuda_runtime.h>
 
 #include <cstdint>

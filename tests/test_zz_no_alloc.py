@@ -1,8 +1,9 @@
 """The allocation-free multi-dot entry point against the regular path (needs a GPU).
 
-mpsxx_multidot_noalloc serves callers that must not allocate device memory while
-they run (work recorded into a CUDA graph, a framework that owns the device memory
-through its own pool): its reduction scratch is a fixed array inside the library.
+mpsxx_multidot_noalloc serves callers that cannot call cudaMalloc while they run
+(a host application that owns the device memory through its own pool, a loop that
+cannot afford an allocation's device-wide synchronisation): its reduction scratch
+is a fixed array inside the library.
 This file is collected last so that a failure here cannot hide any other test.
 Tolerance: 1e-12 relative, the FP64 reduction order differs from NumPy's.
 """
