@@ -226,6 +226,14 @@ int mpsxx_renormalize_mpo(mpsxx_context* ctx, int forward, const mpsxx_tensor* m
 int mpsxx_renormalize_overlap(mpsxx_context* ctx, int forward, const mpsxx_tensor* sov0, const mpsxx_tensor* bra,
                               const mpsxx_tensor* ket, mpsxx_tensor** sov1);
 
+/* Guess wavefunction of the next site, mpsxx::compute_guesswave
+ * (src/compute_guesswave.hpp:11-38): forward (mps0 = L(i), wfn0 = C(i), mps1 = R(i+1))
+ * wfn1 = (L(i)^+ C(i)) R(i+1); backward (mps0 = R(i+1), wfn0 = C(i+1), mps1 = L(i))
+ * wfn1 = L(i) (C(i+1) R(i+1)^+).  Two Gemms; *wfn1 is allocated when NULL, else the
+ * result is added to it (quantum numbers and shapes checked). */
+int mpsxx_compute_guesswave(mpsxx_context* ctx, int forward, const mpsxx_tensor* mps0, const mpsxx_tensor* wfn0,
+                            const mpsxx_tensor* mps1, mpsxx_tensor** wfn1);
+
 /* Merged super-block operator of one MPO site and one block operator.
  * Replaces the per-group body of mpsxx::compute_merged_operator
  * (src/optimize.hpp:273-368).  mpo must have been uploaded from the host. */

@@ -182,6 +182,16 @@ inline void compute_diagonal_elements(Context& ctx, const QSDArray& lmpo, const 
                                                 diag.get()));
 }
 
+// wfn1 += guess wavefunction of the next site (src/compute_guesswave.hpp:11-38): forward
+// (L(i), C(i), R(i+1)) -> C(i+1), backward (R(i+1), C(i+1), L(i)) -> C(i); an empty wfn1
+// receives the result.
+inline void compute_guesswave(Context& ctx, bool forward, const QSDArray& mps0, const QSDArray& wfn0,
+                              const QSDArray& mps1, QSDArray& wfn1) {
+  detail::into(wfn1, [&](mpsxx_tensor** o) {
+    return mpsxx_compute_guesswave(ctx.get(), forward ? 1 : 0, mps0.get(), wfn0.get(), mps1.get(), o);
+  });
+}
+
 // opr1 = renormalised merged operator (allocated here, as a Gemm into an empty array).
 // With a two-index opr0 it renormalises an overlap matrix (src/renormalize.hpp:35-54),
 // allocate-or-accumulate.

@@ -68,6 +68,7 @@ SIGNATURES = {
     "mpsxx_compute_sigma_vector_overlap": (C.c_int, [vp, vp, vp, vp, vpp]),
     "mpsxx_renormalize_mpo": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vpp]),
     "mpsxx_renormalize_overlap": (C.c_int, [vp, C.c_int, vp, vp, vp, vpp]),
+    "mpsxx_compute_guesswave": (C.c_int, [vp, C.c_int, vp, vp, vp, vpp]),
     "mpsxx_compute_diagonal_elements_onesite": (C.c_int, [vp, vp, vp, vp, vp]),
     "mpsxx_compute_diagonal_elements_twosite": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "mpsxx_noise_sequence": (C.c_int, [C.c_int64, c_dbl_p]),

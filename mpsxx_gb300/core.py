@@ -316,6 +316,14 @@ def renormalize_overlap(ctx: Context, forward: bool, sov0: Tensor, bra: Tensor, 
                                                                          ket.h, o))
 
 
+def compute_guesswave(ctx: Context, forward: bool, mps0: Tensor, wfn0: Tensor, mps1: Tensor,
+                      wfn1: Optional[Tensor] = None) -> Tensor:
+    """compute_guesswave (src/compute_guesswave.hpp:11-38): the one-site centre moved to
+    the next site (forward: (L^+ C) R; backward: L (C R^+)), allocate-or-accumulate."""
+    return _in_out(ctx, wfn1, lambda o: lib().mpsxx_compute_guesswave(ctx.h, int(bool(forward)), mps0.h, wfn0.h,
+                                                                       mps1.h, o))
+
+
 def compute_diagonal_elements_onesite(ctx: Context, mpo: Tensor, lopr: Tensor, ropr: Tensor, diag: Tensor):
     """diag += one-site diagonal (src/compute_diagonal_elements.hpp:10-32); diag grows
     by any allowed blocks it lacks."""

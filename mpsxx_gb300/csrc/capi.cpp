@@ -452,6 +452,18 @@ int mpsxx_renormalize_overlap(mpsxx_context* ctx, int forward, const mpsxx_tenso
   });
 }
 
+int mpsxx_compute_guesswave(mpsxx_context* ctx, int forward, const mpsxx_tensor* mps0, const mpsxx_tensor* wfn0,
+                            const mpsxx_tensor* mps1, mpsxx_tensor** wfn1) {
+  return guard([&] {
+    need(wfn1 != nullptr, "null output");
+    Context& c = ctx_of(ctx);
+    need_device(ten(mps0));
+    need_device(ten(wfn0));
+    need_device(ten(mps1));
+    deliver(ctx, guesswave(c, forward != 0, ten(mps0), ten(wfn0), ten(mps1)), wfn1);
+  });
+}
+
 int mpsxx_compute_diagonal_elements_onesite(mpsxx_context* ctx, const mpsxx_tensor* mpo, const mpsxx_tensor* lopr,
                                             const mpsxx_tensor* ropr, mpsxx_tensor* diag) {
   return guard([&] {

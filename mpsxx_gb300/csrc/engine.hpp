@@ -480,6 +480,10 @@ std::unique_ptr<DTensor> renormalize_mpo(Context& ctx, bool forward, const DTens
                                          const DTensor& bra, const DTensor& ket);
 std::unique_ptr<DTensor> renormalize_overlap(Context& ctx, bool forward, const DTensor& sov0, const DTensor& bra,
                                              const DTensor& ket);
+// compute_guesswave (src/compute_guesswave.hpp:11-38): forward C(i+1) = L(i)^+ C(i) R(i+1),
+// backward C(i) = L(i) C(i+1) R(i+1)^+, result allocated by the callee
+std::unique_ptr<DTensor> guesswave(Context& ctx, bool forward, const DTensor& mps0, const DTensor& wfn0,
+                                   const DTensor& mps1);
 // compute_diagonal_elements, one-site (src/compute_diagonal_elements.hpp:10-32) and
 // four-index two-site (:35-62): the diagonal on every allowed block of like's sectors
 std::unique_ptr<DTensor> diagonal_onesite(Context& ctx, const DTensor& mpo, const DTensor& lopr, const DTensor& ropr,

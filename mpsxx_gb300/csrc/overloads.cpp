@@ -7,6 +7,7 @@
 //   renormalize (src/renormalize.hpp): with the site MPO (:10-32), overlap (:35-54)
 //   compute_diagonal_elements (src/compute_diagonal_elements.hpp): one-site (:10-32),
 //     two-site four-index (:35-62)
+//   compute_guesswave (src/compute_guesswave.hpp:11-38): the centre moved one site
 // The H forms run as the merged products: the block operator is merged with its site
 // MPO (compute_merged_operator), the site tensors are merged over the same index
 // pairs, the merged kernels run (on every allowed merged block where the result's
@@ -174,6 +175,22 @@ std::unique_ptr<DTensor> renormalize_overlap(Context& ctx, bool forward, const D
   }
   auto scr1 = gemm_new(ctx, kNoTrans, kNoTrans, 1.0, *cbra, sov0, 3);
   return gemm_new(ctx, kNoTrans, kTrans, 1.0, *scr1, ket, 2);
+}
+
+std::unique_ptr<DTensor> guesswave(Context& ctx, bool forward, const DTensor& mps0, const DTensor& wfn0,
+                                   const DTensor& mps1) {
+  if (mps0.sh.rank != 3 || wfn0.sh.rank != 3 || mps1.sh.rank != 3)
+    throw Error(kInvalidArgument, "compute_guesswave: site tensors of 3 indices");
+  // ConjTrans of a real QSDArray = Trans of its conjugate (negated quantum numbers,
+  // same blocks and data): btas_contract_qshape.h takes -q for ConjTrans, the dense
+  // layer treats it as Trans, and ST_Gemm_thread enumerates both alike
+  auto c0 = conjugate_view(mps0);
+  if (forward) {
+    auto gmat = gemm_new(ctx, kTrans, kNoTrans, 1.0, *c0, wfn0, 2);
+    return gemm_new(ctx, kNoTrans, kNoTrans, 1.0, *gmat, mps1, 3);
+  }
+  auto gmat = gemm_new(ctx, kNoTrans, kTrans, 1.0, wfn0, *c0, 2);
+  return gemm_new(ctx, kNoTrans, kNoTrans, 1.0, mps1, *gmat, 3);
 }
 
 std::unique_ptr<DTensor> diagonal_onesite(Context& ctx, const DTensor& mpo, const DTensor& lopr, const DTensor& ropr,

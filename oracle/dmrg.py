@@ -85,6 +85,21 @@ def renormalize_mpo(forward: bool, mpo0: QSDArray, opr0: QSDArray, bra0: QSDArra
     return contract(scr2, "aswm", ket0, "bms", "awb")
 
 
+def compute_guesswave(forward: bool, mps0: QSDArray, wfn0: QSDArray, mps1: QSDArray, wfn1: QSDArray) -> QSDArray:
+    """compute_guesswave (``src/compute_guesswave.hpp:11-38``): two Gemms into wfn1.  The
+    reference's ConjTrans operand is the Trans of its conjugate for real data (the
+    q-shape rule of ``include/btas/QSPARSE/btas_contract_qshape.h:76-79, 94-100`` negates
+    the quantum numbers; the dense layer treats ConjTrans of doubles as Trans)."""
+    gmat = QSDArray()
+    if forward:  # C(i+1) = L(i)^+ C(i) R(i+1)
+        gemm(Trans, NoTrans, 1.0, mps0.conjugate(), wfn0, 1.0, gmat, nc=2)
+        gemm(NoTrans, NoTrans, 1.0, gmat, mps1, 1.0, wfn1, nc=3)
+    else:  # C(i) = L(i) C(i+1) R(i+1)^+
+        gemm(NoTrans, Trans, 1.0, wfn0, mps0.conjugate(), 1.0, gmat, nc=2)
+        gemm(NoTrans, NoTrans, 1.0, mps1, gmat, 1.0, wfn1, nc=3)
+    return wfn1
+
+
 def renormalize_overlap(forward: bool, sov0: QSDArray, bra0: QSDArray, ket0: QSDArray) -> QSDArray:
     """renormalize an overlap matrix (``src/renormalize.hpp:35-54``): two Gemms."""
     scr1, sov1 = QSDArray(), QSDArray()

@@ -51,3 +51,21 @@ def repeated_sector_psi() -> oq.QSDArray:
 
 def to_dict(a: oq.QSDArray) -> dict:
     return {"q": a.q, "qshape": a.qshape, "dshape": a.dshape, "blocks": a.blocks}
+
+
+def guesswave_case(seed=3):
+    """Site tensors of a Hubbard bond (left-normalised L(i-1), centre C(i), right-normalised
+    R(i+1)) and random tensors with the same block layouts."""
+    import numpy as np
+
+    case = hubbard_bond()
+    st, i = case["st"], case["i"]
+    rng = np.random.default_rng(seed)
+
+    def rand_like(a):
+        r = a.copy()
+        for t in r.blocks:
+            r.blocks[t] = rng.standard_normal(r.blocks[t].shape)
+        return r
+
+    return st.wave[i - 1], st.wave[i], st.wave[i + 1], rand_like

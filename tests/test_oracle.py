@@ -193,3 +193,44 @@ def test_renormalize_and_diagonal_overloads_equal_the_merged_forms():
     dm.allocate(0.0)
     od.compute_diagonal_elements(mL, st.renv[i], dm)
     assert _max_diff(d, oq.expand_rows(rows, dm)) < 1e-13
+
+
+def _dense(a):
+    offs = [np.concatenate([[0], np.cumsum(d)]).astype(int) for d in a.dshape]
+    out = np.zeros([int(o[-1]) for o in offs])
+    for t, b in a.blocks.items():
+        idx = a.index(t)
+        out[tuple(slice(offs[k][i], offs[k][i + 1]) for k, i in enumerate(idx))] = b
+    return out
+
+
+def test_guesswave_restatement():
+    """compute_guesswave (src/compute_guesswave.hpp:11-38) restated: forward (L^T C) R and
+    backward L (C R^T) on dense copies of random tensors, and the gauge move of a
+    canonical state: an isometry against itself gives back the other site unchanged."""
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+
+    from tests.bondcase import guesswave_case
+
+    L, C, R, rand_like = guesswave_case()
+    Lr, Lc, Cr = rand_like(L), rand_like(L), rand_like(C)
+    f = od.compute_guesswave(True, Lr, Lc, Cr, oq.QSDArray())
+    ref = np.einsum("lnp,lnr,rmq->pmq", _dense(Lr), _dense(Lc), _dense(Cr))
+    assert np.abs(_dense(f) - ref).max() < 1e-12 * np.abs(ref).max()
+    Rr, Rc = rand_like(R), rand_like(R)
+    b = od.compute_guesswave(False, Rr, Rc, Cr, oq.QSDArray())
+    ref = np.einsum("asx,xy->asy", _dense(Cr), np.einsum("xnr,ynr->xy", _dense(Rc), _dense(Rr)))
+    assert np.abs(_dense(b) - ref).max() < 1e-12 * np.abs(ref).max()
+    assert _max_diff(od.compute_guesswave(True, L, L, C, oq.QSDArray()), C) < 1e-12
+    assert _max_diff(od.compute_guesswave(False, R, R, C, oq.QSDArray()), C) < 1e-12
+    acc = C.copy()  # accumulates into a non-empty wfn1
+    od.compute_guesswave(True, L, L, C, acc)
+    assert _max_diff(acc, _twice(C)) < 1e-12
+
+
+def _twice(a):
+    t = a.copy()
+    for k in t.blocks:
+        t.blocks[k] = 2.0 * t.blocks[k]
+    return t
