@@ -449,25 +449,3 @@ def test_diagonal_overloads_match_oracle(ctx, kind):
     oq.axpy(1.0, ref, expect)
     assert max_block_diff(expect.blocks, D.to_blocks()) < 1e-12
 
-
-@pytest.mark.parametrize("forward", [True, False])
-def test_guesswave_matches_oracle(ctx, forward):
-    """compute_guesswave (src/compute_guesswave.hpp:11-38) on random tensors with the
-    layouts of a Hubbard bond's sites, allocated and accumulated."""
-    from oracle import dmrg as od
-    from oracle import qsd as oq
-    from tests.bondcase import guesswave_case
-    from mpsxx_gb300 import core
-
-    L, C, R, rand_like = guesswave_case()
-    mps0, wfn0 = (rand_like(L), rand_like(L)) if forward else (rand_like(R), rand_like(R))
-    mps1 = rand_like(C)
-    ref = od.compute_guesswave(forward, mps0, wfn0, mps1, oq.QSDArray())
-    ops = [dev(ctx, x) for x in (mps0, wfn0, mps1)]
-    got = core.compute_guesswave(ctx, forward, *ops)
-    assert max_block_diff(ref.blocks, got.to_blocks()) < 1e-12
-    acc = dev(ctx, C)
-    core.compute_guesswave(ctx, forward, *ops, acc)
-    expect = C.copy()
-    oq.axpy(1.0, ref, expect)
-    assert max_block_diff(expect.blocks, acc.to_blocks()) < 1e-12
