@@ -51,9 +51,14 @@ def parse():
     ap.add_argument("--tole", type=float, default=1e-9, help="sweep tolerance (Davidson |r|^2 < 0.1 tole)")
     ap.add_argument("--bond-step", action="store_true", help="also time one full bond step at the bench bond")
     ap.add_argument("--no-sweep", action="store_true", help="skip the FP64-vs-split sweep comparison")
-    ap.add_argument("--sweep-norb", type=int, default=16)
-    ap.add_argument("--sweep-M", type=int, default=256)
-    ap.add_argument("--sweep-max", type=int, default=12)
+    ap.add_argument("--sweep-norb", type=int, default=20)
+    ap.add_argument("--sweep-M", type=int, default=512)
+    ap.add_argument("--sweep-max", type=int, default=16)
+    ap.add_argument("--sweep-conv", type=float, default=1e-10,
+                    help="sweep convergence: |dE| between consecutive sweeps")
+    ap.add_argument("--no-sweep-control", action="store_true",
+                    help="skip the FP64 control arm (ten times tighter Davidson tolerance)")
+    ap.add_argument("--mpo", default="qc", choices=["qc"], help="QC MPO construction")
     ap.add_argument("--gradient", action="store_true",
                     help="also run the energy-gradient workloads (site-dependent Hubbard L=32 M=512, QC n=16 M=256)")
     ap.add_argument("--grad-fd", type=int, default=2, help="parameters checked by central differences per workload")
@@ -61,7 +66,7 @@ def parse():
                     help="also run the batched scan: 64 Hubbard chains, L ~ U{16..32}, U ~ U(0,8), M 64->256 over 6 sweeps")
     ap.add_argument("--scan-chains", type=int, default=64)
     ap.add_argument("--scan-compare", type=int, default=8, help="chains also swept one by one for comparison")
-    ap.add_argument("--warm-sweeps", type=int, default=3,
+    ap.add_argument("--warm-sweeps", type=int, default=2,
                     help="sweeps in each precision from the FP64-converged state")
     ap.add_argument("--sweep-split-all", action="store_true",
                     help="also sweep with the renormalisation contractions in split precision")
@@ -158,11 +163,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.samples)}
 
 
+def mpo_dicts(args, h1, eri):
+    from mpsxx_gb300 import mpogen
+
+    return mpogen.qc_mpo(h1, eri)
+
+
 def build_workload(args, ctx):
     from mpsxx_gb300 import core, dmrg, mpogen
 
     h1, eri = mpogen.synthetic_qc_integrals(args.norb, args.nchol, args.seed)
-    mpo_d = mpogen.qc_mpo(h1, eri)
+    mpo_d = mpo_dicts(args, h1, eri)
     mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
     st = dmrg.make_random_state(ctx, mpo, args.norb, 0, args.M, seed=args.seed)
     bond = args.bond if args.bond >= 0 else args.norb // 2 - 1
@@ -172,55 +183,69 @@ def build_workload(args, ctx):
 
 
 def sweep_compare(args, device: int):
-    """Two-site DMRG from the reference's initial state on a smaller synthetic QC
-    system: FP64 until |dE| < tole after >= 2 sweeps, then split precision for the
-    same number of sweeps, so that the energies are compared sweep by sweep."""
+    """Cold two-site DMRG from the reference's initial state (constant-filled sites,
+    src/make_random_mpss.cpp:97-271) on the synthetic QC system, in three arms, each
+    swept until the sweep energy changes by less than ``sweep_conv`` after at least two
+    sweeps (src/dmrg.cpp:57-65), at most ``sweep_max`` sweeps:
+
+    * ``fp64``: FP64 H_eff*psi, Davidson |r|^2 < 0.1*tole;
+    * ``split``: split-precision H_eff*psi with the FP64 refinement, same tolerance;
+    * ``fp64_control``: FP64 again with a ten times tighter Davidson tolerance.
+
+    The two FP64 arms differ only in where each Davidson stops; the energy they settle
+    at differs by the path dependence of the truncated (fixed M) problem, the floor
+    against which the split-vs-FP64 difference is read."""
     from mpsxx_gb300 import core, dmrg, mpogen
 
     n, M = args.sweep_norb, args.sweep_M
     h1, eri = mpogen.synthetic_qc_integrals(n, 2 * n, args.seed)
-    mpo_d = mpogen.qc_mpo(h1, eri)
-    res = {"workload": f"qc n={n} K={2 * n} seed={args.seed} M={M} tole={args.tole}"}
-    nsweeps = args.sweep_max
-    arms = [("fp64", core.FP64), ("split", core.SPLIT_TF32)]
+    mpo_d = mpo_dicts(args, h1, eri)
+    res = {"workload": f"qc n={n} K={2 * n} seed={args.seed} M={M} mpo={args.mpo}", "tole": args.tole,
+           "sweep_conv": args.sweep_conv, "start": "reference initial state (constant-filled sites)"}
+    arms = [("fp64", core.FP64, args.tole), ("split", core.SPLIT_TF32, args.tole)]
+    if not args.no_sweep_control:
+        arms.append(("fp64_control", core.FP64, 0.1 * args.tole))
     if args.sweep_split_all:
-        arms.append(("split_all", core.SPLIT_TF32_ALL))
+        arms.append(("split_all", core.SPLIT_TF32_ALL, args.tole))
     warm = None
-    for name, prec in arms:
+    for name, prec, tole in arms:
         ctx = core.Context(device)
         core.set_precision(ctx, prec)
         mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
         st = dmrg.make_initial_state(ctx, mpo, n, 0, M)
-        sweeps, e_prev = [], 0.0
-        for it in range(nsweeps):
-            log = dmrg.make_sweep(ctx, st, args.tole)
+        sweeps, e_prev, conv = [], None, False
+        for it in range(args.sweep_max):
+            log = dmrg.make_sweep(ctx, st, tole)
             sweeps.append({"seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma,
                            "sigma_flops": log.sigma_flops, **{k: round(v, 4) for k, v in log.times.items()}})
-            de = log.energy - e_prev
-            e_prev = log.energy
-            if prec == core.FP64 and it > 0 and abs(de) < args.tole:
-                nsweeps = it + 1
+            if e_prev is not None and it >= 1 and abs(log.energy - e_prev) < args.sweep_conv:
+                conv = True
                 break
-        res[name] = {"sweeps": len(sweeps), "energy": sweeps[-1]["energy"],
+            e_prev = log.energy
+        last = sweeps[-1]
+        res[name] = {"sweeps": len(sweeps), "converged": conv, "davidson_tole": 0.1 * tole,
+                     "energy": last["energy"],
+                     "last_dE": abs(last["energy"] - sweeps[-2]["energy"]) if len(sweeps) > 1 else None,
                      "seconds_total": sum(s["seconds"] for s in sweeps),
-                     "seconds_last_sweep": sweeps[-1]["seconds"],
+                     "seconds_last_sweep": last["seconds"],
                      "n_sigma_total": sum(s["n_sigma"] for s in sweeps),
-                     "sigma_tflops_last_sweep": sweeps[-1]["sigma_flops"] / sweeps[-1]["seconds"] / 1e12,
+                     "sigma_tflops_last_sweep": last["sigma_flops"] / last["seconds"] / 1e12,
                      "per_sweep": sweeps}
-        if prec == core.FP64 and args.warm_sweeps > 0:
+        if name == "fp64" and args.warm_sweeps > 0:
             warm = warm_compare(args, ctx, st)
         del st, mpo
         ctx.close()
+    e64 = res["fp64"]["energy"]
+    res["cold"] = {"abs_dE_split_vs_fp64": abs(res["split"]["energy"] - e64),
+                   "abs_dE_fp64_control_vs_fp64": (abs(res["fp64_control"]["energy"] - e64)
+                                                   if "fp64_control" in res else None),
+                   "seconds_per_sweep_fp64": res["fp64"]["seconds_last_sweep"],
+                   "seconds_per_sweep_split": res["split"]["seconds_last_sweep"],
+                   "speedup_last_sweep": res["fp64"]["seconds_last_sweep"] / res["split"]["seconds_last_sweep"],
+                   "speedup_total": res["fp64"]["seconds_total"] / res["split"]["seconds_total"]}
     if "split_all" in res:
-        res["split_all"]["abs_dE"] = abs(res["split_all"]["energy"] - res["fp64"]["energy"])
-        res["split_all"]["speedup_last_sweep"] = (res["fp64"]["seconds_last_sweep"] /
-                                                  res["split_all"]["seconds_last_sweep"])
+        res["split_all"]["abs_dE"] = abs(res["split_all"]["energy"] - e64)
     res["warm"] = warm
-    de = [abs(a["energy"] - b["energy"]) for a, b in zip(res["split"]["per_sweep"], res["fp64"]["per_sweep"])]
-    res["abs_dE"] = de[-1]
-    res["abs_dE_max_over_sweeps"] = max(de)
-    res["speedup_last_sweep"] = res["fp64"]["seconds_last_sweep"] / res["split"]["seconds_last_sweep"]
-    res["speedup_total"] = res["fp64"]["seconds_total"] / res["split"]["seconds_total"]
     return res
 
 
@@ -431,10 +456,10 @@ def measure_fp64_peak(torch) -> float:
     return 5 * 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
 
 
-def cpu_sigma_sample(wl, budget_s: float):
-    """Oracle sigma on the same bond (host cores), a bounded sample of the block tasks."""
-    import numpy as np
-
+def cpu_sigma_oracle(wl):
+    """The oracle's H_eff*psi on the same bond (host cores, NumPy BLAS threads): every
+    block task of both Gemm's, timed as one whole step.  Returns the baseline record and
+    the oracle's sigma blocks {tag: ndarray} for the parity check."""
     from oracle import dmrg as od
     from oracle import qsd as oq
 
@@ -445,30 +470,34 @@ def cpu_sigma_sample(wl, budget_s: float):
         return a
 
     mL, mR, psi = to_oracle(wl["mL"]), to_oracle(wl["mR"]), to_oracle(wl["psi"])
-    # sample: the sigma of a subset of psi blocks (the tasks writing those sigma blocks)
-    tags = sorted(psi.blocks)
-    rng = np.random.default_rng(0)
-    order = list(rng.permutation(len(tags)))
-    done_flops = 0.0
-    t_used = 0.0
-    nblk = 0
     cores = os.cpu_count() or 1
-    while order and t_used < budget_s:
-        sub = psi.empty_like()
-        take = order[:max(1, len(tags) // 16)]
-        order = order[len(take):]
-        for i in take:
-            sub.blocks[tags[i]] = psi.blocks[tags[i]]
-        tasks = []
-        t0 = time.perf_counter()
-        out = oq.QSDArray()
-        scr = od.compute_sigma_vector(mL, mR, sub, out, tasks)
-        t_used += time.perf_counter() - t0
-        nblk += len(take)
-        done_flops += sigma_task_flops(tasks, mL, mR, sub, scr)
-    return {"value": done_flops / t_used / 1e12 if t_used else 0.0, "unit": "TFLOP/s", "cores": cores,
-            "kind": "port", "sample": f"oracle sigma on {nblk}/{len(tags)} psi blocks of the same bond, "
-                                      f"{t_used:.1f} s, NumPy BLAS threads on {cores} cores"}
+    tasks = []
+    out = oq.QSDArray()
+    t0 = time.perf_counter()
+    scr = od.compute_sigma_vector(mL, mR, psi, out, tasks)
+    dt = time.perf_counter() - t0
+    fl = sigma_task_flops(tasks, mL, mR, psi, scr)
+    rec = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+           "sample": f"oracle (NumPy) H_eff*psi on all {len(psi.blocks)} psi blocks of the same bond, "
+                     f"one full step of {dt:.1f} s, NumPy BLAS threads on {cores} cores"}
+    return rec, out.blocks
+
+
+def sigma_vs_oracle(gpu_blocks, oracle_blocks) -> dict:
+    """Largest block-wise difference of the device FP64 sigma from the oracle's, relative
+    to the largest |sigma| element."""
+    import numpy as np
+
+    scale = max(float(np.abs(b).max()) for b in oracle_blocks.values() if b.size)
+    worst = 0.0
+    for t, b in oracle_blocks.items():
+        g = gpu_blocks.get(t)
+        if g is None:
+            worst = max(worst, float(np.abs(b).max()) / scale)
+        else:
+            worst = max(worst, float(np.abs(g - b).max()) / scale)
+    extra = [t for t in gpu_blocks if t not in oracle_blocks and np.abs(gpu_blocks[t]).max() > 0]
+    return {"max_rel_err": worst, "blocks": len(oracle_blocks), "extra_nonzero_blocks": len(extra)}
 
 
 def sigma_task_flops(tasks, mL, mR, psi, scr) -> float:
@@ -500,10 +529,8 @@ def run_reference(args, ws, rank):
     ctx = core.Context(0)
     wl = build_workload(args, ctx)
     samples = []
-    for _ in range(args.warmup):  # untimed: one psi-block chunk each (BLAS threads, page-in)
-        cpu_sigma_sample(wl, 1e-9)
     for _ in range(max(1, args.steps)):
-        s = cpu_sigma_sample(wl, args.cpu_seconds / max(1, args.steps))
+        s, _ = cpu_sigma_oracle(wl)
         samples.append(s["value"])
     v = sum(samples) / len(samples)
     out = {"impl": "reference", "metric": "H_eff*psi TFLOP/s (FP64-equivalent), n=20 QC, M=512, middle bond",
@@ -600,9 +627,16 @@ def main():
     bond = bond_compare(ctx, wl, args.M, args.tole) if args.bond_step else None
     # the sweep comparison and the CPU baseline belong to the one-GPU line; replicas
     # (N > 1) time H_eff*psi only
+    sections = {}
+    t_sec = time.perf_counter()
     sweep = sweep_compare(args, local) if not args.no_sweep and ws == 1 else None
+    sections["sweeps"] = time.perf_counter() - t_sec
+    t_sec = time.perf_counter()
     grad = gradient_bench(args, local) if args.gradient else None
+    sections["gradient"] = time.perf_counter() - t_sec
+    t_sec = time.perf_counter()
     scan_res = scan_bench(args, local) if args.scan else None
+    sections["scan"] = time.perf_counter() - t_sec
     out = None
     if rank == 0:
         achieved = fl_per_step / kt["sigma_kernels_s"] / 1e12
@@ -650,9 +684,17 @@ def main():
             "gradient": grad,
             "scan": scan_res,
             "clocks": clk.summary(),
+            "section_seconds": {k: round(v, 1) for k, v in sections.items()},
         }
         if not args.no_cpu_baseline and ws == 1:
-            out["cpu_baseline"] = cpu_sigma_sample(wl, args.cpu_seconds)
+            rec, oblocks = cpu_sigma_oracle(wl)
+            out["cpu_baseline"] = rec
+            # a fresh FP64 sigma (the timing loops above accumulate into their outputs)
+            core.set_precision(ctx, core.FP64)
+            s_par = psi.like()
+            core.compute_sigma_vector(ctx, mL, mR, psi, s_par)
+            core.set_precision(ctx, core.SPLIT_TF32 if args.precision == "split" else core.FP64)
+            out["parity"] = {"sigma_vs_oracle_c2": sigma_vs_oracle(s_par.to_dict()["blocks"], oblocks)}
         print(json.dumps(out), flush=True)
     barrier(ws)
 

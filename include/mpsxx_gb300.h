@@ -75,6 +75,14 @@ int mpsxx_context_get_precision(const mpsxx_context* ctx, int* precision);
  * tie_rtol < 0 restores the default, 1e-10. */
 int mpsxx_context_set_truncation(mpsxx_context* ctx, double tie_rtol);
 
+/* Split-precision diagonalize (MPSXX_SPLIT_TF32): the tensor-core Davidson runs until
+ * |r|^2 < (residual_floor * E)^2, the resolution of the inexact operator; then up to
+ * `rounds` continuations, each anchored by one FP64 H_eff*psi of the current vector,
+ * bring |r|^2 under the caller's tolerance (src/diagonalize.hpp:337-437 with the FP64
+ * operator).  Negative values restore the defaults, 1e-5 and 2 rounds.  No reference
+ * counterpart: the reference has one (FP64) operator. */
+int mpsxx_context_set_split_refinement(mpsxx_context* ctx, double residual_floor, int rounds);
+
 /* Kernel launches issued, FP64-equivalent sigma FLOPs and sigma calls so far. */
 int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* sigma_flops, int64_t* sigma_calls);
 

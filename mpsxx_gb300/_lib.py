@@ -25,6 +25,7 @@ SIGNATURES = {
     "mpsxx_context_sync": (C.c_int, [vp]),
     "mpsxx_context_counters": (C.c_int, [vp, c_i64_p, c_dbl_p, c_i64_p]),
     "mpsxx_context_set_truncation": (C.c_int, [vp, C.c_double]),
+    "mpsxx_context_set_split_refinement": (C.c_int, [vp, C.c_double, C.c_int]),
     "mpsxx_context_tuning": (C.c_int, [vp, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_context_set_sigma_schedule": (C.c_int, [vp, C.c_int64, C.c_int, C.c_int]),
     "mpsxx_context_set_svd_routes": (C.c_int, [vp, C.c_int, C.c_int]),

@@ -45,6 +45,11 @@ class Context:
         """Relative tie window at the truncation cutoff (< 0: the precision's default)."""
         check(lib().mpsxx_context_set_truncation(self.h, float(tie_rtol)))
 
+    def set_split_refinement(self, residual_floor: float = -1.0, rounds: int = -1):
+        """Split-precision diagonalize: tensor-core Davidson down to |r|^2 < (floor*E)^2,
+        then up to ``rounds`` FP64-anchored continuations (negative: defaults 1e-5, 2)."""
+        check(lib().mpsxx_context_set_split_refinement(self.h, float(residual_floor), int(rounds)))
+
     def set_sigma_schedule(self, w_budget_bytes: int = -1, target_tiles: int = 0, fp32_intermediate: bool = False):
         """Fix the split H_eff*psi schedule (w scratch budget, tile target, FP32 L*psi
         intermediate split on chip); budget < 0: autotune."""

@@ -18,8 +18,6 @@ namespace {
 
 constexpr int kMaxRitz = 10;
 constexpr int kSlotSigma = 10, kSlotRes = 20, kSlotDiag = 21, kSlotIn = 22, kSlotOut = 23, kSlots = 24;
-constexpr double kSplitFloor = 1.0e-5;  // relative resolution of the split operator (as the single path)
-constexpr int kRefineRounds = 2;
 
 struct Item {
   const DTensor *L, *R, *diag;
@@ -73,10 +71,10 @@ class Batch {
     if (ctx_.precision == kFP64) {
       davidson(all, tol, 0.0, 4, false, S, E);
     } else {
-      davidson(all, tol, kSplitFloor, 4, false, S, E);
+      davidson(all, tol, ctx_.split_floor, 4, false, S, E);
       for (int c = 0; c < N; ++c) S[c].energy_split = E[c];
       std::vector<int> todo = all;
-      for (int round = 0; round < kRefineRounds && !todo.empty(); ++round) {
+      for (int round = 0; round < ctx_.refine_rounds && !todo.empty(); ++round) {
         std::vector<DavidsonStats> R(N);
         davidson(todo, tol, 0.0, 1, true, R, E);
         std::vector<int> next;

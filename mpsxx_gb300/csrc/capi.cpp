@@ -123,6 +123,15 @@ int mpsxx_context_set_truncation(mpsxx_context* ctx, double tie_rtol) {
   });
 }
 
+int mpsxx_context_set_split_refinement(mpsxx_context* ctx, double residual_floor, int rounds) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    need(rounds <= 64, "mpsxx_context_set_split_refinement: at most 64 rounds");
+    ctx->ctx->split_floor = residual_floor >= 0.0 ? residual_floor : mpsxx::kSplitResidualFloorDefault;
+    ctx->ctx->refine_rounds = rounds >= 0 ? rounds : mpsxx::kRefineRoundsDefault;
+  });
+}
+
 int mpsxx_context_counters(const mpsxx_context* ctx, int64_t* launches, double* sigma_flops, int64_t* sigma_calls) {
   return guard([&] {
     need(ctx && ctx->ctx, "null context");

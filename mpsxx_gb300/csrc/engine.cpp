@@ -2240,13 +2240,6 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
   return eval;
 }
 
-// Relative resolution of the split-TF32 operator: |H_split psi - H psi| stays
-// below ~1e-5 |H psi| (measured a few 1e-6), so a residual under (1e-5 E)^2 is
-// as converged as that operator allows.
-constexpr double kSplitResidualFloor = 1.0e-5;
-// FP64-anchored refinement rounds of a split-precision diagonalisation
-constexpr int kRefineRounds = 2;
-
 double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTensor& diag, DTensor& wfnc, double tol,
                    DavidsonStats* stats) {
   DavidsonStats local;
@@ -2261,11 +2254,11 @@ double diagonalize(Context& ctx, const DTensor& L, const DTensor& R, const DTens
   // through the small correction components, at second order; with a start vector
   // already within the tolerance the accepted value is the FP64 Rayleigh quotient.
   // A continuation that ends unconverged (subspace full) is anchored once more.
-  const double e_split = davidson_run(ctx, L, R, diag, wfnc, tol, kSplitResidualFloor, 4, S);
+  const double e_split = davidson_run(ctx, L, R, diag, wfnc, tol, ctx.split_floor, 4, S);
   check_device_error(ctx);
   S.energy_split = e_split;
   double e = e_split;
-  for (int round = 0; round < kRefineRounds; ++round) {
+  for (int round = 0; round < ctx.refine_rounds; ++round) {
     DavidsonStats R1;
     e = davidson_run(ctx, L, R, diag, wfnc, tol, 0.0, 1, R1, /*anchor=*/true);
     check_device_error(ctx);

@@ -114,6 +114,12 @@ constexpr int kTargetCtas = 152 * 8;
 
 // plans kept per kind in a context before the cache is emptied
 constexpr size_t kMaxCachedPlans = 512;  // default of Context::max_plans
+// Relative resolution of the split-TF32 operator: |H_split psi - H psi| stays below
+// ~1e-5 |H psi| (measured a few 1e-6), so a residual under (1e-5 E)^2 is as converged
+// as that operator allows.
+constexpr double kSplitResidualFloorDefault = 1.0e-5;
+// FP64-anchored refinement rounds of a split-precision diagonalisation
+constexpr int kRefineRoundsDefault = 2;
 
 // GEMM plan into a C whose layout is `c` (block offsets).  C blocks may be
 // sub-blocks of a larger block when `cmap` is provided (fused merges).
@@ -307,6 +313,11 @@ struct Context {
   // eigensolver; < 0 selects the defaults
   int svd_jacobi_cols = -1;
   int svd_gram_max = -1;
+  // split-precision diagonalize: the tensor-core Davidson stops at |r|^2 <
+  // (split_floor * E)^2 (the operator's resolution); then up to refine_rounds
+  // FP64-anchored continuations bring |r|^2 under the tolerance
+  double split_floor = kSplitResidualFloorDefault;
+  int refine_rounds = kRefineRoundsDefault;
   // make_noise: the leading values of the noise sequence on the device (grown on demand)
   DevArray<double> noise_seq;
   // plan caches are shared with the planning threads of a batched step: lookups and

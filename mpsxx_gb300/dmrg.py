@@ -224,6 +224,7 @@ def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None, noise
         flops += stats["sigma_flops"]
         for k in ("t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "n_sigma_fp64"):
             times[k] = times.get(k, 0.0) + stats[k]
+        times["n_unconverged"] = times.get("n_unconverged", 0.0) + (0.0 if stats["converged"] else 1.0)
 
     for i in range(N - 1):
         e, env, nl, nr, stats = core.optimize_twosite_merged(ctx, True, st.mpo[i], st.mpo[i + 1], st.lenv[i],

@@ -1,0 +1,1 @@
+#include <boost/mpsxx_shim.hpp>

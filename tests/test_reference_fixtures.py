@@ -1,0 +1,232 @@
+"""The oracle, the product's host planner and the C++ port of the reference's CPU
+sigma against fixtures produced by the mpsxx reference itself (compiled from its
+sources with stand-in Boost headers and scipy's OpenBLAS, run through its own
+mpogen.x / dmrg.x; tests/golden/make_ref_fixtures.py).
+
+Fixtures (tests/golden/ref/):
+* runs.json: sweep and bond energies of C1 (Hubbard L=12, U=4, M=64, tole 1e-10),
+  a synthetic QC case (n=8, M=64) and the reference's FCIDUMP12 input (M=64);
+* tasks.npz: for every bond of the C1 and QC runs, the operand layouts and the
+  ST_Gemm_thread task lists of both sigma Gemm's and both renormalisation Gemm's;
+* bonds.npz: for six bonds, the dumped inputs of optimize_twosite_merged and the
+  reference's merged wavefunction, sigma, diagonal, truncated factors and
+  renormalised operator on them.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import ref_io
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REF = os.path.join(GOLD, "ref")
+
+
+def runs():
+    with open(os.path.join(REF, "runs.json")) as f:
+        return json.load(f)
+
+
+def npz(name):
+    return np.load(os.path.join(REF, name))
+
+
+def keys(z, suffix):
+    return sorted({k[: -len(suffix)] for k in z.files if k.endswith(suffix)})
+
+
+def oracle_tensor(d):
+    from oracle import from_site_dict
+
+    return from_site_dict(d)
+
+
+def rel_diff(a: dict, b: dict) -> float:
+    """max |a - b| over the union of blocks, relative to max |b|."""
+    scale = max([float(np.abs(x).max()) for x in b.values() if x.size] + [1e-300])
+    worst = 0.0
+    for t in set(a) | set(b):
+        x, y = a.get(t), b.get(t)
+        if x is None:
+            worst = max(worst, float(np.abs(y).max()) if y.size else 0.0)
+        elif y is None:
+            worst = max(worst, float(np.abs(x).max()) if x.size else 0.0)
+        else:
+            worst = max(worst, float(np.abs(x - y).max()) if x.size else 0.0)
+    return worst / scale
+
+
+def test_oracle_c1_sweeps_equal_the_reference():
+    """C1 through the oracle (tests/golden/hubbard12_u4_m64.json) against dmrg.x.
+    Bond energies: in sweep 1 several Davidson runs stop on the reference's iteration
+    cap (4 x 10), where the two summation orders leave different unconverged vectors
+    (observed up to 4.8e-8 Eh apart); that difference decays through sweep 2 (4.4e-10)
+    and sweeps 3-4 agree to 1e-12 (observed 7e-14).  Sweep energies (minimum over
+    bonds) agree to 1e-9 for sweep 1 and 1e-12 afterwards."""
+    ref = runs()["c1"]
+    with open(os.path.join(GOLD, "hubbard12_u4_m64.json")) as f:
+        orc = json.load(f)
+    assert len(ref["sweep_energies"]) == 4
+    assert abs(orc["sweeps"][0]["energy"] - ref["sweep_energies"][0]) < 1e-9
+    for k in range(1, 4):
+        assert abs(orc["sweeps"][k]["energy"] - ref["sweep_energies"][k]) < 1e-12
+    ob = [e for s in orc["sweeps"] for e in s["bond_energies"]]
+    assert len(ob) == len(ref["bond_energies"]) == 88
+    d = [abs(a - b) for a, b in zip(ob, ref["bond_energies"])]
+    assert max(d[:22]) < 1e-7 and max(d[22:44]) < 1e-9 and max(d[44:]) < 1e-12
+
+
+def _bond_inputs(z, key):
+    return {t: oracle_tensor(ref_io.unpack_tensor(z, f"{key}/{t}"))
+            for t in ("lmpo", "rmpo", "lopr", "ropr", "lwfn", "rwfn")}
+
+
+BOND_KEYS = keys(np.load(os.path.join(REF, "bonds.npz")), "/meta")
+
+
+@pytest.mark.parametrize("key", BOND_KEYS)
+def test_oracle_bond_operations_equal_the_reference(key):
+    """From the reference's own bond inputs: the oracle's merged wavefunction, sigma,
+    diagonal and renormalised operator within 1e-13 of the reference's; the truncated
+    factors keep the same sectors and dimensions and their product U*sV^T matches."""
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+
+    z = npz("bonds.npz")
+    forward, M = bool(z[f"{key}/meta"][0]), int(z[f"{key}/meta"][1])
+    b = _bond_inputs(z, key)
+    mL = od.compute_merged_operator(True, b["lmpo"], b["lopr"])
+    mR = od.compute_merged_operator(False, b["rmpo"], b["ropr"])
+    ql, qr = od.wave_merge_infos(b["lmpo"], b["rmpo"], b["lopr"], b["ropr"])
+    twf = oq.QSDArray()
+    oq.gemm("N", "N", 1.0, b["lwfn"], b["rwfn"], 1.0, twf, nc=4)
+    psi = oq.merge_cols(oq.merge_rows(ql, twf), qr)
+    ref = {t: ref_io.unpack_tensor(z, f"{key}/{t}") for t in ("psi", "sigma", "diag", "lmat", "rmat", "env")}
+    assert rel_diff(psi.blocks, ref["psi"]["blocks"]) < 1e-14
+    sig = oq.QSDArray()
+    od.compute_sigma_vector(mL, mR, psi, sig)
+    assert rel_diff(sig.blocks, ref["sigma"]["blocks"]) < 1e-13
+    diag = oq.QSDArray(psi.q, psi.qshape, psi.dshape)
+    od.compute_diagonal_elements(mL, mR, diag)
+    assert rel_diff(diag.blocks, ref["diag"]["blocks"]) < 1e-13
+    U, V, _ = od.canonicalize_merged(forward, psi.copy(), M)
+    rl, rr = oracle_tensor(ref["lmat"]), oracle_tensor(ref["rmat"])
+    assert U.qshape == rl.qshape and U.dshape == rl.dshape and V.dshape == rr.dshape
+    prod, rprod = oq.QSDArray(), oq.QSDArray()
+    oq.gemm("N", "N", 1.0, U, V, 1.0, prod, nc=2)
+    oq.gemm("N", "N", 1.0, rl, rr, 1.0, rprod, nc=2)
+    assert rel_diff(prod.blocks, rprod.blocks) < 1e-12
+    # the renormalised operator with the reference's own kept factor (its gauge)
+    env = od.renormalize_merged(forward, mL if forward else mR, rl if forward else rr, rl if forward else rr)
+    assert rel_diff(env.blocks, ref["env"]["blocks"]) < 1e-13
+
+
+TASK_KEYS = keys(np.load(os.path.join(REF, "tasks.npz")), "/forward")
+
+
+def _layout(z, key, name):
+    return ref_io.unpack_tensor(z, f"{key}/{name}")
+
+
+def _host(d):
+    from mpsxx_gb300 import core
+
+    return core.Tensor.create(None, tuple(d["q"]), d["qshape"], d["dshape"], sorted(d["blocks"]))
+
+
+def _scr_layout(a, b, ta, tb, nc, c_tags):
+    """The intermediate of a Gemm: quantum shape by gemm_contract_qshape, blocks = the
+    result tags the reference's task list wrote."""
+    from oracle import qsd as oq
+
+    qc, cq, cd, _ = oq.gemm_contract_qshape(ta, tb, oracle_tensor(a), oracle_tensor(b), nc)
+    t = oq.QSDArray(qc, cq, cd)
+    return {"q": qc, "qshape": cq, "dshape": cd, "blocks": {c: np.zeros(t.block_dims(t.index(c))) for c in c_tags}}
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from mpsxx_gb300._lib import lib as _lib
+
+    return _lib()
+
+
+def test_planner_task_lists_equal_the_reference(lib):
+    """The product's host enumeration (mpsxx_gemm_tasks) against the task lists the
+    reference's ST_Gemm_thread produced, for both sigma Gemm's and both
+    renormalisation Gemm's at every bond of the C1 and QC runs: bit-exact."""
+    from mpsxx_gb300 import core
+
+    z = npz("tasks.npz")
+    assert len(TASK_KEYS) == 88 + 42
+    for key in TASK_KEYS:
+        fwd = bool(z[f"{key}/forward"])
+        mL, mR, psi = (_layout(z, key, t) for t in ("mL", "mR", "psi"))
+        u = _layout(z, key, "lmat" if fwd else "rmat")
+        t1 = ref_io.unpack_tasks(z, f"{key}/LxPsi")
+        assert core.gemm_tasks(0, 0, _host(mL), _host(psi), 3) == t1, key
+        scr = _scr_layout(mL, psi, "N", "N", 3, [c for c, _ in t1])
+        assert core.gemm_tasks(0, 1, _host(scr), _host(mR), 2) == ref_io.unpack_tasks(z, f"{key}/ScrxR"), key
+        bra = {"q": tuple(-x for x in u["q"]), "qshape": [[(-p, -s) for p, s in x] for x in u["qshape"]],
+               "dshape": u["dshape"], "blocks": u["blocks"]}
+        mop = mL if fwd else mR
+        r1 = ref_io.unpack_tasks(z, f"{key}/BraxOp")
+        assert core.gemm_tasks(1 if fwd else 0, 0, _host(bra), _host(mop), 3) == r1, key
+        ta = "T" if fwd else "N"
+        rscr = _scr_layout(bra, mop, ta, "N", 3, [c for c, _ in r1])
+        r2 = ref_io.unpack_tasks(z, f"{key}/ScrxKet")
+        assert core.gemm_tasks(0, 0 if fwd else 1, _host(rscr), _host(u), 3) == r2, key
+
+
+def test_oracle_task_lists_equal_the_reference():
+    """The oracle's restatement of ST_Gemm_thread against the reference's lists (sigma,
+    both stages) on every dumped bond."""
+    from oracle import qsd as oq
+
+    z = npz("tasks.npz")
+    for key in TASK_KEYS:
+        mL, mR, psi = (oracle_tensor(_layout(z, key, t)) for t in ("mL", "mR", "psi"))
+        qc, cq, cd, K = oq.gemm_contract_qshape("N", "N", mL, psi, 3)
+        t1 = oq.st_gemm_tasks("N", "N", mL, psi, oq.QSDArray(qc, cq, cd), K)
+        assert t1 == ref_io.unpack_tasks(z, f"{key}/LxPsi"), key
+        scr = oracle_tensor(_scr_layout(_layout(z, key, "mL"), _layout(z, key, "psi"), "N", "N", 3,
+                                        [c for c, _ in t1]))
+        qc, cq, cd, K = oq.gemm_contract_qshape("N", "T", scr, mR, 2)
+        t2 = oq.st_gemm_tasks("N", "T", scr, mR, oq.QSDArray(qc, cq, cd), K)
+        assert t2 == ref_io.unpack_tasks(z, f"{key}/ScrxR"), key
+
+
+@pytest.mark.parametrize("key", BOND_KEYS)
+def test_cpu_port_sigma_equals_the_reference_bitwise(key):
+    """The C++ port timed as the reference's CPU path (oracle/cpu) computes the
+    reference's sigma bit for bit on the reference's merged operators."""
+    from oracle import cpu
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+
+    z = npz("bonds.npz")
+    b = _bond_inputs(z, key)
+    mL = od.compute_merged_operator(True, b["lmpo"], b["lopr"])
+    mR = od.compute_merged_operator(False, b["rmpo"], b["ropr"])
+    d = lambda t: {"q": t.q, "qshape": t.qshape, "dshape": t.dshape, "blocks": t.blocks}  # noqa: E731
+    psi = ref_io.unpack_tensor(z, f"{key}/psi")
+    blocks, flops, _ = cpu.sigma(cpu.Operands(d(mL), d(mR), psi), threads=2)
+    ref = ref_io.unpack_tensor(z, f"{key}/sigma")["blocks"]
+    for t, v in ref.items():
+        assert np.array_equal(blocks[t], v), (key, t)
+    assert all(not np.any(v) for t, v in blocks.items() if t not in ref)
+    assert flops > 0
+
+
+def test_qc8_and_fcidump12_reference_runs_are_recorded():
+    """Energies of the reference's own runs on the synthetic n=8 QC Hamiltonian and on
+    its FCIDUMP12 test input (M=64): the oracle's values are compared in
+    test_oracle_runs_follow_the_reference; here the record itself is checked."""
+    r = runs()
+    assert len(r["qc8"]["sweep_energies"]) == 3 and len(r["fcidump12"]["sweep_energies"]) == 2
+    assert r["fcidump12"]["sweep_energies"][1] < -50.0
