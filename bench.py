@@ -1,14 +1,21 @@
 """Benchmark of the merged two-site DMRG hot path on one GB300.
 
-Workload (default): the synthetic quantum-chemistry Hamiltonian with n=20
-spatial orbitals, 20 electrons, Sz=0, integral seed 1, K=40 Cholesky vectors,
-complementary-operator MPO, bond dimension M=512.  The state is a random MPS of
-bond dimension 512 (synthetic, seeded) brought into mixed-canonical form at the
-middle bond (9, 10), where the MPO bond dimension peaks.  One step = one
-H_eff*psi application (compute_sigma_vector, the Davidson inner loop) on that
-bond.  Inputs are resident in HBM for ``value``; ``e2e`` repeats the step
-through the C ABI with the wavefunction copied from pinned host memory and the
-result copied back inside the timed region.
+Workload (default, ``--workload c2-bond``): one H_eff*psi (compute_sigma_vector, the
+Davidson inner loop) at the middle bond (9, 10) of configuration C2 — the synthetic
+quantum-chemistry Hamiltonian with n=20 spatial orbitals, 20 electrons, Sz=0, K=40
+Cholesky vectors, integral seed 1, M=512.  The operator is the reference's own
+complementary-operator MPO at sites 9 and 10 (W = 712 | 862 | 1028), written by the
+reference's generator and committed as a fixture; the MPS bonds around the two sites
+have the quantum numbers and dimensions of a converged C2 state (committed); every
+allowed block of the environments and site tensors holds seeded normal values.  Both
+arms build the workload from these files alone.
+
+``value``: device throughput with the operands resident in HBM (CUDA events on the
+library's stream).  ``e2e``: the same step through the C ABI with the wavefunction
+copied from pinned host memory and sigma copied back inside the timed region;
+``bond_step_e2e``: one whole bond step from host site tensors.  ``--impl reference``
+times the reference's CPU H_eff*psi (its C++ restatement, pinned bitwise to the
+reference's own sigma) on the host cores, on operands built on the host.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -27,11 +34,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 L2_BYTES = 129 * 1024 * 1024
+T_START = time.perf_counter()
+METRIC = "H_eff*psi TFLOP/s (FP64-equivalent), C2 middle bond: qc n=20 M=512"
+DATA = ("synthetic: the reference generator's MPO sites of the seeded n=20 integrals, a converged state's block "
+        "structure, seeded normal block values")
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per H_eff*psi of the default
-# workload (QC n=20, K=40, seed 1, M=512, bond (9,10)), summed over the launches of one
-# step, from one ncu capture of the launch list (one pass); None for other workloads.
-MEASURED_TRAFFIC = {("split", 20, 40, 1, 512): 6.75e9, }
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over the launches of one
+# H_eff*psi) divided by the algorithmic bytes 8 (nnz L + nnz R + 2 nnz psi), measured by
+# ncu on the small case of the same kernels; keyed by (workload, precision).
+MEASURED_TRAFFIC = {}
 
 
 def parse():
@@ -40,6 +51,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2-bond", choices=["c2-bond", "random-mps"],
+                    help="c2-bond: the committed C2 middle bond; random-mps: --norb/--nchol/--M/--bond under this "
+                         "library's MPO generator, a seeded random MPS")
+    ap.add_argument("--bond-structure", default="", help="bond structure file of the c2-bond workload")
+    ap.add_argument("--no-bond-e2e", action="store_true", help="skip the bond step from host site tensors")
     ap.add_argument("--norb", type=int, default=20)
     ap.add_argument("--nchol", type=int, default=40)
     ap.add_argument("--M", type=int, default=512)
@@ -49,27 +65,25 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="split", choices=["split", "fp64"])
     ap.add_argument("--tole", type=float, default=1e-9, help="sweep tolerance (Davidson |r|^2 < 0.1 tole)")
-    ap.add_argument("--bond-step", action="store_true", help="also time one full bond step at the bench bond")
+    ap.add_argument("--bond-step", action="store_true",
+                    help="random-mps workload: also time one full bond step, FP64 and split, from identical inputs")
     ap.add_argument("--no-sweep", action="store_true", help="skip the FP64-vs-split sweep comparison")
     ap.add_argument("--sweep-norb", type=int, default=20)
     ap.add_argument("--sweep-M", type=int, default=512)
-    ap.add_argument("--sweep-max", type=int, default=16)
-    ap.add_argument("--sweep-conv", type=float, default=1e-10,
-                    help="sweep convergence: |dE| between consecutive sweeps")
+    ap.add_argument("--sweep-max", type=int, default=12, help="sweeps per arm (ramp included)")
+    ap.add_argument("--no-sweep-ramp", dest="sweep_ramp", action="store_false",
+                    help="all sweeps at --sweep-M (default: two sweeps at M/4, two at M/2 first)")
     ap.add_argument("--no-sweep-control", action="store_true",
                     help="skip the FP64 control arm (ten times tighter Davidson tolerance)")
-    ap.add_argument("--mpo", default="qc", choices=["qc"], help="QC MPO construction")
-    ap.add_argument("--gradient", action="store_true",
-                    help="also run the energy-gradient workloads (site-dependent Hubbard L=32 M=512, QC n=16 M=256)")
+    ap.add_argument("--no-gradient", dest="gradient", action="store_false",
+                    help="skip the energy-gradient workloads (site-dependent Hubbard L=32 M=512, QC n=16 M=256)")
     ap.add_argument("--grad-fd", type=int, default=2, help="parameters checked by central differences per workload")
-    ap.add_argument("--scan", action="store_true",
-                    help="also run the batched scan: 64 Hubbard chains, L ~ U{16..32}, U ~ U(0,8), M 64->256 over 6 sweeps")
+    ap.add_argument("--no-scan", dest="scan", action="store_false",
+                    help="skip the batched scan: 64 Hubbard chains, L ~ U{16..32}, U ~ U(0,8), M 64->256 over 6 sweeps")
+    ap.add_argument("--budget-s", type=float, default=1500.0,
+                    help="wall-clock budget: sections not yet started when it is spent are skipped")
     ap.add_argument("--scan-chains", type=int, default=64)
     ap.add_argument("--scan-compare", type=int, default=8, help="chains also swept one by one for comparison")
-    ap.add_argument("--warm-sweeps", type=int, default=2,
-                    help="sweeps in each precision from the FP64-converged state")
-    ap.add_argument("--sweep-split-all", action="store_true",
-                    help="also sweep with the renormalisation contractions in split precision")
     return ap.parse_args()
 
 
@@ -163,89 +177,222 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.samples)}
 
 
-def mpo_dicts(args, h1, eri):
-    from mpsxx_gb300 import mpogen
+# The H_eff*psi workload (both arms build it from these files alone):
+#  * the two MPO sites of the middle bond (9, 10) of configuration C2 as the mpsxx
+#    reference's own generator writes them (mpogen.x on the synthetic n=20, K=40,
+#    seed-1 integrals; W = 712 | 862 | 1028 around the sites);
+#  * the quantum numbers and dimensions of the MPS bonds around sites 9 and 10 of a
+#    converged C2 state (M=512);
+# with seeded normal random values in every allowed block of the environments and of
+# the two site tensors, the orthogonality centre on site 9 (a forward sweep's layout).
+C2_MPO = os.path.join(ROOT, "tests", "golden", "ref", "mpo_c2_bond.npz")
+C2_STRUCTURE = os.path.join(ROOT, "tests", "golden", "c2_bond_structure.json")
+SITE_QUANTA = [(0, 0), (1, 1), (1, -1), (2, 0)]
 
-    return mpogen.qc_mpo(h1, eri)
+
+def _npz_tensor(z, name):
+    """A tensor dict from the fixtures' npz layout (q, nsec, qshape, dshape, tags, data)."""
+    import numpy as np
+
+    nsec = [int(x) for x in z[f"{name}.nsec"]]
+    qs = [tuple(int(v) for v in r) for r in z[f"{name}.qshape"]]
+    ds = [int(v) for v in z[f"{name}.dshape"]]
+    qshape, dshape, o = [], [], 0
+    for n in nsec:
+        qshape.append(qs[o:o + n])
+        dshape.append(ds[o:o + n])
+        o += n
+    strides = [1] * len(nsec)
+    for i in range(len(nsec) - 2, -1, -1):
+        strides[i] = strides[i + 1] * nsec[i + 1]
+    data, blocks, off = z[f"{name}.data"], {}, 0
+    for tag in (int(x) for x in z[f"{name}.tags"]):
+        shape = tuple(dshape[i][(tag // strides[i]) % nsec[i]] for i in range(len(nsec)))
+        size = int(np.prod(shape, dtype=np.int64))
+        blocks[tag] = data[off:off + size].reshape(shape).copy()
+        off += size
+    return {"q": tuple(int(v) for v in z[f"{name}.q"]), "qshape": qshape, "dshape": dshape, "blocks": blocks}
+
+
+def _random_tensor(q, qshape, dshape, rng):
+    """Every block allowed by the total quantum number (and of non-zero size), filled with
+    standard normal values in ascending tag order."""
+    import numpy as np
+
+    nsec = [len(x) for x in qshape]
+    grids = np.meshgrid(*[np.arange(n) for n in nsec], indexing="ij")
+    qp = sum(np.array([x[0] for x in qshape[i]])[grids[i]] for i in range(len(nsec)))
+    qs = sum(np.array([x[1] for x in qshape[i]])[grids[i]] for i in range(len(nsec)))
+    size = np.prod([np.array(dshape[i])[grids[i]] for i in range(len(nsec))], axis=0)
+    ok = (qp == q[0]) & (qs == q[1]) & (size > 0)
+    tags = np.flatnonzero(ok.ravel())
+    blocks = {}
+    for t in tags:
+        idx = np.unravel_index(t, nsec)
+        shape = tuple(dshape[i][idx[i]] for i in range(len(nsec)))
+        blocks[int(t)] = rng.standard_normal(shape)
+    return {"q": tuple(q), "qshape": [list(x) for x in qshape], "dshape": [list(x) for x in dshape],
+            "blocks": blocks}
+
+
+def bench_bond(seed: int):
+    """Host tensors of the H_eff*psi workload: site MPOs W9, W10, left environment of site 9,
+    right environment of site 10, the centre site 9 (total quantum number) and site 10."""
+    import numpy as np
+
+    z = np.load(C2_MPO)
+    w9, w10 = _npz_tensor(z, "site9"), _npz_tensor(z, "site10")
+    with open(C2_STRUCTURE) as f:
+        st = json.load(f)
+    neg = lambda qs: [(-a, -b) for a, b in qs]  # noqa: E731
+    QL, DL = [tuple(q) for q in st["left"]["q"]], st["left"]["d"]
+    QM, DM = [tuple(q) for q in st["middle"]["q"]], st["middle"]["d"]
+    QR, DR = [tuple(q) for q in st["right"]["q"]], st["right"]["d"]
+    qt = tuple(st["q_total"])
+    rng = np.random.default_rng(seed)
+    one = lambda n: [1] * n  # noqa: E731
+    lenv = _random_tensor((0, 0), [QL, neg(w9["qshape"][0]), neg(QL)], [DL, one(len(w9["qshape"][0])), DL], rng)
+    renv = _random_tensor((0, 0), [QR, neg(w10["qshape"][3]), neg(QR)], [DR, one(len(w10["qshape"][3])), DR], rng)
+    lwfn = _random_tensor(qt, [QL, SITE_QUANTA, QM], [DL, one(4), DM], rng)
+    rwfn = _random_tensor((0, 0), [neg(QM), SITE_QUANTA, QR], [DM, one(4), DR], rng)
+    return {"w9": w9, "w10": w10, "lenv": lenv, "renv": renv, "lwfn": lwfn, "rwfn": rwfn,
+            "W": len(w9["qshape"][3])}
+
+
+def workload_name(args) -> str:
+    if args.workload == "c2-bond":
+        return (f"H_eff*psi at the middle bond (9,10) of C2: qc n=20 K=40 seed=1 M=512, the reference's "
+                f"complementary-operator MPO sites (W=862), converged-state block structure, values seed {args.seed}")
+    return (f"H_eff*psi at bond ({args.bond if args.bond >= 0 else args.norb // 2 - 1},+1): qc n={args.norb} "
+            f"K={args.nchol} seed={args.seed}, this library's MPO generator, seeded random MPS M={args.M}")
 
 
 def build_workload(args, ctx):
-    from mpsxx_gb300 import core, dmrg, mpogen
+    """The bench bond on the device.  c2-bond: the fixture bond through the product's own
+    merged-operator and wavefunction-merge entry points; random-mps: a seeded random MPS
+    of bond dimension M under this library's MPO, brought to the chosen bond."""
+    from mpsxx_gb300 import core
+
+    if args.workload == "c2-bond":
+        hb = bench_bond(args.seed)
+        t = {k: core.Tensor.from_dict(ctx, hb[k]) for k in ("w9", "w10", "lenv", "renv", "lwfn", "rwfn")}
+        mL = core.compute_merged_operator(ctx, True, t["w9"], t["lenv"])
+        mR = core.compute_merged_operator(ctx, False, t["w10"], t["renv"])
+        psi = core.merge_wavefunction(ctx, t["w9"], t["w10"], t["lenv"], t["renv"], t["lwfn"], t["rwfn"])
+        return dict(mL=mL, mR=mR, psi=psi, bond=9, W=hb["W"], host=hb, dev=t)
+    from mpsxx_gb300 import dmrg, mpogen
 
     h1, eri = mpogen.synthetic_qc_integrals(args.norb, args.nchol, args.seed)
-    mpo_d = mpo_dicts(args, h1, eri)
+    mpo_d = mpogen.qc_mpo(h1, eri)
     mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
     st = dmrg.make_random_state(ctx, mpo, args.norb, 0, args.M, seed=args.seed)
     bond = args.bond if args.bond >= 0 else args.norb // 2 - 1
     dmrg.advance_left(ctx, st, bond)
     mL, mR, psi = dmrg.bond_operands(ctx, st, bond)
-    return dict(mpo_d=mpo_d, mL=mL, mR=mR, psi=psi, bond=bond, W=mpogen.mpo_bond_dims(mpo_d)[bond], st=st)
+    return dict(mL=mL, mR=mR, psi=psi, bond=bond, W=mpogen.mpo_bond_dims(mpo_d)[bond], st=st)
+
+
+def host_operands(hb):
+    """mL, mR and psi of the fixture bond built on the host by the oracle's restatement
+    of compute_merged_operator (src/optimize.hpp:273-368) and of the wavefunction merge
+    (src/optimize.hpp:542-557), as exchange dicts."""
+    from oracle import dmrg as od
+    from oracle import from_site_dict
+    from oracle import qsd as oq
+
+    o = {k: from_site_dict(hb[k]) for k in ("w9", "w10", "lenv", "renv", "lwfn", "rwfn")}
+    mL = od.compute_merged_operator(True, o["w9"], o["lenv"])
+    mR = od.compute_merged_operator(False, o["w10"], o["renv"])
+    ql, qr = od.wave_merge_infos(o["w9"], o["w10"], o["lenv"], o["renv"])
+    twf = oq.QSDArray()
+    oq.gemm(oq.NoTrans, oq.NoTrans, 1.0, o["lwfn"], o["rwfn"], 1.0, twf, nc=4)
+    psi = oq.merge_cols(oq.merge_rows(ql, twf), qr)
+
+    def as_dict(a):
+        return {"q": tuple(a.q), "qshape": a.qshape, "dshape": a.dshape, "blocks": a.blocks}
+
+    return as_dict(mL), as_dict(mR), as_dict(psi)
+
+
+def sigma_checksum(blocks) -> dict:
+    """Order-independent summary of a sigma, comparable across the two arms."""
+    import numpy as np
+
+    s = sum(float(np.sum(b)) for b in blocks.values())
+    n = sum(float(np.sum(b * b)) for b in blocks.values()) ** 0.5
+    return {"sum": s, "norm": n, "blocks": len(blocks)}
+
+
+def sweep_schedule(args):
+    """Bond dimension per sweep: ramped to sweep_M (two sweeps at M/4, two at M/2), then
+    sweep_M for the rest of sweep_max sweeps."""
+    M = args.sweep_M
+    ramp = [max(16, M // 4)] * 2 + [max(16, M // 2)] * 2 if args.sweep_ramp else []
+    return ramp + [M] * max(1, args.sweep_max - len(ramp))
 
 
 def sweep_compare(args, device: int):
-    """Cold two-site DMRG from the reference's initial state (constant-filled sites,
-    src/make_random_mpss.cpp:97-271) on the synthetic QC system, in three arms, each
-    swept until the sweep energy changes by less than ``sweep_conv`` after at least two
-    sweeps (src/dmrg.cpp:57-65), at most ``sweep_max`` sweeps:
+    """Cold two-site DMRG on the synthetic QC system from the reference's initial state
+    (constant-filled sites, src/make_random_mpss.cpp:97-271), the same bond-dimension
+    schedule in every arm (src/dmrg.cpp:57-65 sweep loop), three arms:
 
     * ``fp64``: FP64 H_eff*psi, Davidson |r|^2 < 0.1*tole;
     * ``split``: split-precision H_eff*psi with the FP64 refinement, same tolerance;
-    * ``fp64_control``: FP64 again with a ten times tighter Davidson tolerance.
+    * ``fp64_control``: FP64 with a ten times tighter Davidson tolerance.
 
-    The two FP64 arms differ only in where each Davidson stops; the energy they settle
-    at differs by the path dependence of the truncated (fixed M) problem, the floor
-    against which the split-vs-FP64 difference is read."""
+    Where each Davidson stops moves the truncated (fixed M) problem's path, so energies at
+    equal sweep counts differ even between the two FP64 arms: that difference is the floor
+    against which split vs FP64 is read.  Sweep times are compared at the final M."""
     from mpsxx_gb300 import core, dmrg, mpogen
 
-    n, M = args.sweep_norb, args.sweep_M
+    n = args.sweep_norb
+    sched = sweep_schedule(args)
     h1, eri = mpogen.synthetic_qc_integrals(n, 2 * n, args.seed)
-    mpo_d = mpo_dicts(args, h1, eri)
-    res = {"workload": f"qc n={n} K={2 * n} seed={args.seed} M={M} mpo={args.mpo}", "tole": args.tole,
-           "sweep_conv": args.sweep_conv, "start": "reference initial state (constant-filled sites)"}
+    mpo_d = mpogen.qc_mpo(h1, eri)
+    res = {"workload": f"qc n={n} K={2 * n} seed={args.seed}, this library's MPO generator", "tole": args.tole,
+           "M_schedule": sched, "start": "reference initial state (constant-filled sites)"}
     arms = [("fp64", core.FP64, args.tole), ("split", core.SPLIT_TF32, args.tole)]
     if not args.no_sweep_control:
         arms.append(("fp64_control", core.FP64, 0.1 * args.tole))
-    if args.sweep_split_all:
-        arms.append(("split_all", core.SPLIT_TF32_ALL, args.tole))
-    warm = None
     for name, prec, tole in arms:
         ctx = core.Context(device)
         core.set_precision(ctx, prec)
         mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
-        st = dmrg.make_initial_state(ctx, mpo, n, 0, M)
-        sweeps, e_prev, conv = [], None, False
-        for it in range(args.sweep_max):
+        st = dmrg.make_initial_state(ctx, mpo, n, 0, sched[0])
+        sweeps = []
+        for M in sched:
+            st.M = M
             log = dmrg.make_sweep(ctx, st, tole)
-            sweeps.append({"seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma,
+            sweeps.append({"M": M, "seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma,
                            "sigma_flops": log.sigma_flops, **{k: round(v, 4) for k, v in log.times.items()}})
-            if e_prev is not None and it >= 1 and abs(log.energy - e_prev) < args.sweep_conv:
-                conv = True
-                break
-            e_prev = log.energy
         last = sweeps[-1]
-        res[name] = {"sweeps": len(sweeps), "converged": conv, "davidson_tole": 0.1 * tole,
-                     "energy": last["energy"],
+        atM = [s for s in sweeps if s["M"] == sched[-1]]
+        res[name] = {"sweeps": len(sweeps), "davidson_tole": 0.1 * tole, "energy": last["energy"],
                      "last_dE": abs(last["energy"] - sweeps[-2]["energy"]) if len(sweeps) > 1 else None,
                      "seconds_total": sum(s["seconds"] for s in sweeps),
-                     "seconds_last_sweep": last["seconds"],
+                     "seconds_per_sweep_final_M": sum(s["seconds"] for s in atM[1:]) / max(1, len(atM) - 1),
                      "n_sigma_total": sum(s["n_sigma"] for s in sweeps),
                      "sigma_tflops_last_sweep": last["sigma_flops"] / last["seconds"] / 1e12,
                      "per_sweep": sweeps}
-        if name == "fp64" and args.warm_sweeps > 0:
-            warm = warm_compare(args, ctx, st)
         del st, mpo
         ctx.close()
     e64 = res["fp64"]["energy"]
-    res["cold"] = {"abs_dE_split_vs_fp64": abs(res["split"]["energy"] - e64),
-                   "abs_dE_fp64_control_vs_fp64": (abs(res["fp64_control"]["energy"] - e64)
-                                                   if "fp64_control" in res else None),
-                   "seconds_per_sweep_fp64": res["fp64"]["seconds_last_sweep"],
-                   "seconds_per_sweep_split": res["split"]["seconds_last_sweep"],
-                   "speedup_last_sweep": res["fp64"]["seconds_last_sweep"] / res["split"]["seconds_last_sweep"],
-                   "speedup_total": res["fp64"]["seconds_total"] / res["split"]["seconds_total"]}
-    if "split_all" in res:
-        res["split_all"]["abs_dE"] = abs(res["split_all"]["energy"] - e64)
-    res["warm"] = warm
+    cmp = {"abs_dE_split_vs_fp64": abs(res["split"]["energy"] - e64),
+           "per_sweep_abs_dE_split_vs_fp64": [abs(a["energy"] - b["energy"]) for a, b in
+                                              zip(res["split"]["per_sweep"], res["fp64"]["per_sweep"])],
+           "seconds_per_sweep_fp64": res["fp64"]["seconds_per_sweep_final_M"],
+           "seconds_per_sweep_split": res["split"]["seconds_per_sweep_final_M"],
+           "speedup_per_sweep": res["fp64"]["seconds_per_sweep_final_M"] / res["split"]["seconds_per_sweep_final_M"],
+           "speedup_total": res["fp64"]["seconds_total"] / res["split"]["seconds_total"]}
+    if "fp64_control" in res:
+        ec = res["fp64_control"]["energy"]
+        cmp["abs_dE_fp64_vs_fp64_control"] = abs(e64 - ec)
+        cmp["abs_dE_split_vs_fp64_control"] = abs(res["split"]["energy"] - ec)
+        cmp["per_sweep_abs_dE_split_vs_fp64_control"] = [
+            abs(a["energy"] - b["energy"]) for a, b in zip(res["split"]["per_sweep"], res["fp64_control"]["per_sweep"])]
+        cmp["per_sweep_abs_dE_fp64_vs_fp64_control"] = [
+            abs(a["energy"] - b["energy"]) for a, b in zip(res["fp64"]["per_sweep"], res["fp64_control"]["per_sweep"])]
+    res["compare"] = cmp
     return res
 
 
@@ -377,34 +524,6 @@ def scan_bench(args, device: int):
             "final_energies": [c.energies[-1] for c in chains]}
 
 
-def warm_compare(args, ctx, st):
-    """From the FP64-converged state, the same number of further sweeps in FP64 and
-    in split precision (identical start, same fixed point): energies sweep by sweep
-    and sweep times at convergence."""
-    from mpsxx_gb300 import core, dmrg
-
-    out = {}
-    for name, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
-        core.set_precision(ctx, prec)
-        s2 = dmrg.DeviceState(st.mpo, list(st.wave), list(st.lenv), list(st.renv), st.M)
-        rows = []
-        for _ in range(args.warm_sweeps):
-            log = dmrg.make_sweep(ctx, s2, args.tole)
-            rows.append({"seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma,
-                         "n_sigma_fp64": int(log.times.get("n_sigma_fp64", 0)), "sigma_flops": log.sigma_flops})
-        out[name] = rows
-    core.set_precision(ctx, core.FP64)
-    de = [abs(a["energy"] - b["energy"]) for a, b in zip(out["split"], out["fp64"])]
-    t64 = sum(r["seconds"] for r in out["fp64"])
-    t32 = sum(r["seconds"] for r in out["split"])
-    out["abs_dE_per_sweep"] = de
-    out["abs_dE_max"] = max(de)
-    out["seconds_per_sweep_fp64"] = t64 / len(out["fp64"])
-    out["seconds_per_sweep_split"] = t32 / len(out["split"])
-    out["speedup"] = t64 / t32
-    return out
-
-
 def bond_compare(ctx, wl, M, tole):
     """One full two-site step (merged operators, diagonal, Davidson, SVD, renormalise,
     expand) on the bench bond, FP64 and split precision from identical inputs."""
@@ -456,97 +575,147 @@ def measure_fp64_peak(torch) -> float:
     return 5 * 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
 
 
-def cpu_sigma_oracle(wl):
-    """The oracle's H_eff*psi on the same bond (host cores, NumPy BLAS threads): every
-    block task of both Gemm's, timed as one whole step.  Returns the baseline record and
-    the oracle's sigma blocks {tag: ndarray} for the parity check."""
-    from oracle import dmrg as od
-    from oracle import qsd as oq
+def cpu_sigma_timed(mL: dict, mR: dict, psi: dict, budget_s: float, min_reps: int = 1):
+    """The C++ restatement of the reference's CPU H_eff*psi (oracle/cpu: BTAS task
+    enumeration, FLOP-sorted OpenMP task loop, one single-threaded dgemm per block pair,
+    pinned bit for bit to the reference's own sigma) on all host cores, repeated until
+    ``budget_s`` seconds of sigma work.  Returns (sigma blocks, FLOPs per sigma, seconds
+    per sigma, repetitions, threads)."""
+    from oracle import cpu as ocpu
 
-    def to_oracle(t):
-        d = t.to_dict()
-        a = oq.QSDArray(d["q"], d["qshape"], d["dshape"])
-        a.blocks = d["blocks"]
-        return a
-
-    mL, mR, psi = to_oracle(wl["mL"]), to_oracle(wl["mR"]), to_oracle(wl["psi"])
-    cores = os.cpu_count() or 1
-    tasks = []
-    out = oq.QSDArray()
-    t0 = time.perf_counter()
-    scr = od.compute_sigma_vector(mL, mR, psi, out, tasks)
-    dt = time.perf_counter() - t0
-    fl = sigma_task_flops(tasks, mL, mR, psi, scr)
-    rec = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-           "sample": f"oracle (NumPy) H_eff*psi on all {len(psi.blocks)} psi blocks of the same bond, "
-                     f"one full step of {dt:.1f} s, NumPy BLAS threads on {cores} cores"}
-    return rec, out.blocks
+    ops = ocpu.Operands(mL, mR, psi)
+    secs = []
+    blocks, fl = None, 0.0
+    while len(secs) < min_reps or sum(secs) < budget_s:
+        blocks, fl, s = ocpu.sigma(ops)
+        secs.append(s)
+    return blocks, fl, sum(secs) / len(secs), len(secs), ocpu.threads()
 
 
-def sigma_vs_oracle(gpu_blocks, oracle_blocks) -> dict:
-    """Largest block-wise difference of the device FP64 sigma from the oracle's, relative
-    to the largest |sigma| element."""
+def sigma_vs_cpu(gpu_blocks, cpu_blocks) -> dict:
+    """Largest block-wise difference of the device FP64 sigma from the CPU restatement's,
+    relative to the largest |sigma| element; a block present on one side only counts in
+    full."""
     import numpy as np
 
-    scale = max(float(np.abs(b).max()) for b in oracle_blocks.values() if b.size)
+    scale = max(float(np.abs(b).max()) for b in cpu_blocks.values() if b.size)
     worst = 0.0
-    for t, b in oracle_blocks.items():
-        g = gpu_blocks.get(t)
-        if g is None:
-            worst = max(worst, float(np.abs(b).max()) / scale)
+    for t in set(gpu_blocks) | set(cpu_blocks):
+        g, b = gpu_blocks.get(t), cpu_blocks.get(t)
+        if g is None or b is None:
+            x = b if g is None else g
+            worst = max(worst, float(np.abs(x).max()) / scale if x.size else 0.0)
         else:
-            worst = max(worst, float(np.abs(g - b).max()) / scale)
-    extra = [t for t in gpu_blocks if t not in oracle_blocks and np.abs(gpu_blocks[t]).max() > 0]
-    return {"max_rel_err": worst, "blocks": len(oracle_blocks), "extra_nonzero_blocks": len(extra)}
+            worst = max(worst, float(np.abs(g - b).max()) / scale if b.size else 0.0)
+    return {"max_rel_err": worst, "blocks_gpu": len(gpu_blocks), "blocks_cpu": len(cpu_blocks)}
 
 
-def sigma_task_flops(tasks, mL, mR, psi, scr) -> float:
-    """2*m*n*k summed over the enumerated (A, B) pairs of both sigma Gemm's."""
-    fl = 0.0
-    for name, tl in tasks:
-        for _, pairs in tl:
-            for ta, tb in pairs:
-                if name == "LxPsi":
-                    a, b = mL.blocks[ta], psi.blocks[tb]
-                    fl += 2.0 * a.shape[0] * a.shape[2] * b.shape[1]
-                else:
-                    a, b = scr.blocks[ta], mR.blocks[tb]
-                    fl += 2.0 * a.shape[0] * a.shape[2] * b.shape[0]
-    return fl
+def cpu_record(fl, sec, reps, threads, what) -> dict:
+    return {"value": fl / sec / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+            "sample": f"C++ restatement of the reference's CPU H_eff*psi (BTAS block tasks, OpenMP over tasks, "
+                      f"OpenBLAS dgemm per block pair; bitwise equal to the reference's sigma on its dumped bonds) "
+                      f"on {what}: {reps} full H_eff*psi, {sec:.2f} s each, {threads} threads"}
 
 
 def run_reference(args, ws, rank):
-    """Reference arm: the reference's CPU algorithm for the path on the host cores.
+    """Reference arm: the reference's CPU H_eff*psi on the host cores, on the same bond.
 
-    The reference (C++ over Boost, BTAS and MKL) does not build in this image (no
-    Boost, no CBLAS/LAPACKE headers), so its NumPy restatement (the oracle port)
-    is timed; the workload is built on the GPU machine through the product path and
-    copied to the host first."""
+    The reference's sources are not on the GPU host, so its C++ restatement (oracle/cpu,
+    pinned bitwise to the reference's own sigma) is timed.  The operands are built on the
+    host by the oracle from the committed bond files; nothing of the GPU library is
+    imported or loaded.  Other ranks exit without work."""
     if rank != 0:
         return
-    from mpsxx_gb300 import core
+    if args.workload != "c2-bond":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm runs on the c2-bond workload only"}))
+        return
+    t0 = time.perf_counter()
+    mL, mR, psi = host_operands(bench_bond(args.seed))
+    t_build = time.perf_counter() - t0
+    from oracle import cpu as ocpu
 
-    ctx = core.Context(0)
-    wl = build_workload(args, ctx)
-    samples = []
+    ops = ocpu.Operands(mL, mR, psi)
+    for _ in range(args.warmup):
+        ocpu.sigma(ops)
+    secs = []
+    blocks, fl = None, 0.0
     for _ in range(max(1, args.steps)):
-        s, _ = cpu_sigma_oracle(wl)
-        samples.append(s["value"])
-    v = sum(samples) / len(samples)
-    out = {"impl": "reference", "metric": "H_eff*psi TFLOP/s (FP64-equivalent), n=20 QC, M=512, middle bond",
-           "value": v, "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"qc n={args.norb} K={args.nchol} seed={args.seed} M={args.M} bond={wl['bond']}",
-                      "W": wl["W"]},
-           "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": os.cpu_count() or 1, "kind": "port",
-                            "sample": s["sample"]},
-           "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        blocks, fl, s = ocpu.sigma(ops)
+        secs.append(s)
+    sec = sum(secs) / len(secs)
+    v = fl / sec / 1e12
+    th = ocpu.threads()
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": 1, "steps": len(secs),
+           "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": DATA,
+           "config": {"workload": workload_name(args), "W": 862, "flops_per_step": fl, "parallelism": "host cores"},
+           "cpu_baseline": cpu_record(fl, sec, len(secs), th, "operands built on the host by the oracle"),
+           "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "sigma_checksum": sigma_checksum(blocks), "host_setup_s": round(t_build, 1)}
     print(json.dumps(out), flush=True)
 
 
+def measure_tf32_peak(torch) -> float:
+    """cuBLAS TF32 tensor-core GEMM throughput (TFLOP/s, FP32 8192^3 with TF32 math, best
+    of 10): the split path's tensor roofline is a third of it (three products)."""
+    n = 8192
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        a = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        for _ in range(3):
+            a @ b
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(10):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a @ b
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        del a, b
+        return 2 * n ** 3 / best / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def bond_e2e(ctx, hb, M: int, tole: float, precision: int, reps: int = 2) -> dict:
+    """One two-site bond step (merged operators, diagonal, Davidson, SVD, renormalisation,
+    expand) end to end from host site tensors: the six input tensors uploaded, the step,
+    the renormalised environment and both new site tensors downloaded."""
+    from mpsxx_gb300 import core
+
+    core.set_precision(ctx, precision)
+    names = ("w9", "w10", "lenv", "renv", "lwfn", "rwfn")
+    h2d = 8 * sum(int(sum(b.size for b in hb[k]["blocks"].values())) for k in names)
+    rows = []
+    for _ in range(reps):
+        ctx.sync()
+        t0 = time.perf_counter()
+        t = {k: core.Tensor.from_dict(ctx, hb[k]) for k in names}
+        e, env, nl, nr, s = core.optimize_twosite_merged(ctx, True, t["w9"], t["w10"], t["lenv"], t["renv"],
+                                                         t["lwfn"], t["rwfn"], 0.1 * tole, M)
+        outs = [x.download() for x in (env, nl, nr)]
+        dt = time.perf_counter() - t0
+        rows.append({"seconds": dt, "energy": e, "n_sigma": int(s["n_sigma"]), "t_davidson": s["t_davidson"],
+                     "t_svd": s["t_svd"], "t_renorm": s["t_renorm"], "t_merge": s["t_merge"],
+                     "d2h_bytes": 8 * sum(int(o.size) for o in outs)})
+        del t, env, nl, nr
+    core.set_precision(ctx, core.FP64)
+    return {"h2d_bytes": h2d, "runs": rows, "seconds_best": min(r["seconds"] for r in rows)}
+
+
 def main():
+    global T_START
+    T_START = time.perf_counter()
     args = parse()
     ws, rank, local = dist_init(args)
+    if args.workload == "c2-bond" and args.bond_structure:
+        global C2_STRUCTURE
+        C2_STRUCTURE = args.bond_structure
     if args.impl == "reference":
         run_reference(args, ws, rank)
         return
@@ -562,8 +731,26 @@ def main():
     ctx = core.Context(local)
     wl = build_workload(args, ctx)
     mL, mR, psi = wl["mL"], wl["mR"], wl["psi"]
-    sig = psi.like()
+
+    # Parity first, on a fresh FP64 sigma: against the CPU restatement of the reference's
+    # sigma on the same operands (downloaded), which is also the timed CPU baseline.
+    core.set_precision(ctx, core.FP64)
+    s64 = psi.like()
+    core.compute_sigma_vector(ctx, mL, mR, psi, s64)
+    ref64 = s64.download()
+    gpu64_blocks = s64.to_dict()["blocks"]
+    cpu_base, parity = None, None
+    if not args.no_cpu_baseline and ws == 1:
+        cblocks, cfl, csec, creps, cth = cpu_sigma_timed(mL.to_dict(), mR.to_dict(), psi.to_dict(), args.cpu_seconds)
+        cpu_base = cpu_record(cfl, csec, creps, cth, "the same bond's operands downloaded from the device")
+        parity = {"sigma_fp64_vs_cpu_port": sigma_vs_cpu(gpu64_blocks, cblocks),
+                  "sigma_checksum_gpu_fp64": sigma_checksum(gpu64_blocks),
+                  "sigma_checksum_cpu_port": sigma_checksum(cblocks)}
+        del cblocks
+
     # one call builds and caches the plan
+    core.set_precision(ctx, core.SPLIT_TF32 if args.precision == "split" else core.FP64)
+    sig = psi.like()
     core.compute_sigma_vector(ctx, mL, mR, psi, sig)
     ctx.sync()
     c0 = ctx.counters()
@@ -573,11 +760,8 @@ def main():
     l2 = "inputs larger than L2" if inputs_bytes > L2_BYTES else "L2 flushed between steps"
     flush = None if inputs_bytes > L2_BYTES else torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
 
-    # FP64 reference timing of the same step (CUDA events on the context's stream)
+    # FP64 timing of the same step (CUDA events on the context's stream)
     core.set_precision(ctx, core.FP64)
-    s64 = sig.like()
-    core.compute_sigma_vector(ctx, mL, mR, psi, s64)
-    ref64 = s64.download()
     fp64_s = kernel_times(ctx, mL, mR, psi, s64, max(2, min(args.steps, 3)))["sigma_kernels_s"]
 
     # headline: split-precision (3xTF32 tensor-core) path
@@ -605,7 +789,7 @@ def main():
     step_s = max_over_ranks(ws, sum(times) / len(times), device="cuda")
     kt = kernel_times(ctx, mL, mR, psi, sig, args.steps)
     value = job_tflops(ws, fl_per_step, step_s)
-    # accuracy of this step against the FP64 step
+    # accuracy of one step against the FP64 step
     one = sig.like()
     core.compute_sigma_vector(ctx, mL, mR, psi, one)
     got = one.download()
@@ -624,77 +808,84 @@ def main():
 
     peaks, src = roofline_peaks()
     fp64_peak = measure_fp64_peak(torch)
-    bond = bond_compare(ctx, wl, args.M, args.tole) if args.bond_step else None
-    # the sweep comparison and the CPU baseline belong to the one-GPU line; replicas
-    # (N > 1) time H_eff*psi only
-    sections = {}
-    t_sec = time.perf_counter()
-    sweep = sweep_compare(args, local) if not args.no_sweep and ws == 1 else None
-    sections["sweeps"] = time.perf_counter() - t_sec
-    t_sec = time.perf_counter()
-    grad = gradient_bench(args, local) if args.gradient else None
-    sections["gradient"] = time.perf_counter() - t_sec
-    t_sec = time.perf_counter()
-    scan_res = scan_bench(args, local) if args.scan else None
-    sections["scan"] = time.perf_counter() - t_sec
-    out = None
+    tf32_peak = measure_tf32_peak(torch)
+    bond = None
+    if args.workload == "c2-bond" and not args.no_bond_e2e:
+        bond = {p: bond_e2e(ctx, wl["host"], 512, args.tole, prec)
+                for p, prec in (("split", core.SPLIT_TF32), ("fp64", core.FP64))}
+    elif args.bond_step and "st" in wl:
+        bond = bond_compare(ctx, wl, args.M, args.tole)
+    # the sweep comparison, the scan and the gradients belong to the one-GPU line
+    # (replicas, N > 1, time H_eff*psi only); a section not yet started when the
+    # wall-clock budget is spent is skipped and says so
+    sections, results = {}, {}
+    for name, on, fn in (("sweeps", not args.no_sweep, sweep_compare), ("scan", args.scan, scan_bench),
+                         ("gradient", args.gradient, gradient_bench)):
+        if not on or ws > 1:
+            results[name] = None
+            continue
+        if time.perf_counter() - T_START > args.budget_s:
+            results[name] = {"skipped": f"wall-clock budget of {args.budget_s:.0f} s spent before this section"}
+            continue
+        t_sec = time.perf_counter()
+        results[name] = fn(args, local)
+        sections[name] = time.perf_counter() - t_sec
+    sweep, scan_res, grad = results["sweeps"], results["scan"], results["gradient"]
     if rank == 0:
-        achieved = fl_per_step / kt["sigma_kernels_s"] / 1e12
+        ksec = kt["sigma_kernels_s"]
+        achieved_tf = fl_per_step / ksec / 1e12
+        traffic = MEASURED_TRAFFIC.get((args.workload, args.precision))
         if args.precision == "split":
-            # TF32 dense rate = half the measured BF16 rate; 3 products per FP64-equivalent product
-            tf32 = peaks["bf16_tflops"] / 2.0
-            traffic = MEASURED_TRAFFIC.get((args.precision, args.norb, args.nchol, args.seed, args.M))
-            roof = {"bound": "tensor", "achieved": achieved, "peak": tf32 / 3.0, "unit": "TFLOP/s",
-                    "frac": achieved / (tf32 / 3.0), "traffic": traffic,
-                    "traffic_note": "DRAM bytes per H_eff*psi (all launches of the step) from ncu; algorithmic "
-                                    "bytes are hbm_algorithmic_bytes" if traffic else None,
-                    "hbm_algorithmic_bytes": bytes_alg,
-                    "peak_source": f"{src} bf16_tflops/2 (TF32 dense) /3 (3-product split), FP64-equivalent"}
+            roof = {"bound": "hbm", "achieved": bytes_alg / ksec / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                    "frac": bytes_alg / ksec / 1e9 / peaks["hbm_gbs"],
+                    "traffic": traffic * bytes_alg if traffic else None,
+                    "traffic_note": (f"DRAM bytes per H_eff*psi = {traffic:.2f} x the algorithmic bytes, the ratio "
+                                     f"of dram__bytes_read+write to algorithmic bytes measured by ncu on the "
+                                     f"small case of the same kernels" if traffic else None),
+                    "algorithmic_bytes": bytes_alg,
+                    "peak_source": f"{src} hbm_gbs (STREAM-style copy)",
+                    "tensor": {"achieved": achieved_tf, "peak": tf32_peak / 3.0, "unit": "TFLOP/s",
+                               "frac": achieved_tf / (tf32_peak / 3.0),
+                               "peak_source": "cuBLAS TF32 GEMM measured in this run, /3 (three TF32 products "
+                                              "per FP64-equivalent product)",
+                               "tf32_tflops": tf32_peak},
+                    "intensity_flop_per_byte": fl_per_step / bytes_alg,
+                    "ridge_flop_per_byte": tf32_peak / 3.0 * 1e12 / (peaks["hbm_gbs"] * 1e9)}
         else:
-            roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                    "frac": achieved / fp64_peak, "traffic": None,
-                    "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 CUDA-core pipe)"}
-        roof.update({"kernel_ms": kt["sigma_kernels_s"] * 1e3,
-                     "hbm_algorithmic_gbs": bytes_alg / kt["sigma_kernels_s"] / 1e9,
-                     "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_source": src})
+            roof = {"bound": "fp64", "achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                    "frac": achieved_tf / fp64_peak, "traffic": None,
+                    "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe)"}
+        roof.update({"kernel_ms": ksec * 1e3, "hbm_peak_source": src})
         out = {
-            "metric": "H_eff*psi TFLOP/s (FP64-equivalent), n=20 QC, M=512, middle bond",
-            "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
             "dtype": "tf32x3-split (fp64 in/out)" if args.precision == "split" else "f64",
-            "data": "synthetic: seeded integrals, seeded random MPS of bond dimension 512",
-            "config": {"workload": f"qc n={args.norb} K={args.nchol} seed={args.seed} M={args.M} "
-                                   f"bond=({wl['bond']},{wl['bond'] + 1})",
-                       "W": wl["W"], "D_rows": sum(psi.shape()[1][0]), "D_cols": sum(psi.shape()[1][1]),
-                       "nnz_psi": psi.nnz, "nnz_L": mL.nnz, "nnz_R": mR.nnz, "flops_per_step": fl_per_step,
-                       "l2": l2, "parallelism": f"replicas{ws}", "precision": args.precision},
+            "data": DATA,
+            "config": {"workload": workload_name(args), "W": wl["W"], "D_rows": sum(psi.shape()[1][0]),
+                       "D_cols": sum(psi.shape()[1][1]), "nnz_psi": psi.nnz, "nnz_L": mL.nnz, "nnz_R": mR.nnz,
+                       "flops_per_step": fl_per_step, "l2": l2, "parallelism": f"replicas{ws}",
+                       "precision": args.precision},
             "gpu_launches": int(launches),
             "e2e": {"value": job_tflops(ws, fl_per_step, e2e_s), "unit": "TFLOP/s", "ms_per_step": e2e_s * 1e3,
                     "h2d_bytes_per_step": 8 * psi.nnz, "d2h_bytes_per_step": 8 * psi.nnz},
             "roofline": roof,
             "fp64_path": {"ms_per_step": fp64_s * 1e3, "value": fl_per_step / fp64_s / 1e12, "unit": "TFLOP/s",
                           "peak": fp64_peak, "frac": fl_per_step / fp64_s / 1e12 / fp64_peak,
-                          "speedup_of_headline": fp64_s / kt["sigma_kernels_s"]},
+                          "speedup_of_headline": fp64_s / ksec},
             "accuracy": {"max_rel_err_vs_fp64": rel},
+            "parity": parity,
+            "cpu_baseline": cpu_base,
             "sigma_tuning": [{"w_scratch_mb": b / 2**20, "target_tiles": tt, "fp32_intermediate": f, "ms": ms}
                              for b, tt, f, ms in tuning],
             "sigma_plan": plan_stats,
-            "bond_step": bond,
+            "bond_step_e2e": bond,
             "sweeps": sweep,
             "gradient": grad,
             "scan": scan_res,
             "clocks": clk.summary(),
             "section_seconds": {k: round(v, 1) for k, v in sections.items()},
         }
-        if not args.no_cpu_baseline and ws == 1:
-            rec, oblocks = cpu_sigma_oracle(wl)
-            out["cpu_baseline"] = rec
-            # a fresh FP64 sigma (the timing loops above accumulate into their outputs)
-            core.set_precision(ctx, core.FP64)
-            s_par = psi.like()
-            core.compute_sigma_vector(ctx, mL, mR, psi, s_par)
-            core.set_precision(ctx, core.SPLIT_TF32 if args.precision == "split" else core.FP64)
-            out["parity"] = {"sigma_vs_oracle_c2": sigma_vs_oracle(s_par.to_dict()["blocks"], oblocks)}
         print(json.dumps(out), flush=True)
     barrier(ws)
 

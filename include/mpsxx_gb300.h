@@ -206,11 +206,13 @@ int mpsxx_sigma_plan_stats(mpsxx_context* ctx, const mpsxx_tensor* lopr, const m
 int mpsxx_compute_diagonal_elements(mpsxx_context* ctx, const mpsxx_tensor* lopr, const mpsxx_tensor* ropr,
                                     mpsxx_tensor* diag);
 
-/* diag += the diagonal of H for one-site (src/compute_diagonal_elements.hpp:10-32,
+/* diag = the diagonal of H for one-site (src/compute_diagonal_elements.hpp:10-32,
  * diag[l,n,r] = sum lopr[l,w,l] mpo[w,n,n,w'] ropr[r,w',r]) and four-index two-site
- * wavefunctions (:35-62).  diag supplies the sectors and q; every allowed block is
- * computed and blocks diag lacks are added (the handle then refers to the grown
- * tensor), as the reference's group sum does with Axpy (:84-100). */
+ * wavefunctions (:35-62).  diag supplies the sectors and q; as the reference's
+ * Copy(scr, diag, 1) (:31, :58), the blocks diag held are dropped and it holds every
+ * computed block its quantum numbers allow (the handle then refers to the new
+ * tensor).  The reference's operator-group sum (:84-100) is this call into a fresh
+ * tensor per group followed by mpsxx_tensor_accumulate. */
 int mpsxx_compute_diagonal_elements_onesite(mpsxx_context* ctx, const mpsxx_tensor* mpo, const mpsxx_tensor* lopr,
                                             const mpsxx_tensor* ropr, mpsxx_tensor* diag);
 int mpsxx_compute_diagonal_elements_twosite(mpsxx_context* ctx, const mpsxx_tensor* lmpo, const mpsxx_tensor* rmpo,

@@ -170,8 +170,8 @@ inline void compute_diagonal_elements(Context& ctx, const QSDArray& lopr, const 
 }
 
 // One-site and four-index two-site diagonals (src/compute_diagonal_elements.hpp:10-62):
-// diag += the diagonal on every allowed block of diag's sectors (diag grows by the
-// blocks it lacks).
+// diag = the diagonal on every allowed block of diag's sectors; as the reference's
+// Copy(scr, diag, 1), what diag held before is dropped.
 inline void compute_diagonal_elements(Context& ctx, const QSDArray& mpo0, const QSDArray& lopr, const QSDArray& ropr,
                                       QSDArray& diag) {
   check(mpsxx_compute_diagonal_elements_onesite(ctx.get(), mpo0.get(), lopr.get(), ropr.get(), diag.get()));

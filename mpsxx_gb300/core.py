@@ -330,14 +330,17 @@ def compute_guesswave(ctx: Context, forward: bool, mps0: Tensor, wfn0: Tensor, m
 
 
 def compute_diagonal_elements_onesite(ctx: Context, mpo: Tensor, lopr: Tensor, ropr: Tensor, diag: Tensor):
-    """diag += one-site diagonal (src/compute_diagonal_elements.hpp:10-32); diag grows
-    by any allowed blocks it lacks."""
+    """diag = one-site diagonal (src/compute_diagonal_elements.hpp:10-32): as the
+    reference's Copy(scr, diag, 1), diag's previous blocks are dropped and it holds the
+    computed blocks its quantum numbers allow (sum operator groups with
+    Tensor.accumulate on separate results)."""
     check(lib().mpsxx_compute_diagonal_elements_onesite(ctx.h, mpo.h, lopr.h, ropr.h, diag.h))
 
 
 def compute_diagonal_elements_twosite(ctx: Context, lmpo: Tensor, rmpo: Tensor, lopr: Tensor, ropr: Tensor,
                                       diag: Tensor):
-    """diag += four-index two-site diagonal (src/compute_diagonal_elements.hpp:35-62)."""
+    """diag = four-index two-site diagonal (src/compute_diagonal_elements.hpp:35-62),
+    overwritten as by the reference's Copy(scr, diag, 1)."""
     check(lib().mpsxx_compute_diagonal_elements_twosite(ctx.h, lmpo.h, rmpo.h, lopr.h, ropr.h, diag.h))
 
 

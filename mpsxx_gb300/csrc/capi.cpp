@@ -481,8 +481,10 @@ int mpsxx_compute_diagonal_elements_onesite(mpsxx_context* ctx, const mpsxx_tens
     need_device(ten(ropr));
     need_device(ten(diag));
     auto d = diagonal_onesite(c, ten(mpo), ten(lopr), ten(ropr), ten(diag));
-    accumulate_into(c, 1.0, *d, diag->t);
+    // btas::Copy(scr, diag, 1): diag holds exactly the computed blocks its quantum
+    // numbers allow; what it held before is dropped
     c.sync();
+    diag->t = std::move(d);
   });
 }
 
@@ -494,8 +496,10 @@ int mpsxx_compute_diagonal_elements_twosite(mpsxx_context* ctx, const mpsxx_tens
     need_device(ten(ropr));
     need_device(ten(diag));
     auto d = diagonal_twosite(c, ten(lmpo), ten(rmpo), ten(lopr), ten(ropr), ten(diag));
-    accumulate_into(c, 1.0, *d, diag->t);
+    // btas::Copy(scr, diag, 1): diag holds exactly the computed blocks its quantum
+    // numbers allow; what it held before is dropped
     c.sync();
+    diag->t = std::move(d);
   });
 }
 

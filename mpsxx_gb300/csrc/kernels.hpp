@@ -86,6 +86,8 @@ struct DNoise {
 
 // Davidson subspace size: multi-dot and rotation kernels handle up to 10 vectors
 constexpr int kMaxDot = 10;
+// Most CTAs of one multi-dot (each writes kMaxDot * kMaxDot partial sums)
+constexpr int kMultidotMaxBlocks = 304;
 
 // One problem of the batched Davidson: its slice of the vector arena.
 struct DBatchProb {

@@ -446,7 +446,7 @@ void launch_copy_vec(double* y, const double* x, int64_t n, cudaStream_t st) {
 
 int multidot_blocks(int64_t n) {
   int64_t b = (n + 2047) / 2048;
-  if (b > 304) b = 304;
+  if (b > kMultidotMaxBlocks) b = kMultidotMaxBlocks;
   if (b < 1) b = 1;
   return static_cast<int>(b);
 }

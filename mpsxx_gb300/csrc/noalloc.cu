@@ -34,10 +34,13 @@ namespace {
 
 // The multi-dot kernel writes one slot of kPartialStride doubles per CTA and uses
 // at most kMaxBlocks CTAs (see multidot_blocks), so this bounds every call.
-constexpr int kMaxBlocks = 304;
+constexpr int kMaxBlocks = mpsxx::kMultidotMaxBlocks;
 constexpr int kPartialStride = 100;  // up to 10 x 10 dot products per CTA
 constexpr int kNoAllocPartials = kMaxBlocks * kPartialStride;
 constexpr int kMaxVectors = 10;
+// the slot stride and vector limit the multi-dot kernel writes and accepts
+static_assert(kPartialStride == mpsxx::kMaxDot * mpsxx::kMaxDot, "partial slot stride of the multi-dot kernel");
+static_assert(kMaxVectors == mpsxx::kMaxDot, "vector limit of the multi-dot kernel");
 
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
 

@@ -74,7 +74,8 @@ def compute_sigma_vector_overlap(lopr: QSDArray, ropr: QSDArray, wfn0: QSDArray,
 # ----------------------------------------------------------------------------
 
 def renormalize_mpo(forward: bool, mpo0: QSDArray, opr0: QSDArray, bra0: QSDArray, ket0: QSDArray) -> QSDArray:
-    """renormalize with the site MPO (``src/renormalize.hpp:10-32``): three Contracts."""
+    """renormalize with the site MPO (``src/renormalize.hpp:10-32``): three Contracts
+    (also used to build the initial environments)."""
     b = bra0.conjugate()
     if forward:
         scr1 = contract(opr0, "lwk", b, "lna", "wkna")
@@ -129,24 +130,6 @@ def renormalize_merged(forward: bool, opr0: QSDArray, bra0: QSDArray, ket0: QSDA
 
 
 # ----------------------------------------------------------------------------
-# one-site MPO renormalisation, used to build the initial environments
-# (src/renormalize.hpp:10-32)
-# ----------------------------------------------------------------------------
-
-def renormalize_mpo(forward: bool, mpo0: QSDArray, opr0: QSDArray, bra0: QSDArray,
-                    ket0: QSDArray) -> QSDArray:
-    if forward:
-        # opr1[m,w',m'] = sum opr0[l,w,l'] bra[l,n,m] mpo[w,n,n',w'] ket[l',n',m']
-        scr1 = contract(opr0, "lwx", bra0.conjugate(), "lnm", "wxnm")
-        scr2 = contract(scr1, "wxnm", mpo0, "wnsv", "xmsv")
-        return contract(scr2, "xmsv", ket0, "xsy", "mvy")
-    # opr1[b,w,b'] = sum bra[b,n,r] opr0[r,w',r'] mpo[w,n,n',w'] ket[b',n',r']
-    scr1 = contract(bra0.conjugate(), "bnr", opr0, "rvx", "bnvx")
-    scr2 = contract(scr1, "bnvx", mpo0, "wnsv", "bxws")
-    return contract(scr2, "bxws", ket0, "ysx", "bwy")
-
-
-# ----------------------------------------------------------------------------
 # a5: diagonal of H_eff (src/compute_diagonal_elements.hpp:65-80)
 # ----------------------------------------------------------------------------
 
@@ -187,12 +170,13 @@ def _tie_mpo(mpo: QSDArray) -> Dict[tuple, np.ndarray]:
 
 
 def _copy_allowed(scr: Dict[tuple, np.ndarray], diag: QSDArray):
-    """``Copy(scr, diag, 1)`` followed by the group Axpy: add the blocks diag's quantum
-    numbers allow (``src/compute_diagonal_elements.hpp:30,94-95``)."""
+    """``Copy(scr, diag, 1)`` (``src/compute_diagonal_elements.hpp:31,58``;
+    ``include/btas/SPARSE/STBLAS.h:374-388``): diag is resized to scr's shape, which
+    drops every block it held, then takes the blocks of scr its quantum numbers allow."""
+    diag.blocks = {}
     for idx, blk in scr.items():
         if diag.allowed(idx):
-            t = diag.tag(idx)
-            diag.blocks[t] = diag.blocks[t] + blk if t in diag.blocks else blk.copy()
+            diag.blocks[diag.tag(idx)] = blk.copy()
 
 
 def compute_diagonal_elements_onesite(mpo0: QSDArray, lopr: QSDArray, ropr: QSDArray, diag: QSDArray):

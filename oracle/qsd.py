@@ -29,8 +29,9 @@ Restated semantics (reference paths are relative to the mpsxx project root):
   row-major GEMM accumulated serially into its own result block
   (``include/btas/SPARSE/T_arguments.h:517-600``, ``include/btas/DENSE/TBLAS.h:209-245``).
 
-Parity pin: this oracle is pinned by exact diagonalisation and by the golden
-energies the reference's own test logs hold (see ``tests/test_oracle_golden.py``).
+Parity pins: exact diagonalisation (``tests/test_oracle.py``) and the reference
+itself — task lists, bond operations and sweep energies of its own runs
+(``tests/test_reference_fixtures.py``, fixtures in ``tests/golden/ref/``).
 """
 from __future__ import annotations
 

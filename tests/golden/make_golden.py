@@ -6,7 +6,7 @@
 * ``hubbard12_u4_m64.json``: oracle sweep energies of the 12-site Hubbard chain
   (U=4, t=1, half filling, M=64, tole 1e-10, 4 sweeps) and its exact ground state.
 
-Usage: python tests/golden/make_golden.py [--reference-root PATH]
+Usage: python tests/golden/make_golden.py --reference-root PATH   (or MPSXX_REFERENCE_ROOT)
 """
 from __future__ import annotations
 
@@ -38,9 +38,11 @@ def sweep_energies_from_log(path: str):
 
 
 def main():
-    ref_root = "/root/reference"
+    ref_root = os.environ.get("MPSXX_REFERENCE_ROOT", "")
     if "--reference-root" in sys.argv:
         ref_root = sys.argv[sys.argv.index("--reference-root") + 1]
+    if not ref_root:
+        sys.exit("--reference-root PATH (or MPSXX_REFERENCE_ROOT) is required")
     out = {}
     tests = os.path.join(ref_root, "dmrg", "tests")
     if os.path.isdir(tests):

@@ -9,10 +9,12 @@ functions on a dumped bond, recording ST_Gemm_thread's task lists.
 
     python tests/golden/make_ref_fixtures.py --reference-root <mpsxx tree> --work <scratch dir>
 
-Writes tests/golden/ref/{runs.json, tasks.npz, bonds.npz, mpo_qc8.npz}.
+Writes tests/golden/ref/{runs.json, tasks.npz, bonds.npz, mpo_qc8.npz, mpo_c2_bond.npz}.
 Cases: C1 (Hubbard L=12, t=1, U=4, half filling, M=64, tole 1e-10, 4 sweeps), a
 synthetic QC Hamiltonian (n=8, K=16, seed 1, 8 electrons, M=64, tole 1e-9,
-3 sweeps) and the reference's FCIDUMP12 test input (M=64, 2 sweeps, energies only).
+3 sweeps) and the reference's FCIDUMP12 test input (M=64, 2 sweeps, energies only);
+and the reference's MPO of C2 (n=20, K=40, seed 1), of which the two sites of the
+middle bond (9, 10) are kept as the bench's operator.
 """
 from __future__ import annotations
 
@@ -153,6 +155,22 @@ def main():
             for i in range(N):
                 mpo.update(ref_io.pack_tensor(f"site{i}", ref_io.read_qsd(os.path.join(mdir, f"mpo_{i}.qsd"))))
             np.savez_compressed(os.path.join(OUT, "mpo_qc8.npz"), **mpo)
+    # C2's operator: the reference's complementary-operator MPO for the synthetic n=20
+    # Hamiltonian; the two sites of the middle bond are the bench's H_eff*psi operands
+    d = os.path.join(args.work, "c2_mpo")
+    os.makedirs(d, exist_ok=True)
+    qc_fcidump(os.path.join(d, "FCIDUMP"), 20, 40, 1)
+    run([os.path.join(REF_BIN, "mpogen.x"), "-f", "FCIDUMP", "-s", "."], d, log=os.path.join(d, "mpogen.log"))
+    mdir = os.path.join(d, "mpo_qsd")
+    os.makedirs(mdir, exist_ok=True)
+    subprocess.run([os.path.join(REF_BIN, "ref_ops.x"), "dump_mpo", d, "20", mdir], check=True)
+    sites = [ref_io.read_qsd(os.path.join(mdir, f"mpo_{i}.qsd")) for i in range(20)]
+    runs["c2_mpo"] = {"bond_dims": [len(s["qshape"][3]) for s in sites[:-1]],
+                      "nnz": [len(s["blocks"]) for s in sites]}
+    mpo = {}
+    for i in (9, 10):
+        mpo.update(ref_io.pack_tensor(f"site{i}", sites[i]))
+    np.savez_compressed(os.path.join(OUT, "mpo_c2_bond.npz"), **mpo)
     with open(os.path.join(OUT, "runs.json"), "w") as f:
         json.dump(runs, f, indent=1)
     np.savez_compressed(os.path.join(OUT, "tasks.npz"), **tasks)

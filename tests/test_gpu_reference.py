@@ -1,0 +1,121 @@
+"""The CUDA path against outputs of the mpsxx reference itself (compiled from its
+sources, run through its own dmrg.x; fixtures made by tests/golden/make_ref_fixtures.py).
+
+* bonds.npz: six bonds of the reference's C1 (Hubbard L=12, U=4, M=64) and QC n=8 runs,
+  the inputs optimize_twosite_merged received and the reference's merged wavefunction,
+  sigma, diagonal, truncated factors and renormalised operator on them;
+* runs.json: the reference's sweep energies of C1 and of the QC n=8 Hamiltonian.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import ref_io
+
+REF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref")
+BOND_KEYS = sorted({k.split("/")[0] for k in np.load(os.path.join(REF, "bonds.npz")).files})
+
+
+def rel_diff(a: dict, b: dict) -> float:
+    """max |a - b| over the union of blocks, relative to max |b|."""
+    scale = max([float(np.abs(x).max()) for x in b.values() if x.size] + [1e-300])
+    worst = 0.0
+    for t in set(a) | set(b):
+        x, y = a.get(t), b.get(t)
+        if x is None or y is None:
+            z = y if x is None else x
+            worst = max(worst, float(np.abs(z).max()) if z.size else 0.0)
+        else:
+            worst = max(worst, float(np.abs(x - y).max()) if x.size else 0.0)
+    return worst / scale
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from mpsxx_gb300 import core
+
+    c = core.Context(0)
+    yield c
+    c.close()
+
+
+def _dev(ctx, d):
+    from mpsxx_gb300 import core
+
+    return core.Tensor.from_dict(ctx, d)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", BOND_KEYS)
+def test_bond_operations_equal_the_reference(ctx, key):
+    """From the reference's own bond inputs, on the device: merged wavefunction, sigma
+    (FP64 within 1e-13; split precision within 1e-5), diagonal and renormalised operator
+    against the reference's outputs; the truncation keeps the reference's sectors and
+    dimensions and U*sV^T matches its product."""
+    from mpsxx_gb300 import core
+
+    z = np.load(os.path.join(REF, "bonds.npz"))
+    forward, M = bool(z[f"{key}/meta"][0]), int(z[f"{key}/meta"][1])
+    b = {t: _dev(ctx, ref_io.unpack_tensor(z, f"{key}/{t}")) for t in ("lmpo", "rmpo", "lopr", "ropr", "lwfn", "rwfn")}
+    ref = {t: ref_io.unpack_tensor(z, f"{key}/{t}") for t in ("psi", "sigma", "diag", "lmat", "rmat", "env")}
+    core.set_precision(ctx, core.FP64)
+    mL = core.compute_merged_operator(ctx, True, b["lmpo"], b["lopr"])
+    mR = core.compute_merged_operator(ctx, False, b["rmpo"], b["ropr"])
+    psi = core.merge_wavefunction(ctx, b["lmpo"], b["rmpo"], b["lopr"], b["ropr"], b["lwfn"], b["rwfn"])
+    assert rel_diff(psi.to_blocks(), ref["psi"]["blocks"]) < 1e-14
+    sig = psi.like()
+    core.compute_sigma_vector(ctx, mL, mR, psi, sig)
+    assert rel_diff(sig.to_blocks(), ref["sigma"]["blocks"]) < 1e-13
+    core.set_precision(ctx, core.SPLIT_TF32)
+    s32 = psi.like()
+    core.compute_sigma_vector(ctx, mL, mR, psi, s32)
+    core.set_precision(ctx, core.FP64)
+    assert rel_diff(s32.to_blocks(), ref["sigma"]["blocks"]) < 1e-5
+    diag = psi.like()
+    core.compute_diagonal_elements(ctx, mL, mR, diag)
+    assert rel_diff(diag.to_blocks(), ref["diag"]["blocks"]) < 1e-13
+    U, V = core.canonicalize(ctx, forward, psi, M)
+    rl, rr = ref["lmat"], ref["rmat"]
+    uq, ud = U.shape()
+    vq, vd = V.shape()
+    assert [list(map(tuple, x)) for x in uq] == [list(map(tuple, x)) for x in rl["qshape"]]
+    assert ud == [list(x) for x in rl["dshape"]] and vd == [list(x) for x in rr["dshape"]]
+    prod = core.gemm(ctx, 0, 0, 1.0, U, V, 2)
+    rprod = core.gemm(ctx, 0, 0, 1.0, _dev(ctx, rl), _dev(ctx, rr), 2)
+    assert rel_diff(prod.to_blocks(), rprod.to_blocks()) < 1e-12
+    # the renormalised operator with the reference's own kept factor (its gauge)
+    kept = _dev(ctx, rl if forward else rr)
+    env = core.renormalize(ctx, forward, mL if forward else mR, kept, kept)
+    assert rel_diff(env.to_blocks(), ref["env"]["blocks"]) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["c1", "qc8"])
+def test_sweep_energies_equal_the_reference(ctx, case):
+    """Two-site DMRG on the device from the reference's initial state against the
+    reference's own sweep energies (dmrg.x): C1 (Hubbard L=12, t=1, U=4, half filling,
+    M=64, tole 1e-10, 4 sweeps) and the synthetic QC n=8 Hamiltonian (K=16, seed 1,
+    M=64, tole 1e-9, 3 sweeps).  The first sweeps stop Davidson runs on the reference's
+    iteration cap, where summation order moves the stopping point (bound 1e-7); from
+    sweep 2 (C1) and throughout (QC n=8) within 1e-9 Eh."""
+    from mpsxx_gb300 import core, dmrg, mpogen
+
+    with open(os.path.join(REF, "runs.json")) as f:
+        r = json.load(f)[case]
+    if case == "c1":
+        mpo_d = mpogen.hubbard_mpo(r["N"], -1.0, 4.0)
+    else:
+        h1, eri = mpogen.synthetic_qc_integrals(8, 16, 1)
+        mpo_d = mpogen.qc_mpo(h1, eri)
+    core.set_precision(ctx, core.FP64)
+    mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
+    st = dmrg.make_initial_state(ctx, mpo, r["elec"], 0, r["M"])
+    for k, e_ref in enumerate(r["sweep_energies"]):
+        e = dmrg.make_sweep(ctx, st, r["tole"]).energy
+        bound = 1e-7 if (case == "c1" and k == 0) else 1e-9
+        assert abs(e - e_ref) < bound, (case, k, e, e_ref)

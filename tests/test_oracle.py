@@ -234,3 +234,68 @@ def _twice(a):
     for k in t.blocks:
         t.blocks[k] = 2.0 * t.blocks[k]
     return t
+
+
+def _perturbed(a, seed):
+    """a plus 0.3 x seeded normal values on every block a holds (same layout)."""
+    rng = np.random.default_rng(seed)
+    b = a.copy()
+    for k in b.blocks:
+        b.blocks[k] = b.blocks[k] + 0.3 * rng.standard_normal(b.blocks[k].shape)
+    return b
+
+
+def test_renormalize_with_distinct_bra_and_ket_equals_dense_products():
+    """renormalize with the site MPO and of an overlap matrix, bra != ket: forward
+    opr1[a,v,b] = sum bra[l,n,a] opr0[l,w,k] W[w,n,m,v] ket[k,m,b] and backward
+    opr1[a,w,b] = sum bra[a,n,r] opr0[r,v,s] W[w,n,m,v] ket[b,m,s] (src/renormalize.hpp:
+    10-54) on dense copies; a swap of bra and ket changes the result."""
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+    from tests.bondcase import hubbard_bond
+
+    case = hubbard_bond()
+    st, i, mpo = case["st"], case["i"], case["mpo"]
+    for forward, k, opr, w in ((True, i, st.lenv[i], st.wave[i]), (False, i + 1, st.renv[i + 1], st.wave[i + 1])):
+        bra, ket = w, _perturbed(w, 11 + k)
+        got = _dense(od.renormalize_mpo(forward, mpo[k], opr, bra, ket))
+        W, O, B, K = _dense(mpo[k]), _dense(opr), _dense(bra), _dense(ket)
+        if forward:
+            ref = np.einsum("lna,lwk,wnmv,kmb->avb", B, O, W, K)
+        else:
+            ref = np.einsum("anr,rvs,wnmv,bms->awb", B, O, W, K)
+        assert np.abs(got - ref).max() < 1e-12 * np.abs(ref).max()
+        swapped = _dense(od.renormalize_mpo(forward, mpo[k], opr, ket, bra))
+        assert np.abs(swapped - ref).max() > 1e-6 * np.abs(ref).max()
+        # overlap matrix: forward S1[a,b] = sum S0[l,k] bra[l,n,a] ket[k,n,b]
+        rng = np.random.default_rng(3 + k)
+        qs, ds = (w.qshape[0], w.dshape[0]) if forward else (w.qshape[2], w.dshape[2])
+        S = oq.QSDArray((0, 0), [qs, [oq.qneg(q) for q in qs]], [ds, ds])
+        for x in range(len(qs)):
+            for y in range(len(qs)):
+                if S.allowed((x, y)) and ds[x] and ds[y]:
+                    S.blocks[S.tag((x, y))] = rng.standard_normal((ds[x], ds[y]))
+        got = _dense(od.renormalize_overlap(forward, S, bra, ket))
+        if forward:
+            ref = np.einsum("lk,lna,knb->ab", _dense(S), B, K)
+        else:
+            ref = np.einsum("rs,anr,bns->ab", _dense(S), B, K)
+        assert np.abs(got - ref).max() < 1e-12 * np.abs(ref).max()
+
+
+def test_single_group_diagonal_overwrites_like_copy():
+    """The one-site and four-index diagonals end with Copy(scr, diag, 1)
+    (src/compute_diagonal_elements.hpp:31,58): blocks diag held before are dropped."""
+    from oracle import dmrg as od
+    from oracle import qsd as oq
+    from tests.bondcase import hubbard_bond
+
+    case = hubbard_bond()
+    st, i, mpo = case["st"], case["i"], case["mpo"]
+    w = st.wave[i]
+    fresh = oq.QSDArray(w.q, w.qshape, w.dshape)
+    od.compute_diagonal_elements_onesite(mpo[i], st.lenv[i], st.renv[i], fresh)
+    reused = _perturbed(w, 4)
+    od.compute_diagonal_elements_onesite(mpo[i], st.lenv[i], st.renv[i], reused)
+    assert set(reused.blocks) == set(fresh.blocks)
+    assert _max_diff(reused, fresh) == 0.0
