@@ -111,6 +111,12 @@ int mpsxx_context_tuning(const mpsxx_context* ctx, double* out, int n, int* coun
  * tiles (0).  w_budget_bytes < 0 restores autotuning.  Cached plans are dropped. */
 int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes, int target_tiles,
                                      int fp32_intermediate);
+/* Storage of the merged operators for the split-precision H_eff*psi: FP32 tiles that
+ * the tensor-core kernel splits into hi|lo TF32 in shared memory (fp32_operators = 1,
+ * the default: half the HBM bytes per application) or pre-split hi|lo TF32 tiles (0).
+ * Either way x = hi + lo to ~2^-22 relative.  Applies to plans made afterwards; cached
+ * plans are dropped. */
+int mpsxx_context_set_sigma_operator_format(mpsxx_context* ctx, int fp32_operators);
 /* Routing of canonicalize's per-block SVDs: blocks with min(m, n) <= jacobi_max_cols
  * (at most 128) go to the batched one-sided Jacobi kernel; of the rest, blocks whose
  * Gram matrix (rows for a forward step, columns backward) has dimension <=
@@ -209,9 +215,9 @@ int mpsxx_compute_diagonal_elements(mpsxx_context* ctx, const mpsxx_tensor* lopr
 /* diag = the diagonal of H for one-site (src/compute_diagonal_elements.hpp:10-32,
  * diag[l,n,r] = sum lopr[l,w,l] mpo[w,n,n,w'] ropr[r,w',r]) and four-index two-site
  * wavefunctions (:35-62).  diag supplies the sectors and q; as the reference's
- * Copy(scr, diag, 1) (:31, :58), the blocks diag held are dropped and it holds every
- * computed block its quantum numbers allow (the handle then refers to the new
- * tensor).  The reference's operator-group sum (:84-100) is this call into a fresh
+ * Copy(scr, diag, 1) (:31, :58), the values diag held are dropped and it holds every
+ * block its quantum numbers allow (the handle then refers to the new tensor); blocks
+ * no term reaches, which the reference leaves out, are stored as zeros.  The reference's operator-group sum (:84-100) is this call into a fresh
  * tensor per group followed by mpsxx_tensor_accumulate. */
 int mpsxx_compute_diagonal_elements_onesite(mpsxx_context* ctx, const mpsxx_tensor* mpo, const mpsxx_tensor* lopr,
                                             const mpsxx_tensor* ropr, mpsxx_tensor* diag);

@@ -28,6 +28,7 @@ SIGNATURES = {
     "mpsxx_context_set_split_refinement": (C.c_int, [vp, C.c_double, C.c_int]),
     "mpsxx_context_tuning": (C.c_int, [vp, c_dbl_p, C.c_int, C.POINTER(C.c_int)]),
     "mpsxx_context_set_sigma_schedule": (C.c_int, [vp, C.c_int64, C.c_int, C.c_int]),
+    "mpsxx_context_set_sigma_operator_format": (C.c_int, [vp, C.c_int]),
     "mpsxx_context_set_svd_routes": (C.c_int, [vp, C.c_int, C.c_int]),
     "mpsxx_context_set_plan_cache": (C.c_int, [vp, C.c_int64]),
     "mpsxx_context_set_device_timeout": (C.c_int, [vp, C.c_int64]),

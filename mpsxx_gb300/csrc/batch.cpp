@@ -403,8 +403,10 @@ class Batch {
     int* err = device_err_flag(ctx_);
     // the members' intermediates share one format (set in setup)
     const bool single = it_[members[0]].sp->scr1_single;
+    const SigmaPlan& p0 = *it_[members[0]].sp;
     for (int c : members)
-      if (it_[c].sp->scr1_single != single) throw Error(kInternal, "batched sigma: intermediate formats differ");
+      if (it_[c].sp->scr1_single != single || it_[c].sp->ops_single != p0.ops_single)
+        throw Error(kInternal, "batched sigma: operand formats differ");
     // capture: zero the outputs, pack the inputs, both stages, the split-K sums
     cudaGraph_t graph = nullptr;
     cuda_check(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal), "batch capture");
@@ -412,9 +414,11 @@ class Batch {
     launch_bzero(g->probs.get(), nm, g->nmax, vec_.as<double>(), kSlotOut, ctx_.stream);
     launch_pack(g->packs.get(), g->npacks, vec_.as<double>(), arPsi_.as<uint8_t>(), ctx_.stream);
     launch_gemm_pk(arL_.as<uint8_t>(), arPsi_.as<uint8_t>(), 1.0, nullptr, arScr_.as<uint8_t>(), g->t1.get(), g->n1,
-                   g->k1.get(), g->p1.get(), nullptr, single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx_.stream, ctx_.device_timeout_ns);
+                   g->k1.get(), g->p1.get(), nullptr, single ? kOutPackedSingle : kOutPackedSplit, p0.stage1_single(), err, ctx_.stream,
+                   ctx_.device_timeout_ns);
     launch_gemm_pk(arScr_.as<uint8_t>(), arR_.as<uint8_t>(), 1.0, vec_.as<double>(), nullptr, g->t2.get(), g->n2,
-                   g->k2.get(), g->p2.get(), ctx_.gemm_part.as<double>(), kOutFP64, single ? 1 : 0, err, ctx_.stream, ctx_.device_timeout_ns);
+                   g->k2.get(), g->p2.get(), ctx_.gemm_part.as<double>(), kOutFP64, p0.stage2_single(), err, ctx_.stream,
+                   ctx_.device_timeout_ns);
     launch_gemm_pk_reduce(g->red.get(), g->nred, g->k2.get(), 1.0, ctx_.gemm_part.as<double>(), vec_.as<double>(),
                           ctx_.stream);
     cuda_check(cudaStreamEndCapture(ctx_.stream, &graph), "batch capture end");

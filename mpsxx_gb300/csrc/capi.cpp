@@ -166,6 +166,15 @@ int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes,
   });
 }
 
+int mpsxx_context_set_sigma_operator_format(mpsxx_context* ctx, int fp32_operators) {
+  return guard([&] {
+    need(ctx && ctx->ctx, "null context");
+    Context& c = *ctx->ctx;
+    c.sigma_fp32_operators = fp32_operators != 0;
+    c.sigma_plans.clear();  // plans are rebuilt with the new packing on next use
+  });
+}
+
 int mpsxx_context_set_device_timeout(mpsxx_context* ctx, int64_t timeout_ns) {
   return guard([&] {
     need(ctx && ctx->ctx, "null context");

@@ -687,6 +687,7 @@ SigmaPlan& sigma_plan(Context& ctx, const Tensor& L, const Tensor& R, const Tens
   p->bytes_min = 8 * (L.nnz + R.nnz + 2 * psi.nnz);
   p->psi_layout = psi;
   p->psi_layout.d = nullptr;
+  p->ops_single = ctx.sigma_fp32_operators;
   return insert_plan(ctx, ctx.sigma_plans, key, std::move(p));
 }
 
@@ -706,7 +707,7 @@ struct Orient {
 // tile_bytes + tk * tile_bytes / 2 (the pack kernel gets tile_rows 64 and row tile
 // 2 tr, which starts at the same row).
 template <class F>
-static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t tile_bytes, F orient) {
+static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t tile_bytes, F orient, int fp32 = 0) {
   P.base.assign(t.tags.size(), -1);
   P.nks.assign(t.tags.size(), 0);
   P.h_packs.clear();
@@ -724,10 +725,10 @@ static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t ti
       for (int tk = 0; tk < nks; ++tk) {
         if (t64)
           P.h_packs.push_back(DPack{t.offsets[b], off + int64_t(tr) * nks * tile_bytes + int64_t(tk) * (tile_bytes / 2),
-                                    o.rows, o.k, o.ld, o.trans, 64, 2 * tr, tk, 0});
+                                    o.rows, o.k, o.ld, o.trans, 64, 2 * tr, tk, fp32});
         else
           P.h_packs.push_back(DPack{t.offsets[b], off + (int64_t(tr) * nks + tk) * tile_bytes, o.rows, o.k, o.ld,
-                                    o.trans, tile_rows, tr, tk, 0});
+                                    o.trans, tile_rows, tr, tk, fp32});
       }
     }
     const bool last64 = tailed && tail64(o.rows, ntr - 1);
@@ -738,12 +739,13 @@ static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t ti
 
 static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R, const Tensor& psi) {
   auto dims3 = [](const Tensor& t, int32_t b, int* d) { t.block_dims(b, d); };
-  // stage 1: A = L block (dA x dA'), B^T = psi block transposed (dB' x dA')
-  packed_layout(p.pk_L, L, kTcTileM, kPkTileABytes, [&](int32_t b) {
+  // stage 1: A = L block (dA x dA'), B^T = psi block transposed (dB' x dA'); the
+  // operators as FP32 tiles (split on chip) or as hi|lo tiles
+  packed_layout(p.pk_L, L, kTcTileM, p.ops_single ? kPkTileA1Bytes : kPkTileABytes, [&](int32_t b) {
     int d[kMaxRank];
     dims3(L, b, d);
     return Orient{d[0] * d[1], d[2], d[2], 0};
-  });
+  }, p.ops_single ? 1 : 0);
   packed_layout(p.pk_psi, psi, kTcTileN, kPkTileBBytes, [&](int32_t b) {
     int d[kMaxRank];
     dims3(psi, b, d);
@@ -757,11 +759,11 @@ static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Te
     return Orient{d[0] * d[1], d[2], d[2], 0};
   });
   // stage 2: B^T = R block (dB x dB')
-  packed_layout(p.pk_R, R, kTcTileN, kPkTileBBytes, [&](int32_t b) {
+  packed_layout(p.pk_R, R, kTcTileN, p.ops_single ? kPkTileB1Bytes : kPkTileBBytes, [&](int32_t b) {
     int d[kMaxRank];
     dims3(R, b, d);
     return Orient{d[0] * d[1], d[2], d[2], 0};
-  });
+  }, p.ops_single ? 1 : 0);
   auto pairs_of = [](const GemmPlan& g, const Packed& A, const Packed& B, std::vector<DPkPair>& out) {
     out.resize(g.h_pairs.size());
     for (size_t i = 0; i < g.h_pairs.size(); ++i) {
@@ -1052,11 +1054,12 @@ static void sigma_groups_run(Context& ctx, SigmaPlan& p, double* sigma) {
     if (G.t1_count)
       launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.group_scr.as<uint8_t>(),
                      p.gt1.get() + G.t1_begin, G.t1_count, p.gtasks1.get(), p.pk1.get(), nullptr,
-                     p.scr1_single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx.stream, ctx.device_timeout_ns);
+                     p.scr1_single ? kOutPackedSingle : kOutPackedSplit, p.stage1_single(), err, ctx.stream,
+                     ctx.device_timeout_ns);
     if (G.t2_count)
       launch_gemm_pk(p.group_scr.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
                      p.gt2.get() + G.t2_begin, G.t2_count, p.s2.dtasks.get(), p.gpk2.get(), part, kOutFP64,
-                     p.scr1_single ? 1 : 0, err, ctx.stream, ctx.device_timeout_ns);
+                     p.stage2_single(), err, ctx.stream, ctx.device_timeout_ns);
     if (G.r_count)
       launch_gemm_pk_reduce(p.gred.get() + G.r_begin, G.r_count, p.s2.dtasks.get(), 1.0, part, sigma, ctx.stream);
     ctx.kernel_launches += (G.t1_count > 0) + (G.t2_count > 0) + (G.r_count > 0);
@@ -1214,12 +1217,13 @@ static void sigma_run_pk_whole(Context& ctx, SigmaPlan& p, double* sigma) {
   int* err = device_err_flag(ctx);
   launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.pk_scr1.buf.as<uint8_t>(),
                  p.s1.tiles_tc.get(), static_cast<int>(p.s1.h_tiles_tc.size()), p.pk_tasks1.get(), p.pk1.get(),
-                 nullptr, p.scr1_single ? kOutPackedSingle : kOutPackedSplit, 0, err, ctx.stream, ctx.device_timeout_ns);
+                 nullptr, p.scr1_single ? kOutPackedSingle : kOutPackedSplit, p.stage1_single(), err, ctx.stream,
+                 ctx.device_timeout_ns);
   ctx.gemm_part.ensure(std::max<size_t>(p.s2.partial_bytes_tc(), 16), ctx.stream);
   double* part = ctx.gemm_part.as<double>();
   launch_gemm_pk(p.pk_scr1.buf.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
                  p.s2.tiles_tc.get(), static_cast<int>(p.s2.h_tiles_tc.size()), p.s2.dtasks.get(), p.pk2.get(), part,
-                 kOutFP64, p.scr1_single ? 1 : 0, err, ctx.stream, ctx.device_timeout_ns);
+                 kOutFP64, p.stage2_single(), err, ctx.stream, ctx.device_timeout_ns);
   if (p.s2.nslots_tc > 0)
     launch_gemm_pk_reduce(p.s2.reduce_tc.get(), static_cast<int>(p.s2.h_reduce_tc.size()), p.s2.dtasks.get(), 1.0,
                           part, sigma, ctx.stream);

@@ -159,6 +159,12 @@ struct SigmaPlan {
   // L*psi intermediate stored as FP32 tiles split on chip (true) or as hi|lo tiles:
   // half the HBM bytes against more shared-memory traffic; chosen by the autotuner
   bool scr1_single = false;
+  // L and R packed as FP32 tiles split on chip (true) or as hi|lo tiles: half the
+  // operators' HBM bytes; fixed when the plan is made (Context::sigma_fp32_operators)
+  bool ops_single = false;
+  // operand formats of the two stages' tensor-core launches (kSingleA / kSingleB)
+  int stage1_single() const { return ops_single ? kSingleA : 0; }
+  int stage2_single() const { return (scr1_single ? kSingleA : 0) | (ops_single ? kSingleB : 0); }
   Packed pk_L, pk_R, pk_psi, pk_scr1;
   std::vector<DPkPair> h_pk1, h_pk2;
   std::vector<DGemmTask> h_pk_tasks1;
@@ -307,6 +313,9 @@ struct Context {
   int64_t sigma_w_budget = -1;
   int sigma_target_tiles = 0;
   bool sigma_fp32_intermediate = false;  // with a forced schedule: FP32 L*psi tiles
+  // split-precision H_eff*psi: merged operators packed as FP32 tiles (split into hi|lo
+  // on chip) instead of hi|lo TF32 tiles; applies to plans made afterwards
+  bool sigma_fp32_operators = true;
   uint64_t device_timeout_ns = kPkTimeoutNs;  // wait limit of the tensor-core kernels
   // canonicalize routing: blocks with min(m, n) <= svd_jacobi_cols go to the batched
   // Jacobi kernel, the rest with a Gram dimension <= svd_gram_max to the batched

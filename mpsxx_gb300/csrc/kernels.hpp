@@ -118,6 +118,9 @@ constexpr uint32_t kPkTileA1Bytes = 128 * 32 * 4;     // A tile as FP32 values, 
 // FP32 A tiles (the next GEMM splits them in shared memory)
 constexpr int kOutFP64 = 0, kOutPackedSplit = 1, kOutPackedSingle = 2;
 constexpr uint32_t kPkTileBBytes = 128 * 32 * 4 * 2;  // B tile: hi|lo TF32, 128 rows
+constexpr uint32_t kPkTileB1Bytes = 128 * 32 * 4;     // B tile as FP32 values, split on chip
+// operand formats of launch_gemm_pk (bit mask): FP32 A tiles, FP32 B tiles
+constexpr int kSingleA = 1, kSingleB = 2;
 
 // One (A, B) pair over packed operands: byte offsets of the blocks' tile grids.
 struct DPkPair {
@@ -126,21 +129,24 @@ struct DPkPair {
 };
 // One packed tile to produce: element (r, k) of the block is src[src_off + r*ld + k]
 // (trans = 0) or src[src_off + k*ld + r] (trans = 1).
+// fp32: the tile holds FP32 values (split into hi|lo on chip by the GEMM) instead of
+// its hi|lo TF32 halves.
 struct DPack {
   int64_t src_off, dst_off;
-  int rows, k, ld, trans, tile_rows, tr, tk, pad;
+  int rows, k, ld, trans, tile_rows, tr, tk, fp32;
 };
 
 // out_packed (kOut*): C is written as packed A tiles of the next GEMM (c_off = byte
 // offset of the block's grid, ldc = its K slices per row tile) instead of FP64 C /
-// partials.  a_single: the A tiles are FP32 (kPkTileA1Bytes each), split into hi|lo
-// in shared memory before the MMAs; otherwise packed hi|lo (kPkTileABytes).
+// partials.  single (kSingleA | kSingleB): the A (B) tiles are FP32 (kPkTileA1Bytes,
+// kPkTileB1Bytes each), split into hi|lo in shared memory before the MMAs; otherwise
+// packed hi|lo (kPkTileABytes, kPkTileBBytes).
 // Every wait of the kernel gives up after timeout_ns (the whole launch): the kernel then
 // drains its own bulk copies and MMAs, frees its tensor memory, sets *err and returns.
 constexpr uint64_t kPkTimeoutNs = 20000000000ull;  // 20 s
 void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
-                    int out_packed, int a_single, int* err, cudaStream_t st, uint64_t timeout_ns = kPkTimeoutNs);
+                    int out_packed, int single, int* err, cudaStream_t st, uint64_t timeout_ns = kPkTimeoutNs);
 void launch_gemm_pk_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
                            double* C, cudaStream_t st);
 void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst, cudaStream_t st);

@@ -52,6 +52,7 @@ constexpr uint32_t A_BYTES = kPkTileABytes;  // 32 KB
 constexpr uint32_t A1_BYTES = kPkTileA1Bytes;  // 16 KB (FP32 A tile)
 constexpr int CONV_THREADS = 64;               // warps 2-3
 constexpr uint32_t B_BYTES = kPkTileBBytes;  // 32 KB
+constexpr uint32_t B1_BYTES = kPkTileB1Bytes;  // 16 KB (FP32 B tile)
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
 // Each K step is two MMAs: A_hi x [B_hi; B_lo] as one N = 2 Nt operand (the packed B
@@ -197,11 +198,33 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// FP32 values at base (n16 x 16 bytes) -> hi = tf32(x) in place, lo = tf32(x - hi) at
+// base + lo_off; the converter's CONV_THREADS threads share the work.
+__device__ __forceinline__ void split_in_place(uint8_t* base, uint32_t lo_off, int n16, int ct) {
+  uint4* hi = reinterpret_cast<uint4*>(base);
+  uint4* lo = reinterpret_cast<uint4*>(base + lo_off);
+#pragma unroll 4
+  for (int i = ct; i < n16; i += CONV_THREADS) {
+    const uint4 x = hi[i];
+    uint4 h, l;
+    h.x = tf32_rna(__uint_as_float(x.x));
+    h.y = tf32_rna(__uint_as_float(x.y));
+    h.z = tf32_rna(__uint_as_float(x.z));
+    h.w = tf32_rna(__uint_as_float(x.w));
+    l.x = tf32_rna(__uint_as_float(x.x) - __uint_as_float(h.x));
+    l.y = tf32_rna(__uint_as_float(x.y) - __uint_as_float(h.y));
+    l.z = tf32_rna(__uint_as_float(x.z) - __uint_as_float(h.z));
+    l.w = tf32_rna(__uint_as_float(x.w) - __uint_as_float(h.w));
+    hi[i] = h;
+    lo[i] = l;
+  }
+}
+
 __global__ void __launch_bounds__(NTHREADS, 1)
     gemm_pk_kernel(const uint8_t* __restrict__ Apk, const uint8_t* __restrict__ Bpk, double alpha,
                    double* __restrict__ C, uint8_t* __restrict__ Cpk, const DTile* __restrict__ tiles, int ntiles,
                    const DGemmTask* __restrict__ tasks, const DPkPair* __restrict__ pairs,
-                   double* __restrict__ partial, int out_packed, int a_single, int* __restrict__ err,
+                   double* __restrict__ partial, int out_packed, int single, int* __restrict__ err,
                    uint64_t timeout_ns) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -240,7 +263,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_slot;
   const uint64_t deadline = global_ns() + timeout_ns;
+  const bool a_single = single & kSingleA, b_single = single & kSingleB;
   const uint32_t a_bytes = a_single ? A1_BYTES : A_BYTES;  // A tile in global memory
+  const uint32_t b_bytes = b_single ? B1_BYTES : B_BYTES;  // B tile in global memory
 
   // Persistent: the CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...; every
   // role walks the same sequence, so slice and pair counters continue across tiles.
@@ -266,7 +291,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // a 64-row tail tile is packed compact: half the bytes; its hi and lo
             // halves (split format) land where the MMA expects a 128-row tile's
             const uint32_t at = t.h64 ? a_bytes / 2 : a_bytes;
-            mbar_expect_tx(fb, at + (t.n64 ? B_BYTES / 2 : B_BYTES));
+            const uint32_t bt = t.n64 ? b_bytes / 2 : b_bytes;  // compact [hi 64 | lo 64] (or FP32 64 rows) on a tail
+            mbar_expect_tx(fb, at + bt);
             const uint32_t dst = smem_u32(ring + s * STAGE_BYTES);
             const uint8_t* asrc = Apk + pr.a_pk + (int64_t)t.tm * pr.nks * a_bytes + (int64_t)ks * at;
             if (t.h64 && !a_single) {
@@ -275,8 +301,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             } else {
               bulk_g2s(dst, asrc, at, fb);
             }
-            const uint32_t bt = t.n64 ? B_BYTES / 2 : B_BYTES;  // compact [hi 64 | lo 64] on a tail
-            bulk_g2s(dst + A_BYTES, Bpk + pr.b_pk + (int64_t)t.tn * pr.nks * B_BYTES + (int64_t)ks * bt, bt, fb);
+            bulk_g2s(dst + A_BYTES, Bpk + pr.b_pk + (int64_t)t.tn * pr.nks * b_bytes + (int64_t)ks * bt, bt, fb);
           }
         }
       }
@@ -327,7 +352,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           for (int ks = 0; ks < nks; ++ks, ++slice) {
             const int s = slice % STAGES;
             const uint32_t round = slice / STAGES;
-            if (!mbar_wait(smem_u32(a_single ? &conv_bar[s] : &full_bar[s]), round & 1u, deadline, &abort_flag)) {
+            if (!mbar_wait(smem_u32(single ? &conv_bar[s] : &full_bar[s]), round & 1u, deadline, &abort_flag)) {
               ok = false;
               break;
             }
@@ -364,8 +389,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       mbar_drain(smem_u32(&drain_bar), 0u, global_ns() + DRAIN_NS);
     }
   } else if (warp == 2 || warp == 3) {
-    // ---------------- converter (FP32 A tiles) ----------------
-    if (a_single) {
+    // ---------------- converter (FP32 A and/or B tiles) ----------------
+    if (single) {
       const int ct = threadIdx.x - 64;
       int slice = 0;
       bool ok = true;
@@ -384,26 +409,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               ok = false;
               break;
             }
-            // element-wise, so the core-matrix layout carries over: hi in place, lo
-            // at the same offset in the second half of the A region
-            uint4* hi = reinterpret_cast<uint4*>(ring + s * STAGE_BYTES);
-            uint4* lo = reinterpret_cast<uint4*>(ring + s * STAGE_BYTES + A_BYTES / 2);
-            const int n16 = static_cast<int>(A1_BYTES / 16) >> (t.h64 ? 1 : 0);  // rows 0-63 only
-#pragma unroll 4
-            for (int i = ct; i < n16; i += CONV_THREADS) {
-              const uint4 x = hi[i];
-              uint4 h, l;
-              h.x = tf32_rna(__uint_as_float(x.x));
-              h.y = tf32_rna(__uint_as_float(x.y));
-              h.z = tf32_rna(__uint_as_float(x.z));
-              h.w = tf32_rna(__uint_as_float(x.w));
-              l.x = tf32_rna(__uint_as_float(x.x) - __uint_as_float(h.x));
-              l.y = tf32_rna(__uint_as_float(x.y) - __uint_as_float(h.y));
-              l.z = tf32_rna(__uint_as_float(x.z) - __uint_as_float(h.z));
-              l.w = tf32_rna(__uint_as_float(x.w) - __uint_as_float(h.w));
-              hi[i] = h;
-              lo[i] = l;
-            }
+            // element-wise, so the core-matrix layout carries over: hi in place, lo at
+            // the same offset in the operand's lo half.  A: the lo half starts half a
+            // 128-row tile in (where the M = 64 MMA reads it too); B: right after the hi
+            // rows, which the wide N = 2 Nt MMA reads as one operand ([B_hi; B_lo]).
+            if (a_single)
+              split_in_place(ring + s * STAGE_BYTES, A_BYTES / 2, static_cast<int>(A1_BYTES / 16) >> (t.h64 ? 1 : 0),
+                             ct);
+            if (b_single)
+              split_in_place(ring + s * STAGE_BYTES + A_BYTES, t.n64 ? B1_BYTES / 2 : B1_BYTES,
+                             static_cast<int>(B1_BYTES / 16) >> (t.n64 ? 1 : 0), ct);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(smem_u32(&conv_bar[s]));
           }
@@ -553,7 +568,7 @@ __global__ void __launch_bounds__(256) pack_kernel(const DPack* __restrict__ pac
                                                    uint8_t* __restrict__ dst) {
   const DPack pk = packs[blockIdx.x];
   const int rows_t = pk.tile_rows;
-  const uint32_t half = (uint32_t)rows_t * BK * 4;
+  const uint32_t half = (uint32_t)rows_t * BK * 4;  // bytes of one half (hi or lo) of the tile
   uint8_t* tile = dst + pk.dst_off;
   const int r0 = pk.tr * rows_t, k0 = pk.tk * BK;
   for (int e = threadIdx.x; e < rows_t * BK; e += blockDim.x) {
@@ -569,10 +584,14 @@ __global__ void __launch_bounds__(256) pack_kernel(const DPack* __restrict__ pac
     double v = 0.0;
     if (gr < pk.rows && gk < pk.k)
       v = pk.trans ? src[pk.src_off + (int64_t)gk * pk.ld + gr] : src[pk.src_off + (int64_t)gr * pk.ld + gk];
-    uint32_t h, l;
-    split2(v, h, l);
-    *reinterpret_cast<uint32_t*>(tile + core_off(r, kk)) = h;
-    *reinterpret_cast<uint32_t*>(tile + half + core_off(r, kk)) = l;
+    if (pk.fp32) {
+      *reinterpret_cast<float*>(tile + core_off(r, kk)) = static_cast<float>(v);
+    } else {
+      uint32_t h, l;
+      split2(v, h, l);
+      *reinterpret_cast<uint32_t*>(tile + core_off(r, kk)) = h;
+      *reinterpret_cast<uint32_t*>(tile + half + core_off(r, kk)) = l;
+    }
   }
 }
 
@@ -601,7 +620,7 @@ int pk_smem_bytes() { return SMEM_BYTES; }
 
 void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
-                    int out_packed, int a_single, int* err, cudaStream_t st, uint64_t timeout_ns) {
+                    int out_packed, int single, int* err, cudaStream_t st, uint64_t timeout_ns) {
   if (ntiles <= 0) return;
   static int nsm = 0;
   if (nsm == 0) {
@@ -614,7 +633,7 @@ void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double
   // one persistent CTA per SM; the bound covers the whole launch, not one tile
   const int grid = ntiles < nsm ? ntiles : nsm;
   gemm_pk_kernel<<<grid, NTHREADS, SMEM_BYTES, st>>>(Apk, Bpk, alpha, C, Cpk, tiles, ntiles, tasks, pairs, partial,
-                                                     out_packed, a_single, err, timeout_ns);
+                                                     out_packed, single, err, timeout_ns);
 }
 
 void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst, cudaStream_t st) {

@@ -95,15 +95,20 @@ def test_split_sigma_tail_tiles_are_exercised(ctx):
     assert stats["tiles_64col_tail"] < stats["tiles_stage1"] + stats["tiles_stage2"]
     s64, s32 = sigma_both(ctx, mL, mR, psi)
     assert rel_err(s32, s64) < 2e-6
-    # every schedule on these tiles: FP32 intermediate in one pass, w groups in both formats
-    for schedule in ((0, 152 * 8, True), (1 << 20, 0, True), (1 << 20, 0, False)):
-        ctx.set_sigma_schedule(*schedule)
-        try:
-            _, s = sigma_both(ctx, mL, mR, psi)
-        finally:
-            ctx.set_sigma_schedule(-1)
-        print("schedule", schedule, rel_err(s, s64))
-        assert rel_err(s, s64) < 2e-6
+    # every schedule on these tiles: FP32 intermediate in one pass, w groups in both
+    # formats; the merged operators as FP32 tiles split on chip (the default) and as
+    # pre-split hi|lo tiles
+    for fp32_ops in (True, False):
+        ctx.set_sigma_operator_format(fp32_ops)
+        for schedule in ((0, 152 * 8, True), (0, 152 * 8, False), (1 << 20, 0, True), (1 << 20, 0, False)):
+            ctx.set_sigma_schedule(*schedule)
+            try:
+                _, s = sigma_both(ctx, mL, mR, psi)
+            finally:
+                ctx.set_sigma_schedule(-1)
+            print("fp32 operators", fp32_ops, "schedule", schedule, rel_err(s, s64))
+            assert rel_err(s, s64) < 2e-6
+    ctx.set_sigma_operator_format(True)
 
 
 def test_split_davidson_refined_energy_matches_fp64(ctx):
@@ -195,13 +200,15 @@ def test_split_renormalize_matches_fp64_qc_bond(ctx):
         assert err < 2e-6
 
 
+@pytest.mark.parametrize("fp32_ops", [True, False])
 @pytest.mark.parametrize("schedule", [(0, 152 * 4, False), (256 * 1024, 0, False), (4 * 1024 * 1024, 152 * 2, False),
                                       (0, 152 * 8, True), (256 * 1024, 0, True)])
-def test_split_sigma_schedules_agree(ctx, schedule):
+def test_split_sigma_schedules_agree(ctx, schedule, fp32_ops):
     """Every schedule of the split H_eff*psi (one pass over w with different split-K
     targets, and w processed in groups out of an L2-sized scratch, through the CUDA
-    graph; the L*psi intermediate as hi|lo tiles or as FP32 tiles split on chip) gives
-    the same result as FP64 within 2e-6."""
+    graph; the L*psi intermediate as hi|lo tiles or as FP32 tiles split on chip; the
+    merged operators as FP32 tiles split on chip or as hi|lo tiles) gives the same
+    result as FP64 within 2e-6."""
     from mpsxx_gb300 import core, dmrg, mpogen
 
     h, eri = mpogen.synthetic_qc_integrals(8, 16, 5)
@@ -209,6 +216,7 @@ def test_split_sigma_schedules_agree(ctx, schedule):
     st = dmrg.make_random_state(ctx, mpo, 8, 0, 128, seed=4)
     dmrg.advance_left(ctx, st, 3)
     mL, mR, psi = dmrg.bond_operands(ctx, st, 3)
+    ctx.set_sigma_operator_format(fp32_ops)
     ctx.set_sigma_schedule(*schedule)
     try:
         s64, s32 = sigma_both(ctx, mL, mR, psi)
@@ -219,6 +227,7 @@ def test_split_sigma_schedules_agree(ctx, schedule):
         core.set_precision(ctx, core.FP64)
     finally:
         ctx.set_sigma_schedule(-1)
+        ctx.set_sigma_operator_format(True)
     err = rel_err(s32, s64)
     print("schedule", schedule, "split-vs-fp64 rel err", err)
     assert err < 2e-6
