@@ -56,8 +56,8 @@ def parse():
                          "library's MPO generator, a seeded random MPS")
     ap.add_argument("--bond-structure", default="", help="bond structure file of the c2-bond workload")
     ap.add_argument("--no-bond-e2e", action="store_true", help="skip the bond step from host site tensors")
-    ap.add_argument("--hilo-operators", action="store_true",
-                    help="pack the merged operators as hi|lo TF32 tiles (default: FP32 tiles split on chip)")
+    ap.add_argument("--fp32-operators", action="store_true",
+                    help="pack the merged operators as FP32 tiles split on chip (default: hi|lo TF32 tiles)")
     ap.add_argument("--norb", type=int, default=20)
     ap.add_argument("--nchol", type=int, default=40)
     ap.add_argument("--M", type=int, default=512)
@@ -731,7 +731,7 @@ def main():
     from mpsxx_gb300._lib import lib
 
     ctx = core.Context(local)
-    ctx.set_sigma_operator_format(not args.hilo_operators)
+    ctx.set_sigma_operator_format(args.fp32_operators)
     wl = build_workload(args, ctx)
     mL, mR, psi = wl["mL"], wl["mR"], wl["psi"]
 
@@ -869,7 +869,7 @@ def main():
                        "D_cols": sum(psi.shape()[1][1]), "nnz_psi": psi.nnz, "nnz_L": mL.nnz, "nnz_R": mR.nnz,
                        "flops_per_step": fl_per_step, "l2": l2, "parallelism": f"replicas{ws}",
                        "precision": args.precision,
-                       "operators": "hi|lo TF32 tiles" if args.hilo_operators else "FP32 tiles split on chip"},
+                       "operators": "FP32 tiles split on chip" if args.fp32_operators else "hi|lo TF32 tiles"},
             "gpu_launches": int(launches),
             "e2e": {"value": job_tflops(ws, fl_per_step, e2e_s), "unit": "TFLOP/s", "ms_per_step": e2e_s * 1e3,
                     "h2d_bytes_per_step": 8 * psi.nnz, "d2h_bytes_per_step": 8 * psi.nnz},

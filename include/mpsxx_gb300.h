@@ -111,11 +111,12 @@ int mpsxx_context_tuning(const mpsxx_context* ctx, double* out, int n, int* coun
  * tiles (0).  w_budget_bytes < 0 restores autotuning.  Cached plans are dropped. */
 int mpsxx_context_set_sigma_schedule(mpsxx_context* ctx, int64_t w_budget_bytes, int target_tiles,
                                      int fp32_intermediate);
-/* Storage of the merged operators for the split-precision H_eff*psi: FP32 tiles that
- * the tensor-core kernel splits into hi|lo TF32 in shared memory (fp32_operators = 1,
- * the default: half the HBM bytes per application) or pre-split hi|lo TF32 tiles (0).
- * Either way x = hi + lo to ~2^-22 relative.  Applies to plans made afterwards; cached
- * plans are dropped. */
+/* Storage of the merged operators for the split-precision H_eff*psi: pre-split hi|lo
+ * TF32 tiles (fp32_operators = 0, the default) or FP32 tiles that the tensor-core
+ * kernel splits into hi|lo in shared memory (1: half the packed bytes, for operators
+ * that would not fit otherwise; slower, as the on-chip split of both operands costs
+ * shared-memory bandwidth).  Either way x = hi + lo to ~2^-22 relative.  Applies to
+ * plans made afterwards; cached plans are dropped. */
 int mpsxx_context_set_sigma_operator_format(mpsxx_context* ctx, int fp32_operators);
 /* Routing of canonicalize's per-block SVDs: blocks with min(m, n) <= jacobi_max_cols
  * (at most 128) go to the batched one-sided Jacobi kernel; of the rest, blocks whose

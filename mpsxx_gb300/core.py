@@ -56,9 +56,10 @@ class Context:
         check(lib().mpsxx_context_set_sigma_schedule(self.h, int(w_budget_bytes), int(target_tiles),
                                                      int(bool(fp32_intermediate))))
 
-    def set_sigma_operator_format(self, fp32_operators: bool = True):
-        """Merged operators of the split H_eff*psi packed as FP32 tiles split on chip
-        (default) or as hi|lo TF32 tiles; applies to plans made afterwards."""
+    def set_sigma_operator_format(self, fp32_operators: bool = False):
+        """Merged operators of the split H_eff*psi packed as hi|lo TF32 tiles (default)
+        or as FP32 tiles split on chip (half the bytes, slower); applies to plans made
+        afterwards."""
         check(lib().mpsxx_context_set_sigma_operator_format(self.h, int(bool(fp32_operators))))
 
     def set_device_timeout(self, timeout_ns: int = 0):

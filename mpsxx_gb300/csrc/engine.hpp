@@ -314,8 +314,10 @@ struct Context {
   int sigma_target_tiles = 0;
   bool sigma_fp32_intermediate = false;  // with a forced schedule: FP32 L*psi tiles
   // split-precision H_eff*psi: merged operators packed as FP32 tiles (split into hi|lo
-  // on chip) instead of hi|lo TF32 tiles; applies to plans made afterwards
-  bool sigma_fp32_operators = true;
+  // on chip: half the packed bytes, but the on-chip split of both operands makes the
+  // kernel slower, 1.93 vs 1.56 ms at the C2 middle bond) instead of hi|lo TF32 tiles;
+  // applies to plans made afterwards
+  bool sigma_fp32_operators = false;
   uint64_t device_timeout_ns = kPkTimeoutNs;  // wait limit of the tensor-core kernels
   // canonicalize routing: blocks with min(m, n) <= svd_jacobi_cols go to the batched
   // Jacobi kernel, the rest with a Gram dimension <= svd_gram_max to the batched

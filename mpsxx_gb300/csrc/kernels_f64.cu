@@ -3,7 +3,8 @@
 //
 // GB300 (sm_103a) has a very small FP64 pipe, so the FP64 path is FMA-bound on
 // CUDA cores: a 64x64 output tile per 256-thread CTA, 4x4 register micro-tiles,
-// operands staged through shared memory in 16-deep K slices.  Every output tile
+// operands staged through shared memory in 16-deep K slices; warps whose 16x32 band
+// of the tile lies outside a ragged block skip their FMAs.  Every output tile
 // is owned by exactly one CTA and its (A,B) pairs are accumulated in enumeration
 // order, so results are deterministic run to run.
 #include <cuda_runtime.h>
@@ -20,7 +21,7 @@ constexpr int TM = kGemmTile;
 constexpr int TN = kGemmTile;
 constexpr int TK = 16;
 
-__global__ void __launch_bounds__(256) gemm_f64_kernel(int transa, int transb, double alpha,
+__global__ void __launch_bounds__(256, 2) gemm_f64_kernel(int transa, int transb, double alpha,
                                                        const double* __restrict__ A, const double* __restrict__ B,
                                                        double* __restrict__ C, const DTile* __restrict__ tiles,
                                                        const DGemmTask* __restrict__ tasks,
@@ -31,7 +32,14 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(int transa, int transb, d
   const DTile t = tiles[blockIdx.x];
   const DGemmTask task = tasks[t.task];
   const int m0 = t.tm * TM, n0 = t.tn * TN;
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  // Warp w owns a 16-row x 32-column band of the tile (rows 16 (w & 3) + ..., columns
+  // 32 (w >> 2) + ...); its lanes hold 4x4 micro-tiles with rows and columns strided by
+  // 4 and 8.  A band that lies wholly outside the block (a ragged block's last tile)
+  // skips its FMAs: the FP64 pipe, GB300's narrowest, does only useful work there.
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rb = 16 * (warp & 3), cb = 32 * (warp >> 2);
+  const int ty = lane >> 3, tx = lane & 7;
+  const bool live = (m0 + rb < task.m) && (n0 + cb < task.n);
   double acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -72,17 +80,34 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(int transa, int transb, d
         Bs[kk][c] = v;
       }
       __syncthreads();
+      if (live) {
+        const int kn = pr.k - k0 < TK ? pr.k - k0 : TK;  // zero-padded K steps are skipped too
+        if (kn == TK) {
 #pragma unroll
-      for (int kk = 0; kk < TK; ++kk) {
-        double a[4], b[4];
+          for (int kk = 0; kk < TK; ++kk) {
+            double a[4], b[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][rb + ty + 4 * i];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][cb + tx + 8 * j];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+              for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          }
+        } else {
+          for (int kk = 0; kk < kn; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][rb + ty + 4 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][cb + tx + 8 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          }
+        }
       }
       __syncthreads();
     }
@@ -93,16 +118,17 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(int transa, int transb, d
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) part[(ty + 16 * i) * TN + tx + 16 * j] = acc[i][j];
+      for (int j = 0; j < 4; ++j) part[(rb + ty + 4 * i) * TN + cb + tx + 8 * j] = acc[i][j];
     return;
   }
+  if (!live) return;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const int r = m0 + ty + 16 * i;
+    const int r = m0 + rb + ty + 4 * i;
     if (r >= task.m) continue;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int c = n0 + tx + 16 * j;
+      const int c = n0 + cb + tx + 8 * j;
       if (c >= task.n) continue;
       double* dst = C + task.c_off + (int64_t)r * task.ldc + c;
       *dst += alpha * acc[i][j];
@@ -265,36 +291,46 @@ __global__ void copy_vec_kernel(double* y, const double* x, int64_t n) {
 
 
 // Each CTA reduces a contiguous chunk into partial[blk][i*ny+j]; a fixed-order
-// second pass makes the sum deterministic.
+// second pass makes the sum deterministic.  The chunk is walked in tiles of
+// kDotTile elements staged in shared memory (all nx + ny vectors, coalesced loads);
+// each of the nx*ny products is owned by g = 256 / (nx*ny) threads that sum fixed
+// strided parts of the tile in registers, and the g partial sums of a product are
+// added in thread order at the end — no per-thread arrays indexed at run time.
+constexpr int kDotTile = 128;
 __global__ void __launch_bounds__(256) multidot_partial_kernel(const double* __restrict__ X, int nx,
                                                                const double* __restrict__ Y, int ny, int64_t n,
                                                                int64_t stride, double* __restrict__ partial) {
-  __shared__ double red[8][kMaxDot * kMaxDot];
-  double acc[kMaxDot * kMaxDot];
+  __shared__ double xs[kMaxDot][kDotTile];
+  __shared__ double ys[kMaxDot][kDotTile];
+  __shared__ double red[256];
   const int np = nx * ny;
-  for (int q = 0; q < np; ++q) acc[q] = 0.0;
+  const int g = 256 / np;  // threads per product (>= 2 for np <= 100)
+  const int t = threadIdx.x;
+  const int q = t / g, sub = t % g;
+  const bool active = q < np;
+  const int qi = active ? q / ny : 0, qj = active ? q % ny : 0;
+  double acc = 0.0;
   const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
   const int64_t lo = blockIdx.x * chunk;
   const int64_t hi = lo + chunk < n ? lo + chunk : n;
-  for (int64_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
-    double xv[kMaxDot];
-    for (int i = 0; i < nx; ++i) xv[i] = X[i * stride + e];
-    for (int j = 0; j < ny; ++j) {
-      const double yv = Y[j * stride + e];
-      for (int i = 0; i < nx; ++i) acc[i * ny + j] = fma(xv[i], yv, acc[i * ny + j]);
+  for (int64_t e0 = lo; e0 < hi; e0 += kDotTile) {
+    const int len = hi - e0 < kDotTile ? static_cast<int>(hi - e0) : kDotTile;
+    __syncthreads();  // the previous tile is consumed
+    for (int v = 0; v < nx + ny; ++v) {
+      const double* src = v < nx ? X + v * stride : Y + (v - nx) * stride;
+      double* dst = v < nx ? xs[v] : ys[v - nx];
+      for (int k = t; k < len; k += 256) dst[k] = src[e0 + k];
     }
+    __syncthreads();
+    if (active)
+      for (int k = sub; k < len; k += g) acc = fma(xs[qi][k], ys[qj][k], acc);
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = 0; q < np; ++q) {
-    double v = acc[q];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp][q] = v;
-  }
+  red[t] = acc;
   __syncthreads();
-  if (threadIdx.x < np) {
+  if (active && sub == 0) {
     double v = 0.0;
-    for (int w = 0; w < 8; ++w) v += red[w][threadIdx.x];
-    partial[blockIdx.x * (kMaxDot * kMaxDot) + threadIdx.x] = v;
+    for (int k = 0; k < g; ++k) v += red[t + k];
+    partial[blockIdx.x * (kMaxDot * kMaxDot) + q] = v;
   }
 }
 
@@ -307,14 +343,22 @@ __global__ void multidot_final_kernel(const double* __restrict__ partial, int nb
   out[q] = v;
 }
 
+// V[:, j] = sum_i V[:, i] R[i, j] for j < m, in place per element (loops unrolled to
+// kMaxDot so that the element's m values stay in registers).
 __global__ void rotate_kernel(double* V, int m, int64_t n, int64_t stride, const double* __restrict__ R, int ldr) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     double old[kMaxDot];
-    for (int i = 0; i < m; ++i) old[i] = V[i * stride + e];
-    for (int j = 0; j < m; ++j) {
-      double v = 0.0;
-      for (int i = 0; i < m; ++i) v = fma(R[i * ldr + j], old[i], v);
-      V[j * stride + e] = v;
+#pragma unroll
+    for (int i = 0; i < kMaxDot; ++i) old[i] = i < m ? V[i * stride + e] : 0.0;
+#pragma unroll
+    for (int j = 0; j < kMaxDot; ++j) {
+      if (j < m) {
+        double v = 0.0;
+#pragma unroll
+        for (int i = 0; i < kMaxDot; ++i)
+          if (i < m) v = fma(R[i * ldr + j], old[i], v);
+        V[j * stride + e] = v;
+      }
     }
   }
 }

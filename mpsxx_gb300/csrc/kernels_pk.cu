@@ -264,6 +264,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const uint32_t tmem = tmem_slot;
   const uint64_t deadline = global_ns() + timeout_ns;
   const bool a_single = single & kSingleA, b_single = single & kSingleB;
+  const int conv = single & (kSingleA | kSingleB);
   const uint32_t a_bytes = a_single ? A1_BYTES : A_BYTES;  // A tile in global memory
   const uint32_t b_bytes = b_single ? B1_BYTES : B_BYTES;  // B tile in global memory
 
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           for (int ks = 0; ks < nks; ++ks, ++slice) {
             const int s = slice % STAGES;
             const uint32_t round = slice / STAGES;
-            if (!mbar_wait(smem_u32(single ? &conv_bar[s] : &full_bar[s]), round & 1u, deadline, &abort_flag)) {
+            if (!mbar_wait(smem_u32(conv ? &conv_bar[s] : &full_bar[s]), round & 1u, deadline, &abort_flag)) {
               ok = false;
               break;
             }
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
   } else if (warp == 2 || warp == 3) {
     // ---------------- converter (FP32 A and/or B tiles) ----------------
-    if (single) {
+    if (conv) {
       const int ct = threadIdx.x - 64;
       int slice = 0;
       bool ok = true;

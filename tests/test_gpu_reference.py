@@ -15,7 +15,7 @@ import pytest
 from oracle import ref_io
 
 REF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref")
-BOND_KEYS = sorted({k.split("/")[0] for k in np.load(os.path.join(REF, "bonds.npz")).files})
+BOND_KEYS = sorted(k[: -len("/meta")] for k in np.load(os.path.join(REF, "bonds.npz")).files if k.endswith("/meta"))
 
 
 def rel_diff(a: dict, b: dict) -> float:

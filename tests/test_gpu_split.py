@@ -96,8 +96,8 @@ def test_split_sigma_tail_tiles_are_exercised(ctx):
     s64, s32 = sigma_both(ctx, mL, mR, psi)
     assert rel_err(s32, s64) < 2e-6
     # every schedule on these tiles: FP32 intermediate in one pass, w groups in both
-    # formats; the merged operators as FP32 tiles split on chip (the default) and as
-    # pre-split hi|lo tiles
+    # formats; the merged operators as pre-split hi|lo tiles (the default) and as FP32
+    # tiles split on chip
     for fp32_ops in (True, False):
         ctx.set_sigma_operator_format(fp32_ops)
         for schedule in ((0, 152 * 8, True), (0, 152 * 8, False), (1 << 20, 0, True), (1 << 20, 0, False)):
@@ -108,7 +108,7 @@ def test_split_sigma_tail_tiles_are_exercised(ctx):
                 ctx.set_sigma_schedule(-1)
             print("fp32 operators", fp32_ops, "schedule", schedule, rel_err(s, s64))
             assert rel_err(s, s64) < 2e-6
-    ctx.set_sigma_operator_format(True)
+    ctx.set_sigma_operator_format(False)
 
 
 def test_split_davidson_refined_energy_matches_fp64(ctx):
@@ -227,7 +227,7 @@ def test_split_sigma_schedules_agree(ctx, schedule, fp32_ops):
         core.set_precision(ctx, core.FP64)
     finally:
         ctx.set_sigma_schedule(-1)
-        ctx.set_sigma_operator_format(True)
+        ctx.set_sigma_operator_format(False)
     err = rel_err(s32, s64)
     print("schedule", schedule, "split-vs-fp64 rel err", err)
     assert err < 2e-6
