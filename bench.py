@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--no-bond-e2e", action="store_true", help="skip the bond step from host site tensors")
     ap.add_argument("--fp32-operators", action="store_true",
                     help="pack the merged operators as FP32 tiles split on chip (default: hi|lo TF32 tiles)")
+    ap.add_argument("--mpo", default="comp", choices=["comp", "mvc"],
+                    help="QC MPO of the sweeps and of random-mps: comp = the reference generator's complementary "
+                         "operators (restated), mvc = this library's vertex-cover construction")
     ap.add_argument("--norb", type=int, default=20)
     ap.add_argument("--nchol", type=int, default=40)
     ap.add_argument("--M", type=int, default=512)
@@ -266,7 +269,7 @@ def workload_name(args) -> str:
         return (f"H_eff*psi at the middle bond (9,10) of C2: qc n=20 K=40 seed=1 M=512, the reference's "
                 f"complementary-operator MPO sites (W=862), converged-state block structure, values seed {args.seed}")
     return (f"H_eff*psi at bond ({args.bond if args.bond >= 0 else args.norb // 2 - 1},+1): qc n={args.norb} "
-            f"K={args.nchol} seed={args.seed}, this library's MPO generator, seeded random MPS M={args.M}")
+            f"K={args.nchol} seed={args.seed}, {MPO_NAMES[args.mpo]}, seeded random MPS M={args.M}")
 
 
 def build_workload(args, ctx):
@@ -285,7 +288,7 @@ def build_workload(args, ctx):
     from mpsxx_gb300 import dmrg, mpogen
 
     h1, eri = mpogen.synthetic_qc_integrals(args.norb, args.nchol, args.seed)
-    mpo_d = mpogen.qc_mpo(h1, eri)
+    mpo_d = qc_mpo_of(args, h1, eri)
     mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
     st = dmrg.make_random_state(ctx, mpo, args.norb, 0, args.M, seed=args.seed)
     bond = args.bond if args.bond >= 0 else args.norb // 2 - 1
@@ -325,6 +328,20 @@ def sigma_checksum(blocks) -> dict:
     return {"sum": s, "norm": n, "blocks": len(blocks)}
 
 
+MPO_NAMES = {"comp": "complementary-operator MPO (the reference generator's scheme, restated)",
+             "mvc": "this library's minimum-vertex-cover MPO"}
+
+
+def qc_mpo_of(args, h1, eri):
+    """The QC MPO of the chosen construction: the reference generator's complementary
+    operators (default) or this library's vertex-cover construction."""
+    from mpsxx_gb300 import mpogen, mpogen_comp
+
+    if args.mpo == "comp":
+        return mpogen_comp.qc_mpo_complementary(h1, eri)
+    return mpogen.qc_mpo(h1, eri)
+
+
 def sweep_schedule(args):
     """Bond dimension per sweep: ramped to sweep_M (two sweeps at M/4, two at M/2), then
     sweep_M for the rest of sweep_max sweeps."""
@@ -350,8 +367,9 @@ def sweep_compare(args, device: int):
     n = args.sweep_norb
     sched = sweep_schedule(args)
     h1, eri = mpogen.synthetic_qc_integrals(n, 2 * n, args.seed)
-    mpo_d = mpogen.qc_mpo(h1, eri)
-    res = {"workload": f"qc n={n} K={2 * n} seed={args.seed}, this library's MPO generator", "tole": args.tole,
+    mpo_d = qc_mpo_of(args, h1, eri)
+    res = {"workload": f"qc n={n} K={2 * n} seed={args.seed}, {MPO_NAMES[args.mpo]}", "tole": args.tole,
+           "mpo_bond_dims": mpogen.mpo_bond_dims(mpo_d),
            "M_schedule": sched, "start": "reference initial state (constant-filled sites)"}
     arms = [("fp64", core.FP64, args.tole), ("split", core.SPLIT_TF32, args.tole)]
     if not args.no_sweep_control:

@@ -95,23 +95,25 @@ def test_bond_operations_equal_the_reference(ctx, key):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["c1", "qc8"])
+@pytest.mark.parametrize("case", ["c1", "qc8", "qc8_comp"])
 def test_sweep_energies_equal_the_reference(ctx, case):
     """Two-site DMRG on the device from the reference's initial state against the
     reference's own sweep energies (dmrg.x): C1 (Hubbard L=12, t=1, U=4, half filling,
     M=64, tole 1e-10, 4 sweeps) and the synthetic QC n=8 Hamiltonian (K=16, seed 1,
-    M=64, tole 1e-9, 3 sweeps).  The first sweeps stop Davidson runs on the reference's
-    iteration cap, where summation order moves the stopping point (bound 1e-7); from
-    sweep 2 (C1) and throughout (QC n=8) within 1e-9 Eh."""
-    from mpsxx_gb300 import core, dmrg, mpogen
+    M=64, tole 1e-9, 3 sweeps), the latter under this library's MPO and under the
+    reference's own complementary-operator MPO (the restated generator: the same
+    operator the reference swept).  The first sweeps stop Davidson runs on the
+    reference's iteration cap, where summation order moves the stopping point (bound
+    1e-7); from sweep 2 (C1) and throughout (QC n=8) within 1e-9 Eh."""
+    from mpsxx_gb300 import core, dmrg, mpogen, mpogen_comp
 
     with open(os.path.join(REF, "runs.json")) as f:
-        r = json.load(f)[case]
+        r = json.load(f)["qc8" if case == "qc8_comp" else case]
     if case == "c1":
         mpo_d = mpogen.hubbard_mpo(r["N"], -1.0, 4.0)
     else:
         h1, eri = mpogen.synthetic_qc_integrals(8, 16, 1)
-        mpo_d = mpogen.qc_mpo(h1, eri)
+        mpo_d = mpogen_comp.qc_mpo_complementary(h1, eri) if case == "qc8_comp" else mpogen.qc_mpo(h1, eri)
     core.set_precision(ctx, core.FP64)
     mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
     st = dmrg.make_initial_state(ctx, mpo, r["elec"], 0, r["M"])
