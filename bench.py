@@ -435,7 +435,10 @@ def gradient_bench(args, device: int):
     (L=32, U_i ~ U(2,6), |t_i| ~ U(0.8,1.2), half filling, M=512) and dE/dh_pq of the
     n=16 synthetic QC Hamiltonian (M=256).  Gradient in FP64 and split precision on
     the same converged state, environments checkpointed every 4 sites; a few
-    parameters checked by central differences (step 1e-4) of warm-restarted DMRG."""
+    parameters checked by central differences (step 1e-4) of the energy, both of
+    warm-restarted DMRG (the state re-converged: the derivative of the truncated
+    problem's energy) and of the converged state held fixed (<psi|H(theta +- h)|psi>:
+    what the adjoint computes, by Hellmann-Feynman)."""
     import numpy as np
 
     from mpsxx_gb300 import core, dmrg, mpogen
@@ -477,7 +480,7 @@ def gradient_bench(args, device: int):
                                           for k in keys)
         fd_rows = []
         for par in checks[: args.grad_fd]:
-            vals = []
+            vals, fixed = [], []
             for sgn in (1.0, -1.0):
                 th = [np.array(x, copy=True) for x in theta]
                 if par[0] == "U":
@@ -492,14 +495,18 @@ def gradient_bench(args, device: int):
                 sites2, _ = build(th)
                 mpo2 = [core.Tensor.from_dict(ctx, d) for d in sites2]
                 st2 = dmrg.restart_state(ctx, mpo2, st)
+                # the converged state's energy under the stepped Hamiltonian (state held)
+                fixed.append(dmrg.gradient_sweep(ctx, st2, checkpoint=4).energy)
                 st2, _, _ = _converge(ctx, mpo2, nel, M, tole * 0.1, 8, st2)
                 vals.append(dmrg.gradient_sweep(ctx, st2, checkpoint=4).energy)
             fd = (vals[0] - vals[1]) / 2e-4
+            fd_fixed = (fixed[0] - fixed[1]) / 2e-4
             adj = grads["fp64"].get(par, 0.0)
             if par[0] == "h" and par[1] != par[2]:
                 adj += grads["fp64"].get(("h", par[2], par[1]), 0.0)
             fd_rows.append({"param": list(map(str, par)), "adjoint": adj, "fd": fd,
-                            "rel": abs(adj - fd) / max(1.0, abs(fd))})
+                            "rel": abs(adj - fd) / max(1.0, abs(fd)), "fd_state_held": fd_fixed,
+                            "rel_state_held": abs(adj - fd_fixed) / max(1.0, abs(fd_fixed))})
         res["fd_checks"] = fd_rows
         out[name] = res
         del st, mpo
