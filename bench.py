@@ -39,10 +39,12 @@ METRIC = "H_eff*psi TFLOP/s (FP64-equivalent), C2 middle bond: qc n=20 M=512"
 DATA = ("synthetic: the reference generator's MPO sites of the seeded n=20 integrals, a converged state's block "
         "structure, seeded normal block values")
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over the launches of one
-# H_eff*psi) divided by the algorithmic bytes 8 (nnz L + nnz R + 2 nnz psi), measured by
-# ncu on the small case of the same kernels; keyed by (workload, precision).
-MEASURED_TRAFFIC = {}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over the two tensor-core
+# launches of one H_eff*psi) divided by the algorithmic bytes 8 (nnz L + nnz R + 2 nnz
+# psi), measured by ncu on the small case of the same kernels (QC n=14, K=28, M=256:
+# 1.129 GB against 0.413 GB) and applied to the bench workloads, whose operators are
+# too large for a multi-metric capture; keyed by (workload, precision).
+MEASURED_TRAFFIC = {("c2-bond", "split"): 2.73, ("random-mps", "split"): 2.73}
 
 
 def parse():
