@@ -510,7 +510,7 @@ static void tile_tc(GemmPlan& plan, int target_ctas) {
   make_tiles(plan, kTcTileM, kTcTileN, plan.h_tiles_tc, plan.h_reduce_tc, plan.nslots_tc, target_ctas);
   for (DTile& t : plan.h_tiles_tc) {
     t.h64 = tail64(plan.h_tasks[t.task].m, t.tm) ? 1 : 0;
-    t.n64 = tail64(plan.h_tasks[t.task].n, t.tn) ? 1 : 0;
+    t.nt = tail_cols(plan.h_tasks[t.task].n, t.tn);
   }
   std::vector<std::pair<int64_t, int>> work(plan.h_tiles_tc.size());
   for (size_t i = 0; i < plan.h_tiles_tc.size(); ++i) {
@@ -703,16 +703,23 @@ struct Orient {
 
 // Packed tile grid of an operand: per block, row tiles x K slices, row tile tr slice tk
 // at base + (tr * nks + tk) * tile_bytes.  Tensor-core operands (128-row tiles) end in
-// a compact 64-row tile where tail64 says so: its slices at base + tr * nks *
-// tile_bytes + tk * tile_bytes / 2 (the pack kernel gets tile_rows 64 and row tile
-// 2 tr, which starts at the same row).
+// a compact tile: A operands (role 'A') in a 64-row tile where tail64 says so, B
+// operands (role 'B') in a tile of tail_cols rows; the compact tile's slices sit at
+// base + tr * nks * tile_bytes + tk * (its bytes per slice).
 template <class F>
-static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t tile_bytes, F orient, int fp32 = 0) {
+static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t tile_bytes, F orient, int fp32 = 0,
+                          char role = 'A') {
   P.base.assign(t.tags.size(), -1);
   P.nks.assign(t.tags.size(), 0);
   P.h_packs.clear();
   const bool tailed = tile_rows == 128;
   int64_t off = 0;
+  // rows of row tile tr of a block of `rows` rows
+  auto rows_of = [&](int rows, int tr) {
+    if (!tailed) return tile_rows;
+    if (role == 'B') return tail_cols(rows, tr);
+    return tail64(rows, tr) ? 64 : tile_rows;
+  };
   for (size_t b = 0; b < t.tags.size(); ++b) {
     const Orient o = orient(static_cast<int32_t>(b));
     if (o.rows <= 0 || o.k <= 0) continue;
@@ -721,18 +728,14 @@ static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t ti
     P.base[b] = off;
     P.nks[b] = nks;
     for (int tr = 0; tr < ntr; ++tr) {
-      const bool t64 = tailed && tail64(o.rows, tr);
-      for (int tk = 0; tk < nks; ++tk) {
-        if (t64)
-          P.h_packs.push_back(DPack{t.offsets[b], off + int64_t(tr) * nks * tile_bytes + int64_t(tk) * (tile_bytes / 2),
-                                    o.rows, o.k, o.ld, o.trans, 64, 2 * tr, tk, fp32});
-        else
-          P.h_packs.push_back(DPack{t.offsets[b], off + (int64_t(tr) * nks + tk) * tile_bytes, o.rows, o.k, o.ld,
-                                    o.trans, tile_rows, tr, tk, fp32});
-      }
+      const int rt = rows_of(o.rows, tr);
+      const int64_t slice = int64_t(tile_bytes) * rt / tile_rows;
+      for (int tk = 0; tk < nks; ++tk)
+        P.h_packs.push_back(DPack{t.offsets[b], off + int64_t(tr) * nks * tile_bytes + int64_t(tk) * slice, o.rows,
+                                  o.k, o.ld, o.trans, rt, tr * tile_rows, tk, fp32});
     }
-    const bool last64 = tailed && tail64(o.rows, ntr - 1);
-    off += int64_t(ntr - (last64 ? 1 : 0)) * nks * tile_bytes + (last64 ? int64_t(nks) * (tile_bytes / 2) : 0);
+    const int rl = rows_of(o.rows, ntr - 1);
+    off += int64_t(ntr - 1) * nks * tile_bytes + int64_t(nks) * (int64_t(tile_bytes) * rl / tile_rows);
   }
   P.bytes = off;
 }
@@ -750,7 +753,7 @@ static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Te
     int d[kMaxRank];
     dims3(psi, b, d);
     return Orient{d[1], d[0], d[1], 1};
-  });
+  }, 0, 'B');
   // stage-1 output = stage-2 A operand: scr1 block (dA x dB')
   // written by stage 1 and read once by stage 2: hi|lo tiles, or FP32 tiles split on chip
   packed_layout(p.pk_scr1, p.scr1, kTcTileM, p.scr1_single ? kPkTileA1Bytes : kPkTileABytes, [&](int32_t b) {
@@ -763,7 +766,7 @@ static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Te
     int d[kMaxRank];
     dims3(R, b, d);
     return Orient{d[0] * d[1], d[2], d[2], 0};
-  }, p.ops_single ? 1 : 0);
+  }, p.ops_single ? 1 : 0, 'B');
   auto pairs_of = [](const GemmPlan& g, const Packed& A, const Packed& B, std::vector<DPkPair>& out) {
     out.resize(g.h_pairs.size());
     for (size_t i = 0; i < g.h_pairs.size(); ++i) {
@@ -821,7 +824,7 @@ static void build_split_gemm(Context& ctx, SplitGemm& sg, const GemmPlan& g, con
     }
   }
   packed_layout(sg.pa, a, kTcTileM, kPkTileABytes, [&](int32_t s) { return oa[s]; });
-  packed_layout(sg.pb, b, kTcTileN, kPkTileBBytes, [&](int32_t s) { return ob[s]; });
+  packed_layout(sg.pb, b, kTcTileN, kPkTileBBytes, [&](int32_t s) { return ob[s]; }, 0, 'B');
   sg.h_pk.resize(g.h_pairs.size());
   for (size_t i = 0; i < g.h_pairs.size(); ++i) {
     const int32_t as = g.pair_a_slot[i], bs = g.pair_b_slot[i];
@@ -965,12 +968,12 @@ static void build_sigma_groups(Context& ctx, SigmaPlan& p, int64_t budget) {
         for (int tn = 0; tn * kTcTileN < dt.n; ++tn) {
           if (nc == 1) {
             t2[g].push_back(DTile{r.task, tm, tn, bnd[0], bnd[1], -1, tail64(dt.m, tm) ? 1 : 0,
-                                  tail64(dt.n, tn) ? 1 : 0});
+                                  tail_cols(dt.n, tn)});
             continue;
           }
           for (int ch = 0; ch < nc; ++ch)
             t2[g].push_back(DTile{r.task, tm, tn, bnd[ch], bnd[ch + 1], slots[g] + ch, tail64(dt.m, tm) ? 1 : 0,
-                                  tail64(dt.n, tn) ? 1 : 0});
+                                  tail_cols(dt.n, tn)});
           red[g].push_back(DReduce{r.task, tm, tn, slots[g], nc, 0});
           slots[g] += nc;
         }
@@ -1255,7 +1258,7 @@ std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor
     double s = 0.0, w = 0.0;
     for (const DTile& t : tiles) {
       // one K slice of the tile (64-row tails counted at their size)
-      const double tf = 2.0 * (t.h64 ? 64 : kTcTileM) * (t.n64 ? 64 : kTcTileN) * kPkTileK;
+      const double tf = 2.0 * (t.h64 ? 64 : kTcTileM) * t.nt * kPkTileK;
       for (int q = t.p0; q < t.p1; ++q) {
         s += pairs[q].nks;
         w += pairs[q].nks * tf;
@@ -1283,7 +1286,7 @@ std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor
   padded(p.s2, &pm2, &pn2, &pk2);
   auto tails = [](const std::vector<DTile>& tiles, bool rows) {
     double c = 0.0;
-    for (const DTile& t : tiles) c += rows ? t.h64 : t.n64;
+    for (const DTile& t : tiles) c += rows ? t.h64 : (t.nt < kTcTileN ? 1 : 0);
     return c;
   };
   // tile FLOPs if a block's last row tile were 64 rows high where its remainder fits

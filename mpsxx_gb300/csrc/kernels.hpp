@@ -24,7 +24,8 @@ struct DGemmPair {
 struct DTile {
   int task, tm, tn, p0, p1, slot;
   int h64;  // tensor-core tiles: the A rows are a block's 64-row tail tile (see tail64)
-  int n64;  // tensor-core tiles: the B rows (output columns) are a 64-row tail tile
+  int nt;   // tensor-core tiles: B rows (output columns) of the tile, 128 or a block's
+            // compact tail (see tail_cols)
 };
 // Reduction of the split partials of one output tile.
 struct DReduce {
@@ -108,6 +109,12 @@ constexpr int kTcTileN = 128;
 __host__ __device__ constexpr bool tail64(int rows, int tm) {
   return rows % 128 != 0 && rows % 128 <= 64 && tm == rows / 128;
 }
+// B operands (the result's columns) are cut into 128-row tiles and a compact last
+// tile of the remaining rows rounded up to 16 (the N granularity of an M = 128 MMA):
+// the number of B rows of column tile tn.
+__host__ __device__ constexpr int tail_cols(int rows, int tn) {
+  return (tn == rows / 128 && rows % 128 != 0) ? (rows % 128 + 15) / 16 * 16 : 128;
+}
 constexpr int kPkTileK = 32;                          // K elements per packed slice
 // a tile's block pairs accumulate in FP32 (tensor memory) until their padded K reaches
 // this, then the group is added into FP64
@@ -130,10 +137,11 @@ struct DPkPair {
 // One packed tile to produce: element (r, k) of the block is src[src_off + r*ld + k]
 // (trans = 0) or src[src_off + k*ld + r] (trans = 1).
 // fp32: the tile holds FP32 values (split into hi|lo on chip by the GEMM) instead of
-// its hi|lo TF32 halves.
+// its hi|lo TF32 halves.  r0: the block row of the tile's first row; tile_rows: its
+// rows (128, or a compact tail).
 struct DPack {
   int64_t src_off, dst_off;
-  int rows, k, ld, trans, tile_rows, tr, tk, fp32;
+  int rows, k, ld, trans, tile_rows, r0, tk, fp32;
 };
 
 // out_packed (kOut*): C is written as packed A tiles of the next GEMM (c_off = byte

@@ -292,7 +292,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // a 64-row tail tile is packed compact: half the bytes; its hi and lo
             // halves (split format) land where the MMA expects a 128-row tile's
             const uint32_t at = t.h64 ? a_bytes / 2 : a_bytes;
-            const uint32_t bt = t.n64 ? b_bytes / 2 : b_bytes;  // compact [hi 64 | lo 64] (or FP32 64 rows) on a tail
+            // a block's last column tile is compact: [hi nt | lo nt] (or nt FP32 rows)
+            const uint32_t bt = b_bytes / BN * t.nt;
             mbar_expect_tx(fb, at + bt);
             const uint32_t dst = smem_u32(ring + s * STAGE_BYTES);
             const uint8_t* asrc = Apk + pr.a_pk + (int64_t)t.tm * pr.nks * a_bytes + (int64_t)ks * at;
@@ -332,7 +333,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
         const DTile t = t_next;
         if (ti + (int)gridDim.x < ntiles) t_next = tiles[ti + gridDim.x];
-        const int mt = t.h64 ? 64 : BM, nt = t.n64 ? 64 : BN;
+        const int mt = t.h64 ? 64 : BM, nt = t.nt;
         const uint32_t idesc_w = tf32_idesc(mt, 2 * nt), idesc = tf32_idesc(mt, nt);
         int kacc = 0;
         int nks_next = t.p0 < t.p1 ? pairs[t.p0].nks : 0;
@@ -418,8 +419,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               split_in_place(ring + s * STAGE_BYTES, A_BYTES / 2, static_cast<int>(A1_BYTES / 16) >> (t.h64 ? 1 : 0),
                              ct);
             if (b_single)
-              split_in_place(ring + s * STAGE_BYTES + A_BYTES, t.n64 ? B1_BYTES / 2 : B1_BYTES,
-                             static_cast<int>(B1_BYTES / 16) >> (t.n64 ? 1 : 0), ct);
+              split_in_place(ring + s * STAGE_BYTES + A_BYTES, B1_BYTES / BN * t.nt,
+                             static_cast<int>(B1_BYTES / BN * t.nt / 16), ct);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(smem_u32(&conv_bar[s]));
           }
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       // nothing for i >= 16); -1: no row
       const int row = t.h64 ? (lane < 16 ? q * 16 + lane : -1) : q * 32 + lane;
       const int r = t.tm * BM + row;
-      const int nt = t.n64 ? 64 : BN;     // output columns of the tile
+      const int nt = t.nt;                // output columns of the tile
       const bool cols = 64 * ch < nt;     // this warp has columns (not on a 64-column tail)
       const uint32_t c1 = 64 * ch, c2 = nt + 64 * ch;  // its columns in both accumulator parts
       if (out_packed) {
@@ -478,6 +479,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk) v[kk] += w[kk];
+            // columns past a compact tail tile hold no product: the next GEMM's K
+            // padding, written as zeros
+            const int cb = 64 * ch + h * BK + k0;
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+              if (cb + kk >= nt) v[kk] = 0.0f;
             const int slice = 4 * t.tn + 2 * ch + h;
             if (slice >= task.ldc || row < 0) continue;
             uint8_t* tile = tile0 + (int64_t)slice * ts;
@@ -571,7 +578,7 @@ __global__ void __launch_bounds__(256) pack_kernel(const DPack* __restrict__ pac
   const int rows_t = pk.tile_rows;
   const uint32_t half = (uint32_t)rows_t * BK * 4;  // bytes of one half (hi or lo) of the tile
   uint8_t* tile = dst + pk.dst_off;
-  const int r0 = pk.tr * rows_t, k0 = pk.tk * BK;
+  const int r0 = pk.r0, k0 = pk.tk * BK;
   for (int e = threadIdx.x; e < rows_t * BK; e += blockDim.x) {
     int r, kk;
     if (!pk.trans) {
