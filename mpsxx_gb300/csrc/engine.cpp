@@ -1433,6 +1433,8 @@ DiagPlan& diag_plan(Context& ctx, const Tensor& L, const Tensor& R, const Tensor
     p->h_tasks.push_back(t);
     p->ref.push_back({diag.tags[b], std::move(refp)});
   }
+  for (const DDiagTask& t : p->h_tasks)
+    p->max_tiles = std::max(p->max_tiles, ((t.m + 31) / 32) * ((t.n + 31) / 32));
   p->tasks.upload(p->h_tasks, ctx.stream);
   p->pairs.upload(p->h_pairs, ctx.stream);
   return insert_plan(ctx, ctx.diag_plans, key, std::move(p));
@@ -1440,7 +1442,8 @@ DiagPlan& diag_plan(Context& ctx, const Tensor& L, const Tensor& R, const Tensor
 
 void compute_diagonal_elements(Context& ctx, const DTensor& L, const DTensor& R, DTensor& diag) {
   DiagPlan& p = diag_plan(ctx, L, R, diag);
-  launch_diag(p.tasks.get(), static_cast<int>(p.h_tasks.size()), p.pairs.get(), L.d, R.d, diag.d, ctx.stream);
+  launch_diag(p.tasks.get(), static_cast<int>(p.h_tasks.size()), p.pairs.get(), L.d, R.d, diag.d, p.max_tiles,
+              ctx.stream);
   ctx.kernel_launches += 1;
 }
 
@@ -2222,17 +2225,20 @@ static double davidson_run(Context& ctx, const DTensor& L, const DTensor& R, con
         break;
       }
       if (m < max_ritz) {
+        // correction vector orthonormalised against the subspace: the reference
+        // projects out one trial vector at a time (src/diagonalize.hpp:425-431); here
+        // classical Gram-Schmidt is applied twice, all m projections per pass in one
+        // multi-dot and one update (the same vector to rounding, 12 launches for m)
         launch_precondition(errv, diag.d, n, eval, st);
-        ctx.kernel_launches += 1;
-        for (int i = 0; i < m; ++i) {
-          normalize(errv);
-          launch_multidot(trial + i * n, 1, errv, 1, n, n, sc + 102, part, nblk, st);
-          launch_axpy_dev(errv, trial + i * n, n, sc + 102, -1.0, st);
+        normalize(errv);
+        for (int pass = 0; pass < 2; ++pass) {
+          launch_multidot(trial, m, errv, 1, n, n, sc + 104, part, nblk, st);
+          launch_project_out(errv, trial, m, n, n, sc + 104, st);
           ctx.kernel_launches += 3;
         }
         normalize(errv);
         launch_copy_vec(trial + m * n, errv, n, st);
-        ctx.kernel_launches += 1;
+        ctx.kernel_launches += 2;
         sigma_of(m, ctx.precision);
       }
     }

@@ -226,6 +226,7 @@ struct RenormPlan {
 };
 
 struct DiagPlan {
+  int max_tiles = 0;  // most 32 x 32 tiles of one block (the kernel's grid height)
   std::vector<DDiagTask> h_tasks;
   std::vector<DDiagPair> h_pairs;
   DevArray<DDiagTask> tasks;

@@ -208,7 +208,7 @@ void launch_adjoint_scatter(const DScatterDst* dsts, int ndst, const DScatterSrc
 // G[e] = sum_{k = ptr[e]}^{ptr[e+1]-1} g[idx[k]], summed in index order.
 void launch_segment_sum(const int* ptr, const int* idx, const double* g, int ne, double* G, cudaStream_t st);
 void launch_diag(const DDiagTask* tasks, int ntasks, const DDiagPair* pairs, const double* L, const double* R,
-                 double* out, cudaStream_t st);
+                 double* out, int max_tiles, cudaStream_t st);
 
 // Level-1 over dense vectors of length n (the block layout of a wavefunction).
 void launch_fill(double* x, int64_t n, double v, cudaStream_t st);
@@ -226,6 +226,9 @@ void launch_multidot(const double* X, int nx, const double* Y, int ny, int64_t n
 // new_j = sum_i R[i*ld + j] * old_i, j < m (in place via scratch `tmp` of m*n)
 void launch_rotate(double* V, int m, int64_t n, int64_t stride, const double* R, int ldr, double* tmp,
                    cudaStream_t st);
+// y -= sum_{i < m} c[i] X[i * stride : i * stride + n], c (m values) on the device
+void launch_project_out(double* y, const double* X, int m, int64_t n, int64_t stride, const double* c,
+                        cudaStream_t st);
 void launch_precondition(double* r, const double* diag, int64_t n, double e, cudaStream_t st);
 void launch_scale_blocks_rows(double* data, const int64_t* off, const int* rows, const int* cols,
                               const int64_t* s_off, int nb, const double* s, cudaStream_t st);

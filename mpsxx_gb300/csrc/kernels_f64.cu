@@ -239,18 +239,45 @@ __global__ void segment_sum_kernel(const int* __restrict__ ptr, const int* __res
   G[e] = acc;
 }
 
-__global__ void diag_kernel(const DDiagTask* __restrict__ tasks, const DDiagPair* __restrict__ pairs,
-                            const double* __restrict__ L, const double* __restrict__ R, double* __restrict__ out) {
+// diag[a, b] += sum_p L_p[a, a] R_p[b, b] over a block's (L, R) pairs, one CTA per
+// 32 x 32 tile of the block (blockIdx.y); the tied diagonals of 32 pairs at a time are
+// gathered into shared memory, each thread sums four outputs over the pairs in order.
+constexpr int kDiagTile = 32, kDiagPairs = 32;
+__global__ void __launch_bounds__(256) diag_kernel(const DDiagTask* __restrict__ tasks,
+                                                   const DDiagPair* __restrict__ pairs, const double* __restrict__ L,
+                                                   const double* __restrict__ R, double* __restrict__ out) {
+  __shared__ double ls[kDiagPairs][kDiagTile];
+  __shared__ double rs[kDiagPairs][kDiagTile];
   const DDiagTask t = tasks[blockIdx.x];
-  const int64_t n = (int64_t)t.m * t.n;
-  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
-    const int a = static_cast<int>(e / t.n), b = static_cast<int>(e % t.n);
-    double acc = 0.0;
-    for (int p = t.p0; p < t.p1; ++p) {
-      const DDiagPair q = pairs[p];
-      acc = fma(L[q.l_off + (int64_t)a * (t.m + 1)], R[q.r_off + (int64_t)b * (t.n + 1)], acc);
+  const int tcols = (t.n + kDiagTile - 1) / kDiagTile;
+  const int ntile = ((t.m + kDiagTile - 1) / kDiagTile) * tcols;
+  if ((int)blockIdx.y >= ntile) return;
+  const int a0 = (blockIdx.y / tcols) * kDiagTile, b0 = (blockIdx.y % tcols) * kDiagTile;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // column tx, rows ty + 8 i
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int p0 = t.p0; p0 < t.p1; p0 += kDiagPairs) {
+    const int np = t.p1 - p0 < kDiagPairs ? t.p1 - p0 : kDiagPairs;
+    __syncthreads();
+    for (int e = threadIdx.x; e < np * kDiagTile; e += blockDim.x) {
+      const int q = e / kDiagTile, i = e % kDiagTile;
+      const DDiagPair pr = pairs[p0 + q];
+      const int a = a0 + i, b = b0 + i;
+      ls[q][i] = a < t.m ? L[pr.l_off + (int64_t)a * (t.m + 1)] : 0.0;
+      rs[q][i] = b < t.n ? R[pr.r_off + (int64_t)b * (t.n + 1)] : 0.0;
     }
-    out[t.out_off + e] += acc;
+    __syncthreads();
+    for (int q = 0; q < np; ++q) {
+      const double r = rs[q][tx];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i] = fma(ls[q][ty + 8 * i], r, acc[i]);
+    }
+  }
+  const int b = b0 + tx;
+  if (b >= t.n) return;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int a = a0 + ty + 8 * i;
+    if (a < t.m) out[t.out_off + (int64_t)a * t.n + b] += acc[i];
   }
 }
 
@@ -341,6 +368,21 @@ __global__ void multidot_final_kernel(const double* __restrict__ partial, int nb
   double v = 0.0;
   for (int b = 0; b < nblocks; ++b) v += partial[b * (kMaxDot * kMaxDot) + q];
   out[q] = v;
+}
+
+// y -= sum_{i < m} c[i] X[:, i] (X's vectors stride apart; c on the device).
+__global__ void project_out_kernel(double* __restrict__ y, const double* __restrict__ X, int m, int64_t n,
+                                   int64_t stride, const double* __restrict__ c) {
+  double cc[kMaxDot];
+#pragma unroll
+  for (int i = 0; i < kMaxDot; ++i) cc[i] = i < m ? c[i] : 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    double v = y[e];
+#pragma unroll
+    for (int i = 0; i < kMaxDot; ++i)
+      if (i < m) v = fma(-cc[i], X[i * stride + e], v);
+    y[e] = v;
+  }
 }
 
 // V[:, j] = sum_i V[:, i] R[i, j] for j < m, in place per element (loops unrolled to
@@ -452,9 +494,10 @@ void launch_segment_sum(const int* ptr, const int* idx, const double* g, int ne,
 }
 
 void launch_diag(const DDiagTask* tasks, int ntasks, const DDiagPair* pairs, const double* L, const double* R,
-                 double* out, cudaStream_t st) {
+                 double* out, int max_tiles, cudaStream_t st) {
   if (ntasks <= 0) return;
-  diag_kernel<<<ntasks, 256, 0, st>>>(tasks, pairs, L, R, out);
+  if (max_tiles <= 0) return;
+  diag_kernel<<<dim3(ntasks, max_tiles), 256, 0, st>>>(tasks, pairs, L, R, out);
 }
 
 void launch_fill(double* x, int64_t n, double v, cudaStream_t st) {
@@ -506,6 +549,12 @@ void launch_rotate(double* V, int m, int64_t n, int64_t stride, const double* R,
   (void)tmp;
   if (n <= 0) return;
   rotate_kernel<<<grid_for(n), 256, 0, st>>>(V, m, n, stride, R, ldr);
+}
+
+void launch_project_out(double* y, const double* X, int m, int64_t n, int64_t stride, const double* c,
+                        cudaStream_t st) {
+  if (n <= 0 || m <= 0) return;
+  project_out_kernel<<<grid_for(n), 256, 0, st>>>(y, X, m, n, stride, c);
 }
 
 void launch_precondition(double* r, const double* diag, int64_t n, double e, cudaStream_t st) {
