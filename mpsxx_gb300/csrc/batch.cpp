@@ -138,7 +138,12 @@ class Batch {
       off += kSlots * std::max<int64_t>(x.n, 1);
       if (ctx_.precision != kFP64) {
         // one launch serves all members: their intermediates share the hi|lo format
-        // (a plan tuned by a single-bond run may hold the FP32 one)
+        // (a plan tuned by a single-bond run may hold the FP32 one) and their L
+        // operators the per-block layout (a single-bond plan may stack stage 1)
+        if (x.sp->allow_stack) {
+          x.sp->allow_stack = false;
+          if (x.sp->stack1) x.sp->pk_built = false;
+        }
         set_scr1_format(ctx_, *x.sp, *x.L, *x.R, false);
         x.bL = bL;
         bL += (x.sp->pk_L.bytes + 255) / 256 * 256;

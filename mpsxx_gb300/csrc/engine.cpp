@@ -732,12 +732,107 @@ static void packed_layout(Packed& P, const Tensor& t, int tile_rows, uint32_t ti
       const int64_t slice = int64_t(tile_bytes) * rt / tile_rows;
       for (int tk = 0; tk < nks; ++tk)
         P.h_packs.push_back(DPack{t.offsets[b], off + int64_t(tr) * nks * tile_bytes + int64_t(tk) * slice, o.rows,
-                                  o.k, o.ld, o.trans, rt, tr * tile_rows, tk, fp32});
+                                  o.k, o.ld, o.trans, rt, tr * tile_rows, tk, fp32, 0, rt});
     }
     const int rl = rows_of(o.rows, ntr - 1);
     off += int64_t(ntr - 1) * nks * tile_bytes + int64_t(nks) * (int64_t(tile_bytes) * rl / tile_rows);
   }
   P.bytes = off;
+}
+
+// Stacked stage 1 (see SigmaPlan::stack1).  Each stage-1 task (an L*psi block) has a
+// single pair (L block, psi block); the tasks sharing a psi block form a panel whose
+// rows are their L blocks' rows in task order, packed as 128-row A tiles (a last tile
+// of at most 64 rows compact, as everywhere).  One pair per panel, one tile per
+// (panel row tile, psi column tile), and a row map from panel rows to output rows.
+static void build_stacked_stage1(Context& ctx, SigmaPlan& p, const Tensor& L) {
+  const GemmPlan& g = p.s1;
+  const uint32_t tile_bytes = p.ops_single ? kPkTileA1Bytes : kPkTileABytes;
+  const int fp32 = p.ops_single ? 1 : 0;
+  // panels: psi block slot -> tasks in task order
+  std::map<int32_t, std::vector<int>> panels;
+  for (size_t ti = 0; ti < g.h_tasks.size(); ++ti) {
+    const DGemmTask& t = g.h_tasks[ti];
+    if (t.p1 - t.p0 != 1) throw Error(kInternal, "stacked stage 1: a task with more than one pair");
+    panels[g.pair_b_slot[t.p0]].push_back(static_cast<int>(ti));
+  }
+  Packed& P = p.pk_L;
+  P.base.assign(L.tags.size(), -1);
+  P.nks.assign(L.tags.size(), 0);
+  P.h_packs.clear();
+  p.h_stpk1.clear();
+  p.h_row_map.clear();
+  std::vector<DTile> tiles;
+  int64_t off = 0;
+  for (const auto& kv : panels) {
+    const std::vector<int>& tk = kv.second;
+    const DGemmPair& pr0 = g.h_pairs[g.h_tasks[tk[0]].p0];
+    const int K = pr0.k, n = g.h_tasks[tk[0]].n;
+    const int nks = (K + kPkTileK - 1) / kPkTileK;
+    int64_t rows = 0;
+    for (int ti : tk) {
+      const DGemmTask& t = g.h_tasks[ti];
+      if (g.h_pairs[t.p0].k != K || t.n != n) throw Error(kInternal, "stacked stage 1: panel shapes differ");
+      rows += t.m;
+    }
+    if (rows > (int64_t(1) << 30)) throw Error(kInternal, "stacked stage 1: panel too tall");
+    const int R = static_cast<int>(rows);
+    const int ntr = (R + kTcTileM - 1) / kTcTileM;
+    const int64_t map0 = static_cast<int64_t>(p.h_row_map.size());
+    // row map: panel rows in task order, then padding up to the last tile's rows
+    for (int ti : tk)
+      for (int r = 0; r < g.h_tasks[ti].m; ++r) p.h_row_map.push_back((int64_t(ti) << 32) | int64_t(r));
+    const int padded = (ntr - 1) * kTcTileM + (tail64(R, ntr - 1) ? 64 : kTcTileM);
+    for (int r = R; r < padded; ++r) p.h_row_map.push_back(-1);
+    // packs: for every row tile and K slice, one pack per block segment of the tile
+    // (the tile's last segment also zero-fills the rows after it)
+    const int64_t base = off;
+    size_t j0 = 0;   // first task overlapping the current row tile
+    int prow0 = 0;   // its first panel row
+    for (int tr = 0; tr < ntr; ++tr) {
+      const int rt = tail64(R, tr) ? 64 : kTcTileM;
+      const int64_t slice = int64_t(tile_bytes) * rt / kTcTileM;
+      const int row0 = tr * kTcTileM;
+      while (j0 < tk.size() && prow0 + g.h_tasks[tk[j0]].m <= row0) prow0 += g.h_tasks[tk[j0++]].m;
+      for (int ks = 0; ks < nks; ++ks) {
+        const int64_t dst = base + int64_t(tr) * nks * tile_bytes + int64_t(ks) * slice;
+        int prow = prow0;
+        for (size_t j = j0; j < tk.size(); ++j) {
+          const DGemmTask& t = g.h_tasks[tk[j]];
+          const int lo = std::max(prow, row0), hi = std::min(prow + t.m, row0 + rt);
+          const bool last = (prow + t.m >= row0 + rt) || j + 1 == tk.size();
+          if (lo < hi || last) {
+            const int32_t as = g.pair_a_slot[t.p0];
+            const int span = last ? row0 + rt - lo : hi - lo;
+            int d[kMaxRank];
+            L.block_dims(as, d);
+            P.h_packs.push_back(DPack{L.offsets[as], dst, d[0] * d[1], d[2], d[2], 0, rt, lo - prow, ks, fp32,
+                                      lo - row0, span});
+          }
+          if (last) break;
+          prow += t.m;
+        }
+      }
+    }
+    off += int64_t(ntr - 1) * nks * tile_bytes + int64_t(nks) * (int64_t(tile_bytes) * (tail64(R, ntr - 1) ? 64 : kTcTileM) / kTcTileM);
+    const int panel = static_cast<int>(p.h_stpk1.size());
+    const int32_t bs = g.pair_b_slot[g.h_tasks[tk[0]].p0];
+    if (p.pk_psi.base[bs] < 0 || p.pk_psi.nks[bs] != nks) throw Error(kInternal, "stacked stage 1: psi packing mismatch");
+    if (map0 > 0x7fffffff) throw Error(kInternal, "stacked stage 1: row map too large");
+    p.h_stpk1.push_back(DPkPair{base, p.pk_psi.base[bs], nks, static_cast<int>(map0)});
+    for (int tr = 0; tr < ntr; ++tr)
+      for (int tn = 0; tn * kTcTileN < n; ++tn)
+        tiles.push_back(DTile{tk[0], tr, tn, panel, panel + 1, -1, tail64(R, tr) ? 1 : 0, tail_cols(n, tn)});
+  }
+  P.bytes = off;
+  // heaviest first (persistent CTAs take tiles round-robin)
+  std::stable_sort(tiles.begin(), tiles.end(), [&](const DTile& a, const DTile& b) {
+    return p.h_stpk1[a.p0].nks > p.h_stpk1[b.p0].nks;
+  });
+  p.h_st1 = std::move(tiles);
+  p.st1.upload(p.h_st1, ctx.stream);
+  p.stpk1.upload(p.h_stpk1, ctx.stream);
+  p.row_map.upload(p.h_row_map, ctx.stream);
 }
 
 static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R, const Tensor& psi) {
@@ -776,13 +871,20 @@ static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Te
       out[i] = DPkPair{A.base[as], B.base[bs], A.nks[as], 0};
     }
   };
-  pairs_of(p.s1, p.pk_L, p.pk_psi, p.h_pk1);
+  // Stacked stage 1 where the schedule allows it (whole-w passes; w groups and batched
+  // steps address L block by block): replaces the per-block packing of L
+  const bool was_stacked = p.stack1;
+  p.stack1 = p.allow_stack && ctx.sigma_w_budget <= 0 && p.pk_scr1.bytes <= kGroupIntermediateBytes;
+  if (p.stack1 != was_stacked) p.pk_L.src_version = ~0ull;  // its packed contents follow the other layout
+  if (p.stack1) build_stacked_stage1(ctx, p, L);
+  else pairs_of(p.s1, p.pk_L, p.pk_psi, p.h_pk1);
   pairs_of(p.s2, p.pk_scr1, p.pk_R, p.h_pk2);
   // Stage 1 writes each tile's result straight into the intermediate's packed tiles,
   // which is right only for a tile summed in one piece: not split along K, one
   // accumulation group (psi has one block per column sector, so each L*psi block has
   // a single contributing pair)
   for (const DTile& t : p.s1.h_tiles_tc) {
+    if (p.stack1) break;  // stacked tiles have one pair by construction
     int64_t kpad = 0;
     for (int q = t.p0; q + 1 < t.p1; ++q) kpad += int64_t(p.h_pk1[q].nks) * kPkTileK;
     if (t.slot >= 0 || kpad >= kFlushK)
@@ -796,7 +898,7 @@ static void build_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Te
     p.h_pk_tasks1[ti].c_off = p.pk_scr1.base[cs];
     p.h_pk_tasks1[ti].ldc = p.pk_scr1.nks[cs];
   }
-  p.pk1.upload(p.h_pk1, ctx.stream);
+  if (!p.stack1) p.pk1.upload(p.h_pk1, ctx.stream);
   p.pk2.upload(p.h_pk2, ctx.stream);
   p.pk_tasks1.upload(p.h_pk_tasks1, ctx.stream);
   p.pk_L.packs.upload(p.pk_L.h_packs, ctx.stream);
@@ -1109,7 +1211,7 @@ static void tune_sigma_groups(Context& ctx, SigmaPlan& p, const Tensor& L, const
   std::vector<Cand> cands;
   for (bool single : {false, true})
     for (int target : {152 * 4, 152 * 8, 152 * 16}) cands.push_back({0, target, single});
-  if (p.pk_scr1.bytes > (int64_t(8) << 30)) cands.push_back({128 * mb, 152 * 8, false});
+  if (p.pk_scr1.bytes > kGroupIntermediateBytes) cands.push_back({128 * mb, 152 * 8, false});
   Cand best = cands[0];
   float best_ms = 0.0f;
   ctx.last_tuning.clear();
@@ -1218,10 +1320,16 @@ static void sigma_run_pk(Context& ctx, SigmaPlan& p, const DTensor& L, const DTe
 // Both stages over all of w at once (the packed L*psi intermediate in HBM).
 static void sigma_run_pk_whole(Context& ctx, SigmaPlan& p, double* sigma) {
   int* err = device_err_flag(ctx);
-  launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.pk_scr1.buf.as<uint8_t>(),
-                 p.s1.tiles_tc.get(), static_cast<int>(p.s1.h_tiles_tc.size()), p.pk_tasks1.get(), p.pk1.get(),
-                 nullptr, p.scr1_single ? kOutPackedSingle : kOutPackedSplit, p.stage1_single(), err, ctx.stream,
-                 ctx.device_timeout_ns);
+  if (p.stack1)
+    launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.pk_scr1.buf.as<uint8_t>(),
+                   p.st1.get(), static_cast<int>(p.h_st1.size()), p.pk_tasks1.get(), p.stpk1.get(), nullptr,
+                   p.scr1_single ? kOutPackedSingle : kOutPackedSplit, p.stage1_single(), err, ctx.stream,
+                   ctx.device_timeout_ns, p.row_map.get());
+  else
+    launch_gemm_pk(p.pk_L.buf.as<uint8_t>(), p.pk_psi.buf.as<uint8_t>(), 1.0, nullptr, p.pk_scr1.buf.as<uint8_t>(),
+                   p.s1.tiles_tc.get(), static_cast<int>(p.s1.h_tiles_tc.size()), p.pk_tasks1.get(), p.pk1.get(),
+                   nullptr, p.scr1_single ? kOutPackedSingle : kOutPackedSplit, p.stage1_single(), err, ctx.stream,
+                   ctx.device_timeout_ns);
   ctx.gemm_part.ensure(std::max<size_t>(p.s2.partial_bytes_tc(), 16), ctx.stream);
   double* part = ctx.gemm_part.as<double>();
   launch_gemm_pk(p.pk_scr1.buf.as<uint8_t>(), p.pk_R.buf.as<uint8_t>(), 1.0, sigma, nullptr,
@@ -1268,7 +1376,8 @@ std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor
     return w;
   };
   double sl1 = 0.0, sl2 = 0.0;
-  const double w1 = work(p.s1.h_tiles_tc, p.h_pk1, &sl1);
+  const std::vector<DTile>& t1 = p.stack1 ? p.h_st1 : p.s1.h_tiles_tc;
+  const double w1 = work(t1, p.stack1 ? p.h_stpk1 : p.h_pk1, &sl1);
   const double w2 = work(p.s2.h_tiles_tc, p.h_pk2, &sl2);
   // FLOPs with one dimension padded at a time (rows to 128, columns to 64, K to 32)
   auto padded = [](const GemmPlan& g, double* pm, double* pn, double* pk) {
@@ -1306,7 +1415,7 @@ std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor
           w2,
           sl1,
           sl2,
-          double(p.s1.h_tiles_tc.size()),
+          double(t1.size()),
           double(p.s2.h_tiles_tc.size()),
           double(p.pk_L.bytes),
           double(p.pk_R.bytes),
@@ -1321,8 +1430,8 @@ std::vector<double> sigma_plan_stats(Context& ctx, const Tensor& L, const Tensor
           pk2,
           tile64(p.s1),
           tile64(p.s2),
-          tails(p.s1.h_tiles_tc, true) + tails(p.s2.h_tiles_tc, true),
-          tails(p.s1.h_tiles_tc, false) + tails(p.s2.h_tiles_tc, false)};
+          tails(t1, true) + tails(p.s2.h_tiles_tc, true),
+          tails(t1, false) + tails(p.s2.h_tiles_tc, false)};
 }
 
 void ensure_sigma_pk(Context& ctx, SigmaPlan& p, const Tensor& L, const Tensor& R) {

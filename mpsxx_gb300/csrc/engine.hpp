@@ -111,6 +111,8 @@ enum Precision : int { kFP64 = 0, kSplitTF32 = 1, kSplitTF32All = 2 };
 
 // target number of CTAs a grouped GEMM is split into (a few waves on 152 SMs)
 constexpr int kTargetCtas = 152 * 8;
+// packed L*psi intermediates above this size make the tuner try w-blocked schedules
+constexpr int64_t kGroupIntermediateBytes = int64_t(8) << 30;
 
 // plans kept per kind in a context before the cache is emptied
 constexpr size_t kMaxCachedPlans = 512;  // default of Context::max_plans
@@ -166,6 +168,20 @@ struct SigmaPlan {
   int stage1_single() const { return ops_single ? kSingleA : 0; }
   int stage2_single() const { return (scr1_single ? kSingleA : 0) | (ops_single ? kSingleB : 0); }
   Packed pk_L, pk_R, pk_psi, pk_scr1;
+  // Stage 1 over stacked panels: the L blocks that multiply the same psi block (same
+  // K and output columns) stacked row-wise into one operand, so that the ~70-row sector
+  // blocks fill 128-row tiles.  pk_L then holds the panels; st1 tiles (task = a block of
+  // the panel, p0 = panel), stpk1 one pair per panel (pad = its first row_map entry),
+  // row_map the output block and row of every panel row.  Off for batched steps and
+  // w-blocked schedules, which use the per-block layout.
+  bool allow_stack = true;
+  bool stack1 = false;
+  std::vector<DTile> h_st1;
+  std::vector<DPkPair> h_stpk1;
+  std::vector<int64_t> h_row_map;
+  DevArray<DTile> st1;
+  DevArray<DPkPair> stpk1;
+  DevArray<int64_t> row_map;
   std::vector<DPkPair> h_pk1, h_pk2;
   std::vector<DGemmTask> h_pk_tasks1;
   DevArray<DPkPair> pk1, pk2;

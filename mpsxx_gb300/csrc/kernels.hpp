@@ -137,11 +137,12 @@ struct DPkPair {
 // One packed tile to produce: element (r, k) of the block is src[src_off + r*ld + k]
 // (trans = 0) or src[src_off + k*ld + r] (trans = 1).
 // fp32: the tile holds FP32 values (split into hi|lo on chip by the GEMM) instead of
-// its hi|lo TF32 halves.  r0: the block row of the tile's first row; tile_rows: its
-// rows (128, or a compact tail).
+// its hi|lo TF32 halves.  tile_rows: the tile's rows (128, or a compact tail).  The
+// pack covers tile rows [ro, ro + span) with block rows r0, r0 + 1, ... (zeros past the
+// block's last row): one pack per tile, or several when blocks are stacked in a tile.
 struct DPack {
   int64_t src_off, dst_off;
-  int rows, k, ld, trans, tile_rows, r0, tk, fp32;
+  int rows, k, ld, trans, tile_rows, r0, tk, fp32, ro, span;
 };
 
 // out_packed (kOut*): C is written as packed A tiles of the next GEMM (c_off = byte
@@ -152,9 +153,14 @@ struct DPack {
 // Every wait of the kernel gives up after timeout_ns (the whole launch): the kernel then
 // drains its own bulk copies and MMAs, frees its tensor memory, sets *err and returns.
 constexpr uint64_t kPkTimeoutNs = 20000000000ull;  // 20 s
+// row_map (packed output only, may be null): the A tiles stack several blocks' rows (a
+// stacked panel; the pair's pad field is the panel's first entry in row_map); entry
+// (task << 32 | block row) per panel row, -1 for padding rows, says which output block
+// and row each tile row is written to.
 void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
-                    int out_packed, int single, int* err, cudaStream_t st, uint64_t timeout_ns = kPkTimeoutNs);
+                    int out_packed, int single, int* err, cudaStream_t st, uint64_t timeout_ns = kPkTimeoutNs,
+                    const int64_t* row_map = nullptr);
 void launch_gemm_pk_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
                            double* C, cudaStream_t st);
 void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst, cudaStream_t st);

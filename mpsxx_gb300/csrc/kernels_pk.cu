@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                    double* __restrict__ C, uint8_t* __restrict__ Cpk, const DTile* __restrict__ tiles, int ntiles,
                    const DGemmTask* __restrict__ tasks, const DPkPair* __restrict__ pairs,
                    double* __restrict__ partial, int out_packed, int single, int* __restrict__ err,
-                   uint64_t timeout_ns) {
+                   uint64_t timeout_ns, const int64_t* __restrict__ row_map) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   __shared__ __align__(8) uint64_t full_bar[STAGES];
@@ -465,9 +465,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const uint32_t ot_bytes = single ? A1_BYTES : A_BYTES;  // output tile (128 rows)
           // the next GEMM's A tile grid for this row tile: a 64-row tail tile is
           // compact (half the bytes, its lo half a quarter tile in)
-          const uint32_t ts = t.h64 ? ot_bytes / 2 : ot_bytes;
-          const uint32_t lo_off = ts / 2;
+          uint32_t ts = t.h64 ? ot_bytes / 2 : ot_bytes;
           uint8_t* tile0 = Cpk + task.c_off + (int64_t)t.tm * task.ldc * ot_bytes;
+          int row_d = row, ldc = task.ldc;  // destination row in its tile, K slices of its block
+          if (row_map != nullptr) {
+            // stacked panel: this row's output block and row from the row map
+            row_d = -1;
+            if (row >= 0) {
+              const int64_t e = row_map[(int64_t)pairs[t.p0].pad + (int64_t)t.tm * BM + row];
+              if (e >= 0) {
+                const DGemmTask dt = tasks[static_cast<int>(e >> 32)];
+                const int br = static_cast<int>(e & 0xffffffffll), tmd = br / BM;
+                row_d = br % BM;
+                ts = tail64(dt.m, tmd) ? ot_bytes / 2 : ot_bytes;
+                tile0 = Cpk + dt.c_off + (int64_t)tmd * dt.ldc * ot_bytes;
+                ldc = dt.ldc;
+              }
+            }
+          }
+          const uint32_t lo_off = ts / 2;
           const float fa = static_cast<float>(alpha);
           // 16 columns at a time: half a K slice of the next GEMM
 #pragma unroll 1
@@ -486,14 +502,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int kk = 0; kk < 16; ++kk)
               if (cb + kk >= nt) v[kk] = 0.0f;
             const int slice = 4 * t.tn + 2 * ch + h;
-            if (slice >= task.ldc || row < 0) continue;
+            if (slice >= ldc || row_d < 0) continue;
             uint8_t* tile = tile0 + (int64_t)slice * ts;
             // 16-byte stores: k .. k+3 of a row are contiguous in the core-matrix
             // layout, and a warp's 32 rows fill four whole 128-byte lines
             if (single) {
 #pragma unroll
               for (int kk = 0; kk < 16; kk += 4)
-                *reinterpret_cast<float4*>(tile + core_off(row, k0 + kk)) =
+                *reinterpret_cast<float4*>(tile + core_off(row_d, k0 + kk)) =
                     make_float4(fa * v[kk], fa * v[kk + 1], fa * v[kk + 2], fa * v[kk + 3]);
             } else {
 #pragma unroll
@@ -507,8 +523,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                   hp[e] = tf32_rna(x);
                   lp[e] = tf32_rna(x - __uint_as_float(hp[e]));
                 }
-                *reinterpret_cast<uint4*>(tile + core_off(row, k0 + kk)) = hi;
-                *reinterpret_cast<uint4*>(tile + lo_off + core_off(row, k0 + kk)) = lo;
+                *reinterpret_cast<uint4*>(tile + core_off(row_d, k0 + kk)) = hi;
+                *reinterpret_cast<uint4*>(tile + lo_off + core_off(row_d, k0 + kk)) = lo;
               }
             }
           }
@@ -578,27 +594,27 @@ __global__ void __launch_bounds__(256) pack_kernel(const DPack* __restrict__ pac
   const int rows_t = pk.tile_rows;
   const uint32_t half = (uint32_t)rows_t * BK * 4;  // bytes of one half (hi or lo) of the tile
   uint8_t* tile = dst + pk.dst_off;
-  const int r0 = pk.r0, k0 = pk.tk * BK;
-  for (int e = threadIdx.x; e < rows_t * BK; e += blockDim.x) {
+  const int r0 = pk.r0, k0 = pk.tk * BK, span = pk.span;
+  for (int e = threadIdx.x; e < span * BK; e += blockDim.x) {
     int r, kk;
     if (!pk.trans) {
       r = e / BK;
       kk = e % BK;
     } else {
-      kk = e / rows_t;
-      r = e % rows_t;
+      kk = e / span;
+      r = e % span;
     }
-    const int gr = r0 + r, gk = k0 + kk;
+    const int gr = r0 + r, gk = k0 + kk, tr = pk.ro + r;
     double v = 0.0;
     if (gr < pk.rows && gk < pk.k)
       v = pk.trans ? src[pk.src_off + (int64_t)gk * pk.ld + gr] : src[pk.src_off + (int64_t)gr * pk.ld + gk];
     if (pk.fp32) {
-      *reinterpret_cast<float*>(tile + core_off(r, kk)) = static_cast<float>(v);
+      *reinterpret_cast<float*>(tile + core_off(tr, kk)) = static_cast<float>(v);
     } else {
       uint32_t h, l;
       split2(v, h, l);
-      *reinterpret_cast<uint32_t*>(tile + core_off(r, kk)) = h;
-      *reinterpret_cast<uint32_t*>(tile + half + core_off(r, kk)) = l;
+      *reinterpret_cast<uint32_t*>(tile + core_off(tr, kk)) = h;
+      *reinterpret_cast<uint32_t*>(tile + half + core_off(tr, kk)) = l;
     }
   }
 }
@@ -628,7 +644,8 @@ int pk_smem_bytes() { return SMEM_BYTES; }
 
 void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double* C, uint8_t* Cpk,
                     const DTile* tiles, int ntiles, const DGemmTask* tasks, const DPkPair* pairs, double* partial,
-                    int out_packed, int single, int* err, cudaStream_t st, uint64_t timeout_ns) {
+                    int out_packed, int single, int* err, cudaStream_t st, uint64_t timeout_ns,
+                    const int64_t* row_map) {
   if (ntiles <= 0) return;
   static int nsm = 0;
   if (nsm == 0) {
@@ -641,7 +658,7 @@ void launch_gemm_pk(const uint8_t* Apk, const uint8_t* Bpk, double alpha, double
   // one persistent CTA per SM; the bound covers the whole launch, not one tile
   const int grid = ntiles < nsm ? ntiles : nsm;
   gemm_pk_kernel<<<grid, NTHREADS, SMEM_BYTES, st>>>(Apk, Bpk, alpha, C, Cpk, tiles, ntiles, tasks, pairs, partial,
-                                                     out_packed, single, err, timeout_ns);
+                                                     out_packed, single, err, timeout_ns, row_map);
 }
 
 void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst, cudaStream_t st) {
