@@ -81,7 +81,7 @@ def parse():
     ap.add_argument("--no-sweep-ramp", dest="sweep_ramp", action="store_false",
                     help="all sweeps at --sweep-M (default: two sweeps at M/4, two at M/2 first)")
     ap.add_argument("--no-sweep-control", action="store_true",
-                    help="skip the FP64 control arm (ten times tighter Davidson tolerance)")
+                    help="skip the control arms (FP64 and split at a ten times tighter Davidson tolerance)")
     ap.add_argument("--no-gradient", dest="gradient", action="store_false",
                     help="skip the energy-gradient workloads (site-dependent Hubbard L=32 M=512, QC n=16 M=256)")
     ap.add_argument("--grad-fd", type=int, default=2, help="parameters checked by central differences per workload")
@@ -359,11 +359,13 @@ def sweep_compare(args, device: int):
 
     * ``fp64``: FP64 H_eff*psi, Davidson |r|^2 < 0.1*tole;
     * ``split``: split-precision H_eff*psi with the FP64 refinement, same tolerance;
-    * ``fp64_control``: FP64 with a ten times tighter Davidson tolerance.
+    * ``fp64_control`` and ``split_control``: both again with a ten times tighter
+      Davidson tolerance.
 
     Where each Davidson stops moves the truncated (fixed M) problem's path, so energies at
-    equal sweep counts differ even between the two FP64 arms: that difference is the floor
-    against which split vs FP64 is read.  Sweep times are compared at the final M."""
+    equal sweep counts differ even between two FP64 runs: the FP64-vs-FP64 difference
+    across the two tolerances is the floor against which split vs FP64 (at either
+    tolerance) is read.  Sweep times are compared at the final M."""
     from mpsxx_gb300 import core, dmrg, mpogen
 
     n = args.sweep_norb
@@ -375,7 +377,7 @@ def sweep_compare(args, device: int):
            "M_schedule": sched, "start": "reference initial state (constant-filled sites)"}
     arms = [("fp64", core.FP64, args.tole), ("split", core.SPLIT_TF32, args.tole)]
     if not args.no_sweep_control:
-        arms.append(("fp64_control", core.FP64, 0.1 * args.tole))
+        arms += [("fp64_control", core.FP64, 0.1 * args.tole), ("split_control", core.SPLIT_TF32, 0.1 * args.tole)]
     for name, prec, tole in arms:
         ctx = core.Context(device)
         core.set_precision(ctx, prec)
@@ -407,13 +409,21 @@ def sweep_compare(args, device: int):
            "speedup_per_sweep": res["fp64"]["seconds_per_sweep_final_M"] / res["split"]["seconds_per_sweep_final_M"],
            "speedup_total": res["fp64"]["seconds_total"] / res["split"]["seconds_total"]}
     if "fp64_control" in res:
-        ec = res["fp64_control"]["energy"]
-        cmp["abs_dE_fp64_vs_fp64_control"] = abs(e64 - ec)
+        ec, esc = res["fp64_control"]["energy"], res["split_control"]["energy"]
+
+        def per(a, b):
+            return [abs(x["energy"] - y["energy"]) for x, y in zip(res[a]["per_sweep"], res[b]["per_sweep"])]
+
+        cmp["abs_dE_split_vs_fp64_tight"] = abs(esc - ec)
+        cmp["abs_dE_fp64_vs_fp64_tight"] = abs(e64 - ec)
+        cmp["abs_dE_split_vs_split_tight"] = abs(res["split"]["energy"] - esc)
         cmp["abs_dE_split_vs_fp64_control"] = abs(res["split"]["energy"] - ec)
-        cmp["per_sweep_abs_dE_split_vs_fp64_control"] = [
-            abs(a["energy"] - b["energy"]) for a, b in zip(res["split"]["per_sweep"], res["fp64_control"]["per_sweep"])]
-        cmp["per_sweep_abs_dE_fp64_vs_fp64_control"] = [
-            abs(a["energy"] - b["energy"]) for a, b in zip(res["fp64"]["per_sweep"], res["fp64_control"]["per_sweep"])]
+        cmp["seconds_per_sweep_fp64_tight"] = res["fp64_control"]["seconds_per_sweep_final_M"]
+        cmp["seconds_per_sweep_split_tight"] = res["split_control"]["seconds_per_sweep_final_M"]
+        cmp["speedup_per_sweep_tight"] = cmp["seconds_per_sweep_fp64_tight"] / cmp["seconds_per_sweep_split_tight"]
+        cmp["per_sweep_abs_dE_split_vs_fp64_tight"] = per("split_control", "fp64_control")
+        cmp["per_sweep_abs_dE_fp64_vs_fp64_tight"] = per("fp64", "fp64_control")
+        cmp["per_sweep_abs_dE_split_vs_fp64_control"] = per("split", "fp64_control")
     res["compare"] = cmp
     return res
 
