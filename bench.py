@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--sweep-max", type=int, default=12, help="sweeps per arm (ramp included)")
     ap.add_argument("--no-sweep-ramp", dest="sweep_ramp", action="store_false",
                     help="all sweeps at --sweep-M (default: two sweeps at M/4, two at M/2 first)")
+    ap.add_argument("--sweep-arms", default="",
+                    help="comma list of sweep arms to run (fp64, split, fp64_control, split_control; default all)")
     ap.add_argument("--no-sweep-control", action="store_true",
                     help="skip the control arms (FP64 and split at a ten times tighter Davidson tolerance)")
     ap.add_argument("--no-gradient", dest="gradient", action="store_false",
@@ -344,6 +346,16 @@ def qc_mpo_of(args, h1, eri):
     return mpogen.qc_mpo(h1, eri)
 
 
+def _device_bytes_in_use():
+    """Device memory in use (nvidia-smi's view of this process's GPU), or None."""
+    try:
+        out = subprocess.run(["nvidia-smi", "--query-gpu=memory.used", "--format=csv,noheader,nounits"],
+                             capture_output=True, text=True, timeout=10).stdout.split()
+        return int(float(out[0])) * 1024 * 1024 if out else None
+    except Exception:
+        return None
+
+
 def sweep_schedule(args):
     """Bond dimension per sweep: ramped to sweep_M (two sweeps at M/4, two at M/2), then
     sweep_M for the rest of sweep_max sweeps."""
@@ -378,6 +390,9 @@ def sweep_compare(args, device: int):
     arms = [("fp64", core.FP64, args.tole), ("split", core.SPLIT_TF32, args.tole)]
     if not args.no_sweep_control:
         arms += [("fp64_control", core.FP64, 0.1 * args.tole), ("split_control", core.SPLIT_TF32, 0.1 * args.tole)]
+    if args.sweep_arms:
+        keep = set(args.sweep_arms.split(","))
+        arms = [a for a in arms if a[0] in keep]
     for name, prec, tole in arms:
         ctx = core.Context(device)
         core.set_precision(ctx, prec)
@@ -398,8 +413,11 @@ def sweep_compare(args, device: int):
                      "n_sigma_total": sum(s["n_sigma"] for s in sweeps),
                      "sigma_tflops_last_sweep": last["sigma_flops"] / last["seconds"] / 1e12,
                      "per_sweep": sweeps}
+        res[name]["device_bytes_in_use_after"] = _device_bytes_in_use()
         del st, mpo
         ctx.close()
+    if "fp64" not in res or "split" not in res:
+        return res
     e64 = res["fp64"]["energy"]
     cmp = {"abs_dE_split_vs_fp64": abs(res["split"]["energy"] - e64),
            "per_sweep_abs_dE_split_vs_fp64": [abs(a["energy"] - b["energy"]) for a, b in
@@ -408,7 +426,7 @@ def sweep_compare(args, device: int):
            "seconds_per_sweep_split": res["split"]["seconds_per_sweep_final_M"],
            "speedup_per_sweep": res["fp64"]["seconds_per_sweep_final_M"] / res["split"]["seconds_per_sweep_final_M"],
            "speedup_total": res["fp64"]["seconds_total"] / res["split"]["seconds_total"]}
-    if "fp64_control" in res:
+    if "fp64_control" in res and "split_control" in res:
         ec, esc = res["fp64_control"]["energy"], res["split_control"]["energy"]
 
         def per(a, b):
