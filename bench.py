@@ -404,6 +404,7 @@ def sweep_compare(args, device: int):
             log = dmrg.make_sweep(ctx, st, tole)
             sweeps.append({"M": M, "seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma,
                            "sigma_flops": log.sigma_flops, **{k: round(v, 4) for k, v in log.times.items()}})
+            print(f"sweep {name} M={M} E={log.energy:.12f} {log.seconds:.1f} s", file=sys.stderr, flush=True)
         last = sweeps[-1]
         atM = [s for s in sweeps if s["M"] == sched[-1]]
         res[name] = {"sweeps": len(sweeps), "davidson_tole": 0.1 * tole, "energy": last["energy"],
@@ -873,6 +874,16 @@ def main():
                 for p, prec in (("split", core.SPLIT_TF32), ("fp64", core.FP64))}
     elif args.bond_step and "st" in wl:
         bond = bond_compare(ctx, wl, args.M, args.tole)
+    # The headline workload's device memory is given back before the sections, which
+    # build their own (the largest configurations need all of the GPU's memory).
+    shape_info = {"W": wl["W"], "D_rows": sum(psi.shape()[1][0]), "D_cols": sum(psi.shape()[1][1]),
+                  "nnz_psi": psi.nnz, "nnz_L": mL.nnz, "nnz_R": mR.nnz}
+    psi_nnz = psi.nnz
+    del mL, mR, psi, sig, s64, one, wl
+    import gc
+
+    gc.collect()
+    ctx.close()
     # the sweep comparison, the scan and the gradients belong to the one-GPU line
     # (replicas, N > 1, time H_eff*psi only); a section not yet started when the
     # wall-clock budget is spent is skipped and says so
@@ -920,14 +931,13 @@ def main():
             "vs_baseline": None,
             "dtype": "tf32x3-split (fp64 in/out)" if args.precision == "split" else "f64",
             "data": DATA,
-            "config": {"workload": workload_name(args), "W": wl["W"], "D_rows": sum(psi.shape()[1][0]),
-                       "D_cols": sum(psi.shape()[1][1]), "nnz_psi": psi.nnz, "nnz_L": mL.nnz, "nnz_R": mR.nnz,
+            "config": {"workload": workload_name(args), **shape_info,
                        "flops_per_step": fl_per_step, "l2": l2, "parallelism": f"replicas{ws}",
                        "precision": args.precision,
                        "operators": "FP32 tiles split on chip" if args.fp32_operators else "hi|lo TF32 tiles"},
             "gpu_launches": int(launches),
             "e2e": {"value": job_tflops(ws, fl_per_step, e2e_s), "unit": "TFLOP/s", "ms_per_step": e2e_s * 1e3,
-                    "h2d_bytes_per_step": 8 * psi.nnz, "d2h_bytes_per_step": 8 * psi.nnz},
+                    "h2d_bytes_per_step": 8 * psi_nnz, "d2h_bytes_per_step": 8 * psi_nnz},
             "roofline": roof,
             "fp64_path": {"ms_per_step": fp64_s * 1e3, "value": fl_per_step / fp64_s / 1e12, "unit": "TFLOP/s",
                           "peak": fp64_peak, "frac": fl_per_step / fp64_s / 1e12 / fp64_peak,
