@@ -39,12 +39,13 @@ METRIC = "H_eff*psi TFLOP/s (FP64-equivalent), C2 middle bond: qc n=20 M=512"
 DATA = ("synthetic: the reference generator's MPO sites of the seeded n=20 integrals, a converged state's block "
         "structure, seeded normal block values")
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over the two tensor-core
-# launches of one H_eff*psi) divided by the algorithmic bytes 8 (nnz L + nnz R + 2 nnz
-# psi), measured by ncu on the small case of the same kernels (QC n=14, K=28, M=256:
-# 1.129 GB against 0.413 GB) and applied to the bench workloads, whose operators are
-# too large for a multi-metric capture; keyed by (workload, precision).
-MEASURED_TRAFFIC = {("c2-bond", "split"): 2.73, ("random-mps", "split"): 2.73}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over the launches of one
+# H_eff*psi: psi pack, the two tensor-core stages, split-K reduce) divided by the
+# algorithmic bytes 8 (nnz L + nnz R + 2 nnz psi), measured by ncu on the small case of
+# the same kernels (QC n=14, K=28, M=256, complementary-operator MPO: 0.857 GB against
+# 0.402 GB) and applied to the bench workloads, whose operators are too large for a
+# multi-metric capture; keyed by (workload, precision).
+MEASURED_TRAFFIC = {("c2-bond", "split"): 2.14, ("random-mps", "split"): 2.14}
 
 
 def parse():
@@ -78,6 +79,8 @@ def parse():
     ap.add_argument("--sweep-norb", type=int, default=20)
     ap.add_argument("--sweep-M", type=int, default=512)
     ap.add_argument("--sweep-max", type=int, default=12, help="sweeps per arm (ramp included)")
+    ap.add_argument("--sweep-env-checkpoint", type=int, default=0,
+                    help="keep every k-th block operator a sweep pass leaves for the other (0: all)")
     ap.add_argument("--no-sweep-ramp", dest="sweep_ramp", action="store_false",
                     help="all sweeps at --sweep-M (default: two sweeps at M/4, two at M/2 first)")
     ap.add_argument("--sweep-arms", default="",
@@ -386,7 +389,8 @@ def sweep_compare(args, device: int):
     mpo_d = qc_mpo_of(args, h1, eri)
     res = {"workload": f"qc n={n} K={2 * n} seed={args.seed}, {MPO_NAMES[args.mpo]}", "tole": args.tole,
            "mpo_bond_dims": mpogen.mpo_bond_dims(mpo_d),
-           "M_schedule": sched, "start": "reference initial state (constant-filled sites)"}
+           "M_schedule": sched, "start": "reference initial state (constant-filled sites)",
+           "env_checkpoint": args.sweep_env_checkpoint}
     arms = [("fp64", core.FP64, args.tole), ("split", core.SPLIT_TF32, args.tole)]
     if not args.no_sweep_control:
         arms += [("fp64_control", core.FP64, 0.1 * args.tole), ("split_control", core.SPLIT_TF32, 0.1 * args.tole)]
@@ -401,10 +405,12 @@ def sweep_compare(args, device: int):
         sweeps = []
         for M in sched:
             st.M = M
-            log = dmrg.make_sweep(ctx, st, tole)
+            log = dmrg.make_sweep(ctx, st, tole, env_checkpoint=args.sweep_env_checkpoint)
             sweeps.append({"M": M, "seconds": log.seconds, "energy": log.energy, "n_sigma": log.n_sigma,
-                           "sigma_flops": log.sigma_flops, **{k: round(v, 4) for k, v in log.times.items()}})
-            print(f"sweep {name} M={M} E={log.energy:.12f} {log.seconds:.1f} s", file=sys.stderr, flush=True)
+                           "sigma_flops": log.sigma_flops, **{k: round(v, 4) for k, v in log.times.items()},
+                           "device_gb_after": round((_device_bytes_in_use() or 0) / 1e9, 2)})
+            print(f"sweep {name} M={M} E={log.energy:.12f} {log.seconds:.1f} s {sweeps[-1]['device_gb_after']} GB",
+                  file=sys.stderr, flush=True)
         last = sweeps[-1]
         atM = [s for s in sweeps if s["M"] == sched[-1]]
         res[name] = {"sweeps": len(sweeps), "davidson_tole": 0.1 * tole, "energy": last["energy"],

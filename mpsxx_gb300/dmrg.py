@@ -207,11 +207,36 @@ class SweepLog:
     kind: str = "twosite"
 
 
-def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None, noise: float = 0.0) -> SweepLog:
+def _left_env_step(ctx: Context, st: DeviceState, L: Tensor, k: int) -> Tensor:
+    """L_{k+1} from L_k and the left-canonical site tensor k (the product a forward
+    bond step forms from the same operands)."""
+    mL = core.compute_merged_operator(ctx, True, st.mpo[k], L)
+    um = core.merge_rows(ctx, st.wave[k])
+    return core.renormalize(ctx, True, mL, um, um)
+
+
+def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None, noise: float = 0.0,
+               env_checkpoint: int = 0) -> SweepLog:
     """Forward then backward sweep; Davidson tolerance 0.1*tole; sweep energy =
     minimum over bonds (src/make_sweep.cpp:12-253); ``noise`` is added to every bond's
-    wavefunction before its truncation (make_noise, src/canonicalize.hpp:11-24)."""
+    wavefunction before its truncation (make_noise, src/canonicalize.hpp:11-24).
+
+    Block operators that a pass has made stale are dropped as it goes (the right
+    ones behind the forward pass, the left ones behind the backward pass), so about
+    one operator per site is resident instead of two; the sweep ends with the
+    orthogonality centre at site 0, the right operators current and the left ones
+    (but the boundary) dropped.  The reference keeps each in a file per site and
+    reads back the ones a bond needs.
+
+    ``env_checkpoint`` = k > 0 keeps, of the operators a pass leaves behind for the
+    other pass, only those at every k-th site (and the boundaries); a bond whose
+    operator was dropped rebuilds it, with the ones between, from the nearest kept
+    one by the same merged-operator and renormalisation products that made it (so
+    the sweep's results do not change), and drops each once used.  Resident
+    operators fall from ~N to ~2N/k + 2k at the cost of ~(k-1)/k extra
+    renormalisations per bond."""
     N = len(st.mpo)
+    k = int(env_checkpoint)
     t0 = time.perf_counter()
     es: List[float] = []
     nsig = 0
@@ -222,26 +247,58 @@ def make_sweep(ctx: Context, st: DeviceState, tole: float, bond_hook=None, noise
         nonlocal nsig, flops
         nsig += int(stats["n_sigma"])
         flops += stats["sigma_flops"]
-        for k in ("t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "n_sigma_fp64"):
-            times[k] = times.get(k, 0.0) + stats[k]
+        for key in ("t_merge", "t_diag", "t_davidson", "t_svd", "t_renorm", "n_sigma_fp64"):
+            times[key] = times.get(key, 0.0) + stats[key]
         times["n_unconverged"] = times.get("n_unconverged", 0.0) + (0.0 if stats["converged"] else 1.0)
 
+    def kept(j: int) -> bool:
+        return k <= 0 or j % k == 0 or j == 0 or j == N - 1
+
+    def rebuild(side: str, j: int):
+        """st.lenv[j] (or st.renv[j]) and the dropped ones between it and the nearest kept one."""
+        t = time.perf_counter()
+        if side == "l":
+            c = max(m for m in range(j) if st.lenv[m] is not None)
+            for m in range(c, j):
+                st.lenv[m + 1] = _left_env_step(ctx, st, st.lenv[m], m)
+            n = j - c
+        else:
+            c = min(m for m in range(j + 1, N) if st.renv[m] is not None)
+            for m in range(c, j, -1):
+                st.renv[m - 1] = _right_env_step(ctx, st, st.renv[m], m)
+            n = c - j
+        times["env_rebuilt"] = times.get("env_rebuilt", 0.0) + n
+        times["t_env_rebuild"] = times.get("t_env_rebuild", 0.0) + time.perf_counter() - t
+
     for i in range(N - 1):
+        if st.renv[i + 1] is None:
+            rebuild("r", i + 1)
         e, env, nl, nr, stats = core.optimize_twosite_merged(ctx, True, st.mpo[i], st.mpo[i + 1], st.lenv[i],
                                                              st.renv[i + 1], st.wave[i], st.wave[i + 1],
                                                              0.1 * tole, st.M, noise)
-        st.lenv[i + 1] = env
+        # L_{N-1} is used by no two-site bond
+        st.lenv[i + 1] = env if i + 1 < N - 1 else None
         st.wave[i], st.wave[i + 1] = nl, nr
+        if i + 1 < N - 1:
+            st.renv[i + 1] = None  # stale once the bond moves on; rebuilt by the backward pass
+        if not kept(i) and i < N - 2:
+            st.lenv[i] = None  # rebuilt from the nearest kept one when the backward pass needs it
         es.append(e)
         acc(stats)
         if bond_hook:
             bond_hook(True, i, e, stats)
     for i in range(N - 1, 0, -1):
+        if st.lenv[i - 1] is None:
+            rebuild("l", i - 1)
         e, env, nl, nr, stats = core.optimize_twosite_merged(ctx, False, st.mpo[i - 1], st.mpo[i], st.lenv[i - 1],
                                                              st.renv[i], st.wave[i - 1], st.wave[i], 0.1 * tole,
                                                              st.M, noise)
         st.renv[i - 1] = env
         st.wave[i - 1], st.wave[i] = nl, nr
+        if i - 1 > 0:
+            st.lenv[i - 1] = None  # stale; rebuilt by the next forward pass
+        if not kept(i) and i > 1:
+            st.renv[i] = None  # rebuilt from the nearest kept one when the next forward pass needs it
         es.append(e)
         acc(stats)
         if bond_hook:

@@ -145,10 +145,8 @@ def test_split_dmrg_hubbard12_matches_fp64(ctx):
     assert abs(es[-1] - gold["sweeps"][-1]["energy"]) < 1e-8
 
 
-def test_split_bond_step_refines_with_few_fp64_products(ctx):
-    """One bond of a converged QC n=8 sweep from identical inputs: the split step's
-    refined energy matches the FP64 step within 1e-9 Eh with at most two FP64
-    H_eff*psi (the anchor, and a second one only if the continuation fills up)."""
+def _qc8_bond(ctx, i=3):
+    """The operands of bond (i, i+1) of a converged QC n=8 M=64 state (FP64 sweeps)."""
     from mpsxx_gb300 import core, dmrg, mpogen
 
     h, eri = mpogen.synthetic_qc_integrals(8, 16, 3)
@@ -157,22 +155,62 @@ def test_split_bond_step_refines_with_few_fp64_products(ctx):
     st = dmrg.make_initial_state(ctx, mpo, 8, 0, 64)
     for _ in range(3):
         dmrg.make_sweep(ctx, st, 1e-9)
-    i = 3
     dmrg.advance_left(ctx, st, i)  # orthogonality centre from site 0 to the bond
-    res = {}
+    return (st.mpo[i], st.mpo[i + 1], st.lenv[i], st.renv[i + 1], st.wave[i], st.wave[i + 1])
+
+
+def _bond_step(ctx, prec, args, tole):
+    from mpsxx_gb300 import core
+
+    core.set_precision(ctx, prec)
     try:
-        for name, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
-            core.set_precision(ctx, prec)
-            e, _, _, _, s = core.optimize_twosite_merged(ctx, True, st.mpo[i], st.mpo[i + 1], st.lenv[i],
-                                                         st.renv[i + 1], st.wave[i], st.wave[i + 1], 1e-11, 64)
-            res[name] = (e, s)
+        e, _, nl, nr, s = core.optimize_twosite_merged(ctx, True, *args, tole, 64)
     finally:
         core.set_precision(ctx, core.FP64)
-    (e64, s64), (e32, s32) = res["fp64"], res["split"]
+    return e, s, nl, nr
+
+
+def test_split_bond_step_refines_with_few_fp64_products(ctx):
+    """One bond of a converged QC n=8 sweep from identical inputs: the split step's
+    refined energy matches the FP64 step within 1e-9 Eh with at most two FP64
+    H_eff*psi (the anchor, and a second one only if the continuation fills up)."""
+    from mpsxx_gb300 import core
+
+    args = _qc8_bond(ctx)
+    e64, s64, _, _ = _bond_step(ctx, core.FP64, args, 1e-11)
+    e32, s32, _, _ = _bond_step(ctx, core.SPLIT_TF32, args, 1e-11)
     print("bond step fp64", e64, s64["n_sigma"], "split", e32, s32["n_sigma"], s32["n_sigma_fp64"], s32["rnorm"])
     assert abs(e32 - e64) < 1e-9
     assert 1 <= s32["n_sigma_fp64"] <= 2
     assert s32["converged"] == 1
+
+
+def test_split_bond_step_when_refinement_rounds_run_out(ctx):
+    """The refinement's limits.  Without refinement rounds the step returns the split
+    Davidson's energy (no FP64 product; within the operator's 1e-5 relative
+    resolution of the FP64 step).  With a tolerance below FP64 rounding of |r|^2
+    (1e-40) every round ends unconverged: the step still returns, reports
+    converged = 0 with one FP64 anchor per round, and its energy — the FP64-anchored
+    Rayleigh quotient of the last round — matches the converged FP64 step within
+    1e-9 Eh; the new site tensors are finite."""
+    from mpsxx_gb300 import core
+
+    args = _qc8_bond(ctx)
+    e64, _, _, _ = _bond_step(ctx, core.FP64, args, 1e-11)
+    try:
+        ctx.set_split_refinement(rounds=0)
+        e0, s0, _, _ = _bond_step(ctx, core.SPLIT_TF32, args, 1e-11)
+        ctx.set_split_refinement(rounds=2)
+        e2, s2, nl, nr = _bond_step(ctx, core.SPLIT_TF32, args, 1e-40)
+    finally:
+        ctx.set_split_refinement()
+    print("no rounds", e0 - e64, s0["n_sigma_fp64"], "rounds exhausted", e2 - e64, s2["n_sigma_fp64"], s2["rnorm"])
+    assert s0["n_sigma_fp64"] == 0
+    assert abs(e0 - e64) < 1e-5 * abs(e64)
+    assert s2["converged"] == 0
+    assert s2["n_sigma_fp64"] == 2
+    assert abs(e2 - e64) < 1e-9
+    assert np.all(np.isfinite(nl.download())) and np.all(np.isfinite(nr.download()))
 
 
 def test_split_renormalize_matches_fp64_qc_bond(ctx):
