@@ -619,10 +619,10 @@ __global__ void __launch_bounds__(256) pack_kernel(const DPack* __restrict__ pac
   }
 }
 
-// Split-K partials of one output tile summed into C.  Threads cover only the tile's
-// valid rows x columns (tail tiles are mostly padding), and each sums its element's
-// slots four at a time into independent accumulators, so that four loads are in
-// flight per thread; the summation order is fixed.
+// Split-K partials of one output tile summed into C: one thread per valid element of
+// the tile (tail tiles are mostly padding; threads past the valid ones exit at once),
+// its slots summed four at a time into independent accumulators so that four loads are
+// in flight; the summation order is fixed.
 __global__ void __launch_bounds__(256) gemm_pk_reduce_kernel(const DReduce* __restrict__ red,
                                                              const DGemmTask* __restrict__ tasks, double alpha,
                                                              const double* __restrict__ partial,
@@ -631,24 +631,21 @@ __global__ void __launch_bounds__(256) gemm_pk_reduce_kernel(const DReduce* __re
   const DGemmTask task = tasks[rd.task];
   const int m0 = rd.tm * BM, n0 = rd.tn * BN;
   const int vm = min(BM, task.m - m0), vn = min(BN, task.n - n0);
-  if (vm <= 0 || vn <= 0) return;
+  const int e = blockIdx.y * blockDim.x + threadIdx.x;
+  if (vm <= 0 || vn <= 0 || e >= vm * vn) return;
   constexpr int64_t SLOT = BM * BN;
-  const double* __restrict__ p0 = partial + (int64_t)rd.slot0 * SLOT;
-  const int nvalid = vm * vn;
-  for (int e = blockIdx.y * blockDim.x + threadIdx.x; e < nvalid; e += gridDim.y * blockDim.x) {
-    const int r = e / vn, c = e - r * vn;
-    const double* __restrict__ p = p0 + r * BN + c;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    int k = 0;
-    for (; k + 4 <= rd.nslot; k += 4) {
-      s0 += p[(k + 0) * SLOT];
-      s1 += p[(k + 1) * SLOT];
-      s2 += p[(k + 2) * SLOT];
-      s3 += p[(k + 3) * SLOT];
-    }
-    for (; k < rd.nslot; ++k) s0 += p[k * SLOT];
-    C[task.c_off + (int64_t)(m0 + r) * task.ldc + (n0 + c)] += alpha * ((s0 + s1) + (s2 + s3));
+  const int r = e / vn, c = e - r * vn;
+  const double* __restrict__ p = partial + (int64_t)rd.slot0 * SLOT + r * BN + c;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int k = 0;
+  for (; k + 4 <= rd.nslot; k += 4) {
+    s0 += p[(k + 0) * SLOT];
+    s1 += p[(k + 1) * SLOT];
+    s2 += p[(k + 2) * SLOT];
+    s3 += p[(k + 3) * SLOT];
   }
+  for (; k < rd.nslot; ++k) s0 += p[k * SLOT];
+  C[task.c_off + (int64_t)(m0 + r) * task.ldc + (n0 + c)] += alpha * ((s0 + s1) + (s2 + s3));
 }
 
 }  // namespace
@@ -682,7 +679,7 @@ void launch_pack(const DPack* packs, int npacks, const double* src, uint8_t* dst
 void launch_gemm_pk_reduce(const DReduce* red, int nred, const DGemmTask* tasks, double alpha, const double* partial,
                            double* C, cudaStream_t st) {
   if (nred <= 0) return;
-  gemm_pk_reduce_kernel<<<dim3(nred, 8), 256, 0, st>>>(red, tasks, alpha, partial, C);
+  gemm_pk_reduce_kernel<<<dim3(nred, (BM * BN) / 256), 256, 0, st>>>(red, tasks, alpha, partial, C);
 }
 
 }  // namespace mpsxx
