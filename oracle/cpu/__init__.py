@@ -122,3 +122,8 @@ def sigma(ops: Operands, threads: int = 0) -> Tuple[dict, float, float]:
 
 def threads() -> int:
     return int(load().cpu_sigma_threads())
+
+
+def set_threads(n: int) -> None:
+    """OpenMP threads of the following sigma runs (n <= 0: the process's default)."""
+    load().cpu_sigma_set_threads(int(n))

@@ -36,6 +36,7 @@ using dgemm_t = void (*)(int, int, int, int, int, int, double, const double*, in
 using setthreads_t = void (*)(int);
 dgemm_t g_dgemm = nullptr;
 std::string g_error;
+int g_default_threads = 1;
 
 // A block-sparse tensor as the caller lays it out: sector counts and dims per index,
 // stored tags ascending, each block's offset into one data array.
@@ -162,9 +163,14 @@ int cpu_sigma_init(const char* blas_path, int threads) {
     return 2;
   }
   if (st) st(1);
+  g_default_threads = omp_get_max_threads();
   if (threads > 0) omp_set_num_threads(threads);
   return 0;
 }
+
+// OpenMP threads of the following runs: n > 0 threads, n <= 0 the count the process
+// started with (OMP_NUM_THREADS or all cores).
+void cpu_sigma_set_threads(int n) { omp_set_num_threads(n > 0 ? n : g_default_threads); }
 
 const char* cpu_sigma_error() { return g_error.c_str(); }
 
