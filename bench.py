@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--sweep-norb", type=int, default=20)
     ap.add_argument("--sweep-M", type=int, default=512)
     ap.add_argument("--sweep-max", type=int, default=12, help="sweeps per arm (ramp included)")
+    ap.add_argument("--split-floor", type=float, default=-1.0,
+                    help="split Davidson residual floor (relative to E) before the FP64 anchor (< 0: default)")
     ap.add_argument("--sweep-env-checkpoint", type=int, default=0,
                     help="keep every k-th block operator a sweep pass leaves for the other (0: all)")
     ap.add_argument("--no-sweep-ramp", dest="sweep_ramp", action="store_false",
@@ -390,7 +392,7 @@ def sweep_compare(args, device: int):
     res = {"workload": f"qc n={n} K={2 * n} seed={args.seed}, {MPO_NAMES[args.mpo]}", "tole": args.tole,
            "mpo_bond_dims": mpogen.mpo_bond_dims(mpo_d),
            "M_schedule": sched, "start": "reference initial state (constant-filled sites)",
-           "env_checkpoint": args.sweep_env_checkpoint}
+           "env_checkpoint": args.sweep_env_checkpoint, "split_floor": args.split_floor}
     arms = [("fp64", core.FP64, args.tole), ("split", core.SPLIT_TF32, args.tole)]
     if not args.no_sweep_control:
         arms += [("fp64_control", core.FP64, 0.1 * args.tole), ("split_control", core.SPLIT_TF32, 0.1 * args.tole)]
@@ -400,6 +402,7 @@ def sweep_compare(args, device: int):
     for name, prec, tole in arms:
         ctx = core.Context(device)
         core.set_precision(ctx, prec)
+        ctx.set_split_refinement(residual_floor=args.split_floor)
         mpo = [core.Tensor.from_dict(ctx, d) for d in mpo_d]
         st = dmrg.make_initial_state(ctx, mpo, n, 0, sched[0])
         sweeps = []
