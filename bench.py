@@ -472,8 +472,9 @@ def _converge(ctx, mpo, n_elec, M, tole, max_sweeps, st=None):
 
 def gradient_bench(args, device: int):
     """Adjoint energy gradients: dE/dU_i, dE/dt_i of a site-dependent Hubbard chain
-    (L=32, U_i ~ U(2,6), |t_i| ~ U(0.8,1.2), half filling, M=512) and dE/dh_pq of the
-    n=16 synthetic QC Hamiltonian (M=256).  Gradient in FP64 and split precision on
+    (L=32, U_i ~ U(2,6), |t_i| ~ U(0.8,1.2), half filling, M=512) and dE/dh_pq (with the
+    reference's MPO also dE/d(pq|rs)) of the n=16 synthetic QC Hamiltonian (M=256),
+    through the generators' Jacobians.  Gradient in FP64 and split precision on
     the same converged state, environments checkpointed every 4 sites; a few
     parameters checked by central differences (step 1e-4) of the energy, both of
     warm-restarted DMRG (the state re-converged: the derivative of the truncated
@@ -481,7 +482,7 @@ def gradient_bench(args, device: int):
     what the adjoint computes, by Hellmann-Feynman)."""
     import numpy as np
 
-    from mpsxx_gb300 import core, dmrg, mpogen
+    from mpsxx_gb300 import core, dmrg, mpogen, mpogen_comp
 
     out = {}
     rng = np.random.default_rng(args.seed)
@@ -493,9 +494,12 @@ def gradient_bench(args, device: int):
     cases = [
         ("hubbard_L32_M512", lambda th: mpogen.hubbard_mpo(L, th[0], th[1], jacobian=True), (t, U), L, 512,
          [("U", 0), ("U", L // 2), ("t", L // 2)]),
-        ("qc_n16_M256", lambda th: mpogen.qc_mpo(th[0], eri, jacobian=True), (h1,), n, 256,
+        ("qc_n16_M256", lambda th: mpogen.qc_mpo(th[0], th[1], jacobian=True), (h1, eri), n, 256,
          [("h", 0, 0), ("h", 3, 5), ("h", 7, 8)]),
     ]
+    if args.mpo == "comp":  # the reference's generator: keys of the integrals it reads
+        cases[1] = ("qc_n16_M256", lambda th: mpogen_comp.qc_mpo_complementary(th[0], th[1], jacobian=True),
+                    (h1, eri), n, 256, [("h", 0, 0), ("eri", 5, 3, 5, 3), ("h", 8, 7), ("eri", 3, 3, 3, 3)])
     tole = 1e-10
     for name, build, theta, nel, M, checks in cases:
         ctx = core.Context(device)
@@ -506,6 +510,8 @@ def gradient_bench(args, device: int):
         t_dmrg = time.perf_counter() - t0
         tags = [m.blocks()[0] for m in st.mpo]
         res = {"energy": e0, "sweeps": nsw, "dmrg_seconds": t_dmrg, "checkpoint": 4}
+        if name.startswith("qc"):
+            res["mpo"] = MPO_NAMES[args.mpo]
         grads = {}
         for pname, prec in (("fp64", core.FP64), ("split", core.SPLIT_TF32)):
             core.set_precision(ctx, prec)
@@ -527,6 +533,11 @@ def gradient_bench(args, device: int):
                     th[1][par[1]] += sgn * 1e-4
                 elif par[0] == "t":
                     th[0][par[1]] += sgn * 1e-4
+                elif par[0] == "eri":  # every entry of the 8-fold class
+                    p, q, r, s_ = par[1:]
+                    for a, b, c, d in {(p, q, r, s_), (q, p, r, s_), (p, q, s_, r), (q, p, s_, r),
+                                       (r, s_, p, q), (s_, r, p, q), (r, s_, q, p), (s_, r, q, p)}:
+                        th[1][a, b, c, d] += sgn * 1e-4
                 else:  # symmetric step of h_pq and h_qp
                     p, q = par[1], par[2]
                     th[0][p, q] += sgn * 1e-4

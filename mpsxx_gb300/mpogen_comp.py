@@ -25,7 +25,7 @@ Site tensors are returned in the neutral exchange format of ``mpogen``:
 """
 from __future__ import annotations
 
-from typing import Dict, List, Sequence, Tuple
+from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -226,7 +226,8 @@ INT2E_TYPE = {
 }
 
 
-def int1e_component(l_op: int, s_op: int, r_op: int, h: np.ndarray) -> float:
+def _int1e_index(l_op: int, s_op: int, r_op: int) -> Tuple[int, List[int]]:
+    """(type code, [i, j]) of the one-electron entry an operator triple reads."""
     idx, itype = [], 0
     for op in (l_op, s_op):
         if (op & NORMAL & TYPE) == SINGLE:
@@ -240,11 +241,24 @@ def int1e_component(l_op: int, s_op: int, r_op: int, h: np.ndarray) -> float:
         idx.append(_first(r_op))
         itype |= (r_op & MASK & FIRST) >> (INDEX_SHIFT + FIELD_SHIFT + 2 * len(idx) - 4)
     assert len(idx) == 2
+    return itype, idx
+
+
+def int1e_component(l_op: int, s_op: int, r_op: int, h: np.ndarray) -> float:
+    itype, idx = _int1e_index(l_op, s_op, r_op)
     if itype in (0xD, 0x8):
         return float(h[idx[0], idx[1]])
     if itype in (0x7, 0x2):
         return -float(h[idx[0], idx[1]])
     return 0.0
+
+
+def int1e_derivative(l_op: int, s_op: int, r_op: int) -> Dict[object, float]:
+    """d(int1e_component)/d(parameter): the entry h[i, j] read is the lower-triangle
+    element h1[max(i, j), min(i, j)] (the one the FCIDUMP holds), key ("h", p, q)."""
+    itype, (i, j) = _int1e_index(l_op, s_op, r_op)
+    sign = 1.0 if itype in (0xD, 0x8) else -1.0 if itype in (0x7, 0x2) else 0.0
+    return {("h", max(i, j), min(i, j)): sign} if sign else {}
 
 
 def _add_ops(op: int, idx: list, itype: int, single_mask: int) -> int:
@@ -260,8 +274,9 @@ def _add_ops(op: int, idx: list, itype: int, single_mask: int) -> int:
     return itype
 
 
-def int2e_component(l_op: int, s_op: int, r_op: int, v: np.ndarray) -> float:
-    """v[i,j,k,l] in the reference's layout: v[i,k,j,l] holds (ij|kl)."""
+def _int2e_index(l_op: int, s_op: int, r_op: int) -> Tuple[int, List[int]]:
+    """(combination code from INT2E_TYPE, [i, j, k, l]) of the two-electron entries an
+    operator triple reads."""
     idx: list = []
     itype = _add_ops(l_op, idx, 0, NORMAL)
     st = s_op & TYPE
@@ -280,7 +295,26 @@ def int2e_component(l_op: int, s_op: int, r_op: int, v: np.ndarray) -> float:
         itype = 0xD8
     itype = _add_ops(r_op, idx, itype, NORMAL)
     assert len(idx) == 4 and itype < 256
-    m = INT2E_TYPE.get(itype, 0)
+    return INT2E_TYPE.get(itype, 0), idx
+
+
+def _int2e_terms(m: int, idx: List[int]) -> List[Tuple[float, Tuple[int, int, int, int]]]:
+    """The signed entries of v (reference layout) that combination m adds up."""
+    i, j, k, l = idx
+    first = {1: (i, j, l, k), 2: (i, j, k, l), 3: (i, k, j, l)}.get(m % 4)
+    if first is None:
+        return []
+    second = {1: (i, j, k, l), 2: (i, k, j, l), 3: (i, j, l, k)}[m % 4]
+    sign = -1.0 if m & 4 else 1.0
+    out = [(sign, first)]
+    if m & 8:
+        out.append((-sign, second))
+    return out
+
+
+def int2e_component(l_op: int, s_op: int, r_op: int, v: np.ndarray) -> float:
+    """v[i,j,k,l] in the reference's layout: v[i,k,j,l] holds (ij|kl)."""
+    m, idx = _int2e_index(l_op, s_op, r_op)
     i, j, k, l = idx
     val = 0.0
     if m % 4 == 1:
@@ -298,103 +332,151 @@ def int2e_component(l_op: int, s_op: int, r_op: int, v: np.ndarray) -> float:
     return float(-val if m & 4 else val)
 
 
+def _canonical_eri(p: int, q: int, r: int, s: int) -> Tuple[int, int, int, int]:
+    """The canonical index of (pq|rs) under 8-fold symmetry (p >= q, r >= s, pq >= rs)."""
+    a, b = max(p, q), min(p, q)
+    c, d = max(r, s), min(r, s)
+    if a * (a + 1) // 2 + b < c * (c + 1) // 2 + d:
+        a, b, c, d = c, d, a, b
+    return a, b, c, d
+
+
+def int2e_derivative(l_op: int, s_op: int, r_op: int) -> Dict[object, float]:
+    """d(int2e_component)/d(parameter), key ("eri", canonical p, q, r, s): the entry
+    v[a, b, c, d] is (ac|bd), which the reference fills from the canonical element."""
+    out: Dict[object, float] = {}
+    for sign, (a, b, c, d) in _int2e_terms(*_int2e_index(l_op, s_op, r_op)):
+        key = ("eri",) + _canonical_eri(a, c, b, d)
+        out[key] = out.get(key, 0.0) + sign
+    return {k: x for k, x in out.items() if x != 0.0}
+
+
 # ---------------------------------------------------------------------------
 # one site tensor (src/gen_site_operator.cpp:9-169, src/prime_operators.h:167-187)
 # ---------------------------------------------------------------------------
 class _Site:
-    def __init__(self, lq: Sequence[Tuple[int, int]], rq: Sequence[Tuple[int, int]]):
+    def __init__(self, lq: Sequence[Tuple[int, int]], rq: Sequence[Tuple[int, int]], track: bool = False):
         self.lq, self.rq = lq, rq  # left sector charges; right sector charges (before negation)
         self.blocks: Dict[Tuple[int, int, int, int], float] = {}
+        # with track: d(block)/d(parameter) per block, parameters as int1e_derivative /
+        # int2e_derivative name them
+        self.jac: Optional[Dict[Tuple[int, int, int, int], Dict[object, float]]] = {} if track else None
 
-    def prime(self, name: str, li: int, ri: int, scale: float):
+    def prime(self, name: str, li: int, ri: int, scale: float, dscale: Optional[Dict[object, float]] = None):
         if abs(scale) < 1.0e-16:
             return
         odd_l = self.lq[li][0] & 1
         for bra, ket, x in PRIME[name]:
-            val = -scale * x if (odd_l and SITE_Q[bra][0] & 1) else scale * x
+            flip = odd_l and SITE_Q[bra][0] & 1
+            val = -scale * x if flip else scale * x
             key = (li, bra, ket, ri)
             if key in self.blocks:
                 self.blocks[key] = self.blocks[key] + val
             else:
                 self.blocks[key] = val
+            if self.jac is not None and dscale:
+                jk = self.jac.setdefault(key, {})
+                f = -x if flip else x
+                for par, dv in dscale.items():
+                    jk[par] = jk.get(par, 0.0) + f * dv
+
+    def remap(self, fn):
+        """Re-key blocks (and their derivatives) by fn(key) -> new key or None (dropped)."""
+        keep = {k: fn(k) for k in self.blocks}
+        self.blocks = {nk: x for k, x in self.blocks.items() if (nk := keep[k]) is not None}
+        if self.jac is not None:
+            self.jac = {nk: d for k, d in self.jac.items() if (nk := keep.get(k)) is not None}
 
 
 def gen_site_operator(site: _Site, l_op: int, li: int, s_op: int, r_op: int, ri: int, ecore: float,
                       h: np.ndarray, v: np.ndarray):
+    track = site.jac is not None
+
+    def i1(l, s_, r):
+        return int1e_component(l, s_, r, h), (int1e_derivative(l, s_, r) if track else None)
+
+    def i2(l, s_, r):
+        return int2e_component(l, s_, r, v), (int2e_derivative(l, s_, r) if track else None)
+
     st = s_op & TYPE
     if st == IDEN:
-        v2 = 1.0
+        v2, d2 = 1.0, None
         if (l_op & TYPE) == DOUBLE and (r_op & TYPE) == DOUBLE and (l_op & INDEX) != (r_op & INDEX):
-            v2 = int2e_component(l_op, s_op, r_op, v)
-        site.prime("I", li, ri, v2)
+            v2, d2 = i2(l_op, s_op, r_op)
+        site.prime("I", li, ri, v2, d2)
     elif st == HAM:
         if not (s_op & INDEX) and abs(ecore) > 1.0e-16:
             site.prime("I", li, ri, ecore)
-        v1 = int1e_component(l_op, s_op, r_op, h)
-        v2 = int2e_component(l_op, s_op, r_op, v)
-        site.prime("CaDa", li, ri, v1)
-        site.prime("CbDb", li, ri, v1)
-        site.prime("CaDaCbDb", li, ri, v2)
+        v1, d1 = i1(l_op, s_op, r_op)
+        v2, d2 = i2(l_op, s_op, r_op)
+        site.prime("CaDa", li, ri, v1, d1)
+        site.prime("CbDb", li, ri, v1, d1)
+        site.prime("CaDaCbDb", li, ri, v2, d2)
     elif st == SINGLE:
-        v2 = 1.0
+        v2, d2 = 1.0, None
         if (l_op & NORMAL & TYPE) == SINGLE and (r_op & TYPE) == DOUBLE:
             conj = (COMP | CONJ_S) if (l_op & COMP) else 0
             lc = (l_op ^ conj) & U32
             if (DOUBLE | (lc & FIRST) | ((s_op & FIRST) >> INDEX_SHIFT)) != r_op and \
                     (DOUBLE | ((lc & FIRST) >> INDEX_SHIFT) | (s_op & FIRST)) != r_op:
-                v2 = int2e_component(lc, s_op, r_op, v)
+                v2, d2 = i2(lc, s_op, r_op)
         elif (l_op & TYPE) == DOUBLE and (r_op & NORMAL & TYPE) == SINGLE:
             conj = (COMP | CONJ_S) if (r_op & COMP) else 0
             rc = (r_op ^ conj) & U32
             if (DOUBLE | (s_op & FIRST) | ((rc & FIRST) >> INDEX_SHIFT)) != l_op and \
                     (DOUBLE | ((s_op & FIRST) >> INDEX_SHIFT) | (rc & FIRST)) != l_op:
-                v2 = int2e_component(l_op, s_op, rc, v)
+                v2, d2 = i2(l_op, s_op, rc)
         name = {CRE_A: "Ca", CRE_B: "Cb", DES_A: "Da", DES_B: "Db"}.get(s_op & MASK)
         if name:
-            site.prime(name, li, ri, v2)
+            site.prime(name, li, ri, v2, d2)
     elif st == SINGLE_COMP:
         v1 = v2 = 0.0
+        d1 = d2 = None
         if (l_op & NORMAL & TYPE) == SINGLE:
             conj = (COMP | CONJ_S) if (l_op & COMP) else 0
             lc = (l_op ^ conj) & U32
-            v1 = int1e_component(lc, s_op, r_op, h) * 0.5
-            v2 = int2e_component(lc, s_op, r_op, v)
+            v1, d1 = i1(lc, s_op, r_op)
+            v2, d2 = i2(lc, s_op, r_op)
+            v1 *= 0.5
         elif (r_op & NORMAL & TYPE) == SINGLE:
             conj = (COMP | CONJ_S) if (r_op & COMP) else 0
             rc = (r_op ^ conj) & U32
-            v1 = int1e_component(l_op, s_op, rc, h) * 0.5
-            v2 = int2e_component(l_op, s_op, rc, v)
+            v1, d1 = i1(l_op, s_op, rc)
+            v2, d2 = i2(l_op, s_op, rc)
+            v1 *= 0.5
+        if d1:
+            d1 = {k: 0.5 * x for k, x in d1.items()}
         pair = {CRE_A: ("Ca", "CaCbDb"), CRE_B: ("Cb", "CbCaDa"), DES_A: ("Da", "CbDbDa"),
                 DES_B: ("Db", "CaDaDb")}.get(s_op & MASK)
         if pair:
-            site.prime(pair[0], li, ri, v1)
-            site.prime(pair[1], li, ri, v2)
+            site.prime(pair[0], li, ri, v1, d1)
+            site.prime(pair[1], li, ri, v2, d2)
     elif st == DOUBLE:
-        v2 = 1.0
+        v2, d2 = 1.0, None
         lt, rt = l_op & TYPE, r_op & TYPE
         if lt == SINGLE and rt == SINGLE:
-            v2 = int2e_component(l_op, s_op, r_op, v)
+            v2, d2 = i2(l_op, s_op, r_op)
         elif lt == SINGLE and rt == SINGLE_COMP:
-            v2 = int2e_component(l_op, s_op, (r_op ^ COMP ^ CONJ_S) & U32, v)
+            v2, d2 = i2(l_op, s_op, (r_op ^ COMP ^ CONJ_S) & U32)
         elif rt == SINGLE and lt == SINGLE_COMP:
-            v2 = int2e_component((l_op ^ COMP ^ CONJ_S) & U32, s_op, r_op, v)
+            v2, d2 = i2((l_op ^ COMP ^ CONJ_S) & U32, s_op, r_op)
         elif lt == DOUBLE and (l_op & INDEX) != (s_op & INDEX):
-            v2 = int2e_component(l_op, s_op, r_op, v)
+            v2, d2 = i2(l_op, s_op, r_op)
         elif rt == DOUBLE and (r_op & INDEX) != (s_op & INDEX):
-            v2 = int2e_component(l_op, s_op, r_op, v)
+            v2, d2 = i2(l_op, s_op, r_op)
         m = s_op & MASK
         if m == CRE_A_DES_A:
-            site.prime("CaDa", li, ri, v2)
+            site.prime("CaDa", li, ri, v2, d2)
         elif m == CRE_B_DES_B:
-            site.prime("CbDb", li, ri, v2)
+            site.prime("CbDb", li, ri, v2, d2)
         elif m == CRE_A_CRE_B:
-            site.prime("CaCb", li, ri, v2)
+            site.prime("CaCb", li, ri, v2, d2)
         elif m == CRE_A_DES_B:
-            site.prime("CaDb", li, ri, v2)
+            site.prime("CaDb", li, ri, v2, d2)
         elif m == DES_A_CRE_B:
-            site.prime("CbDa", li, ri, -v2)
+            site.prime("CbDa", li, ri, -v2, {k: -x for k, x in d2.items()} if d2 else None)
         elif m == DES_A_DES_B:
-            site.prime("DaDb", li, ri, v2)
+            site.prime("DaDb", li, ri, v2, d2)
 
 
 # ---------------------------------------------------------------------------
@@ -419,9 +501,15 @@ def reference_integrals(h1: np.ndarray, eri: np.ndarray, tol: float = 1.0e-16):
     return h, v
 
 
-def qc_mpo_complementary(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0) -> List[dict]:
+def qc_mpo_complementary(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0, jacobian: bool = False):
     """The reference generator's MPO for H = sum h_pq a+_p a_q + 1/2 sum (pq|rs) ...
-    (integrals in chemist order, 8-fold symmetric), one dict per site."""
+    (integrals in chemist order, 8-fold symmetric), one dict per site.
+
+    With ``jacobian`` also, per site, {block tag: {parameter: d(block)/d(parameter)}}:
+    every block is a linear combination of the integrals the reference reads, which
+    are h1[p, q] with p >= q (key ("h", p, q)) and the canonical (pq|rs) of each
+    8-fold class (key ("eri", p, q, r, s), p >= q, r >= s, pq >= rs).  A derivative
+    is with respect to the symmetric parameter, i.e. all its equal entries at once."""
     N = h1.shape[0]
     h, v = reference_integrals(h1, eri)
     l_ops = boundary_ops(0, N)
@@ -436,7 +524,7 @@ def qc_mpo_complementary(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0) ->
         rq = [None] * len(r_ops)
         for c, k in r_ops.items():
             rq[k] = get_quantum(c)
-        site = _Site(lq, rq)
+        site = _Site(lq, rq, track=jacobian)
         s_sorted = sorted(s_ops)
         for l_op in sorted(l_ops):
             li = l_ops[l_op]
@@ -448,7 +536,7 @@ def qc_mpo_complementary(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0) ->
         # forward removal: right sectors no block reaches (BoundaryOpInfo::clean)
         used = sorted({k[3] for k in site.blocks})
         remap = {old: new for new, old in enumerate(used)}
-        site.blocks = {(a, b, c, remap[d]): x for (a, b, c, d), x in site.blocks.items()}
+        site.remap(lambda k: (k[0], k[1], k[2], remap[k[3]]))
         site.rq = [rq[o] for o in used]
         kept = {c: remap[k] for c, k in r_ops.items() if k in remap}
         sites.append(site)
@@ -460,21 +548,27 @@ def qc_mpo_complementary(h1: np.ndarray, eri: np.ndarray, ecore: float = 0.0) ->
     for i in range(N - 1, -1, -1):
         s = sites[i]
         keep_r = {old: new for new, old in enumerate(r_keep)}
-        blocks = {(a, b, c, keep_r[d]): x for (a, b, c, d), x in s.blocks.items() if d in keep_r}
-        used_l = sorted({k[0] for k in blocks})
+        s.remap(lambda k: (k[0], k[1], k[2], keep_r[k[3]]) if k[3] in keep_r else None)
+        used_l = sorted({k[0] for k in s.blocks})
         remap_l = {old: new for new, old in enumerate(used_l)}
-        s.blocks = {(remap_l[a], b, c, d): x for (a, b, c, d), x in blocks.items()}
+        s.remap(lambda k: (remap_l[k[0]], k[1], k[2], k[3]))
         s.rq = [s.rq[o] for o in r_keep]
         s.lq = [s.lq[o] for o in used_l]
         r_keep = used_l
-    out = []
+    out, jacs = [], []
     neg = lambda q: (-q[0], -q[1])  # noqa: E731
     for s in sites:
         qshape = [list(s.lq), list(SITE_Q), [neg(q) for q in SITE_Q], [neg(q) for q in s.rq]]
         dshape = [[1] * len(x) for x in qshape]
         n1, n2, n3 = len(qshape[1]), len(qshape[2]), len(qshape[3])
+        tag = lambda k: ((k[0] * n1 + k[1]) * n2 + k[2]) * n3 + k[3]  # noqa: E731
         blocks = {}
-        for (a, b, c, d), x in s.blocks.items():
-            blocks[((a * n1 + b) * n2 + c) * n3 + d] = np.full((1, 1, 1, 1), x)
+        for key, x in s.blocks.items():
+            blocks[tag(key)] = np.full((1, 1, 1, 1), x)
         out.append({"q": (0, 0), "qshape": qshape, "dshape": dshape, "blocks": dict(sorted(blocks.items()))})
+        if jacobian:
+            jacs.append({tag(key): {p: x for p, x in d.items() if x != 0.0}
+                         for key, d in s.jac.items() if key in s.blocks and any(x != 0.0 for x in d.values())})
+    if jacobian:
+        return out, jacs
     return out

@@ -139,6 +139,48 @@ def test_qc_h_gradient_matches_exact_finite_differences(ctx):
     assert worst < 1e-6
 
 
+def test_qc_gradient_through_the_reference_mpo_matches_exact_finite_differences(ctx):
+    """The same check through the reference scheme's MPO generator (complementary
+    operators), for h_pq and for (pq|rs) classes: every entry of an 8-fold class
+    stepped together, the adjoint read at the class's canonical key."""
+    from oracle import ed
+    from mpsxx_gb300 import mpogen, mpogen_comp
+
+    n = 6
+    h1, eri = mpogen.synthetic_qc_integrals(n, 2 * n, 4)
+    sites, jacs = mpogen_comp.qc_mpo_complementary(h1, eri, jacobian=True)
+    st, log = converge(ctx, sites, n, 64, 1e-12, 5)
+    e_ed = ed.qc_ground_energy(h1, eri, n // 2, n // 2)[0]
+    assert abs(log.energy - e_ed) < 1e-9
+    _, dE = params_gradient(ctx, st, jacs, checkpoint=2)
+    step = 1e-4
+
+    def energy(h, v):
+        return ed.qc_ground_energy(h, v, n // 2, n // 2)[0]
+
+    worst = 0.0
+    for p, q in [(0, 0), (2, 2), (1, 0), (3, 1), (5, 2), (5, 4)]:
+        hp, hm = h1.copy(), h1.copy()
+        for hh, sgn in ((hp, 1.0), (hm, -1.0)):
+            hh[p, q] += sgn * step
+            if p != q:
+                hh[q, p] += sgn * step
+        fd = (energy(hp, eri) - energy(hm, eri)) / (2 * step)
+        adj = dE.get(("h", p, q), 0.0)
+        worst = max(worst, abs(adj - fd) / max(1.0, abs(fd)))
+    for p, q, r, s in [(2, 2, 2, 2), (3, 1, 2, 0), (4, 4, 1, 1), (5, 2, 5, 2), (3, 3, 3, 0)]:
+        vp, vm = eri.copy(), eri.copy()
+        for vv, sgn in ((vp, 1.0), (vm, -1.0)):
+            for a, b, c, d in {(p, q, r, s), (q, p, r, s), (p, q, s, r), (q, p, s, r),
+                               (r, s, p, q), (s, r, p, q), (r, s, q, p), (s, r, q, p)}:
+                vv[a, b, c, d] += sgn * step
+        fd = (energy(h1, vp) - energy(h1, vm)) / (2 * step)
+        adj = dE.get(("eri", p, q, r, s), 0.0)
+        worst = max(worst, abs(adj - fd) / max(1.0, abs(fd)))
+    print("qc n=6, reference MPO: dE/dh and dE/d(pq|rs) adjoint vs exact FD, worst relative error", worst)
+    assert worst < 1e-6
+
+
 def test_autograd_harness_backward_is_the_adjoint(ctx):
     """torch.autograd through the C ABI: backward gives the adjoint gradient, and a
     central difference of the harness's own energies (warm restarts) agrees."""
