@@ -3,8 +3,9 @@
 //
 // GB300 (sm_103a) has a very small FP64 pipe, so the FP64 path is FMA-bound on
 // CUDA cores: a 64x64 output tile per 256-thread CTA, 4x4 register micro-tiles,
-// operands staged through shared memory in 16-deep K slices; warps whose 16x32 band
-// of the tile lies outside a ragged block skip their FMAs.  Every output tile
+// operands staged through shared memory in 16-deep K slices; warps own bands of the
+// tile shaped per tile to its valid extent, and bands outside a ragged block skip
+// their FMAs.  Every output tile
 // is owned by exactly one CTA and its (A,B) pairs are accumulated in enumeration
 // order, so results are deterministic run to run.
 #include <cuda_runtime.h>
@@ -32,13 +33,29 @@ __global__ void __launch_bounds__(256, 2) gemm_f64_kernel(int transa, int transb
   const DTile t = tiles[blockIdx.x];
   const DGemmTask task = tasks[t.task];
   const int m0 = t.tm * TM, n0 = t.tn * TN;
-  // Warp w owns a 16-row x 32-column band of the tile (rows 16 (w & 3) + ..., columns
-  // 32 (w >> 2) + ...); its lanes hold 4x4 micro-tiles with rows and columns strided by
-  // 4 and 8.  A band that lies wholly outside the block (a ragged block's last tile)
-  // skips its FMAs: the FP64 pipe, GB300's narrowest, does only useful work there.
+  // Each warp owns a band of 4 LR rows x 128 / LR columns of the tile: its lanes form
+  // an LR x (32 / LR) grid of 4x4 micro-tiles with rows strided by LR and columns by
+  // 32 / LR; the 8 bands tile the 64x64 output.  LR (2, 4, 8 or 16) is chosen per tile
+  // so that the bands touching the block's valid rows x columns cover the least area,
+  // and bands wholly outside skip their FMAs: a ragged block's narrow last tiles (64
+  // rows x 6 columns, say) take one band shaped like them instead of several 16 x 32
+  // bands, so the FP64 pipe, GB300's narrowest, does little beyond the useful work.
+  // The band shape changes which lane computes an element, not its summation order.
+  const int vm = min(TM, task.m - m0), vn = min(TN, task.n - n0);
+  int LR = 4, best = 1 << 30;
+  for (int lr : {4, 2, 8, 16}) {
+    const int bh = 4 * lr, bw = 128 / lr;
+    const int area = ((vm + bh - 1) / bh) * bh * (((vn + bw - 1) / bw) * bw);
+    if (area < best) {
+      best = area;
+      LR = lr;
+    }
+  }
+  const int LC = 32 / LR;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rb = 16 * (warp & 3), cb = 32 * (warp >> 2);
-  const int ty = lane >> 3, tx = lane & 7;
+  const int wr = warp / (LR / 2), wc = warp % (LR / 2);
+  const int rb = wr * 4 * LR, cb = wc * (128 / LR);
+  const int ty = lane / LC, tx = lane % LC;
   const bool live = (m0 + rb < task.m) && (n0 + cb < task.n);
   double acc[4][4];
 #pragma unroll
@@ -87,9 +104,9 @@ __global__ void __launch_bounds__(256, 2) gemm_f64_kernel(int transa, int transb
           for (int kk = 0; kk < TK; ++kk) {
             double a[4], b[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[kk][rb + ty + 4 * i];
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][rb + ty + LR * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][cb + tx + 8 * j];
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][cb + tx + LC * j];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -99,9 +116,9 @@ __global__ void __launch_bounds__(256, 2) gemm_f64_kernel(int transa, int transb
           for (int kk = 0; kk < kn; ++kk) {
             double a[4], b[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[kk][rb + ty + 4 * i];
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][rb + ty + LR * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][cb + tx + 8 * j];
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][cb + tx + LC * j];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -118,17 +135,17 @@ __global__ void __launch_bounds__(256, 2) gemm_f64_kernel(int transa, int transb
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) part[(rb + ty + 4 * i) * TN + cb + tx + 8 * j] = acc[i][j];
+      for (int j = 0; j < 4; ++j) part[(rb + ty + LR * i) * TN + cb + tx + LC * j] = acc[i][j];
     return;
   }
   if (!live) return;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const int r = m0 + rb + ty + 4 * i;
+    const int r = m0 + rb + ty + LR * i;
     if (r >= task.m) continue;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int c = n0 + cb + tx + 8 * j;
+      const int c = n0 + cb + tx + LC * j;
       if (c >= task.n) continue;
       double* dst = C + task.c_off + (int64_t)r * task.ldc + c;
       *dst += alpha * acc[i][j];
