@@ -388,20 +388,33 @@ def make_sweep_onesite(ctx: Context, st: DeviceState, tole: float, noise: float 
     return SweepLog(min(es), es, nsig, 0.0, time.perf_counter() - t0, kind="onesite")
 
 
+def fill_right_envs(ctx: Context, st: DeviceState):
+    """Rebuild every dropped right block operator of a state whose orthogonality centre
+    is at site 0 (as a two-site sweep with checkpointed operators leaves it)."""
+    for j in range(len(st.mpo) - 2, -1, -1):
+        if st.renv[j] is None:
+            st.renv[j] = _right_env_step(ctx, st, st.renv[j + 1], j + 1)
+
+
 def dmrg(ctx: Context, mpo_dicts: List[dict], n_elec: int, two_sz: int, M: int, tole: float, max_sweeps: int,
-         min_sweeps: int = 0, verbose: bool = False, onesite: bool = False, noise: float = 0.0):
+         min_sweeps: int = 0, verbose: bool = False, onesite: bool = False, noise: float = 0.0,
+         env_checkpoint: int = 0):
     """Sweeps until |dE| < tole after at least one iteration (src/dmrg.cpp:37-79); with
     ``onesite``, the reference's second stage follows: one-site sweeps from the
     converged two-site state until |dE| < tole again (src/dmrg.cpp:80-115).  ``noise``
-    is the dmrg.conf keyword of that name, passed to every truncation."""
+    is the dmrg.conf keyword of that name, passed to every truncation;
+    ``env_checkpoint`` is make_sweep's (two-site stage)."""
     mpo = [Tensor.from_dict(ctx, d) for d in mpo_dicts]
     st = make_initial_state(ctx, mpo, n_elec, two_sz, M)
     e_prev = 0.0
     logs = []
     stages = [make_sweep] + ([make_sweep_onesite] if onesite else [])
     for stage in stages:
+        if stage is make_sweep_onesite:
+            fill_right_envs(ctx, st)  # the one-site stage reads every right operator
+        extra = {"env_checkpoint": env_checkpoint} if stage is make_sweep else {}
         for it in range(max_sweeps):
-            log = stage(ctx, st, tole, noise=noise)
+            log = stage(ctx, st, tole, noise=noise, **extra)
             logs.append(log)
             de = log.energy - e_prev
             e_prev = log.energy

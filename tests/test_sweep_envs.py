@@ -115,3 +115,13 @@ def test_checkpointing_holds_fewer_operators_and_rebuilds_each_once_per_pass(fak
     assert held[0] <= N + 2
     assert held[4] <= 2 * (N // 4) + 2 * 4 + 4
     assert held[4] < held[0]
+
+
+def test_fill_right_envs_restores_every_operator_after_a_checkpointed_sweep(fake):
+    N = 11
+    st = _state(fake, N)
+    for _ in range(2):
+        dmrg.make_sweep(None, st, 1e-9, env_checkpoint=3)
+    assert any(x is None for x in st.renv)
+    dmrg.fill_right_envs(None, st)
+    assert all(st.renv[j] == fake.right(j) for j in range(N))
