@@ -56,3 +56,17 @@ def test_checkpointed_environments_leave_the_sweep_unchanged(ctx, k):
     e_full = dmrg.make_sweep(ctx, st_full, 1e-9).energy
     e_ckpt = dmrg.make_sweep(ctx, st_ckpt, 1e-9, env_checkpoint=k).energy
     assert abs(e_full - e_ckpt) < 1e-12
+
+
+def test_dmrg_driver_with_checkpointed_operators_and_a_onesite_stage(ctx):
+    """dmrg() with checkpointed operators in the two-site stage, then the one-site stage
+    (which first rebuilds the dropped right operators): every sweep energy as without."""
+    from mpsxx_gb300 import core, dmrg
+    from mpsxx_gb300.mpogen import hubbard_mpo
+
+    core.set_precision(ctx, core.FP64)
+    mpo = hubbard_mpo(8, -1.0, 4.0)
+    _, full = dmrg.dmrg(ctx, mpo, 8, 0, 32, 1e-10, 6, onesite=True)
+    _, ckpt = dmrg.dmrg(ctx, mpo, 8, 0, 32, 1e-10, 6, onesite=True, env_checkpoint=3)
+    assert [log.kind for log in full] == [log.kind for log in ckpt]
+    assert max(abs(a.energy - b.energy) for a, b in zip(full, ckpt)) < 1e-12
